@@ -1,0 +1,214 @@
+"""Generate golden vectors by running the reference's own C++.
+
+Builds oracle/_ref/libflipref.so (oracle/Makefile `ref`: the reference
+sources compiled where they lie, plus oracle/ref_harness.cpp) and runs its
+sorter, mapper, solver, corrector and N=32 driver stages on seeded inputs.
+Writes tests/golden/*.npz. Needs the reference tree, so it runs in the build
+container only; the committed .npz files travel instead.
+
+Each task runs in its own child process, in a scratch working directory
+(the reference appends progress to render/log/console.out and sizes its
+solver scratch once per process), with stdout silenced.
+
+    python tests/golden/make_golden.py [task ...]
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+REF_LIB = os.path.join(ROOT, "oracle", "_ref", "libflipref.so")
+
+from flip3d_gb300 import scenes  # noqa: E402
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+SEED = 7
+SUBSET = 4096
+
+
+def digest(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def load_ref():
+    L = C.CDLL(REF_LIB)
+    L.fr_sort.argtypes = [C.c_int, C.c_int, f32p, u8p, u32p, u32p]
+    L.fr_mark_water.argtypes = [C.c_int, C.c_int, f32p, u8p, f32p, u8p, f32p]
+    L.fr_p2g.argtypes = [C.c_int, C.c_int, f32p, f32p, u8p, f32p, f32p, f32p]
+    L.fr_g2p.argtypes = [C.c_int, C.c_int, f32p, u8p, f32p, f32p, f32p, f32p]
+    L.fr_solve.argtypes = [C.c_int, C.c_int, C.c_double, u8p, f32p, f32p, f32p]
+    L.fr_solve.restype = C.c_int
+    L.fr_correct.argtypes = [C.c_int, C.c_int, f32p, f32p, u8p, f32p, C.c_float, C.c_float,
+                             C.c_uint64, C.c_int64]
+    L.fr_sim_setup.argtypes = [C.c_int, f32p, f32p, u8p, f32p, C.c_float, C.c_uint64,
+                               C.c_double]
+    L.fr_sim_stage.argtypes = [C.c_int]
+    L.fr_sim_get.argtypes = [f32p, f32p, f32p, u8p]
+    L.fr_sim_get_grid.argtypes = [f32p, f32p, f32p, u8p, f32p, f32p]
+    L.fr_sim_stuck.restype = C.c_int
+    L.fr_max_density.restype = C.c_float
+    L.fr_grid_n.restype = C.c_int
+    return L
+
+
+def component_scene(n: int) -> scenes.Scene:
+    """A pool+sphere scene with positions and velocities scrambled so that
+    clamping, empty cells, crowded cells and close pairs all occur."""
+    sc = scenes.pool_sphere(n, seed=SEED)
+    rng = np.random.default_rng(SEED)
+    fl = sc.type == scenes.FLUID
+    pos = sc.pos.copy()
+    pos[fl] += rng.normal(0.0, 0.6 / n, size=(fl.sum(), 3)).astype(np.float32)
+    # a few particles outside the box (clamping) and a few stacked pairs
+    idx = rng.choice(np.nonzero(fl)[0], 40, replace=False)
+    pos[idx[:10]] = rng.uniform(-0.2, 1.2, size=(10, 3)).astype(np.float32)
+    pos[idx[10:25]] = pos[idx[25:40]] + rng.normal(0, 0.01 / n, size=(15, 3)).astype(np.float32)
+    vel = np.where(fl[:, None], rng.normal(0.0, 0.5, size=pos.shape), 0.0).astype(np.float32)
+    sc.pos = np.ascontiguousarray(pos)
+    sc.vel = np.ascontiguousarray(vel)
+    return sc
+
+
+def task_components(out: str, n: int = 16):
+    L = load_ref()
+    sc = component_scene(n)
+    P = sc.count
+    cs = np.zeros(n ** 3 + 1, np.uint32)
+    perm = np.zeros(P, np.uint32)
+    L.fr_sort(n, P, sc.pos, sc.type, cs, perm)
+    rng = np.random.default_rng(SEED + 1)
+    dens = np.where(sc.type == scenes.FLUID, rng.uniform(0.0, 0.12, P), 1.0).astype(np.float32)
+    A = np.zeros(n ** 3, np.uint8)
+    Ls = np.zeros(n ** 3, np.float32)
+    L.fr_mark_water(n, P, sc.pos, sc.type, dens, A, Ls)
+    fs = (n + 1) * n * n
+    u = [np.zeros(fs, np.float32) for _ in range(3)]
+    L.fr_p2g(n, P, sc.pos, sc.vel, sc.type, u[0], u[1], u[2])
+    grid = [rng.normal(0, 1, fs).astype(np.float32) for _ in range(3)]
+    g2p = np.zeros((P, 3), np.float32)
+    L.fr_g2p(n, P, sc.pos, sc.type, grid[0], grid[1], grid[2], g2p)
+    cpos, cvel = sc.pos.copy(), sc.vel.copy()
+    L.fr_correct(n, P, cpos, cvel, sc.type, sc.nrm, np.float32(0.006), np.float32(0.5 / n),
+                 SEED, 3)
+    np.savez_compressed(out, n=n, pos=sc.pos, vel=sc.vel, type=sc.type, nrm=sc.nrm,
+                        cell_start=cs, perm=perm, dens=dens, A=A, L=Ls, u0=u[0], u1=u[1],
+                        u2=u[2], grid0=grid[0], grid1=grid[1], grid2=grid[2], g2p=g2p,
+                        corr_pos=cpos, corr_vel=cvel, corr_seed=SEED, corr_step=3)
+
+
+def task_solver(out: str, n: int = 16):
+    L = load_ref()
+    from oracle import pyoracle as orc  # the oracle only prepares a realistic input
+    sc = scenes.pool_sphere(n, seed=SEED)
+    cs, perm = orc.sort(n, sc.pos)
+    md = orc.max_density(n)
+    dens = orc.density(n, sc.pos, sc.type, cs, perm, md)
+    A = orc.mark_water(n, sc.type, dens, cs, perm)
+    Ls = orc.levelset(n, sc.type, dens, cs, perm)
+    rng = np.random.default_rng(SEED + 2)
+    b = np.where(A == 1, rng.normal(0, 3.0, n ** 3), rng.normal(0, 1, n ** 3)).astype(np.float32)
+    x0 = np.where(A == 1, rng.normal(0, 0.02, n ** 3), 0).astype(np.float32)
+    res = {}
+    for tag, rel in (("abs", 0.0), ("rel6", 1e-6)):
+        x = x0.copy()
+        bb = b.copy()
+        k = L.fr_solve(n, 1, rel, A, Ls, x, bb)
+        res[f"x_{tag}"] = x
+        res[f"b_{tag}"] = bb
+        res[f"k_{tag}"] = k
+    np.savez_compressed(out, n=n, A=A, L=Ls, x0=x0, b=b, **res)
+
+
+def task_driver(out: str, steps: int = 10, rel_tol: float = 1e-6):
+    L = load_ref()
+    n = L.fr_grid_n()
+    sc = scenes.pool_sphere(n, seed=0)
+    md = L.fr_max_density()
+    L.fr_sim_setup(sc.count, sc.pos, sc.vel, sc.type, sc.nrm, md, SEED, rel_tol)
+    P = sc.count
+    fs = (n + 1) * n * n
+    rng = np.random.default_rng(SEED + 3)
+    sub = np.sort(rng.choice(P, min(SUBSET, P), replace=False))
+    rec = {"n": n, "max_dens": np.float32(md), "seed": SEED, "rel_tol": rel_tol,
+           "steps": steps, "subset": sub, "scene_pos_sha": digest(sc.pos)}
+
+    def snap(tag):
+        pos = np.zeros((P, 3), np.float32)
+        vel = np.zeros((P, 3), np.float32)
+        dens = np.zeros(P, np.float32)
+        typ = np.zeros(P, np.uint8)
+        L.fr_sim_get(pos, vel, dens, typ)
+        u = [np.zeros(fs, np.float32) for _ in range(3)]
+        A = np.zeros(n ** 3, np.uint8)
+        Ls = np.zeros(n ** 3, np.float32)
+        pr = np.zeros(n ** 3, np.float32)
+        L.fr_sim_get_grid(u[0], u[1], u[2], A, Ls, pr)
+        fluid = typ == 1
+        for name, arr in (("pos", pos), ("vel_fluid", np.where(fluid[:, None], vel, 0)),
+                          ("dens", dens), ("u0", u[0]), ("u1", u[1]), ("u2", u[2]), ("A", A),
+                          ("L", Ls), ("press", pr)):
+            arr = np.ascontiguousarray(arr)
+            rec[f"{tag}_{name}_sha"] = digest(arr)
+            if arr.shape[0] == P:
+                rec[f"{tag}_{name}_sub"] = arr[sub]
+            else:
+                rec[f"{tag}_{name}_sub"] = arr[:: max(1, arr.shape[0] // SUBSET)]
+        rec[f"{tag}_stuck"] = L.fr_sim_stuck()
+
+    for st in range(5):
+        L.fr_sim_stage(st)
+        snap(f"s1_stage{st}")
+    for k in range(2, steps + 1):
+        for st in range(5):
+            L.fr_sim_stage(st)
+        if k in (2, 5, steps):
+            snap(f"step{k}")
+    np.savez_compressed(out, **rec)
+
+
+TASKS = {
+    "components_n16": lambda out: task_components(out, 16),
+    "components_n13": lambda out: task_components(out, 13),
+    "solver_n16": lambda out: task_solver(out, 16),
+    "solver_n13": lambda out: task_solver(out, 13),
+    "driver_n32": lambda out: task_driver(out, 10, 1e-6),
+    "driver_n32_abs": lambda out: task_driver(out, 5, 0.0),
+}
+
+
+def run_child(task: str, out: str):
+    os.chdir(tempfile.mkdtemp(prefix="flipref_"))
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    os.environ["OMP_NUM_THREADS"] = "1"
+    TASKS[task](out)
+
+
+def main(argv):
+    if len(argv) >= 3 and argv[1] == "--child":
+        run_child(argv[2], argv[3])
+        return
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    tasks = argv[1:] or list(TASKS)
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    for t in tasks:
+        out = os.path.join(HERE, f"{t}.npz")
+        subprocess.check_call([sys.executable, os.path.abspath(__file__), "--child", t, out],
+                              env=env)
+        print(f"wrote {out} ({os.path.getsize(out) // 1024} KiB)")
+
+
+if __name__ == "__main__":
+    main(sys.argv)
