@@ -1,0 +1,328 @@
+"""Benchmark of the FLIP step on GB300.
+
+One step = one simulateStep of the hot path (sort, density, P2G, markWater,
+projection with PCG to relative residual 1e-6, G2P + FLIP blend, advection
+with wall constraint and reposition, position correction) on the dam-break
+scene at N=128 (liquid column x<0.4, y<0.8; 8 particles per liquid cell,
+about 5.4M particles), synthetic seeded data.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is particle-steps/s over all ranks with the
+state resident on the device; `e2e` is the same metric through the C ABI with
+the particle state copied from pinned host memory before each step and back
+after it. Multi-GPU runs are independent replicas (the step has no exchange).
+The CPU baseline (and the reference arm) time the CPU restatement of the
+reference step on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "learned-warm-start vs plain MIC-PCG ms/solve @ rel-res 1e-6; particle-steps/s"
+UNIT = "particle-steps/s"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+FALLBACK_HBM = 6800.0
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def stage_bytes(stage, P, n, iters):
+    """Algorithmic bytes of one call of a stage: every input read once and
+    every output written once, nothing else."""
+    C = n ** 3
+    F = 3 * (n + 1) * n * n
+    table = {
+        # count: pos 12 r, key 4 w, rank 4 w; scatter: key+rank 8 r, perm 4 w;
+        # cell counts/starts 3*4*C; payload: perm 4 + pos 12 + vel 12 + type 1 + dens 4 r,
+        # 52 w (spos, spg, svel 16 each, sdens 4)
+        "sort": P * (12 + 8 + 8 + 4) + 12 * C + P * (33 + 52),
+        "density": P * (16 + 4) + 4 * C,
+        "mark_water": P * 8 + 4 * C + 5 * C,
+        "p2g": P * 32 + 4 * C + C + 2 * 4 * F,
+        "divergence": C + 4 * F + 4 * C,
+        "solve": max(iters, 1) * 41 * C,
+        "gradient": 4 * F * 2 + 9 * C,
+        "extrapolate": 4 * F * 3 + C,
+        "g2p_flip": P * (12 + 1 + 12 + 12) + 2 * 4 * F,
+        "advect": P * (12 + 12 + 1 + 4 + 12 + 12 + 1) + 4 * F + C,
+        "reposition": P * 1 + C,
+        "correct": P * (16 + 16 + 12 + 12 + 4) + 4 * C,
+    }
+    return table.get(stage, 0)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_step_rate(scene, seconds_cap=60.0):
+    """Time the CPU restatement of the reference step (all host threads)."""
+    from oracle import pyoracle as orc
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    prm = orc.params(scene.n, orc.PRECOND_REF, rel_tol=1e-6, seed=1)
+    sim = orc.Sim(scene, prm, orc.max_density(scene.n))
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        sim.step()
+        steps += 1
+        if time.perf_counter() - t0 > seconds_cap / 4 or steps >= 1:
+            break
+    dt = time.perf_counter() - t0
+    return scene.count * steps / dt, cores, steps, dt
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from flip3d_gb300 import scenes
+    from oracle import pyoracle as orc
+    sc = scenes.dam_break(args.n, seed=0)
+    cores = os.cpu_count() or 1
+    orc.set_threads(cores)
+    prm = orc.params(sc.n, orc.PRECOND_REF, rel_tol=1e-6, seed=1)
+    sim = orc.Sim(sc, prm, orc.max_density(sc.n))
+    for _ in range(args.warmup):
+        sim.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    value = sc.count * args.steps / dt
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"dam_break N={args.n} ({sc.count} particles)",
+                      "particles": sc.count, "grid": args.n, "solver": "reference PCG",
+                      "rel_res": 1e-6},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{args.steps} full steps of dam_break N={args.n}"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "ref"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import numpy as np
+    import torch
+
+    from flip3d_gb300 import gpu, scenes
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    sc = scenes.dam_break(args.n, seed=rank)
+    P = sc.count
+    pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "ref": gpu.PRECOND_REF}[args.precond]
+    mode = gpu.SOLVE_REF if args.precond == "ref" else gpu.SOLVE_FAST
+    prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1)
+    sim = gpu.Simulation(prm)
+    sim.set_scene(sc)
+    sim.calibrate_max_density()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # the library launches on this stream; the events are recorded on it
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    solve_ms, iters = [], []
+    for _ in range(args.warmup):
+        sim.step()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = sim.launches
+    start_ev = torch.cuda.Event(enable_timing=True)
+    end_ev = torch.cuda.Event(enable_timing=True)
+    stream.synchronize()
+    start_ev.record(stream)
+    for _ in range(args.steps):
+        st = sim.step()
+        solve_ms.append(st.ms)
+        iters.append(st.iterations)
+    end_ev.record(stream)
+    stream.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = sim.launches - launches0
+    ms = start_ev.elapsed_time(end_ev)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    total_particles = P * world
+    value = total_particles * args.steps / (ms / 1e3)
+
+    # per-stage profile (separate pass; events between stages)
+    sim.set_profiling(True)
+    for _ in range(2):
+        st = sim.step()
+    prof = sim.profile()
+    sim.set_profiling(False)
+    dom = max(prof, key=lambda s: prof[s][0])
+    dom_ms = prof[dom][0] / max(prof[dom][1], 1)
+    it_prof = int(st.iterations)
+    nbytes = stage_bytes(dom, P, args.n, it_prof)
+    peak, peak_kind = hbm_peak()
+    achieved = nbytes / (dom_ms / 1e3) / 1e9
+    traffic = None
+    try:
+        with open(TRAFFIC) as f:
+            traffic = json.load(f).get(dom)
+    except Exception:
+        pass
+
+    # end to end through the C ABI with pinned host buffers
+    hpos = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
+    hvel = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
+    pos0, vel0, _, _ = sim.get_particles()
+    hpos.numpy()[:] = pos0
+    hvel.numpy()[:] = vel0
+    for _ in range(2):
+        sim.put_state(hpos.numpy(), hvel.numpy())
+        sim.step()
+        sim.get_state_into(hpos.data_ptr(), hvel.data_ptr())
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.put_state(hpos.numpy(), hvel.numpy())
+        sim.step()
+        sim.get_state_into(hpos.data_ptr(), hvel.data_ptr())
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = total_particles * args.steps / e2e_s
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, cores, steps, dt = cpu_step_rate(scenes.dam_break(args.n, seed=0))
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{steps} full step(s) of dam_break N={args.n} ({P} particles), "
+                         f"{dt:.1f} s"}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"dam_break N={args.n}, 8 particles/cell, rel-res 1e-6",
+                       "particles": P, "grid": args.n, "solver": f"FP32 PCG {args.precond}, FP64 dots",
+                       "l2": "inputs larger than L2 (state ~0.6 GB per step)",
+                       "parallelism": f"replicas x{world}"},
+            "solve": {"ms_per_solve": statistics.mean(solve_ms), "iters": statistics.mean(iters),
+                      "kind": f"plain PCG ({args.precond})"},
+            "stages_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof.items()},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_kind, "algorithmic_bytes": nbytes,
+                         "ms_per_launch": dom_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": P * 24,
+                    "d2h_bytes_per_step": P * 24},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,661 @@
+/*
+ * api.cu — the C ABI of include/flipgpu.h: handle lifetime, transfers and
+ * the orchestration of the per-step stages.
+ */
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "devcommon.cuh"
+
+namespace {
+
+int fail(FlipGpu *h, int code, const char *fmt, ...) {
+  if (h) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(h->err, sizeof h->err, fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define CK(h, call)                                                              \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess)                                                       \
+      return fail((h), FLIPGPU_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T> cudaError_t dalloc(T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+float largest_float_le(double d) {
+  float f = (float)d;
+  if ((double)f > d) f = nextafterf(f, -INFINITY);
+  return f;
+}
+float largest_float_lt(double d) {
+  float f = largest_float_le(d);
+  if ((double)f == d) f = nextafterf(f, -INFINITY);
+  return f;
+}
+float smallest_float_ge(double d) {
+  float f = (float)d;
+  if ((double)f < d) f = nextafterf(f, INFINITY);
+  return f;
+}
+void split(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+constexpr int BLK = 256;
+
+__global__ void k_deinterleave(int np, const float *__restrict__ aos, float *__restrict__ x,
+                               float *__restrict__ y, float *__restrict__ z) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= np) return;
+  x[p] = aos[3 * (size_t)p];
+  y[p] = aos[3 * (size_t)p + 1];
+  z[p] = aos[3 * (size_t)p + 2];
+}
+__global__ void k_interleave(int np, const float *__restrict__ x, const float *__restrict__ y,
+                             const float *__restrict__ z, float *__restrict__ aos) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= np) return;
+  aos[3 * (size_t)p] = x[p];
+  aos[3 * (size_t)p + 1] = y[p];
+  aos[3 * (size_t)p + 2] = z[p];
+}
+__global__ void k_add_force(SimConst c, const uint8_t *__restrict__ type, float *__restrict__ vy) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np || type[p] != CELL_FLUID) return;
+  vy[p] = refmath::add_fd(vy[p], c.grav_h, c.grav_l, c.grav);
+}
+
+/* Upload an AoS float[np][3] (host or device) into three SoA arrays. */
+int put3(FlipGpu *h, const float *src, int on_device, float *x, float *y, float *z) {
+  if (!src) return FLIPGPU_OK;
+  size_t bytes = (size_t)h->np * 3 * sizeof(float);
+  float *stage = (float *)h->spos; /* 16 B per slot >= 12 B per particle */
+  CK(h, cudaMemcpyAsync(stage, src, bytes,
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+  k_deinterleave<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, stage, x, y, z);
+  FG_LAUNCHED(h, 1);
+  CK(h, cudaGetLastError());
+  return FLIPGPU_OK;
+}
+
+int get3(FlipGpu *h, float *dst, int on_device, const float *x, const float *y, const float *z,
+         float *stage) {
+  if (!dst) return FLIPGPU_OK;
+  size_t bytes = (size_t)h->np * 3 * sizeof(float);
+  k_interleave<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, x, y, z, stage);
+  FG_LAUNCHED(h, 1);
+  CK(h, cudaGetLastError());
+  CK(h, cudaMemcpyAsync(dst, stage, bytes,
+                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+  return FLIPGPU_OK;
+}
+
+/* Static wall lists: wall particles grouped by cell in particle order
+ * (walls never move, so the wall part of every cell list is fixed). */
+int build_walls(FlipGpu *h, const std::vector<float> &pos, const std::vector<uint8_t> &type) {
+  const int n = h->n;
+  const float fn = (float)n;
+  std::vector<uint32_t> start(h->nc + 1, 0);
+  std::vector<uint32_t> key;
+  std::vector<int> idx;
+  for (int p = 0; p < h->np; p++) {
+    if (type[p] != CELL_WALL) continue;
+    int c[3];
+    for (int a = 0; a < 3; a++)
+      c[a] = (int)fmaxf(0.0f, fminf((float)(n - 1), fn * pos[3 * (size_t)p + a]));
+    uint32_t kk = (uint32_t)(((size_t)c[0] * n + c[1]) * n + c[2]);
+    key.push_back(kk);
+    idx.push_back(p);
+    start[kk + 1]++;
+  }
+  for (size_t c = 0; c < h->nc; c++) start[c + 1] += start[c];
+  const size_t nw = idx.size();
+  std::vector<uint32_t> fillp(start.begin(), start.end() - 1);
+  std::vector<float4> wpos(nw), wnrm(nw);
+  /* nrm is uploaded separately; read it back from the canonical arrays */
+  std::vector<float> nx(h->np), ny(h->np), nz(h->np);
+  CK(h, cudaMemcpyAsync(nx.data(), h->nx, h->np * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaMemcpyAsync(ny.data(), h->ny, h->np * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaMemcpyAsync(nz.data(), h->nz, h->np * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  for (size_t w = 0; w < nw; w++) {
+    int p = idx[w];
+    uint32_t slot = fillp[key[w]]++;
+    wpos[slot] = make_float4(pos[3 * (size_t)p], pos[3 * (size_t)p + 1], pos[3 * (size_t)p + 2], 0.0f);
+    wnrm[slot] = make_float4(nx[p], ny[p], nz[p], 0.0f);
+  }
+  cudaFree(h->wall_pos);
+  cudaFree(h->wall_nrm);
+  h->wall_pos = h->wall_nrm = nullptr;
+  CK(h, dalloc(&h->wall_pos, nw));
+  CK(h, dalloc(&h->wall_nrm, nw));
+  h->nwall = (int)nw;
+  CK(h, cudaMemcpyAsync(h->wall_start, start.data(), (h->nc + 1) * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice, h->stream));
+  if (nw) {
+    CK(h, cudaMemcpyAsync(h->wall_pos, wpos.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->wall_nrm, wnrm.data(), nw * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+void free_all(FlipGpu *h) {
+  void *ptrs[] = {h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->dens, h->type, h->nx, h->ny,
+                  h->nz, h->key, h->rank, h->perm, h->cell_start, h->cell_count, h->spos,
+                  h->spg, h->svel, h->sdens, h->wall_start, h->wall_pos, h->wall_nrm, h->u[0],
+                  h->u[1], h->u[2], h->us[0], h->us[1], h->us[2], h->A, h->L, h->press,
+                  h->div, h->r, h->z, h->s, h->P, h->Pf, h->diag, h->partial, h->scal,
+                  h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
+                  h->water_idx, h->stage};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+}
+
+/* Stage timing: one event per stage boundary; flushed after the step. */
+struct StageClock {
+  FlipGpu *h;
+  int last = -1;
+  bool used[FLIPGPU_NSTAGES] = {};
+  int order[FLIPGPU_NSTAGES + 1];
+  int nmark = 0;
+  explicit StageClock(FlipGpu *hh) : h(hh) {}
+  void mark(int stage) {
+    if (!h->prof_on) return;
+    cudaEventRecord(h->prof_ev[nmark], h->stream);
+    order[nmark++] = stage;
+  }
+  void flush() {
+    if (!h->prof_on || nmark < 2) return;
+    cudaEventSynchronize(h->prof_ev[nmark - 1]);
+    for (int i = 0; i + 1 < nmark; i++) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, h->prof_ev[i], h->prof_ev[i + 1]);
+      h->prof_ms[order[i]] += ms;
+      h->prof_calls[order[i]]++;
+    }
+  }
+};
+
+} // namespace
+
+SimConst make_const(const FlipGpu *h) {
+  SimConst c;
+  const FlipGpuParams &p = h->prm;
+  const int n = h->n;
+  c.n = n;
+  c.np = h->np;
+  c.fn = (float)n;
+  c.h = (float)(1.0 / n);
+  c.density = p.density;
+  float kh = (float)(4.0 * (double)p.density / n);
+  c.kd_hh = kh * kh;
+  c.max_dens = h->max_dens;
+  const float RE = (float)1.4;
+  c.re_p2g_hh = RE * RE;
+  c.re_corr = (float)((double)p.density / n);
+  c.re_corr_hh = c.re_corr * c.re_corr;
+  c.re_repo = (float)(1.0 / n);
+  c.re_repo_hh = c.re_repo * c.re_repo;
+  c.r2_floor = smallest_float_ge(1.0e-5);
+  c.sharp_small_p2g = (float)fmax((double)c.re_p2g_hh / 1.0e-5 - 1.0, 0.0);
+  c.sharp_small_corr = (float)fmax((double)c.re_corr_hh / 1.0e-5 - 1.0, 0.0);
+  c.sharp_small_repo = (float)fmax((double)c.re_repo_hh / 1.0e-5 - 1.0, 0.0);
+  c.wall_r = (float)(1.0 / n);
+  c.wall_hi = (float)(1.0 - (double)c.wall_r);
+  c.wall_hi_thr = largest_float_le(1.0 - (double)c.wall_r);
+  c.push_re = 1.5 * (double)p.density / n;
+  c.push_re_thr = largest_float_lt(c.push_re);
+  c.corr_near_thr = largest_float_le(0.1 * (double)c.re_corr);
+  double re2 = (double)c.re_corr * (double)c.re_corr;
+  c.corr_cut2 = smallest_float_ge(re2 * (1.0 + 1.0 / 256.0));
+  c.dt = p.dt;
+  c.dt_f = (float)p.dt;
+  split(p.dt, c.dt_h, c.dt_l);
+  c.grav = -p.dt * p.gravity;
+  split(c.grav, c.grav_h, c.grav_l);
+  c.c1 = 1.0 - p.alpha;
+  c.c2 = p.alpha;
+  split(c.c1, c.c1h, c.c1l);
+  split(c.c2, c.c2h, c.c2l);
+  float dens3 = p.density * p.density * p.density;
+  float n0 = (float)(1.0 / (double)dens3);
+  c.l0 = 0.2 * (double)n0;
+  split(c.l0, c.l0h, c.l0l);
+  c.seed = p.seed;
+  c.step = h->step;
+  return c;
+}
+
+extern "C" {
+
+void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles) {
+  std::memset(p, 0, sizeof *p);
+  p->n = n;
+  p->max_particles = max_particles;
+  p->density = 0.5f;
+  p->alpha = 0.95;
+  p->dt = 0.6e-2;
+  p->gravity = 9.8;
+  p->subcell = 1;
+  p->seed = 0;
+  p->solve_mode = FLIPGPU_SOLVE_REF;
+  p->precond = FLIPGPU_PRECOND_REF;
+  p->mic_tau = 0.0;
+  p->rel_tol = 0.0;
+  p->eps_abs = -1.0;
+  p->max_iters = 0;
+  p->refine_steps = 0;
+}
+
+const char *flipgpu_last_error(const FlipGpu *h) { return h ? h->err : "null handle"; }
+
+int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
+  if (!p || !out) return FLIPGPU_EINVAL;
+  *out = nullptr;
+  if (p->n < 3 || p->n > 1024 || p->max_particles < 0) return FLIPGPU_EINVAL;
+  const size_t n = (size_t)p->n;
+  if (n * n * n >= 0xffffffffull) return FLIPGPU_EINVAL;
+  FlipGpu *h = new (std::nothrow) FlipGpu();
+  if (!h) return FLIPGPU_ENOMEM;
+  std::memset((void *)h, 0, sizeof *h);
+  h->prm = *p;
+  h->n = p->n;
+  h->cap = p->max_particles;
+  h->nc = n * n * n;
+  h->nf = (n + 1) * n * n;
+  h->max_dens = 1.0f;
+  const size_t cap = (size_t)h->cap;
+  const size_t nc = h->nc, nf = h->nf;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return FLIPGPU_ECUDA;
+  }
+  h->stream = h->own_stream;
+  cudaEventCreate(&h->ev0);
+  cudaEventCreate(&h->ev1);
+  for (int i = 0; i <= FLIPGPU_NSTAGES; i++) cudaEventCreate(&h->prof_ev[i]);
+  size_t scan_n = cap > nc + 1 ? cap : nc + 1;
+  h->scan_cap = (scan_n + 4095) / 4096 + 1;
+#define AL(ptr, cnt)                                                  \
+  if ((e = dalloc(&(ptr), (cnt))) != cudaSuccess) {                   \
+    free_all(h);                                                      \
+    cudaStreamDestroy(h->own_stream);                                 \
+    delete h;                                                         \
+    return FLIPGPU_ENOMEM;                                            \
+  }
+  AL(h->px, cap) AL(h->py, cap) AL(h->pz, cap) AL(h->vx, cap) AL(h->vy, cap) AL(h->vz, cap)
+  AL(h->dens, cap) AL(h->type, cap) AL(h->nx, cap) AL(h->ny, cap) AL(h->nz, cap)
+  AL(h->key, cap) AL(h->rank, cap) AL(h->perm, cap) AL(h->cell_start, nc + 1)
+  AL(h->cell_count, nc + 1) AL(h->spos, cap) AL(h->spg, cap) AL(h->svel, cap)
+  AL(h->sdens, cap) AL(h->wall_start, nc + 1)
+  for (int c = 0; c < 3; c++) {
+    AL(h->u[c], nf) AL(h->us[c], nf)
+  }
+  AL(h->A, nc) AL(h->L, nc) AL(h->press, nc) AL(h->div, nc) AL(h->r, nc) AL(h->z, nc)
+  AL(h->s, nc) AL(h->P, 2 * nc) AL(h->Pf, nc) AL(h->diag, nc) AL(h->partial, 4096)
+  AL(h->scal, SC_COUNT) AL(h->iflags, IF_COUNT) AL(h->flag, cap) AL(h->scan_a, scan_n)
+  AL(h->scan_b, scan_n) AL(h->scan_tmp, h->scan_cap) AL(h->stuck_idx, cap)
+  AL(h->water_idx, nc) AL(h->stage, 3 * cap)
+#undef AL
+  for (int c = 0; c < 3; c++) {
+    cudaMemsetAsync(h->u[c], 0, nf * sizeof(float), h->stream);
+    cudaMemsetAsync(h->us[c], 0, nf * sizeof(float), h->stream);
+  }
+  cudaMemsetAsync(h->A, 0, nc, h->stream);
+  cudaMemsetAsync(h->L, 0, nc * sizeof(float), h->stream);
+  cudaMemsetAsync(h->press, 0, nc * sizeof(float), h->stream);
+  cudaMemsetAsync(h->div, 0, nc * sizeof(float), h->stream);
+  cudaMemsetAsync(h->wall_start, 0, (nc + 1) * sizeof(uint32_t), h->stream);
+  cudaMemsetAsync(h->iflags, 0, IF_COUNT * sizeof(int), h->stream);
+  e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    free_all(h);
+    delete h;
+    return FLIPGPU_ECUDA;
+  }
+  *out = h;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_destroy(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  cudaStreamSynchronize(h->stream);
+  free_all(h);
+  cudaEventDestroy(h->ev0);
+  cudaEventDestroy(h->ev1);
+  for (int i = 0; i <= FLIPGPU_NSTAGES; i++) cudaEventDestroy(h->prof_ev[i]);
+  cudaStreamDestroy(h->own_stream);
+  delete h;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_stream(FlipGpu *h, void *stream) {
+  if (!h) return FLIPGPU_EINVAL;
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_sync(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_step(FlipGpu *h, int64_t step) {
+  if (!h) return FLIPGPU_EINVAL;
+  h->step = step;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_count(const FlipGpu *h) { return h ? h->np : -1; }
+int64_t flipgpu_launch_count(const FlipGpu *h) { return h ? h->launches : -1; }
+
+int flipgpu_set_particles(FlipGpu *h, int count, const float *pos, const float *vel,
+                          const uint8_t *type, const float *nrm, const float *dens,
+                          int on_device) {
+  if (!h || count < 0 || count > h->cap) return fail(h, FLIPGPU_EINVAL, "bad particle count %d", count);
+  if (!pos || !type) return fail(h, FLIPGPU_EINVAL, "pos and type are required");
+  h->np = count;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  CK(h, cudaMemsetAsync(h->vx, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->vy, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->vz, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->nx, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->ny, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->nz, 0, h->cap * sizeof(float), h->stream));
+  CK(h, cudaMemsetAsync(h->dens, 0, h->cap * sizeof(float), h->stream));
+  int r;
+  if ((r = put3(h, pos, on_device, h->px, h->py, h->pz)) != FLIPGPU_OK) return r;
+  if ((r = put3(h, vel, on_device, h->vx, h->vy, h->vz)) != FLIPGPU_OK) return r;
+  if ((r = put3(h, nrm, on_device, h->nx, h->ny, h->nz)) != FLIPGPU_OK) return r;
+  CK(h, cudaMemcpyAsync(h->type, type, count, kind, h->stream));
+  if (dens) CK(h, cudaMemcpyAsync(h->dens, dens, count * sizeof(float), kind, h->stream));
+  /* host copies of positions and types for the static wall lists */
+  std::vector<float> hpos((size_t)count * 3);
+  std::vector<uint8_t> htype(count);
+  CK(h, cudaMemcpyAsync(hpos.data(), pos, hpos.size() * sizeof(float),
+                        on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, h->stream));
+  CK(h, cudaMemcpyAsync(htype.data(), type, count,
+                        on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->cells_valid = false;
+  return build_walls(h, hpos, htype);
+}
+
+int flipgpu_get_particles(FlipGpu *h, float *pos, float *vel, float *dens, uint8_t *type,
+                          int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r;
+  if ((r = get3(h, pos, on_device, h->px, h->py, h->pz, h->stage)) != FLIPGPU_OK) return r;
+  if ((r = get3(h, vel, on_device, h->vx, h->vy, h->vz, h->stage + 0)) != FLIPGPU_OK) return r;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (dens) CK(h, cudaMemcpyAsync(dens, h->dens, h->np * sizeof(float), kind, h->stream));
+  if (type) CK(h, cudaMemcpyAsync(type, h->type, h->np, kind, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_grid(FlipGpu *h, const float *u0, const float *u1, const float *u2,
+                     const uint8_t *A, const float *L, const float *press, const float *div,
+                     int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const float *us[3] = {u0, u1, u2};
+  for (int c = 0; c < 3; c++)
+    if (us[c]) CK(h, cudaMemcpyAsync(h->u[c], us[c], h->nf * sizeof(float), kind, h->stream));
+  if (A) CK(h, cudaMemcpyAsync(h->A, A, h->nc, kind, h->stream));
+  if (L) CK(h, cudaMemcpyAsync(h->L, L, h->nc * sizeof(float), kind, h->stream));
+  if (press) CK(h, cudaMemcpyAsync(h->press, press, h->nc * sizeof(float), kind, h->stream));
+  if (div) CK(h, cudaMemcpyAsync(h->div, div, h->nc * sizeof(float), kind, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_grid(FlipGpu *h, float *u0, float *u1, float *u2, uint8_t *A, float *L,
+                     float *press, float *div, int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  float *us[3] = {u0, u1, u2};
+  for (int c = 0; c < 3; c++)
+    if (us[c]) CK(h, cudaMemcpyAsync(us[c], h->u[c], h->nf * sizeof(float), kind, h->stream));
+  if (A) CK(h, cudaMemcpyAsync(A, h->A, h->nc, kind, h->stream));
+  if (L) CK(h, cudaMemcpyAsync(L, h->L, h->nc * sizeof(float), kind, h->stream));
+  if (press) CK(h, cudaMemcpyAsync(press, h->press, h->nc * sizeof(float), kind, h->stream));
+  if (div) CK(h, cudaMemcpyAsync(div, h->div, h->nc * sizeof(float), kind, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_cells(FlipGpu *h, uint32_t *cell_start, uint32_t *perm, int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) return fail(h, FLIPGPU_EINVAL, "no cell lists: call flipgpu_sort first");
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (cell_start)
+    CK(h, cudaMemcpyAsync(cell_start, h->cell_start, (h->nc + 1) * sizeof(uint32_t), kind, h->stream));
+  if (perm) CK(h, cudaMemcpyAsync(perm, h->perm, h->np * sizeof(uint32_t), kind, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_max_density(FlipGpu *h, float md) {
+  if (!h || !(md > 0.0f)) return FLIPGPU_EINVAL;
+  h->max_dens = md;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_calibrate_max_density(FlipGpu *h, float *out) {
+  if (!h) return FLIPGPU_EINVAL;
+  FlipGpuParams p = h->prm;
+  p.max_particles = 1000;
+  FlipGpu *t = nullptr;
+  int r = flipgpu_create(&p, &t);
+  if (r != FLIPGPU_OK) return fail(h, r, "calibration handle: %d", r);
+  const float hh = (float)((double)p.density / p.n);
+  std::vector<float> pos(3000);
+  std::vector<uint8_t> type(1000, CELL_FLUID);
+  int m = 0;
+  for (int i = 0; i < 10; i++)
+    for (int j = 0; j < 10; j++)
+      for (int k = 0; k < 10; k++, m++) {
+        pos[3 * m] = (float)((i + 0.5) * (double)hh);
+        pos[3 * m + 1] = (float)((j + 0.5) * (double)hh);
+        pos[3 * m + 2] = (float)((k + 0.5) * (double)hh);
+      }
+  std::vector<float> dens(1000);
+  r = flipgpu_set_particles(t, 1000, pos.data(), nullptr, type.data(), nullptr, nullptr, 0);
+  if (r == FLIPGPU_OK) r = flipgpu_set_max_density(t, 1.0f);
+  if (r == FLIPGPU_OK) r = flipgpu_sort(t);
+  if (r == FLIPGPU_OK) r = flipgpu_compute_density(t);
+  if (r == FLIPGPU_OK) r = flipgpu_get_particles(t, nullptr, nullptr, dens.data(), nullptr, 0);
+  h->launches += t->launches;
+  flipgpu_destroy(t);
+  if (r != FLIPGPU_OK) return fail(h, r, "calibration failed");
+  float md = 0.0f;
+  for (float d : dens) md = fmaxf(md, d);
+  h->max_dens = md;
+  if (out) *out = md;
+  return FLIPGPU_OK;
+}
+
+/* ------------------------------------------------------------- stages */
+
+int flipgpu_sort(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  CK(h, launch_sort(h, 0));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_compute_density(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) CK(h, launch_sort(h, 0));
+  CK(h, launch_density(h));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_mark_water(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) CK(h, launch_sort(h, 0));
+  CK(h, launch_mark_water(h));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_add_force(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  SimConst c = make_const(h);
+  if (h->np) {
+    k_add_force<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->type, h->vy);
+    FG_LAUNCHED(h, 1);
+    CK(h, cudaGetLastError());
+    if (h->cells_valid) CK(h, launch_payload(h, 0));
+  }
+  return FLIPGPU_OK;
+}
+
+int flipgpu_p2g(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) CK(h, launch_sort(h, 0));
+  CK(h, launch_p2g(h, 0));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_g2p(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  CK(h, launch_g2p(h));
+  if (h->cells_valid) CK(h, launch_payload(h, 0));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_solve(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  return run_solve(h, st);
+}
+
+int flipgpu_project(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) CK(h, launch_sort(h, 0));
+  CK(h, launch_mark_water(h)); /* L = levelset per cell (src/flip3D.cpp:824-826) */
+  CK(h, launch_divergence(h));
+  int r = run_solve(h, st);
+  if (r != FLIPGPU_OK) return r;
+  CK(h, launch_gradient_enforce(h, 0));
+  return FLIPGPU_OK;
+}
+
+static int picflip(FlipGpu *h, FlipGpuSolveStats *st, StageClock *clk) {
+  StageClock none(h);
+  if (!clk) clk = &none;
+  clk->mark(FLIPGPU_STAGE_MARK);
+  CK(h, launch_mark_water(h));
+  clk->mark(FLIPGPU_STAGE_P2G);
+  CK(h, launch_p2g(h, 1));
+  clk->mark(FLIPGPU_STAGE_DIV);
+  CK(h, launch_divergence(h));
+  clk->mark(FLIPGPU_STAGE_SOLVE);
+  int r = run_solve(h, st);
+  if (r != FLIPGPU_OK) return r;
+  clk->mark(FLIPGPU_STAGE_GRAD);
+  CK(h, launch_gradient_enforce(h, 1));
+  clk->mark(FLIPGPU_STAGE_EXTRAP);
+  CK(h, launch_extrapolate_delta(h));
+  clk->mark(FLIPGPU_STAGE_FLIP);
+  CK(h, launch_flip_blend(h));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_picflip(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cells_valid) CK(h, launch_sort(h, 0));
+  int r = picflip(h, st, nullptr);
+  if (r == FLIPGPU_OK && h->cells_valid) CK(h, launch_payload(h, 0));
+  return r;
+}
+
+int flipgpu_advect(FlipGpu *h, int *stuck) {
+  if (!h) return FLIPGPU_EINVAL;
+  CK(h, cudaMemsetAsync(h->iflags + IF_NSTUCK, 0, 2 * sizeof(int), h->stream));
+  CK(h, launch_advect(h));
+  CK(h, launch_reposition(h, stuck));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_correct(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  CK(h, launch_sort(h, 0)); /* src/corrector.cpp:52 */
+  CK(h, launch_correct(h));
+  h->cells_valid = false;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  h->step++;
+  StageClock clk(h);
+  /* sort + add_ExtForce fused into the payload, then computeDensity */
+  clk.mark(FLIPGPU_STAGE_SORT);
+  CK(h, launch_sort(h, 1));
+  clk.mark(FLIPGPU_STAGE_DENSITY);
+  CK(h, launch_density(h));
+  int r = picflip(h, st, &clk);
+  if (r != FLIPGPU_OK) return r;
+  /* advect_particle with reposition; its closing sort serves the corrector,
+   * whose own sort would see the same positions */
+  clk.mark(FLIPGPU_STAGE_ADVECT);
+  CK(h, cudaMemsetAsync(h->iflags + IF_NSTUCK, 0, 2 * sizeof(int), h->stream));
+  CK(h, launch_advect(h));
+  clk.mark(FLIPGPU_STAGE_REPOSITION);
+  CK(h, launch_reposition(h, nullptr));
+  clk.mark(FLIPGPU_STAGE_CORRECT);
+  CK(h, launch_correct(h));
+  clk.mark(FLIPGPU_NSTAGES);
+  clk.flush();
+  h->cells_valid = false;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_put_state(FlipGpu *h, const float *pos, const float *vel, int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r;
+  if ((r = put3(h, pos, on_device, h->px, h->py, h->pz)) != FLIPGPU_OK) return r;
+  if ((r = put3(h, vel, on_device, h->vx, h->vy, h->vz)) != FLIPGPU_OK) return r;
+  h->cells_valid = false;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_profiling(FlipGpu *h, int on) {
+  if (!h) return FLIPGPU_EINVAL;
+  h->prof_on = on;
+  for (int i = 0; i < FLIPGPU_NSTAGES; i++) {
+    h->prof_ms[i] = 0.0;
+    h->prof_calls[i] = 0;
+  }
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max) {
+  if (!h || max < 0) return FLIPGPU_EINVAL;
+  for (int i = 0; i < FLIPGPU_NSTAGES && i < max; i++) {
+    if (ms) ms[i] = h->prof_ms[i];
+    if (calls) calls[i] = h->prof_calls[i];
+  }
+  return FLIPGPU_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,74 @@
+/*
+ * devcommon.cuh — device helpers shared by the kernels: the reference's cell
+ * index clamps, type packing in float4.w, and block reductions.
+ */
+#ifndef FLIP_DEVCOMMON_CUH
+#define FLIP_DEVCOMMON_CUH
+
+#include "flipgpu_impl.h"
+#include "refmath.h"
+#include "../../include/flip_rng.h"
+
+/* int i = fmax(0, fmin(gn-1, gn*p)) (src/sorter.cpp:35-37): the double
+ * clamp of a float product is exact in float. */
+__device__ __forceinline__ int cell_clamp(float p, float fn, int n) {
+  return (int)fmaxf(0.0f, fminf((float)(n - 1), fn * p));
+}
+
+/* int i = fmin(N-1, fmax(0, p*N)) (src/flip3D.cpp:903-905, 944). */
+__device__ __forceinline__ int cell_clamp_minmax(float p, float fn, int n) {
+  return (int)fminf((float)(n - 1), fmaxf(0.0f, p * fn));
+}
+
+/* FLOAT x = max(0, min(cs, cs*p)) with the macros of src/utility.h:16-17
+ * (src/corrector.cpp:59-61), truncated by the int parameter: range [0, n]. */
+__device__ __forceinline__ int cell_clamp_macro(float p, float fn) {
+  float v = fn * p;
+  float mn = (fn > v) ? v : fn;
+  float mx = (0.0f > mn) ? 0.0f : mn;
+  return (int)mx;
+}
+
+__device__ __forceinline__ size_t cell_id(int n, int i, int j, int k) {
+  return ((size_t)i * n + j) * n + k;
+}
+
+__device__ __forceinline__ float pack_type(uint8_t t) {
+  return __int_as_float((int)t);
+}
+__device__ __forceinline__ int unpack_type(float w) { return __float_as_int(w); }
+
+/* Deterministic block sum of doubles: fixed shuffle tree, then warp 0. */
+template <int BLOCK>
+__device__ __forceinline__ double block_sum_double(double v) {
+  __shared__ double warp_part[BLOCK / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (wid == 0) {
+    r = (lane < BLOCK / 32) ? warp_part[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r; /* valid in thread 0 */
+}
+
+template <int BLOCK>
+__device__ __forceinline__ uint32_t block_sum_u32(uint32_t v) {
+  __shared__ uint32_t warp_part[BLOCK / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  uint32_t r = 0;
+  if (wid == 0) {
+    r = (lane < BLOCK / 32) ? warp_part[lane] : 0u;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+  }
+  __syncthreads();
+  return r;
+}
+
+#endif

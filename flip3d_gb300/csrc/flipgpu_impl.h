@@ -1,0 +1,175 @@
+/*
+ * flipgpu_impl.h — device-resident state of one simulation and the kernel
+ * launchers shared by the translation units of libflipgpu.so.
+ *
+ * Particle data lives twice:
+ *   canonical  SoA in the caller's particle order (px..vz, dens, type, nrm):
+ *              per-particle stages read and write it coalesced;
+ *   sorted     a copy grouped by cell (spos/spg/svel/sdens, index = slot of
+ *              the cell lists): gather stages read neighbours as contiguous
+ *              runs, k-adjacent cells being adjacent in memory.
+ */
+#ifndef FLIPGPU_IMPL_H
+#define FLIPGPU_IMPL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/flipgpu.h"
+
+enum { CELL_AIR = 0, CELL_FLUID = 1, CELL_WALL = 2 };
+
+/* Per-run constants handed to kernels by value. */
+struct SimConst {
+  int n;              /* grid cells per axis */
+  int np;             /* particle count */
+  float fn;           /* (float)n */
+  float h;            /* (float)(1.0/n): cell width (src/flip3D.cpp:809) */
+  float density;      /* DENSITY */
+  float kd_hh;        /* density kernel radius^2: h*h of (float)(4*DENSITY/N) */
+  float max_dens;
+  float re_p2g_hh;    /* RE*RE for P2G (src/mapper.cpp:14) */
+  float re_corr;      /* DENSITY/N (src/flip3D.cpp:1242) */
+  float re_corr_hh;
+  float re_repo;      /* 1.0/gn: resample radius in reposition (src/flip3D.cpp:435) */
+  float re_repo_hh;
+  float r2_floor;     /* smallest float above 1e-5 (sharp kernel clamp) */
+  float sharp_small_p2g, sharp_small_corr, sharp_small_repo;
+  float wall_r;       /* (float)WALL_THICK */
+  float wall_hi;      /* (float)(1.0 - WALL_THICK) */
+  float wall_hi_thr;  /* largest float <= 1.0 - WALL_THICK */
+  double push_re;     /* 1.5*DENSITY/N (src/flip3D.cpp:909) */
+  float push_re_thr;  /* largest float < push_re */
+  float corr_near_thr;/* largest float <= 0.1*re (src/corrector.cpp:68) */
+  float corr_cut2;    /* squared distance beyond which the spring weight is 0 */
+  float dt_f;         /* (float)DT, the corrector's dt */
+  double dt;
+  float dt_h, dt_l;   /* DT split into floats */
+  double grav;        /* -DT*GRAVITY */
+  float grav_h, grav_l;
+  double c1, c2;      /* 1-ALPHA, ALPHA */
+  float c1h, c1l, c2h, c2l;
+  double l0;          /* 0.2 * n0 of sorter::levelset */
+  float l0h, l0l;
+  uint64_t seed;
+  int64_t step;
+};
+
+struct FlipGpu {
+  FlipGpuParams prm;
+  int n;
+  int np;
+  int cap;
+  size_t nc;          /* n^3 */
+  size_t nf;          /* (n+1)*n*n faces per component */
+  cudaStream_t stream;
+  cudaStream_t own_stream;
+  float max_dens;
+  int64_t step;
+  int64_t launches;
+  char err[512];
+
+  /* canonical particles */
+  float *px, *py, *pz, *vx, *vy, *vz, *dens;
+  uint8_t *type;
+  float *nx, *ny, *nz;
+
+  /* cell lists */
+  uint32_t *key, *rank, *perm, *cell_start, *cell_count;
+  float4 *spos;       /* world position, w = type */
+  float4 *spg;        /* clamp(n*pos, 0, n), w = type (P2G) */
+  float4 *svel;       /* velocity, w unused */
+  float *sdens;
+  bool cells_valid;
+
+  /* static wall lists (walls never move) */
+  int nwall;
+  uint32_t *wall_start;
+  float4 *wall_pos;   /* w = unused */
+  float4 *wall_nrm;
+
+  /* grid */
+  float *u[3], *us[3];
+  uint8_t *A;
+  float *L, *press, *div;
+
+  /* solver */
+  float *r, *z, *s;
+  double *P;          /* REF preconditioner diagonal (double, as the reference) */
+  float *Pf;          /* FP32 preconditioner diagonal / IC factor */
+  float *diag;        /* FP32 matvec diagonal (FAST mode) */
+  double *partial;    /* per-block reduction partials */
+  double *scal;       /* device scalars of the CG recurrence */
+  int *iflags;        /* device flags/counters */
+  int npartial;
+
+  /* reposition */
+  uint8_t *flag;      /* per particle / per cell */
+  uint32_t *scan_a, *scan_b, *scan_tmp;
+  uint32_t *stuck_idx, *water_idx;
+  size_t scan_cap;
+
+  float *stage;       /* AoS staging for downloads */
+  cudaEvent_t ev0, ev1;
+
+  /* per-stage profiling */
+  int prof_on;
+  cudaEvent_t prof_ev[FLIPGPU_NSTAGES + 1];
+  double prof_ms[FLIPGPU_NSTAGES];
+  int64_t prof_calls[FLIPGPU_NSTAGES];
+};
+
+/* Device scalar slots (FlipGpu::scal). */
+enum {
+  SC_A = 0,      /* z.r of the previous iteration */
+  SC_ALPHA,
+  SC_BETA,
+  SC_ERR2,       /* float(r.r) */
+  SC_EPS,
+  SC_B2,
+  SC_DOT,        /* scratch result of the last dot */
+  SC_ERR2_0,
+  SC_COUNT
+};
+/* Device int slots (FlipGpu::iflags). */
+enum {
+  IF_DONE = 0,   /* CG converged */
+  IF_ITERS,      /* iterations taken */
+  IF_EXOTIC,     /* REF preconditioner has a diagonal entry equal to 1.0 */
+  IF_NSTUCK,
+  IF_NWATER,
+  IF_NAN,
+  IF_COUNT
+};
+
+SimConst make_const(const FlipGpu *h);
+
+/* launchers (one per reference stage or sub-stage); return cudaError_t */
+cudaError_t launch_sort(FlipGpu *h, int apply_gravity);
+cudaError_t launch_payload(FlipGpu *h, int apply_gravity);
+cudaError_t launch_density(FlipGpu *h);
+cudaError_t launch_mark_water(FlipGpu *h);
+cudaError_t launch_add_force(FlipGpu *h);
+cudaError_t launch_p2g(FlipGpu *h, int enforce);
+cudaError_t launch_g2p(FlipGpu *h);
+cudaError_t launch_divergence(FlipGpu *h);
+cudaError_t launch_gradient_enforce(FlipGpu *h, int enforce);
+cudaError_t launch_extrapolate_delta(FlipGpu *h);
+cudaError_t launch_flip_blend(FlipGpu *h);
+cudaError_t launch_advect(FlipGpu *h);
+cudaError_t launch_reposition(FlipGpu *h, int *stuck_host);
+cudaError_t launch_correct(FlipGpu *h);
+int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
+
+/* device-wide exclusive scan of n uint32 (in may equal out) */
+cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,
+                           size_t n);
+
+/* kernel-count bookkeeping */
+#define FG_LAUNCHED(h, k) ((h)->launches += (k))
+
+static inline unsigned grid_for(size_t n, int block) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+#endif

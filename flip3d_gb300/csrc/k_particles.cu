@@ -1,0 +1,593 @@
+/*
+ * k_particles.cu — particle stages of the FLIP step.
+ *
+ * Gathers run one thread per sorted slot, so a warp works on particles of
+ * the same few cells and re-reads the same neighbour runs from L1. A
+ * neighbourhood of cells [i0,i1]x[j0,j1]x[k0,k1] is visited as in
+ * sorter::getNeigboringParticles_* (src/sorter.cpp:42-64): si, then sj,
+ * then sk, each cell in particle order; for fixed (si,sj) the k-range is one
+ * contiguous run of slots. Every float expression follows the reference's
+ * evaluation order and promotions (nvcc -fmad=false; refmath.h for the
+ * double-promoted ones), so the results are the reference's bit for bit.
+ */
+#include "devcommon.cuh"
+
+using namespace refmath;
+
+namespace {
+
+constexpr int BLK = 256;
+
+/* Visit the slots of cells [i0,i1]x[j0,j1]x[k0,k1] (clipped to the grid) in
+ * the reference's order; f(slot). */
+template <class F>
+__device__ __forceinline__ void visit_cells(int n, const uint32_t *__restrict__ cs, int i0,
+                                            int i1, int j0, int j1, int k0, int k1, F f) {
+  i0 = max(i0, 0);
+  i1 = min(i1, n - 1);
+  j0 = max(j0, 0);
+  j1 = min(j1, n - 1);
+  k0 = max(k0, 0);
+  k1 = min(k1, n - 1);
+  if (k0 > k1) return;
+  for (int si = i0; si <= i1; si++)
+    for (int sj = j0; sj <= j1; sj++) {
+      size_t base = ((size_t)si * n + sj) * n;
+      uint32_t s = __ldg(cs + base + k0), e = __ldg(cs + base + k1 + 1);
+      for (uint32_t b = s; b < e; b++) f(b);
+    }
+}
+
+/* linear() (src/mapper.cpp:96-106) with the k clamp of the reference (h-2);
+ * k+1 is kept inside the row where the reference reads one past it. */
+__device__ __forceinline__ float linear(const float *__restrict__ q, float x, float y, float z,
+                                        int w, int h, int d) {
+  x = fmaxf(0.0f, fminf((float)w, x));
+  y = fmaxf(0.0f, fminf((float)h, y));
+  z = fmaxf(0.0f, fminf((float)d, z));
+  int i = (int)((x > (float)(w - 2)) ? (float)(w - 2) : x);
+  int j = (int)((y > (float)(h - 2)) ? (float)(h - 2) : y);
+  int k = (int)((z > (float)(h - 2)) ? (float)(h - 2) : z);
+  int k1 = min(k + 1, d - 1);
+  auto Q = [&](int a, int b, int c) { return __ldg(q + ((size_t)a * h + b) * d + c); };
+  float fx0 = (float)(i + 1) - x, fx1 = x - (float)i;
+  float fy0 = (float)(j + 1) - y, fy1 = y - (float)j;
+  float fz0 = (float)(k + 1) - z, fz1 = z - (float)k;
+  return fz0 * ((fx0 * Q(i, j, k) + fx1 * Q(i + 1, j, k)) * fy0 +
+                (fx0 * Q(i, j + 1, k) + fx1 * Q(i + 1, j + 1, k)) * fy1) +
+         fz1 * ((fx0 * Q(i, j, k1) + fx1 * Q(i + 1, j, k1)) * fy0 +
+                (fx0 * Q(i, j + 1, k1) + fx1 * Q(i + 1, j + 1, k1)) * fy1);
+}
+
+/* mapper::fetchVelocity (src/mapper.cpp:108-112). gy - 0.5 is exact in
+ * double, so one float subtraction rounds it as the reference does. */
+__device__ __forceinline__ void fetch_velocity(int n, float fn, const float *__restrict__ u0,
+                                               const float *__restrict__ u1,
+                                               const float *__restrict__ u2, float x, float y,
+                                               float z, float out[3]) {
+  float gx = fn * x, gy = fn * y, gz = fn * z;
+  out[0] = linear(u0, gx, gy - 0.5f, gz - 0.5f, n + 1, n, n);
+  out[1] = linear(u1, gx - 0.5f, gy, gz - 0.5f, n, n + 1, n);
+  out[2] = linear(u2, gx - 0.5f, gy - 0.5f, gz, n, n, n + 1);
+}
+
+/* ------------------------------------------------------ computeDensity */
+
+__global__ void __launch_bounds__(BLK)
+k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+          const float4 *__restrict__ spos, float *__restrict__ dens,
+          float *__restrict__ sdens) {
+  int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  float4 P = spos[a];
+  uint32_t p = perm[a];
+  if (unpack_type(P.w) == CELL_WALL) {
+    dens[p] = 1.0f;
+    sdens[a] = 1.0f;
+    return;
+  }
+  int ci = cell_clamp(P.x, c.fn, c.n), cj = cell_clamp(P.y, c.fn, c.n),
+      ck = cell_clamp(P.z, c.fn, c.n);
+  float wsum = 0.0f;
+  visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+    float4 Q = __ldg(spos + b);
+    if (unpack_type(Q.w) == CELL_WALL) return;
+    float d2 = hypot2_ref(Q.x - P.x, Q.y - P.y, Q.z - P.z);
+    wsum += smooth_ref(d2, c.kd_hh);
+  });
+  float d = wsum / c.max_dens;
+  dens[p] = d;
+  sdens[a] = d;
+}
+
+/* ------------------------------------------------------------ mapP2G */
+
+/* One MAC face per thread (src/mapper.cpp:17-88). The reference gathers
+ * cells [i-1,i] along the normal and [j-2,j+1] along each tangent; the
+ * tangent cell j-2 lies at least 1.5 cells from the face centre, beyond the
+ * kernel radius RE=1.4, so its weights are exactly 0 and it is skipped.
+ * Writes the saved grid (save_grid) and the boundary-enforced grid
+ * (enforce_boundary, src/flip3D.cpp:783-805) in one pass. */
+__global__ void __launch_bounds__(BLK)
+k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__restrict__ spg,
+      const float4 *__restrict__ svel, const uint8_t *__restrict__ A, float *__restrict__ u0,
+      float *__restrict__ u1, float *__restrict__ u2, float *__restrict__ us0,
+      float *__restrict__ us1, float *__restrict__ us2) {
+  const int n = c.n;
+  const int comp = blockIdx.y;
+  size_t f = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const size_t nf = (size_t)(n + 1) * n * n;
+  if (f >= nf) return;
+  int ex[3] = {n, n, n};
+  ex[comp] = n + 1;
+  int k = (int)(f % ex[2]);
+  int j = (int)((f / ex[2]) % ex[1]);
+  int i = (int)(f / ((size_t)ex[2] * ex[1]));
+  float fp[3] = {(float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f};
+  int lo[3] = {i - 1, j - 1, k - 1}, hi[3] = {i + 1, j + 1, k + 1};
+  if (comp == 0) { fp[0] = (float)i; hi[0] = i; }
+  if (comp == 1) { fp[1] = (float)j; hi[1] = j; }
+  if (comp == 2) { fp[2] = (float)k; hi[2] = k; }
+  const float hh = c.re_p2g_hh;
+  float sumw = 0.0f, sumx = 0.0f;
+  visit_cells(n, cs, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], [&](uint32_t b) {
+    float4 Q = __ldg(spg + b);
+    if (unpack_type(Q.w) != CELL_FLUID) return;
+    float r2 = hypot2_ref(Q.x - fp[0], Q.y - fp[1], Q.z - fp[2]);
+    if (!(r2 < hh)) return; /* weight exactly 0 */
+    float w = sharp_ref(r2, hh, c.r2_floor, c.sharp_small_p2g);
+    float4 V = __ldg(svel + b);
+    float vc = comp == 0 ? V.x : (comp == 1 ? V.y : V.z);
+    sumx += w * vc;
+    sumw += w;
+  });
+  float val = (sumw != 0.0f) ? sumx / sumw : 0.0f;
+  /* enforce_boundary */
+  int a = comp == 0 ? i : (comp == 1 ? j : k);
+  float out = val;
+  if (!enforce) {
+  } else if (a == 0 || a == n) {
+    out = 0.0f;
+  } else {
+    size_t c1 = cell_id(n, i, j, k);
+    size_t c0 = comp == 0 ? cell_id(n, i - 1, j, k)
+                          : (comp == 1 ? cell_id(n, i, j - 1, k) : cell_id(n, i, j, k - 1));
+    bool w1 = A[c1] == CELL_WALL, w0 = A[c0] == CELL_WALL;
+    if (w1 != w0) out = 0.0f;
+  }
+  float *u = comp == 0 ? u0 : (comp == 1 ? u1 : u2);
+  float *us = comp == 0 ? us0 : (comp == 1 ? us1 : us2);
+  us[f] = val;
+  u[f] = out;
+}
+
+/* ----------------------------------------------------- mapG2P / FLIP */
+
+/* mapper::mapG2P for the fluid particles (wall velocities are never read
+ * by any stage). */
+__global__ void __launch_bounds__(BLK)
+k_g2p(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
+      const float *__restrict__ pz, const uint8_t *__restrict__ type,
+      const float *__restrict__ u0, const float *__restrict__ u1,
+      const float *__restrict__ u2, float *__restrict__ vx, float *__restrict__ vy,
+      float *__restrict__ vz) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np || type[p] != CELL_FLUID) return;
+  float v[3];
+  fetch_velocity(c.n, c.fn, u0, u1, u2, px[p], py[p], pz[p], v);
+  vx[p] = v[0];
+  vy[p] = v[1];
+  vz[p] = v[2];
+}
+
+/* The FLIP block of solve_picflip (src/flip3D.cpp:1071-1097): sample the
+ * grid change and the new grid, then u = (1-ALPHA)*pic + ALPHA*(u + du). */
+__global__ void __launch_bounds__(BLK)
+k_flip_blend(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
+             const float *__restrict__ pz, const uint8_t *__restrict__ type,
+             const float *__restrict__ u0, const float *__restrict__ u1,
+             const float *__restrict__ u2, const float *__restrict__ d0,
+             const float *__restrict__ d1, const float *__restrict__ d2,
+             float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np || type[p] != CELL_FLUID) return;
+  float x = px[p], y = py[p], z = pz[p];
+  float du[3], pic[3];
+  fetch_velocity(c.n, c.fn, d0, d1, d2, x, y, z, du);
+  fetch_velocity(c.n, c.fn, u0, u1, u2, x, y, z, pic);
+  float v[3] = {vx[p], vy[p], vz[p]};
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    float flip = du[q] + v[q];
+    v[q] = blend_ref(pic[q], flip, c.c1h, c.c1l, c.c2h, c.c2l, c.c1, c.c2);
+  }
+  vx[p] = v[0];
+  vy[p] = v[1];
+  vz[p] = v[2];
+}
+
+/* ----------------------------------------------------- advect_particle */
+
+/* advect_particle (src/flip3D.cpp:877-969) for one fluid particle: Euler
+ * step through the grid, clamp inside the walls, push out of wall particles
+ * closer than 1.5*DENSITY/N and drop the normal velocity, then flag it if it
+ * is stuck. Each particle only reads itself and the (static) wall
+ * particles, so the reference's serial loop is order-independent. */
+__global__ void __launch_bounds__(BLK)
+k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz,
+         float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz,
+         const uint8_t *__restrict__ type, const float *__restrict__ dens,
+         const float *__restrict__ u0, const float *__restrict__ u1,
+         const float *__restrict__ u2, const uint8_t *__restrict__ A,
+         const uint32_t *__restrict__ wall_start, const float4 *__restrict__ wall_pos,
+         const float4 *__restrict__ wall_nrm, uint8_t *__restrict__ stuck) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np) return;
+  if (type[p] != CELL_FLUID) {
+    stuck[p] = 0;
+    return;
+  }
+  const int n = c.n;
+  float pp[3] = {px[p], py[p], pz[p]};
+  float v[3];
+  fetch_velocity(n, c.fn, u0, u1, u2, pp[0], pp[1], pp[2], v);
+#pragma unroll
+  for (int q = 0; q < 3; q++) pp[q] = axpy_fd(pp[q], v[q], c.dt_h, c.dt_l, c.dt);
+  /* p = fmax(r, fmin(1.0-r, p)) */
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    float t = pp[q];
+    if (t != t || t > c.wall_hi_thr) t = c.wall_hi;
+    if (t < c.wall_r) t = c.wall_r;
+    pp[q] = t;
+  }
+  float uu[3] = {vx[p], vy[p], vz[p]};
+  int i = cell_clamp_minmax(pp[0], c.fn, n), j = cell_clamp_minmax(pp[1], c.fn, n),
+      k = cell_clamp_minmax(pp[2], c.fn, n);
+  visit_cells(n, wall_start, i - 1, i + 1, j - 1, j + 1, k - 1, k + 1, [&](uint32_t w) {
+    float4 Q = __ldg(wall_pos + w);
+    float dist = length_ref(pp[0] - Q.x, pp[1] - Q.y, pp[2] - Q.z);
+    if (!(dist <= c.push_re_thr)) return; /* (double)dist < 1.5*DENSITY/N */
+    float4 Nw = __ldg(wall_nrm + w);
+    float nrm[3] = {Nw.x, Nw.y, Nw.z};
+    if (nrm[0] == 0.0f && nrm[1] == 0.0f && nrm[2] == 0.0f && dist != 0.0f) {
+      nrm[0] = (pp[0] - Q.x) / dist;
+      nrm[1] = (pp[1] - Q.y) / dist;
+      nrm[2] = (pp[2] - Q.z) / dist;
+    }
+    double push = c.push_re - (double)dist;
+#pragma unroll
+    for (int q = 0; q < 3; q++) pp[q] = (float)((double)pp[q] + push * (double)nrm[q]);
+    float dot = uu[0] * nrm[0] + uu[1] * nrm[1] + uu[2] * nrm[2];
+#pragma unroll
+    for (int q = 0; q < 3; q++) uu[q] -= dot * nrm[q];
+  });
+  px[p] = pp[0];
+  py[p] = pp[1];
+  pz[p] = pp[2];
+  vx[p] = uu[0];
+  vy[p] = uu[1];
+  vz[p] = uu[2];
+  /* stuck detection (src/flip3D.cpp:933-955) */
+  uint8_t s = 0;
+  int ai = cell_clamp_minmax(pp[0], c.fn, n), aj = cell_clamp_minmax(pp[1], c.fn, n),
+      ak = cell_clamp_minmax(pp[2], c.fn, n);
+  if (A[cell_id(n, ai, aj, ak)] == CELL_WALL) s = 1;
+  int si = (int)fminf((float)(n - 3), fmaxf(2.0f, pp[0] * c.fn));
+  int sj = (int)fminf((float)(n - 3), fmaxf(2.0f, pp[1] * c.fn));
+  int sk = (int)fminf((float)(n - 3), fmaxf(2.0f, pp[2] * c.fn));
+  if ((double)dens[p] < 0.04 && (A[cell_id(n, si, max(0, sj - 1), sk)] == CELL_WALL ||
+                                 A[cell_id(n, si, min(n - 1, sj + 1), sk)] == CELL_WALL))
+    s = 1;
+  stuck[p] = s;
+}
+
+/* ------------------------------------------------------------ reposition */
+
+/* Deep-water cells: FLUID with every in-range face neighbour FLUID
+ * (src/flip3D.cpp:412-421). */
+__global__ void k_deep_water(int n, const uint8_t *__restrict__ A, uint32_t *__restrict__ flag) {
+  size_t cidx = (size_t)blockIdx.x * BLK + threadIdx.x;
+  size_t nc = (size_t)n * n * n;
+  if (cidx >= nc) return;
+  int k = (int)(cidx % n), j = (int)((cidx / n) % n), i = (int)(cidx / ((size_t)n * n));
+  uint32_t ok = A[cidx] == CELL_FLUID;
+  if (ok && i > 0 && A[cell_id(n, i - 1, j, k)] != CELL_FLUID) ok = 0;
+  if (ok && i < n - 1 && A[cell_id(n, i + 1, j, k)] != CELL_FLUID) ok = 0;
+  if (ok && j > 0 && A[cell_id(n, i, j - 1, k)] != CELL_FLUID) ok = 0;
+  if (ok && j < n - 1 && A[cell_id(n, i, j + 1, k)] != CELL_FLUID) ok = 0;
+  if (ok && k > 0 && A[cell_id(n, i, j, k - 1)] != CELL_FLUID) ok = 0;
+  if (ok && k < n - 1 && A[cell_id(n, i, j, k + 1)] != CELL_FLUID) ok = 0;
+  flag[cidx] = ok;
+}
+
+__global__ void k_u8_to_u32(size_t n, const uint8_t *__restrict__ in, uint32_t *__restrict__ out) {
+  size_t i = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (i < n) out[i] = in[i];
+}
+
+/* Stable compaction: idx[offset[i]] = i where flag[i]; count in *count. */
+__global__ void k_compact(size_t n, const uint32_t *__restrict__ flag,
+                          const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx,
+                          int *__restrict__ count) {
+  size_t i = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (i >= n) return;
+  if (flag[i]) idx[offset[i]] = (uint32_t)i;
+  if (i == n - 1) *count = (int)(offset[i] + flag[i]);
+}
+
+/* reposition (src/flip3D.cpp:405-441): deep-water cells in order, repeated
+ * until there are as many as stuck particles, shuffled with the keyed
+ * Fisher-Yates, then each stuck particle placed at a keyed spot in its
+ * cell. One thread: the shuffle is sequential and the lists are short. */
+__global__ void k_repo_place(SimConst c, const int *__restrict__ counts,
+                             const uint32_t *__restrict__ stuck_idx,
+                             const uint32_t *__restrict__ water_idx,
+                             uint32_t *__restrict__ waters, float *__restrict__ px,
+                             float *__restrict__ py, float *__restrict__ pz) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (m == 0 || w == 0) return;
+  for (int q = 0; q < m; q++) waters[q] = water_idx[q % w];
+  for (int q = m - 1; q >= 1; q--) {
+    uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_SHUFFLE, (uint64_t)c.step, 0),
+                             (uint64_t)q, 0);
+    int j = (int)(r % (uint32_t)(q + 1));
+    uint32_t t = waters[q];
+    waters[q] = waters[j];
+    waters[j] = t;
+  }
+  const int n = c.n;
+  const double h = (double)c.re_repo;
+  for (int q = 0; q < m; q++) {
+    uint32_t cell = waters[q];
+    int cc[3] = {(int)(cell / ((uint32_t)n * n)), (int)((cell / n) % n), (int)(cell % n)};
+    float out[3];
+    for (int d = 0; d < 3; d++) {
+      uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_PLACE, (uint64_t)c.step, 0),
+                               (uint64_t)(3 * q + d), 0);
+      double frac = 0.5 * (double)(int)(r % 101) / 100;
+      out[d] = (float)(h * ((double)cc[d] + 0.25 + frac));
+    }
+    uint32_t p = stuck_idx[q];
+    px[p] = out[0];
+    py[p] = out[1];
+    pz[p] = out[2];
+  }
+}
+
+/* corrector::resample (src/corrector.cpp:15-47) at particle position p for
+ * the repositioned particles, in order, one thread: a later particle sees
+ * the already-resampled velocity of an earlier one, as in the reference's
+ * loop (src/flip3D.cpp:445-450). Neighbour velocities come from the
+ * canonical arrays for that reason. */
+__global__ void k_repo_resample(SimConst c, const int *__restrict__ counts,
+                                const uint32_t *__restrict__ stuck_idx,
+                                const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                                const float4 *__restrict__ spos, const float *__restrict__ px,
+                                const float *__restrict__ py, const float *__restrict__ pz,
+                                float *__restrict__ vx, float *__restrict__ vy,
+                                float *__restrict__ vz) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (m == 0 || w == 0) return;
+  for (int q = 0; q < m; q++) {
+    uint32_t p = stuck_idx[q];
+    float P[3] = {px[p], py[p], pz[p]};
+    int ci = cell_clamp(P[0], c.fn, c.n), cj = cell_clamp(P[1], c.fn, c.n),
+        ck = cell_clamp(P[2], c.fn, c.n);
+    float u[3] = {0.0f, 0.0f, 0.0f};
+    float wsum = 0.0f;
+    visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+      float4 Q = spos[b];
+      if (unpack_type(Q.w) != CELL_FLUID) return;
+      float d2 = hypot2_ref(P[0] - Q.x, P[1] - Q.y, P[2] - Q.z);
+      if (!(d2 < c.re_repo_hh)) return;
+      float wt = sharp_ref(d2, c.re_repo_hh, c.r2_floor, c.sharp_small_repo);
+      uint32_t o = perm[b];
+      u[0] += wt * vx[o];
+      u[1] += wt * vy[o];
+      u[2] += wt * vz[o];
+      wsum += wt;
+    });
+    if (wsum != 0.0f) {
+      u[0] /= wsum;
+      u[1] /= wsum;
+      u[2] /= wsum;
+    }
+    vx[p] = u[0];
+    vy[p] = u[1];
+    vz[p] = u[2];
+  }
+}
+
+/* ------------------------------------------------------ corrector */
+
+/* Spring displacement (src/corrector.cpp:54-100): writes the moved position
+ * to the canonical arrays (neighbours are read from the sorted snapshot). A
+ * neighbour whose float squared distance exceeds corr_cut2 has weight
+ * exactly 0 (its distance is at least re*(1+2^-9)) and adds nothing. */
+__global__ void __launch_bounds__(BLK)
+k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+         const float4 *__restrict__ spos, const float *__restrict__ nx,
+         const float *__restrict__ ny, const float *__restrict__ nz, float *__restrict__ px,
+         float *__restrict__ py, float *__restrict__ pz) {
+  int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  float4 P = spos[a];
+  if (unpack_type(P.w) != CELL_FLUID) return;
+  uint32_t p = perm[a];
+  const float re = c.re_corr;
+  int x = cell_clamp_macro(P.x, c.fn), y = cell_clamp_macro(P.y, c.fn),
+      z = cell_clamp_macro(P.z, c.fn);
+  float spring[3] = {0.0f, 0.0f, 0.0f};
+  visit_cells(c.n, cs, x - 1, x + 1, y - 1, y + 1, z - 1, z + 1, [&](uint32_t b) {
+    if (b == (uint32_t)a) return;
+    float4 Q = __ldg(spos + b);
+    float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+    if (hypot2_ref(dx, dy, dz) > c.corr_cut2) return;
+    float dist = length_ref(dx, dy, dz);
+    float w = 50.0f * smooth_ref(dist * dist, c.re_corr_hh);
+    if (dist > c.corr_near_thr) {
+      spring[0] += w * dx / dist * re;
+      spring[1] += w * dy / dist * re;
+      spring[2] += w * dz / dist * re;
+    } else if (unpack_type(Q.w) == CELL_FLUID) {
+      uint32_t o = perm[b];
+      for (int q = 0; q < 3; q++) {
+        uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)c.step, q),
+                                 (uint64_t)p, (uint64_t)o);
+        spring[q] = (float)((double)spring[q] + 0.01 * (double)re / (double)c.dt_f *
+                                                    (double)(int)(r % 101) / 100.0);
+      }
+    } else {
+      uint32_t o = perm[b];
+      float nn[3] = {nx[o], ny[o], nz[o]};
+      for (int q = 0; q < 3; q++)
+        spring[q] = (float)((double)spring[q] +
+                            0.05 * (double)re / (double)c.dt_f * (double)nn[q]);
+    }
+  });
+  px[p] = P.x + c.dt_f * spring[0];
+  py[p] = P.y + c.dt_f * spring[1];
+  pz[p] = P.z + c.dt_f * spring[2];
+}
+
+/* Velocity resample at the moved position (src/corrector.cpp:91-114 with
+ * resample at :15-47), then the commit (the position was already
+ * written). */
+__global__ void __launch_bounds__(BLK)
+k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+           const float4 *__restrict__ spos, const float4 *__restrict__ svel,
+           const float *__restrict__ px, const float *__restrict__ py,
+           const float *__restrict__ pz, float *__restrict__ vx, float *__restrict__ vy,
+           float *__restrict__ vz) {
+  int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  if (unpack_type(spos[a].w) != CELL_FLUID) return;
+  uint32_t p = perm[a];
+  float T[3] = {px[p], py[p], pz[p]};
+  int ci = cell_clamp(T[0], c.fn, c.n), cj = cell_clamp(T[1], c.fn, c.n),
+      ck = cell_clamp(T[2], c.fn, c.n);
+  float u[3] = {0.0f, 0.0f, 0.0f};
+  float wsum = 0.0f;
+  visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+    float4 Q = __ldg(spos + b);
+    if (unpack_type(Q.w) != CELL_FLUID) return;
+    float d2 = hypot2_ref(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
+    if (!(d2 < c.re_corr_hh)) return;
+    float w = sharp_ref(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
+    float4 V = __ldg(svel + b);
+    u[0] += w * V.x;
+    u[1] += w * V.y;
+    u[2] += w * V.z;
+    wsum += w;
+  });
+  if (wsum != 0.0f) {
+    vx[p] = u[0] / wsum;
+    vy[p] = u[1] / wsum;
+    vz[p] = u[2] / wsum;
+  }
+}
+
+} // namespace
+
+cudaError_t launch_density(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_density<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
+                                                         h->dens, h->sdens);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_p2g(FlipGpu *h, int enforce) {
+  SimConst c = make_const(h);
+  dim3 grid(grid_for(h->nf, BLK), 3);
+  k_p2g<<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0],
+                                     h->u[1], h->u[2], h->us[0], h->us[1], h->us[2]);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_g2p(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_g2p<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->px, h->py, h->pz, h->type, h->u[0],
+                                                     h->u[1], h->u[2], h->vx, h->vy, h->vz);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flip_blend(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_flip_blend<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(
+      c, h->px, h->py, h->pz, h->type, h->u[0], h->u[1], h->u[2], h->us[0], h->us[1],
+      h->us[2], h->vx, h->vy, h->vz);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_advect(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_advect<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(
+      c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
+      h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+/* Compute stuck and deep-water lists, place the stuck particles. The sort
+ * and the ordered resample follow in launch_reposition_resample. */
+cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
+  SimConst c = make_const(h);
+  cudaError_t e;
+  if (h->np > 0) {
+    k_u8_to_u32<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, h->flag, h->scan_a);
+    FG_LAUNCHED(h, 1);
+    if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->np)) != cudaSuccess) return e;
+    k_compact<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, h->scan_a, h->scan_b,
+                                                           h->stuck_idx, h->iflags + IF_NSTUCK);
+    FG_LAUNCHED(h, 1);
+  }
+  k_deep_water<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->n, h->A, h->scan_a);
+  FG_LAUNCHED(h, 1);
+  if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->nc)) != cudaSuccess) return e;
+  k_compact<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->nc, h->scan_a, h->scan_b,
+                                                         h->water_idx, h->iflags + IF_NWATER);
+  k_repo_place<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->water_idx, h->scan_b,
+                                        h->px, h->py, h->pz);
+  FG_LAUNCHED(h, 2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  /* sorter::sort (src/flip3D.cpp:443), shared with the corrector's sort. */
+  if ((e = launch_sort(h, 0)) != cudaSuccess) return e;
+  k_repo_resample<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start, h->perm,
+                                           h->spos, h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+  FG_LAUNCHED(h, 1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  /* refresh the sorted velocities of the resampled particles */
+  if ((e = launch_payload(h, 0)) != cudaSuccess) return e;
+  if (stuck_host) {
+    int v = 0;
+    e = cudaMemcpyAsync(&v, h->iflags + IF_NSTUCK, sizeof(int), cudaMemcpyDeviceToHost,
+                        h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    *stuck_host = v;
+  }
+  return e;
+}
+
+cudaError_t launch_correct(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_spring<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
+                                                        h->nx, h->ny, h->nz, h->px, h->py,
+                                                        h->pz);
+  k_resample<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
+                                                          h->svel, h->px, h->py, h->pz, h->vx,
+                                                          h->vy, h->vz);
+  FG_LAUNCHED(h, 2);
+  return cudaGetLastError();
+}

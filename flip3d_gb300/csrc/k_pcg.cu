@@ -1,0 +1,569 @@
+/*
+ * k_pcg.cu — solver::solve (src/solver.cpp:183-241) on the GPU.
+ *
+ * The CG recurrence keeps its scalars (alpha, beta, z.r, r.r, the stop
+ * bound) in device memory; every kernel of an iteration first reads the
+ * device `done` flag, so the host launches iterations in chunks and polls the
+ * flag once per chunk instead of once per iteration. Dot products are FP64,
+ * reduced in a fixed order (grid-stride per thread, fixed block tree, fixed
+ * spine), so a solve is deterministic.
+ *
+ * REF mode follows the reference's arithmetic: the 7-point sum of
+ * compute_Ax in double (src/solver.cpp:29-41), op() in float, float(r.r) in
+ * the stop test, and the preconditioner as written (src/solver.cpp:119-180),
+ * whose neighbour terms act only on entries equal to 1.0: with no diagonal
+ * entry equal to 1.0 it is an exact diagonal scaling (two double
+ * multiplies); otherwise a sequential pass reproduces it. The one departure
+ * is the order of the FP64 dot sums (tree instead of sequential), which
+ * moves alpha/beta by ~1e-16 relative.
+ *
+ * FAST mode: FP32 matvec with a precomputed diagonal (the same operator),
+ * Jacobi or IC preconditioner in FP32, FP64 dots, stop when
+ * r.r <= rel_tol^2 * b.b.
+ */
+#include <cstdio>
+#include <vector>
+
+#include "devcommon.cuh"
+
+namespace {
+
+constexpr int BLK = 256;
+constexpr int RED_BLOCKS = 1024; /* fixed grid for deterministic reductions */
+constexpr int SPINE = 1024;
+
+struct SolveArgs {
+  int n;
+  int subcell;
+  int pow2;        /* n is a power of two: dividing by h2 is exact scaling */
+  double inv_h2;   /* 1/(double)h2 */
+  double h2;       /* (double)(float)(1.0/(n*n)) */
+  float inv_h2_f;
+};
+
+__device__ __forceinline__ bool in_range(int n, int i, int j, int k) {
+  return i >= 0 && i < n && j >= 0 && j < n && k >= 0 && k < n;
+}
+
+__device__ __forceinline__ void decode(size_t c, int n, int &i, int &j, int &k) {
+  k = (int)(c % n);
+  j = (int)((c / n) % n);
+  i = (int)(c / ((size_t)n * n));
+}
+
+/* A_diag (src/solver.cpp:103-117) in float with the reference's double
+ * promotions. */
+__device__ float a_diag(const uint8_t *__restrict__ A, const float *__restrict__ L, int n,
+                        int subcell, int i, int j, int k) {
+  float diag = 6.0f;
+  const int q[6][3] = {{i - 1, j, k}, {i + 1, j, k}, {i, j - 1, k},
+                       {i, j + 1, k}, {i, j, k - 1}, {i, j, k + 1}};
+  const float Lc = L[cell_id(n, i, j, k)];
+#pragma unroll
+  for (int m = 0; m < 6; m++) {
+    int qi = q[m][0], qj = q[m][1], qk = q[m][2];
+    if (!in_range(n, qi, qj, qk) || A[cell_id(n, qi, qj, qk)] == CELL_WALL) {
+      diag = (float)((double)diag - 1.0);
+    } else if (A[cell_id(n, qi, qj, qk)] == CELL_AIR && subcell) {
+      diag = (float)((double)diag -
+                     (double)L[cell_id(n, qi, qj, qk)] / fmin(1.0e-6, (double)Lc));
+    }
+  }
+  return diag;
+}
+
+/* --------------------------------------------------------------- setup */
+
+/* flip(b) over every cell (src/solver.cpp:76-80); REF preconditioner
+ * diagonal P = 1/sqrtf(diag) for FLUID cells, or FAST-mode FP32 diagonal;
+ * flags a REF entry equal to 1.0. */
+__global__ void __launch_bounds__(BLK)
+k_setup(SolveArgs s, int mode, const uint8_t *__restrict__ A, const float *__restrict__ L,
+        float *__restrict__ b, double *__restrict__ P, float *__restrict__ diag,
+        float *__restrict__ Pf, int *__restrict__ iflags) {
+  size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const size_t nc = (size_t)s.n * s.n * s.n;
+  if (c >= nc) return;
+  b[c] = -b[c];
+  if (A[c] != CELL_FLUID) {
+    if (P) P[c] = 0.0;
+    if (diag) diag[c] = 0.0f;
+    if (Pf) Pf[c] = 0.0f;
+    return;
+  }
+  int i, j, k;
+  decode(c, s.n, i, j, k);
+  float d = a_diag(A, L, s.n, s.subcell, i, j, k);
+  if (mode == FLIPGPU_SOLVE_REF) {
+    double pv = 1.0 / (double)sqrtf(d);
+    P[c] = pv;
+    if (pv == 1.0) atomicOr(iflags + IF_EXOTIC, 1);
+  } else {
+    diag[c] = d;
+    if (Pf) Pf[c] = 1.0f / d;
+  }
+}
+
+/* The reference's buildPreconditioner as written, sequentially, for the
+ * rare case of a diagonal entry equal to 1.0 (then neighbour terms act). */
+__global__ void k_build_ref_seq(int n, const uint8_t *__restrict__ A, double *__restrict__ P,
+                                const float *__restrict__ dummy, const int *__restrict__ iflags,
+                                const float *__restrict__ L, int subcell) {
+  if (threadIdx.x || blockIdx.x || !iflags[IF_EXOTIC]) return;
+  (void)dummy;
+  auto Pref = [&](int i, int j, int k) -> float {
+    if (!in_range(n, i, j, k) || P[cell_id(n, i, j, k)] != 1.0) return 0.0f;
+    return (float)P[cell_id(n, i, j, k)];
+  };
+  auto Aref = [&](int i, int j, int k, int qi, int qj, int qk) -> float {
+    if (!in_range(n, i, j, k) || A[cell_id(n, i, j, k)] != CELL_FLUID) return 0.0f;
+    if (!in_range(n, qi, qj, qk) || A[cell_id(n, qi, qj, qk)] != CELL_FLUID) return 0.0f;
+    return -1.0f;
+  };
+  for (size_t c = 0; c < (size_t)n * n * n; c++) P[c] = 0.0;
+  for (int k = 0; k < n; k++)
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        if (A[cell_id(n, i, j, k)] != CELL_FLUID) continue;
+        double left = (double)(Aref(i - 1, j, k, i, j, k) * Pref(i - 1, j, k));
+        double bottom = (double)(Aref(i, j - 1, k, i, j, k) * Pref(i, j - 1, k));
+        double back = (double)(Aref(i, j, k - 1, i, j, k) * Pref(i, j, k - 1));
+        double diag = (double)a_diag(A, L, n, subcell, i, j, k);
+        float sl = (float)left, sb = (float)bottom, sk = (float)back;
+        double e = diag - (double)(sl * sl) - (double)(sb * sb) - (double)(sk * sk);
+        if (e < 0.25 * diag) e = diag;
+        P[cell_id(n, i, j, k)] = 1.0 / (double)sqrtf((float)e);
+      }
+}
+
+/* ------------------------------------------------------------- matvec */
+
+/* compute_Ax (src/solver.cpp:29-41) with its double arithmetic. */
+__global__ void __launch_bounds__(BLK)
+k_matvec_ref(SolveArgs s, const int *__restrict__ iflags, const uint8_t *__restrict__ A,
+             const float *__restrict__ L, const float *__restrict__ x, float *__restrict__ ans) {
+  if (iflags[IF_DONE]) return;
+  size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const int n = s.n;
+  const size_t nc = (size_t)n * n * n;
+  if (c >= nc) return;
+  if (A[c] != CELL_FLUID) {
+    ans[c] = 0.0f;
+    return;
+  }
+  int i, j, k;
+  decode(c, n, i, j, k);
+  const float xc = x[c];
+  const float Lc = L[c];
+  auto xref = [&](int qi, int qj, int qk) -> float {
+    qi = min(max(0, qi), n - 1);
+    qj = min(max(0, qj), n - 1);
+    qk = min(max(0, qk), n - 1);
+    size_t q = cell_id(n, qi, qj, qk);
+    uint8_t a = A[q];
+    if (a == CELL_FLUID) return x[q];
+    if (a == CELL_WALL) return xc;
+    return s.subcell ? (float)((double)L[q] / fmin(1.0e-6, (double)Lc) * (double)xc) : 0.0f;
+  };
+  double v = 6.0 * (double)xc;
+  v -= (double)xref(i + 1, j, k);
+  v -= (double)xref(i - 1, j, k);
+  v -= (double)xref(i, j + 1, k);
+  v -= (double)xref(i, j - 1, k);
+  v -= (double)xref(i, j, k + 1);
+  v -= (double)xref(i, j, k - 1);
+  ans[c] = s.pow2 ? (float)(v * s.inv_h2) : (float)(v / s.h2);
+}
+
+/* FP32 matvec of the same operator: (diag*x - sum of fluid neighbours)/h2. */
+__global__ void __launch_bounds__(BLK)
+k_matvec_fast(SolveArgs s, const int *__restrict__ iflags, const uint8_t *__restrict__ A,
+              const float *__restrict__ diag, const float *__restrict__ x,
+              float *__restrict__ ans) {
+  if (iflags[IF_DONE]) return;
+  size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const int n = s.n;
+  const size_t nc = (size_t)n * n * n;
+  if (c >= nc) return;
+  if (A[c] != CELL_FLUID) {
+    ans[c] = 0.0f;
+    return;
+  }
+  int i, j, k;
+  decode(c, n, i, j, k);
+  float acc = diag[c] * x[c];
+  const size_t sj = n, si = (size_t)n * n;
+  if (i + 1 < n && A[c + si] == CELL_FLUID) acc -= x[c + si];
+  if (i > 0 && A[c - si] == CELL_FLUID) acc -= x[c - si];
+  if (j + 1 < n && A[c + sj] == CELL_FLUID) acc -= x[c + sj];
+  if (j > 0 && A[c - sj] == CELL_FLUID) acc -= x[c - sj];
+  if (k + 1 < n && A[c + 1] == CELL_FLUID) acc -= x[c + 1];
+  if (k > 0 && A[c - 1] == CELL_FLUID) acc -= x[c - 1];
+  ans[c] = acc * s.inv_h2_f;
+}
+
+/* ------------------------------------------------------ preconditioner */
+
+/* applyPreconditioner as written with no entry equal to 1.0: every
+ * neighbour term is a signed zero, so q = r*P and z = float(q*P) in double;
+ * the zeros' signs are reproduced for exact-zero residuals. */
+__global__ void __launch_bounds__(BLK)
+k_apply_ref_diag(SolveArgs s, const int *__restrict__ iflags, const uint8_t *__restrict__ A,
+                 const double *__restrict__ P, const float *__restrict__ r,
+                 float *__restrict__ z) {
+  if (iflags[IF_DONE] || iflags[IF_EXOTIC]) return;
+  size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const int n = s.n;
+  const size_t nc = (size_t)n * n * n;
+  if (c >= nc || A[c] != CELL_FLUID) return;
+  int i, j, k;
+  decode(c, n, i, j, k);
+  const float rc = r[c];
+  double t = (double)rc;
+  if (rc == 0.0f) {
+    bool back = (i > 0 && A[cell_id(n, i - 1, j, k)] == CELL_FLUID) ||
+                (j > 0 && A[cell_id(n, i, j - 1, k)] == CELL_FLUID) ||
+                (k > 0 && A[cell_id(n, i, j, k - 1)] == CELL_FLUID);
+    t = (signbit(rc) && !back) ? -0.0 : 0.0;
+  }
+  const double pc = P[c];
+  double q = t * pc;
+  double t2 = q;
+  if (q == 0.0) {
+    bool fwd = (i + 1 < n && A[cell_id(n, i + 1, j, k)] == CELL_FLUID) ||
+               (j + 1 < n && A[cell_id(n, i, j + 1, k)] == CELL_FLUID) ||
+               (k + 1 < n && A[cell_id(n, i, j, k + 1)] == CELL_FLUID);
+    t2 = (signbit(q) && !fwd) ? -0.0 : 0.0;
+  }
+  z[c] = (float)(t2 * pc);
+}
+
+/* applyPreconditioner as written (src/solver.cpp:141-180), sequentially,
+ * when some diagonal entry equals 1.0. */
+__global__ void k_apply_ref_seq(int n, const int *__restrict__ iflags,
+                                const uint8_t *__restrict__ A, const double *__restrict__ P,
+                                const float *__restrict__ r, float *__restrict__ z,
+                                double *__restrict__ q) {
+  if (threadIdx.x || blockIdx.x || iflags[IF_DONE] || !iflags[IF_EXOTIC]) return;
+  auto Aref = [&](int i, int j, int k, int qi, int qj, int qk) -> float {
+    if (!in_range(n, i, j, k) || A[cell_id(n, i, j, k)] != CELL_FLUID) return 0.0f;
+    if (!in_range(n, qi, qj, qk) || A[cell_id(n, qi, qj, qk)] != CELL_FLUID) return 0.0f;
+    return -1.0f;
+  };
+  auto PrefD = [&](const double *X, int i, int j, int k) -> float {
+    if (!in_range(n, i, j, k) || X[cell_id(n, i, j, k)] != 1.0) return 0.0f;
+    return (float)X[cell_id(n, i, j, k)];
+  };
+  auto PrefF = [&](const float *X, int i, int j, int k) -> float {
+    if (!in_range(n, i, j, k) || X[cell_id(n, i, j, k)] != 1.0f) return 0.0f;
+    return X[cell_id(n, i, j, k)];
+  };
+  const size_t nc = (size_t)n * n * n;
+  for (size_t c = 0; c < nc; c++) q[c] = 0.0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      for (int k = 0; k < n; k++) {
+        if (A[cell_id(n, i, j, k)] != CELL_FLUID) continue;
+        double left = (double)(Aref(i - 1, j, k, i, j, k) * PrefD(P, i - 1, j, k) * PrefD(q, i - 1, j, k));
+        double bottom = (double)(Aref(i, j - 1, k, i, j, k) * PrefD(P, i, j - 1, k) * PrefD(q, i, j - 1, k));
+        double back = (double)(Aref(i, j, k - 1, i, j, k) * PrefD(P, i, j, k - 1) * PrefD(q, i, j, k - 1));
+        double t = (double)r[cell_id(n, i, j, k)] - left - bottom - back;
+        q[cell_id(n, i, j, k)] = t * P[cell_id(n, i, j, k)];
+      }
+  for (int i = n - 1; i >= 0; i--)
+    for (int j = n - 1; j >= 0; j--)
+      for (int k = n - 1; k >= 0; k--) {
+        if (A[cell_id(n, i, j, k)] != CELL_FLUID) continue;
+        double right = (double)(Aref(i, j, k, i + 1, j, k) * PrefD(P, i, j, k) * PrefF(z, i + 1, j, k));
+        double top = (double)(Aref(i, j, k, i, j + 1, k) * PrefD(P, i, j, k) * PrefF(z, i, j + 1, k));
+        double front = (double)(Aref(i, j, k, i, j, k + 1) * PrefD(P, i, j, k) * PrefF(z, i, j, k + 1));
+        double t = q[cell_id(n, i, j, k)] - right - top - front;
+        z[cell_id(n, i, j, k)] = (float)(t * P[cell_id(n, i, j, k)]);
+      }
+}
+
+/* FAST Jacobi: z = r / diag on FLUID cells. */
+__global__ void __launch_bounds__(BLK)
+k_apply_jacobi(SolveArgs s, const int *__restrict__ iflags, const uint8_t *__restrict__ A,
+               const float *__restrict__ Pf, const float *__restrict__ r,
+               float *__restrict__ z) {
+  if (iflags[IF_DONE]) return;
+  size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const size_t nc = (size_t)s.n * s.n * s.n;
+  if (c >= nc) return;
+  z[c] = (A[c] == CELL_FLUID) ? r[c] * Pf[c] : 0.0f;
+}
+
+/* ---------------------------------------------------- vector updates */
+
+/* FP64 partial sums of float(x*y) over FLUID cells (product,
+ * src/solver.cpp:44-54); grid-stride over a fixed grid. */
+__global__ void __launch_bounds__(BLK)
+k_dot(size_t nc, const int *__restrict__ iflags, int check_done, const uint8_t *__restrict__ A,
+      const float *__restrict__ x, const float *__restrict__ y, double *__restrict__ partial) {
+  if (check_done && iflags[IF_DONE]) return;
+  double acc = 0.0;
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK)
+    if (A[c] == CELL_FLUID) acc += (double)(x[c] * y[c]);
+  double t = block_sum_double<BLK>(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+/* r = b - z (op with a = -1, src/solver.cpp:190) and r.r partials. */
+__global__ void __launch_bounds__(BLK)
+k_residual(size_t nc, const uint8_t *__restrict__ A, const float *__restrict__ b,
+           const float *__restrict__ z, float *__restrict__ r, double *__restrict__ partial) {
+  double acc = 0.0;
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK) {
+    float v = 0.0f;
+    if (A[c] == CELL_FLUID) {
+      v = b[c] + -1.0f * z[c];
+      acc += (double)(v * v);
+    }
+    r[c] = v;
+  }
+  double t = block_sum_double<BLK>(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+/* x = x + alpha*s, r = r - alpha*z (op, src/solver.cpp:202-203) and r.r. */
+__global__ void __launch_bounds__(BLK)
+k_update_xr(size_t nc, const int *__restrict__ iflags, const double *__restrict__ scal,
+            const uint8_t *__restrict__ A, float *__restrict__ x, float *__restrict__ r,
+            const float *__restrict__ s, const float *__restrict__ z,
+            double *__restrict__ partial) {
+  if (iflags[IF_DONE]) return;
+  const float alpha = (float)scal[SC_ALPHA];
+  const float nalpha = (float)(-scal[SC_ALPHA]);
+  double acc = 0.0;
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK) {
+    if (A[c] == CELL_FLUID) {
+      x[c] = x[c] + alpha * s[c];
+      float rv = r[c] + nalpha * z[c];
+      r[c] = rv;
+      acc += (double)(rv * rv);
+    } else {
+      x[c] = 0.0f;
+      r[c] = 0.0f;
+    }
+  }
+  double t = block_sum_double<BLK>(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+/* s = z + beta*s (op, src/solver.cpp:215). */
+__global__ void __launch_bounds__(BLK)
+k_update_s(size_t nc, const int *__restrict__ iflags, const double *__restrict__ scal,
+           const uint8_t *__restrict__ A, const float *__restrict__ z, float *__restrict__ s) {
+  if (iflags[IF_DONE]) return;
+  const float beta = (float)scal[SC_BETA];
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK)
+    s[c] = (A[c] == CELL_FLUID) ? z[c] + beta * s[c] : 0.0f;
+}
+
+/* ------------------------------------------------------------ scalars */
+
+enum { ST_B2 = 0, ST_ERR0, ST_A0, ST_ALPHA, ST_CHECK, ST_BETA };
+
+/* Sums the fixed partials (one block, fixed order) and advances the CG
+ * recurrence by one scalar step. */
+__global__ void __launch_bounds__(SPINE)
+k_scalar(int what, int mode, int nparts, const double *__restrict__ partial,
+         double *__restrict__ scal, int *__restrict__ iflags, double eps_abs, double rel_tol,
+         double ref_eps, int max_iters) {
+  if (what >= ST_ALPHA && iflags[IF_DONE]) return;
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += SPINE) v += partial[i];
+  double sum = block_sum_double<SPINE>(v);
+  if (threadIdx.x != 0) return;
+  switch (what) {
+  case ST_B2: {
+    scal[SC_B2] = sum;
+    double eps;
+    if (mode == FLIPGPU_SOLVE_REF) {
+      eps = ref_eps;
+      if (eps_abs >= 0.0) {
+        eps = eps_abs;
+      } else if (rel_tol > 0.0) {
+        double target = rel_tol * rel_tol * sum;
+        while (eps > target && eps > 0.0) eps *= 0.25;
+      }
+    } else {
+      eps = rel_tol * rel_tol * sum;
+    }
+    scal[SC_EPS] = eps;
+    iflags[IF_DONE] = 0;
+    iflags[IF_ITERS] = 0;
+    iflags[IF_NAN] = 0;
+    break;
+  }
+  case ST_ERR0:
+    scal[SC_ERR2_0] = sum;
+    scal[SC_ERR2] = sum;
+    /* FAST mode stops before iterating when the guess already meets the
+     * bound; REF mode always iterates once, as conjGrad does. */
+    if (mode != FLIPGPU_SOLVE_REF && sum <= scal[SC_EPS]) iflags[IF_DONE] = 1;
+    break;
+  case ST_A0:
+    scal[SC_A] = sum;
+    break;
+  case ST_ALPHA:
+    scal[SC_ALPHA] = scal[SC_A] / sum;
+    break;
+  case ST_CHECK: {
+    double e2 = (mode == FLIPGPU_SOLVE_REF) ? (double)(float)sum : sum;
+    scal[SC_ERR2] = e2;
+    int it = ++iflags[IF_ITERS];
+    if (e2 <= scal[SC_EPS]) iflags[IF_DONE] = 1;
+    else if (!(e2 == e2)) {
+      iflags[IF_NAN] = 1;
+      iflags[IF_DONE] = 2;
+    } else if (it >= max_iters)
+      iflags[IF_DONE] = 3;
+    break;
+  }
+  case ST_BETA:
+    scal[SC_BETA] = sum / scal[SC_A];
+    scal[SC_A] = sum;
+    break;
+  }
+}
+
+} // namespace
+
+int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
+  const int n = h->n;
+  const size_t nc = h->nc;
+  const int mode = h->prm.solve_mode;
+  int precond = h->prm.precond;
+  if (mode == FLIPGPU_SOLVE_REF) precond = FLIPGPU_PRECOND_REF;
+  if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_REF) precond = FLIPGPU_PRECOND_JACOBI;
+  SolveArgs sa;
+  sa.n = n;
+  sa.subcell = h->prm.subcell;
+  sa.pow2 = (n & (n - 1)) == 0;
+  float h2f = (float)(1.0 / ((double)n * n));
+  sa.h2 = (double)h2f;
+  sa.inv_h2 = 1.0 / (double)h2f;
+  sa.inv_h2_f = (float)sa.inv_h2;
+  const double ref_eps = 1.0e-2 * ((double)n * n * n);
+  const long cap = h->prm.max_iters > 0 ? h->prm.max_iters : (long)nc;
+  const int max_iters = cap > 0x7fffffff ? 0x7fffffff : (int)cap;
+  cudaStream_t S = h->stream;
+  const unsigned G = grid_for(nc, BLK);
+  auto scalar = [&](int what) {
+    k_scalar<<<1, SPINE, 0, S>>>(what, mode, RED_BLOCKS, h->partial, h->scal, h->iflags,
+                                 h->prm.eps_abs, h->prm.rel_tol, ref_eps, max_iters);
+    FG_LAUNCHED(h, 1);
+  };
+  cudaEventRecord(h->ev0, S);
+  cudaMemsetAsync(h->iflags, 0, IF_COUNT * sizeof(int), S);
+  /* setup: flip b, preconditioner / diagonal */
+  k_setup<<<G, BLK, 0, S>>>(sa, mode, h->A, h->L, h->div,
+                            mode == FLIPGPU_SOLVE_REF ? h->P : nullptr,
+                            mode == FLIPGPU_SOLVE_REF ? nullptr : h->diag,
+                            precond == FLIPGPU_PRECOND_JACOBI ? h->Pf : nullptr, h->iflags);
+  FG_LAUNCHED(h, 1);
+  if (mode == FLIPGPU_SOLVE_REF) {
+    k_build_ref_seq<<<1, 1, 0, S>>>(n, h->A, h->P, nullptr, h->iflags, h->L, h->prm.subcell);
+    FG_LAUNCHED(h, 1);
+  }
+  /* b.b and the stop bound */
+  k_dot<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, 0, h->A, h->div, h->div, h->partial);
+  FG_LAUNCHED(h, 1);
+  scalar(ST_B2);
+
+  auto matvec = [&](const float *x, float *out) {
+    if (mode == FLIPGPU_SOLVE_REF)
+      k_matvec_ref<<<G, BLK, 0, S>>>(sa, h->iflags, h->A, h->L, x, out);
+    else
+      k_matvec_fast<<<G, BLK, 0, S>>>(sa, h->iflags, h->A, h->diag, x, out);
+    FG_LAUNCHED(h, 1);
+  };
+  auto apply = [&](const float *r, float *z) {
+    if (precond == FLIPGPU_PRECOND_REF) {
+      k_apply_ref_diag<<<G, BLK, 0, S>>>(sa, h->iflags, h->A, h->P, r, z);
+      k_apply_ref_seq<<<1, 1, 0, S>>>(n, h->iflags, h->A, h->P, r, z, h->P + nc);
+      FG_LAUNCHED(h, 2);
+    } else if (precond == FLIPGPU_PRECOND_JACOBI) {
+      k_apply_jacobi<<<G, BLK, 0, S>>>(sa, h->iflags, h->A, h->Pf, r, z);
+      FG_LAUNCHED(h, 1);
+    } else {
+      cudaMemcpyAsync(z, r, nc * sizeof(float), cudaMemcpyDeviceToDevice, S);
+    }
+  };
+
+  /* z = A x; r = b - z; z = M^-1 r; s = z; a = z.r */
+  matvec(h->press, h->z);
+  k_residual<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->A, h->div, h->z, h->r, h->partial);
+  FG_LAUNCHED(h, 1);
+  scalar(ST_ERR0);
+  apply(h->r, h->z);
+  cudaMemcpyAsync(h->s, h->z, nc * sizeof(float), cudaMemcpyDeviceToDevice, S);
+  k_dot<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, 0, h->A, h->z, h->r, h->partial);
+  FG_LAUNCHED(h, 1);
+  scalar(ST_A0);
+
+  const int CHUNK = 8;
+  int done = 0;
+  int host_flags[IF_COUNT];
+  for (long it = 0; it < max_iters && !done; it += CHUNK) {
+    for (int u = 0; u < CHUNK; u++) {
+      matvec(h->s, h->z);
+      k_dot<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, 1, h->A, h->z, h->s, h->partial);
+      FG_LAUNCHED(h, 1);
+      scalar(ST_ALPHA);
+      k_update_xr<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, h->scal, h->A, h->press, h->r,
+                                             h->s, h->z, h->partial);
+      FG_LAUNCHED(h, 1);
+      scalar(ST_CHECK);
+      apply(h->r, h->z);
+      k_dot<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, 1, h->A, h->z, h->r, h->partial);
+      FG_LAUNCHED(h, 1);
+      scalar(ST_BETA);
+      k_update_s<<<RED_BLOCKS, BLK, 0, S>>>(nc, h->iflags, h->scal, h->A, h->z, h->s);
+      FG_LAUNCHED(h, 1);
+    }
+    cudaError_t e = cudaMemcpyAsync(host_flags, h->iflags, sizeof(host_flags),
+                                    cudaMemcpyDeviceToHost, S);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S);
+    if (e != cudaSuccess) {
+      snprintf(h->err, sizeof h->err, "solve: %s", cudaGetErrorString(e));
+      return FLIPGPU_ECUDA;
+    }
+    done = host_flags[IF_DONE];
+  }
+  cudaEventRecord(h->ev1, S);
+  double sc[SC_COUNT];
+  cudaMemcpyAsync(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost, S);
+  cudaMemcpyAsync(host_flags, h->iflags, sizeof(host_flags), cudaMemcpyDeviceToHost, S);
+  cudaError_t e = cudaStreamSynchronize(S);
+  if (e != cudaSuccess) {
+    snprintf(h->err, sizeof h->err, "solve: %s", cudaGetErrorString(e));
+    return FLIPGPU_ECUDA;
+  }
+  int status = FLIPGPU_OK;
+  if (host_flags[IF_NAN]) status = FLIPGPU_ENAN;
+  else if (host_flags[IF_DONE] == 3 || (!host_flags[IF_DONE] && mode != FLIPGPU_SOLVE_REF))
+    status = FLIPGPU_ENOCONV;
+  if (st) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    st->iterations = host_flags[IF_ITERS];
+    st->status = status;
+    st->r2 = sc[SC_ERR2];
+    st->b2 = sc[SC_B2];
+    st->ms = ms;
+  }
+  /* The reference stops silently at its cap; only non-finite residuals are
+   * errors in REF mode. */
+  if (status == FLIPGPU_ENAN) {
+    snprintf(h->err, sizeof h->err, "solve: non-finite residual");
+    return status;
+  }
+  if (status == FLIPGPU_ENOCONV && mode != FLIPGPU_SOLVE_REF) {
+    snprintf(h->err, sizeof h->err, "solve: no convergence in %d iterations", host_flags[IF_ITERS]);
+    return status;
+  }
+  return FLIPGPU_OK;
+}

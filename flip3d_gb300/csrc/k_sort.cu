@@ -1,0 +1,234 @@
+/*
+ * k_sort.cu — sorter::sort (src/sorter.cpp:22-40) as a stable counting sort.
+ *
+ *   count    key = cell of the clamped position (the reference's clamp),
+ *            rank = atomic ticket within the cell (integer atomics: the
+ *            counts are deterministic, the tickets are not)
+ *   scan     cell_start = exclusive prefix sum of the counts
+ *   scatter  perm[cell_start[key] + rank] = particle
+ *   fixup    each cell's slots sorted by particle index, which makes the
+ *            lists identical to the reference's push_back order
+ *   payload  sorted copies of position / clamped grid position / velocity
+ *            for the gather stages (optionally applying add_ExtForce)
+ *
+ * Also the device-wide exclusive scan used by the sort and the reposition
+ * compactions.
+ */
+#include "devcommon.cuh"
+
+namespace {
+
+constexpr int SCAN_BLOCK = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
+
+/* Exclusive block scan of one value per thread; returns the block total. */
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &total) {
+  __shared__ uint32_t warp_tot[SCAN_BLOCK / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t w = (lane < SCAN_BLOCK / 32) ? warp_tot[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < SCAN_BLOCK / 32) warp_tot[lane] = w;
+  }
+  __syncthreads();
+  uint32_t warp_off = wid ? warp_tot[wid - 1] : 0u;
+  total = warp_tot[SCAN_BLOCK / 32 - 1];
+  __syncthreads();
+  return warp_off + x - v;
+}
+
+__global__ void k_scan_reduce(const uint32_t *__restrict__ in, size_t n,
+                              uint32_t *__restrict__ bsum) {
+  size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++)
+    if (base + i < n) s += in[base + i];
+  uint32_t tot = block_sum_u32<SCAN_BLOCK>(s);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+/* One block scans the block sums in chunks, carrying the running total. */
+__global__ void k_scan_spine(uint32_t *__restrict__ bsum, size_t nb) {
+  uint32_t carry = 0;
+  for (size_t base = 0; base < nb; base += SCAN_BLOCK) {
+    size_t i = base + threadIdx.x;
+    uint32_t v = (i < nb) ? bsum[i] : 0u;
+    uint32_t tot;
+    uint32_t ex = block_exclusive_scan(v, tot);
+    if (i < nb) bsum[i] = carry + ex;
+    carry += tot;
+  }
+}
+
+__global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                            size_t n, const uint32_t *__restrict__ bsum) {
+  size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    v[i] = (base + i < n) ? in[base + i] : 0u;
+    s += v[i];
+  }
+  uint32_t tot;
+  uint32_t run = block_exclusive_scan(s, tot) + bsum[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+__global__ void k_sort_count(SimConst c, const float *__restrict__ px,
+                             const float *__restrict__ py, const float *__restrict__ pz,
+                             uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
+                             uint32_t *__restrict__ count) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= c.np) return;
+  int i = cell_clamp(px[p], c.fn, c.n);
+  int j = cell_clamp(py[p], c.fn, c.n);
+  int k = cell_clamp(pz[p], c.fn, c.n);
+  uint32_t kk = (uint32_t)cell_id(c.n, i, j, k);
+  key[p] = kk;
+  rank[p] = atomicAdd(&count[kk], 1u);
+}
+
+__global__ void k_sort_scatter(int np, const uint32_t *__restrict__ key,
+                               const uint32_t *__restrict__ rank,
+                               const uint32_t *__restrict__ cell_start,
+                               uint32_t *__restrict__ perm) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  perm[cell_start[key[p]] + rank[p]] = (uint32_t)p;
+}
+
+/* Order each cell's slots by particle index: insertion sort for the usual
+ * handful, heapsort for crowded cells. */
+__global__ void k_sort_fixup(size_t nc, const uint32_t *__restrict__ cell_start,
+                             uint32_t *__restrict__ perm) {
+  size_t cidx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cidx >= nc) return;
+  uint32_t s = cell_start[cidx], e = cell_start[cidx + 1];
+  uint32_t len = e - s;
+  if (len < 2) return;
+  uint32_t *a = perm + s;
+  if (len <= 32) {
+    for (uint32_t i = 1; i < len; i++) {
+      uint32_t v = a[i];
+      uint32_t j = i;
+      while (j > 0 && a[j - 1] > v) {
+        a[j] = a[j - 1];
+        j--;
+      }
+      a[j] = v;
+    }
+    return;
+  }
+  auto sift = [&](uint32_t root, uint32_t end) {
+    while (true) {
+      uint32_t child = 2 * root + 1;
+      if (child >= end) break;
+      if (child + 1 < end && a[child] < a[child + 1]) child++;
+      if (a[root] >= a[child]) break;
+      uint32_t t = a[root];
+      a[root] = a[child];
+      a[child] = t;
+      root = child;
+    }
+  };
+  for (uint32_t i = len / 2; i-- > 0;) sift(i, len);
+  for (uint32_t end = len - 1; end > 0; end--) {
+    uint32_t t = a[0];
+    a[0] = a[end];
+    a[end] = t;
+    sift(0, end);
+  }
+}
+
+/* Sorted payload; with apply_gravity also add_ExtForce (src/flip3D.cpp:
+ * 870-875) on the fluid velocities, canonical and sorted. */
+__global__ void k_payload(SimConst c, int apply_gravity, const uint32_t *__restrict__ perm,
+                          const float *__restrict__ px, const float *__restrict__ py,
+                          const float *__restrict__ pz, float *__restrict__ vx,
+                          float *__restrict__ vy, float *__restrict__ vz,
+                          const uint8_t *__restrict__ type, const float *__restrict__ dens,
+                          float4 *__restrict__ spos, float4 *__restrict__ spg,
+                          float4 *__restrict__ svel, float *__restrict__ sdens) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= c.np) return;
+  uint32_t p = perm[a];
+  float x = px[p], y = py[p], z = pz[p];
+  uint8_t t = type[p];
+  float ux = vx[p], uy = vy[p], uz = vz[p];
+  if (apply_gravity && t == CELL_FLUID) {
+    uy = refmath::add_fd(uy, c.grav_h, c.grav_l, c.grav);
+    vy[p] = uy;
+  }
+  float tw = pack_type(t);
+  spos[a] = make_float4(x, y, z, tw);
+  /* FLOAT x = fmax(0, fmin(gn, gn*p)) (src/mapper.cpp:28-30) */
+  spg[a] = make_float4(fmaxf(0.0f, fminf(c.fn, c.fn * x)), fmaxf(0.0f, fminf(c.fn, c.fn * y)),
+                       fmaxf(0.0f, fminf(c.fn, c.fn * z)), tw);
+  svel[a] = make_float4(ux, uy, uz, 0.0f);
+  sdens[a] = dens[p];
+}
+
+} // namespace
+
+cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n) {
+  if (n == 0) return cudaSuccess;
+  size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb > h->scan_cap) return cudaErrorInvalidValue;
+  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, h->scan_tmp);
+  k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(h->scan_tmp, nb);
+  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, h->scan_tmp);
+  FG_LAUNCHED(h, 3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_payload(FlipGpu *h, int apply_gravity) {
+  SimConst c = make_const(h);
+  if (h->np == 0) return cudaSuccess;
+  k_payload<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
+      c, apply_gravity, h->perm, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens,
+      h->spos, h->spg, h->svel, h->sdens);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort(FlipGpu *h, int apply_gravity) {
+  SimConst c = make_const(h);
+  cudaError_t e = cudaMemsetAsync(h->cell_count, 0, (h->nc + 1) * sizeof(uint32_t), h->stream);
+  if (e != cudaSuccess) return e;
+  if (h->np > 0) {
+    k_sort_count<<<grid_for(h->np, 256), 256, 0, h->stream>>>(c, h->px, h->py, h->pz, h->key,
+                                                              h->rank, h->cell_count);
+    FG_LAUNCHED(h, 1);
+  }
+  /* cell_count has nc+1 entries (last = 0), so cell_start[nc] = np. */
+  e = scan_exclusive(h, h->cell_count, h->cell_start, h->nc + 1);
+  if (e != cudaSuccess) return e;
+  if (h->np > 0) {
+    k_sort_scatter<<<grid_for(h->np, 256), 256, 0, h->stream>>>(h->np, h->key, h->rank,
+                                                                h->cell_start, h->perm);
+    k_sort_fixup<<<grid_for(h->nc, 256), 256, 0, h->stream>>>(h->nc, h->cell_start, h->perm);
+    FG_LAUNCHED(h, 2);
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = launch_payload(h, apply_gravity);
+  h->cells_valid = true;
+  return e;
+}

@@ -1,0 +1,285 @@
+"""Python access to libflipgpu.so through its C ABI (include/flipgpu.h).
+
+There is no CPU path: constructing a Simulation without the CUDA library or
+without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+OK = 0
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOCONV", -5: "ENAN", -6: "ETIMEOUT"}
+PRECOND_NONE, PRECOND_REF, PRECOND_IC, PRECOND_JACOBI = 0, 1, 2, 3
+SOLVE_REF, SOLVE_FAST = 0, 1
+
+f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+
+class Params(C.Structure):
+    _fields_ = [("n", C.c_int), ("max_particles", C.c_int), ("density", C.c_float),
+                ("alpha", C.c_double), ("dt", C.c_double), ("gravity", C.c_double),
+                ("subcell", C.c_int), ("seed", C.c_uint64), ("solve_mode", C.c_int),
+                ("precond", C.c_int), ("mic_tau", C.c_double), ("rel_tol", C.c_double),
+                ("eps_abs", C.c_double), ("max_iters", C.c_int), ("refine_steps", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
+                ("b2", C.c_double), ("ms", C.c_double)]
+
+
+class FlipGpuError(RuntimeError):
+    pass
+
+
+_lib = None
+
+# every exported entry point and its argument types
+SIGNATURES = {
+    "flipgpu_default_params": (None, [C.POINTER(Params), C.c_int, C.c_int]),
+    "flipgpu_create": (C.c_int, [C.POINTER(Params), C.POINTER(C.c_void_p)]),
+    "flipgpu_destroy": (C.c_int, [C.c_void_p]),
+    "flipgpu_last_error": (C.c_char_p, [C.c_void_p]),
+    "flipgpu_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipgpu_sync": (C.c_int, [C.c_void_p]),
+    "flipgpu_set_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "flipgpu_set_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_get_particles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_void_p, C.c_int]),
+    "flipgpu_count": (C.c_int, [C.c_void_p]),
+    "flipgpu_set_grid": (C.c_int, [C.c_void_p] + [C.c_void_p] * 7 + [C.c_int]),
+    "flipgpu_get_grid": (C.c_int, [C.c_void_p] + [C.c_void_p] * 7 + [C.c_int]),
+    "flipgpu_get_cells": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_set_max_density": (C.c_int, [C.c_void_p, C.c_float]),
+    "flipgpu_calibrate_max_density": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "flipgpu_sort": (C.c_int, [C.c_void_p]),
+    "flipgpu_compute_density": (C.c_int, [C.c_void_p]),
+    "flipgpu_mark_water": (C.c_int, [C.c_void_p]),
+    "flipgpu_add_force": (C.c_int, [C.c_void_p]),
+    "flipgpu_p2g": (C.c_int, [C.c_void_p]),
+    "flipgpu_g2p": (C.c_int, [C.c_void_p]),
+    "flipgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_project": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_picflip": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_advect": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "flipgpu_correct": (C.c_int, [C.c_void_p]),
+    "flipgpu_step": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_launch_count": (C.c_int64, [C.c_void_p]),
+    "flipgpu_put_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipgpu_get_profile": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+}
+
+STAGES = ["sort", "density", "mark_water", "p2g", "divergence", "solve", "gradient",
+          "extrapolate", "g2p_flip", "advect", "reposition", "correct"]
+
+
+def load(path: str | None = None):
+    """Load libflipgpu.so (building it if stale). Raises if it cannot."""
+    global _lib
+    if _lib is None:
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            _build.build()
+        if not os.path.exists(path):
+            raise FlipGpuError(f"CUDA library missing: {path}")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def default_params(n: int, max_particles: int, **kw) -> Params:
+    p = Params()
+    load().flipgpu_default_params(C.byref(p), n, max_particles)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _c(a, dt):
+    return None if a is None else np.ascontiguousarray(a, dtype=dt)
+
+
+class Simulation:
+    """One device-resident simulation (a FlipGpu handle)."""
+
+    def __init__(self, params: Params):
+        self.lib = load()
+        self.params = params
+        self.n = params.n
+        h = C.c_void_p()
+        rc = self.lib.flipgpu_create(C.byref(params), C.byref(h))
+        if rc != OK:
+            raise FlipGpuError(f"flipgpu_create failed: {ERRORS.get(rc, rc)}")
+        self.h = h
+        self.np = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.flipgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            msg = self.lib.flipgpu_last_error(self.h)
+            raise FlipGpuError(f"{what}: {ERRORS.get(rc, rc)}: {msg.decode() if msg else ''}")
+        return rc
+
+    # ------------------------------------------------------------ state
+    def set_particles(self, pos, typ, vel=None, nrm=None, dens=None):
+        pos = _c(pos, np.float32)
+        self.np = pos.shape[0]
+        self._keep = [pos, _c(typ, np.uint8), _c(vel, np.float32), _c(nrm, np.float32),
+                      _c(dens, np.float32)]
+        k = self._keep
+        self._ck(self.lib.flipgpu_set_particles(self.h, self.np, _ptr(k[0]), _ptr(k[2]),
+                                                _ptr(k[1]), _ptr(k[3]), _ptr(k[4]), 0),
+                 "set_particles")
+
+    def set_scene(self, scene):
+        self.set_particles(scene.pos, scene.type, scene.vel, scene.nrm)
+
+    def get_particles(self):
+        pos = np.zeros((self.np, 3), np.float32)
+        vel = np.zeros((self.np, 3), np.float32)
+        dens = np.zeros(self.np, np.float32)
+        typ = np.zeros(self.np, np.uint8)
+        self._ck(self.lib.flipgpu_get_particles(self.h, _ptr(pos), _ptr(vel), _ptr(dens),
+                                                _ptr(typ), 0), "get_particles")
+        return pos, vel, dens, typ
+
+    def set_grid(self, u=None, A=None, L=None, press=None, div=None):
+        u = [None] * 3 if u is None else [_c(x, np.float32) for x in u]
+        arrs = u + [_c(A, np.uint8), _c(L, np.float32), _c(press, np.float32),
+                    _c(div, np.float32)]
+        self._ck(self.lib.flipgpu_set_grid(self.h, *[_ptr(a) for a in arrs], 0), "set_grid")
+
+    def get_grid(self):
+        n = self.n
+        nf = (n + 1) * n * n
+        u = [np.zeros(nf, np.float32) for _ in range(3)]
+        A = np.zeros(n ** 3, np.uint8)
+        L = np.zeros(n ** 3, np.float32)
+        p = np.zeros(n ** 3, np.float32)
+        d = np.zeros(n ** 3, np.float32)
+        self._ck(self.lib.flipgpu_get_grid(self.h, *[_ptr(a) for a in (*u, A, L, p, d)], 0),
+                 "get_grid")
+        return u, A, L, p, d
+
+    def get_cells(self):
+        cs = np.zeros(self.n ** 3 + 1, np.uint32)
+        perm = np.zeros(self.np, np.uint32)
+        self._ck(self.lib.flipgpu_get_cells(self.h, _ptr(cs), _ptr(perm), 0), "get_cells")
+        return cs, perm
+
+    def set_max_density(self, md):
+        self._ck(self.lib.flipgpu_set_max_density(self.h, C.c_float(md)), "set_max_density")
+
+    def calibrate_max_density(self):
+        out = C.c_float(0)
+        self._ck(self.lib.flipgpu_calibrate_max_density(self.h, C.byref(out)), "calibrate")
+        return out.value
+
+    def set_step(self, step):
+        self._ck(self.lib.flipgpu_set_step(self.h, step), "set_step")
+
+    def set_stream(self, stream_handle):
+        """Launch on an external cudaStream_t (an integer handle); None restores
+        the handle's own stream."""
+        self._ck(self.lib.flipgpu_set_stream(self.h, C.c_void_p(stream_handle)), "set_stream")
+
+    def sync(self):
+        self._ck(self.lib.flipgpu_sync(self.h), "sync")
+
+    def put_state(self, pos, vel, on_device=False):
+        """pos/vel: numpy arrays (host) or raw device addresses (on_device)."""
+        if on_device:
+            self._ck(self.lib.flipgpu_put_state(self.h, C.c_void_p(pos), C.c_void_p(vel), 1),
+                     "put_state")
+        else:
+            self._ck(self.lib.flipgpu_put_state(self.h, _ptr(pos), _ptr(vel), 0), "put_state")
+
+    def get_state_into(self, pos_ptr, vel_ptr):
+        """Download positions/velocities into host buffers given by address."""
+        self._ck(self.lib.flipgpu_get_particles(self.h, C.c_void_p(pos_ptr),
+                                                C.c_void_p(vel_ptr), None, None, 0),
+                 "get_particles")
+
+    def set_profiling(self, on=True):
+        self._ck(self.lib.flipgpu_set_profiling(self.h, int(on)), "set_profiling")
+
+    def profile(self):
+        ms = np.zeros(len(STAGES), np.float64)
+        calls = np.zeros(len(STAGES), np.int64)
+        self._ck(self.lib.flipgpu_get_profile(self.h, _ptr(ms), _ptr(calls), len(STAGES)),
+                 "get_profile")
+        return {s: (float(ms[i]), int(calls[i])) for i, s in enumerate(STAGES)}
+
+    @property
+    def launches(self):
+        return self.lib.flipgpu_launch_count(self.h)
+
+    # ----------------------------------------------------------- stages
+    def sort(self):
+        self._ck(self.lib.flipgpu_sort(self.h), "sort")
+
+    def compute_density(self):
+        self._ck(self.lib.flipgpu_compute_density(self.h), "compute_density")
+
+    def mark_water(self):
+        self._ck(self.lib.flipgpu_mark_water(self.h), "mark_water")
+
+    def add_force(self):
+        self._ck(self.lib.flipgpu_add_force(self.h), "add_force")
+
+    def p2g(self):
+        self._ck(self.lib.flipgpu_p2g(self.h), "p2g")
+
+    def g2p(self):
+        self._ck(self.lib.flipgpu_g2p(self.h), "g2p")
+
+    def _stats_call(self, fn, what):
+        st = SolveStats()
+        self._ck(fn(self.h, C.byref(st)), what)
+        return st
+
+    def solve(self):
+        return self._stats_call(self.lib.flipgpu_solve, "solve")
+
+    def project(self):
+        return self._stats_call(self.lib.flipgpu_project, "project")
+
+    def picflip(self):
+        return self._stats_call(self.lib.flipgpu_picflip, "picflip")
+
+    def advect(self, want_stuck=True):
+        s = C.c_int(0)
+        self._ck(self.lib.flipgpu_advect(self.h, C.byref(s) if want_stuck else None), "advect")
+        return s.value
+
+    def correct(self):
+        self._ck(self.lib.flipgpu_correct(self.h), "correct")
+
+    def step(self):
+        return self._stats_call(self.lib.flipgpu_step, "step")

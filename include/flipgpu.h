@@ -1,0 +1,189 @@
+/*
+ * flipgpu.h — C ABI of the GB300 FLIP step (libflipgpu.so).
+ *
+ * One opaque handle holds one simulation resident in device memory: the
+ * particle set (structure of arrays, in the caller's particle order), the
+ * sorted cell lists, the MAC grid and the solver vectors. Each entry point
+ * below replaces one function of the reference's per-step hot path and runs
+ * on the handle's CUDA stream; none synchronises with the host unless it
+ * returns data to host memory.
+ *
+ * Layouts (identical to the CPU oracle and the reference's arrays):
+ *   particles   pos/vel/nrm float[count][3], type uint8 (1 fluid, 2 wall)
+ *   cells       x-major (i*n + j)*n + k, k fastest (the reference's
+ *               A[i][j][k] with k contiguous)
+ *   faces       u0 (n+1)*n*n, u1 n*(n+1)*n, u2 n*n*(n+1), x-major
+ *   cell lists  cell_start[n^3+1], perm[count]: the particles of cell c are
+ *               perm[cell_start[c] .. cell_start[c+1]) in particle order,
+ *               exactly the lists sorter::sort builds
+ *
+ * Every call returns FLIPGPU_OK (0) or a negative FLIPGPU_E* code;
+ * flipgpu_last_error() gives a message. Handles are not thread-safe, like
+ * the reference's static state (src/flip3D.cpp:41-60).
+ */
+#ifndef FLIPGPU_H
+#define FLIPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FLIPGPU_OK 0
+#define FLIPGPU_EINVAL -1      /* bad argument or size */
+#define FLIPGPU_ECUDA -2       /* CUDA runtime error */
+#define FLIPGPU_ENOMEM -3      /* device allocation failed */
+#define FLIPGPU_ENOCONV -4     /* CG hit its iteration cap */
+#define FLIPGPU_ENAN -5        /* non-finite residual */
+#define FLIPGPU_ETIMEOUT -6    /* a bounded device wait expired */
+
+/* Preconditioners. REF reproduces the reference's buildPreconditioner/
+ * applyPreconditioner as written (src/solver.cpp:119-180): its neighbour
+ * terms only act on values equal to 1.0, so in practice it scales by the
+ * diagonal. IC is the same lexicographic incomplete-Cholesky factor with the
+ * neighbour test on the cell flag (mic_tau 0 = IC(0), 0.97 = MIC(0)),
+ * applied as wavefronts. JACOBI is plain diagonal scaling in FP32. */
+#define FLIPGPU_PRECOND_NONE 0
+#define FLIPGPU_PRECOND_REF 1
+#define FLIPGPU_PRECOND_IC 2
+#define FLIPGPU_PRECOND_JACOBI 3
+
+/* Solver arithmetic. REF: the reference's promotions (double matvec sums,
+ * float(r.r) stop test, power-of-4 relative tolerance, see rel_tol). FAST:
+ * FP32 matvec and preconditioner, FP64 dot products, stop on
+ * ||r|| <= rel_tol*||b|| exactly, optional FP64 iterative refinement. */
+#define FLIPGPU_SOLVE_REF 0
+#define FLIPGPU_SOLVE_FAST 1
+
+typedef struct FlipGpuParams {
+  int n;              /* N: grid cells per axis (src/flip3D.cpp:25) */
+  int max_particles;  /* capacity of the particle arrays */
+  float density;      /* DENSITY 0.5: particle spacing in cells */
+  double alpha;       /* ALPHA 0.95: FLIP fraction */
+  double dt;          /* DT 0.006 */
+  double gravity;     /* GRAVITY 9.8 */
+  int subcell;        /* SUBCELL 1: ghost-fluid free surface */
+  uint64_t seed;      /* seed of the keyed random draws */
+  int solve_mode;     /* FLIPGPU_SOLVE_* */
+  int precond;        /* FLIPGPU_PRECOND_* */
+  double mic_tau;     /* IC modification weight */
+  double rel_tol;     /* relative residual target; REF mode divides the
+                         reference's absolute 1e-2*n^3 by 4^k until it is at
+                         most rel_tol^2*b.b; 0 keeps the reference's own */
+  double eps_abs;     /* REF mode: explicit absolute r.r bound if >= 0 */
+  int max_iters;      /* CG iteration cap; <=0: n^3 like the reference */
+  int refine_steps;   /* FAST mode: outer FP64 refinement passes (0 = off) */
+} FlipGpuParams;
+
+typedef struct FlipGpuSolveStats {
+  int iterations;     /* CG iterations of the last solve (all passes) */
+  int status;         /* FLIPGPU_OK / ENOCONV / ENAN */
+  double r2;          /* final r.r */
+  double b2;          /* b.b */
+  double ms;          /* device time of the solve (CUDA events) */
+} FlipGpuSolveStats;
+
+typedef struct FlipGpu FlipGpu;
+
+/* Fill p with the reference's defaults for grid size n. */
+void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles);
+
+int flipgpu_create(const FlipGpuParams *p, FlipGpu **out);
+int flipgpu_destroy(FlipGpu *h);
+const char *flipgpu_last_error(const FlipGpu *h);
+/* Use an external stream (a cudaStream_t); NULL restores the handle's own. */
+int flipgpu_set_stream(FlipGpu *h, void *stream);
+int flipgpu_sync(FlipGpu *h);
+int flipgpu_set_step(FlipGpu *h, int64_t step);
+
+/* Particle state. Pointers are host memory unless on_device != 0. Any
+ * pointer may be NULL to skip that array (set: keeps zeros/old values). */
+int flipgpu_set_particles(FlipGpu *h, int count, const float *pos,
+                          const float *vel, const uint8_t *type,
+                          const float *nrm, const float *dens, int on_device);
+int flipgpu_get_particles(FlipGpu *h, float *pos, float *vel, float *dens,
+                          uint8_t *type, int on_device);
+int flipgpu_count(const FlipGpu *h);
+
+/* Grid state, same host/device rule; NULL skips an array. */
+int flipgpu_set_grid(FlipGpu *h, const float *u0, const float *u1,
+                     const float *u2, const uint8_t *A, const float *L,
+                     const float *press, const float *div, int on_device);
+int flipgpu_get_grid(FlipGpu *h, float *u0, float *u1, float *u2, uint8_t *A,
+                     float *L, float *press, float *div, int on_device);
+int flipgpu_get_cells(FlipGpu *h, uint32_t *cell_start, uint32_t *perm,
+                      int on_device);
+
+/* Density normalisation: set it, or compute it from the calibration
+ * lattice of src/flip3D.cpp:689-709 with the density kernel. */
+int flipgpu_set_max_density(FlipGpu *h, float max_dens);
+int flipgpu_calibrate_max_density(FlipGpu *h, float *out);
+
+/* ---- the hot path, one entry per reference function ------------------ */
+
+/* sorter::sort (src/sorter.cpp:22-40): stable counting sort of particles
+ * into cells. */
+int flipgpu_sort(FlipGpu *h);
+/* computeDensity (src/flip3D.cpp:166-190) on the current cell lists. */
+int flipgpu_compute_density(FlipGpu *h);
+/* sorter::markWater (src/sorter.cpp:83-93) into A, and sorter::levelset for
+ * every cell into L (src/flip3D.cpp:824-826). */
+int flipgpu_mark_water(FlipGpu *h);
+/* add_ExtForce (src/flip3D.cpp:870-875). */
+int flipgpu_add_force(FlipGpu *h);
+/* mapper::mapP2G (src/mapper.cpp:17-88) into the face grids. */
+int flipgpu_p2g(FlipGpu *h);
+/* mapper::mapG2P (src/mapper.cpp:90-94): particle velocity = trilinear
+ * sample of the face grids (fluid particles). */
+int flipgpu_g2p(FlipGpu *h);
+/* solver::solve (src/solver.cpp:224-241) on the handle's A, L, pressure
+ * (initial guess, overwritten) and divergence (negated, as the reference
+ * does). */
+int flipgpu_solve(FlipGpu *h, FlipGpuSolveStats *stats);
+/* project (src/flip3D.cpp:807-868): divergence, solve, subcell gradient. */
+int flipgpu_project(FlipGpu *h, FlipGpuSolveStats *stats);
+/* solve_picflip (src/flip3D.cpp:1057-1103) after its sort. */
+int flipgpu_picflip(FlipGpu *h, FlipGpuSolveStats *stats);
+/* advect_particle (src/flip3D.cpp:877-969), including the wall constraint,
+ * stuck-particle detection and reposition (src/flip3D.cpp:405-451). */
+int flipgpu_advect(FlipGpu *h, int *stuck);
+/* corrector::correct (src/corrector.cpp:49-115). */
+int flipgpu_correct(FlipGpu *h);
+/* simulateStep (src/flip3D.cpp:1194-1264) without preview and mesh I/O. */
+int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *stats);
+
+/* Replace positions and velocities of the current particle set (same count
+ * and types as the last flipgpu_set_particles), host or device AoS. This is
+ * the per-step upload of a host-side driver such as src/flip3D.cpp. */
+int flipgpu_put_state(FlipGpu *h, const float *pos, const float *vel,
+                      int on_device);
+
+/* Number of kernels this library launched on the handle so far. */
+int64_t flipgpu_launch_count(const FlipGpu *h);
+
+/* Per-stage device time of flipgpu_step (CUDA events on the handle's
+ * stream), the analogue of the reference's dumptime() stage prints
+ * (src/flip3D.cpp:1219-1243). Stage ids index the FLIPGPU_STAGE_* list. */
+#define FLIPGPU_STAGE_SORT 0       /* sort + payload (+ add_ExtForce) */
+#define FLIPGPU_STAGE_DENSITY 1
+#define FLIPGPU_STAGE_MARK 2       /* markWater + levelset */
+#define FLIPGPU_STAGE_P2G 3
+#define FLIPGPU_STAGE_DIV 4
+#define FLIPGPU_STAGE_SOLVE 5
+#define FLIPGPU_STAGE_GRAD 6       /* gradient + enforce_boundary */
+#define FLIPGPU_STAGE_EXTRAP 7     /* extrapolate + subtract_grid */
+#define FLIPGPU_STAGE_FLIP 8       /* G2P + FLIP blend */
+#define FLIPGPU_STAGE_ADVECT 9
+#define FLIPGPU_STAGE_REPOSITION 10 /* stuck lists, placement, sort, resample */
+#define FLIPGPU_STAGE_CORRECT 11
+#define FLIPGPU_NSTAGES 12
+int flipgpu_set_profiling(FlipGpu *h, int on);
+/* ms[i] and calls[i] accumulated since profiling was switched on. */
+int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLIPGPU_H */

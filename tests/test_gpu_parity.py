@@ -1,0 +1,209 @@
+"""CUDA path (through the C ABI) against the CPU oracle on the same inputs.
+
+The oracle is pinned bit-exact to the reference (test_oracle_golden.py), so
+equality here is equality with the reference. Integer and index results must
+match exactly; float results of every stage are expected to match bit for bit
+(the kernels follow the reference's evaluation order and promotions), with
+one stated exception: the FP64 dot products of the solver are summed as a
+tree instead of sequentially, which can move the CG scalars by ~1e-16 and a
+pressure value by an ulp. Those comparisons carry an explicit tolerance.
+"""
+import numpy as np
+import pytest
+
+from flip3d_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+GOLD = __import__("os").path.join(__import__("os").path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from flip3d_gb300 import gpu as g
+    g.load()
+    return g
+
+
+@pytest.fixture(scope="module")
+def orc():
+    from oracle import pyoracle
+    return pyoracle
+
+
+def make_sim(gpu, n, np_, **kw):
+    p = gpu.default_params(n, max(np_, 1), **kw)
+    return gpu.Simulation(p)
+
+
+def comp_inputs(name):
+    g = np.load(f"{GOLD}/{name}.npz")
+    return g
+
+
+@pytest.mark.parametrize("name", ["components_n16", "components_n13"])
+def test_sort_matches_reference(gpu, name):
+    g = comp_inputs(name)
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0])
+    sim.set_particles(g["pos"], g["type"], g["vel"], g["nrm"], g["dens"])
+    sim.sort()
+    cs, perm = sim.get_cells()
+    assert np.array_equal(cs, g["cell_start"])
+    assert np.array_equal(perm, g["perm"])
+
+
+@pytest.mark.parametrize("name", ["components_n16", "components_n13"])
+def test_mark_water_matches_reference(gpu, name):
+    g = comp_inputs(name)
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0])
+    sim.set_particles(g["pos"], g["type"], g["vel"], g["nrm"], g["dens"])
+    sim.sort()
+    sim.mark_water()
+    _, A, L, _, _ = sim.get_grid()
+    assert np.array_equal(A, g["A"])
+    assert np.array_equal(L, g["L"])
+
+
+@pytest.mark.parametrize("name", ["components_n16", "components_n13"])
+def test_p2g_matches_reference(gpu, name):
+    g = comp_inputs(name)
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0])
+    sim.set_particles(g["pos"], g["type"], g["vel"], g["nrm"])
+    sim.sort()
+    sim.p2g()
+    u, _, _, _, _ = sim.get_grid()
+    for c in range(3):
+        assert np.array_equal(u[c], g[f"u{c}"]), f"component {c}"
+
+
+@pytest.mark.parametrize("name", ["components_n16", "components_n13"])
+def test_g2p_matches_reference(gpu, orc, name):
+    g = comp_inputs(name)
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0])
+    sim.set_particles(g["pos"], g["type"], g["vel"], g["nrm"])
+    grid = [g["grid0"], g["grid1"], g["grid2"]]
+    sim.set_grid(u=grid)
+    sim.g2p()
+    _, vel, _, _ = sim.get_particles()
+    fl = g["type"] == 1
+    ref = orc.g2p(n, g["pos"], g["type"], grid)
+    assert np.array_equal(vel[fl], ref[fl])
+    ub = (np.float32(n) * g["pos"][:, 2]) > np.float32(n - 0.5)
+    sel = fl & ~ub
+    assert np.array_equal(vel[sel], g["g2p"][sel])
+
+
+@pytest.mark.parametrize("name", ["components_n16", "components_n13"])
+def test_correct_matches_reference(gpu, name):
+    g = comp_inputs(name)
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0], seed=int(g["corr_seed"]))
+    sim.set_particles(g["pos"], g["type"], g["vel"], g["nrm"])
+    sim.set_step(int(g["corr_step"]))
+    sim.correct()
+    pos, vel, _, _ = sim.get_particles()
+    fl = g["type"] == 1
+    assert np.array_equal(pos, g["corr_pos"])
+    assert np.array_equal(vel[fl], g["corr_vel"][fl])
+
+
+def test_density_matches_oracle(gpu, orc):
+    sc = scenes.pool_sphere(32, seed=3)
+    n = sc.n
+    md = orc.max_density(n)
+    sim = make_sim(gpu, n, sc.count)
+    sim.set_scene(sc)
+    assert np.float32(sim.calibrate_max_density()) == np.float32(md)
+    sim.compute_density()
+    _, _, dens, _ = sim.get_particles()
+    cs, perm = orc.sort(n, sc.pos)
+    ref = orc.density(n, sc.pos, sc.type, cs, perm, md)
+    assert np.array_equal(dens, ref)
+
+
+@pytest.mark.parametrize("name", ["solver_n16", "solver_n13"])
+@pytest.mark.parametrize("tag,rel", [("abs", 0.0), ("rel6", 1e-6)])
+def test_solve_ref_mode_matches_reference(gpu, name, tag, rel):
+    """REF-mode PCG against the reference's own solve. Iteration counts equal;
+    pressures equal up to the dot-product summation order (|dp| <= 1e-5 of
+    max|p|, and in practice almost all values bit-identical)."""
+    g = np.load(f"{GOLD}/{name}.npz")
+    n = int(g["n"])
+    sim = make_sim(gpu, n, 1, rel_tol=rel)
+    sim.set_grid(A=g["A"], L=g["L"], press=g["x0"], div=g["b"])
+    st = sim.solve()
+    _, _, _, p, b = sim.get_grid()
+    ref = g[f"x_{tag}"]
+    assert np.array_equal(b, g[f"b_{tag}"])
+    scale = float(np.abs(ref).max())
+    assert np.abs(p - ref).max() <= 1e-5 * scale
+    assert np.mean(p == ref) > 0.9
+
+
+def test_solve_fast_mode_converges_to_fp64(gpu, orc):
+    """FAST mode (FP32 matvec, FP64 dots) to rel-res 1e-6 against an FP64
+    IC(0) solve run to 1e-12 on the oracle."""
+    g = np.load(f"{GOLD}/solver_n16.npz")
+    n = int(g["n"])
+    sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                   precond=gpu.PRECOND_JACOBI)
+    sim.set_grid(A=g["A"], L=g["L"], press=np.zeros(n ** 3, np.float32), div=g["b"])
+    st = sim.solve()
+    assert st.status == 0
+    assert st.r2 <= 1e-12 * st.b2 * (1 + 1e-9)
+    _, _, _, p, _ = sim.get_grid()
+    prm = orc.params(n, orc.PRECOND_IC, rel_tol=1e-12)
+    x, _, it, _, _ = orc.solve(prm, g["A"], g["L"], np.zeros(n ** 3, np.float32), g["b"])
+    fl = g["A"] == 1
+    err = np.linalg.norm((p - x)[fl]) / np.linalg.norm(x[fl])
+    assert err < 1e-4, err
+
+
+def run_steps_both(gpu, orc, sc, steps, rel_tol, seed=11):
+    n = sc.n
+    md = orc.max_density(n)
+    prm = orc.params(n, orc.PRECOND_REF, rel_tol=rel_tol, seed=seed)
+    osim = orc.Sim(sc, prm, md)
+    gsim = make_sim(gpu, n, sc.count, rel_tol=rel_tol, seed=seed)
+    gsim.set_scene(sc)
+    gsim.set_max_density(md)
+    for _ in range(steps):
+        osim.step()
+        gsim.step()
+    return osim, gsim
+
+
+@pytest.mark.parametrize("steps", [1, 3])
+def test_full_step_matches_oracle(gpu, orc, steps):
+    """simulateStep at N=32 on the pool+sphere scene, rel-res 1e-6."""
+    sc = scenes.pool_sphere(32, seed=0)
+    osim, gsim = run_steps_both(gpu, orc, sc, steps, 1e-6)
+    opos, ovel, odens, otyp = osim.get()
+    gpos, gvel, gdens, gtyp = gsim.get_particles()
+    fl = otyp == 1
+    assert np.array_equal(gtyp, otyp)
+    dpos = np.abs(gpos - opos).max()
+    dvel = np.abs(gvel[fl] - ovel[fl]).max()
+    assert dpos <= 1e-5, dpos
+    assert dvel <= 1e-3 * max(1.0, float(np.abs(ovel[fl]).max())), dvel
+    assert np.abs(gdens - odens).max() <= 1e-4
+    # and most values identical
+    assert np.mean(gpos == opos) > 0.95
+
+
+def test_step_deterministic(gpu):
+    sc = scenes.pool_sphere(24, seed=5)
+    outs = []
+    for _ in range(2):
+        sim = make_sim(gpu, sc.n, sc.count, rel_tol=1e-6, seed=2)
+        sim.set_scene(sc)
+        sim.calibrate_max_density()
+        for _ in range(3):
+            sim.step()
+        outs.append(sim.get_particles())
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
