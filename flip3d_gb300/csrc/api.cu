@@ -83,7 +83,7 @@ __global__ void k_add_force(SimConst c, const uint8_t *__restrict__ type, float 
 
 /* Upload an AoS float[np][3] (host or device) into three SoA arrays. */
 int put3(FlipGpu *h, const float *src, int on_device, float *x, float *y, float *z) {
-  if (!src) return FLIPGPU_OK;
+  if (!src || h->np == 0) return FLIPGPU_OK;
   size_t bytes = (size_t)h->np * 3 * sizeof(float);
   float *stage = (float *)h->spos; /* 16 B per slot >= 12 B per particle */
   CK(h, cudaMemcpyAsync(stage, src, bytes,
@@ -96,7 +96,7 @@ int put3(FlipGpu *h, const float *src, int on_device, float *x, float *y, float 
 
 int get3(FlipGpu *h, float *dst, int on_device, const float *x, const float *y, const float *z,
          float *stage) {
-  if (!dst) return FLIPGPU_OK;
+  if (!dst || h->np == 0) return FLIPGPU_OK;
   size_t bytes = (size_t)h->np * 3 * sizeof(float);
   k_interleave<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, x, y, z, stage);
   FG_LAUNCHED(h, 1);
