@@ -15,7 +15,8 @@ from . import build as _build
 LIB_PATH = _build.LIB
 
 OK = 0
-ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOCONV", -5: "ENAN", -6: "ETIMEOUT"}
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOCONV", -5: "ENAN", -6: "ETIMEOUT",
+          -7: "ETOOBIG"}
 PRECOND_NONE, PRECOND_REF, PRECOND_IC, PRECOND_JACOBI = 0, 1, 2, 3
 SOLVE_REF, SOLVE_FAST = 0, 1
 
@@ -78,6 +79,8 @@ SIGNATURES = {
     "flipgpu_put_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "flipgpu_get_profile": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_sort_cells_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                             C.c_void_p, C.c_void_p]),
 }
 
 STAGES = ["sort", "density", "mark_water", "p2g", "divergence", "solve", "gradient",

@@ -38,6 +38,7 @@ extern "C" {
 #define FLIPGPU_ENOCONV -4     /* CG hit its iteration cap */
 #define FLIPGPU_ENAN -5        /* non-finite residual */
 #define FLIPGPU_ETIMEOUT -6    /* a bounded device wait expired */
+#define FLIPGPU_ETOOBIG -7     /* input larger than a fixed scratch limit */
 
 /* Preconditioners. REF reproduces the reference's buildPreconditioner/
  * applyPreconditioner as written (src/solver.cpp:119-180): its neighbour
@@ -182,6 +183,25 @@ int64_t flipgpu_launch_count(const FlipGpu *h);
 int flipgpu_set_profiling(FlipGpu *h, int on);
 /* ms[i] and calls[i] accumulated since profiling was switched on. */
 int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max);
+
+/* Cell sort that allocates no device memory. It has no counterpart in the
+ * reference. It is for callers that may not allocate on the GPU, such as a
+ * plugin inside a host application that owns all device memory, or a frame
+ * loop that cannot take the device-wide stall of cudaMalloc/cudaFree. It
+ * writes the same cell_start[n^3+1] / perm[count] as flipgpu_sort from a
+ * device AoS position buffer pos[count][3]; every pointer is device memory
+ * the caller owns. Its working memory is one fixed array per device, alive
+ * until the process exits, sized for at most FLIPGPU_NOALLOC_MAX_CELLS cells
+ * (n <= 64) and FLIPGPU_NOALLOC_MAX_PARTICLES particles (about 5.3 MB);
+ * larger inputs return FLIPGPU_ETOOBIG. The first call on a device looks that
+ * array up (with the device current); make it before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race and give
+ * undefined results. stream is a cudaStream_t (NULL = default stream). */
+#define FLIPGPU_NOALLOC_MAX_CELLS (64 * 64 * 64)
+#define FLIPGPU_NOALLOC_MAX_PARTICLES (1 << 20)
+int flipgpu_sort_cells_noalloc(int n, int count, const float *pos,
+                               uint32_t *cell_start, uint32_t *perm,
+                               void *stream);
 
 #ifdef __cplusplus
 }
