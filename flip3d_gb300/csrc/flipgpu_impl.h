@@ -94,13 +94,15 @@ struct FlipGpu {
   float *L, *press, *div;
 
   /* solver */
-  float *r, *z, *s;
+  float *r, *z, *s, *s1, *w;
   double *P;          /* REF preconditioner diagonal (double, as the reference) */
   float *Pf;          /* FP32 preconditioner diagonal / IC factor */
   float *diag;        /* FP32 matvec diagonal (FAST mode) */
   double *partial;    /* per-block reduction partials */
   double *scal;       /* device scalars of the CG recurrence */
   int *iflags;        /* device flags/counters */
+  unsigned *bar;      /* grid barrier of the persistent CG: count, generation */
+  int cg_grid;        /* blocks of the cooperative CG launch (0 = unavailable) */
   int npartial;
 
   /* reposition */
@@ -139,6 +141,7 @@ enum {
   IF_NSTUCK,
   IF_NWATER,
   IF_NAN,
+  IF_TIMEOUT,
   IF_COUNT
 };
 
@@ -160,6 +163,7 @@ cudaError_t launch_advect(FlipGpu *h);
 cudaError_t launch_reposition(FlipGpu *h, int *stuck_host);
 cudaError_t launch_correct(FlipGpu *h);
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
+int cg_grid_size(int *out);
 
 /* device-wide exclusive scan of n uint32 (in may equal out) */
 cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,

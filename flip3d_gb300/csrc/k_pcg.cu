@@ -429,7 +429,331 @@ k_scalar(int what, int mode, int nparts, const double *__restrict__ partial,
   }
 }
 
+/* ---------------------------------------------- persistent CG (one launch) */
+
+/* The whole CG loop in one cooperative launch: two grid barriers per
+ * iteration, s = z + beta*s folded into the next matvec (ping-pong s
+ * buffers; neighbour values of s are recomputed from z and the old s), and
+ * every block sums the per-block partials itself in the same fixed order, so
+ * all blocks agree on every scalar without a broadcast and the result does
+ * not depend on timing. Each thread owns the same cells in every phase; the
+ * only cross-thread reads (neighbours, partials) bypass L1 (ld.cg). */
+constexpr int CG_BLOCK = 256;
+constexpr unsigned long long BAR_SPIN_LIMIT = 1ull << 26; /* ~seconds, then ETIMEOUT */
+
+struct CgArgs {
+  SolveArgs s;
+  size_t nc;
+  const uint8_t *A;
+  const float *L;
+  const float *b;
+  float *x, *r, *z, *s0, *s1, *w;
+  const double *P;
+  const float *diag;
+  const float *Pf;
+  double *part;
+  unsigned *bar;
+  int *iflags;
+  double *scal;
+  double eps_abs, rel_tol, ref_eps;
+  int max_iters;
+};
+
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = bar + 1;
+    unsigned g = *gen;
+    __threadfence();
+    unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*gen == g) {
+        if (++spins > BAR_SPIN_LIMIT) {
+          atomicExch(iflags + IF_TIMEOUT, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    ok = *(volatile int *)(iflags + IF_TIMEOUT) == 0;
+  }
+  __syncthreads();
+  /* one value per block, so a block always leaves the loop as a whole */
+  return ok != 0;
+}
+
+/* Sum of the nb partials of slot k, identical in every block (fixed order). */
+__device__ __forceinline__ double sum_partials(const double *part, int k, unsigned nb) {
+  __shared__ double res;
+  if (threadIdx.x < 32) {
+    double v = 0.0;
+    for (unsigned i = threadIdx.x; i < nb; i += 32) v += __ldcg(part + (size_t)k * nb + i);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) res = v;
+  }
+  __syncthreads();
+  double r = res;
+  __syncthreads();
+  return r;
+}
+
+template <int MODE>
+__device__ __forceinline__ float cg_matvec(const CgArgs &a, size_t c, int i, int j, int k,
+                                           float sc, const float *zv, const float *so,
+                                           float beta_f, bool first) {
+  const int n = a.s.n;
+  auto snew = [&](size_t q) -> float {
+    float zq = __ldcg(zv + q);
+    return first ? zq : zq + beta_f * __ldcg(so + q);
+  };
+  if (MODE == FLIPGPU_SOLVE_REF) {
+    const float Lc = a.L[c];
+    auto xref = [&](int qi, int qj, int qk) -> float {
+      qi = min(max(0, qi), n - 1);
+      qj = min(max(0, qj), n - 1);
+      qk = min(max(0, qk), n - 1);
+      size_t q = cell_id(n, qi, qj, qk);
+      uint8_t aa = a.A[q];
+      if (aa == CELL_FLUID) return q == c ? sc : snew(q);
+      if (aa == CELL_WALL) return sc;
+      return a.s.subcell ? (float)((double)a.L[q] / fmin(1.0e-6, (double)Lc) * (double)sc)
+                         : 0.0f;
+    };
+    double v = 6.0 * (double)sc;
+    v -= (double)xref(i + 1, j, k);
+    v -= (double)xref(i - 1, j, k);
+    v -= (double)xref(i, j + 1, k);
+    v -= (double)xref(i, j - 1, k);
+    v -= (double)xref(i, j, k + 1);
+    v -= (double)xref(i, j, k - 1);
+    return a.s.pow2 ? (float)(v * a.s.inv_h2) : (float)(v / a.s.h2);
+  } else {
+    float acc = a.diag[c] * sc;
+    const size_t sj = n, si = (size_t)n * n;
+    if (i + 1 < n && a.A[c + si] == CELL_FLUID) acc -= snew(c + si);
+    if (i > 0 && a.A[c - si] == CELL_FLUID) acc -= snew(c - si);
+    if (j + 1 < n && a.A[c + sj] == CELL_FLUID) acc -= snew(c + sj);
+    if (j > 0 && a.A[c - sj] == CELL_FLUID) acc -= snew(c - sj);
+    if (k + 1 < n && a.A[c + 1] == CELL_FLUID) acc -= snew(c + 1);
+    if (k > 0 && a.A[c - 1] == CELL_FLUID) acc -= snew(c - 1);
+    return acc * a.s.inv_h2_f;
+  }
+}
+
+/* z = M^-1 r at one FLUID cell (REF: the reference's preconditioner with no
+ * entry equal to 1.0, signed zeros included; FAST: Jacobi). */
+template <int MODE>
+__device__ __forceinline__ float cg_precond(const CgArgs &a, size_t c, int i, int j, int k,
+                                            float rc) {
+  if (MODE == FLIPGPU_SOLVE_REF) {
+    const int n = a.s.n;
+    const uint8_t *A = a.A;
+    double t = (double)rc;
+    if (rc == 0.0f) {
+      bool back = (i > 0 && A[cell_id(n, i - 1, j, k)] == CELL_FLUID) ||
+                  (j > 0 && A[cell_id(n, i, j - 1, k)] == CELL_FLUID) ||
+                  (k > 0 && A[cell_id(n, i, j, k - 1)] == CELL_FLUID);
+      t = (signbit(rc) && !back) ? -0.0 : 0.0;
+    }
+    const double pc = a.P[c];
+    double q = t * pc;
+    double t2 = q;
+    if (q == 0.0) {
+      bool fwd = (i + 1 < n && A[cell_id(n, i + 1, j, k)] == CELL_FLUID) ||
+                 (j + 1 < n && A[cell_id(n, i, j + 1, k)] == CELL_FLUID) ||
+                 (k + 1 < n && A[cell_id(n, i, j, k + 1)] == CELL_FLUID);
+      t2 = (signbit(q) && !fwd) ? -0.0 : 0.0;
+    }
+    return (float)(t2 * pc);
+  } else {
+    return rc * a.Pf[c];
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
+  const unsigned nb = gridDim.x;
+  const size_t stride = (size_t)nb * CG_BLOCK;
+  const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
+  const int n = a.s.n;
+  const size_t nc = a.nc;
+
+  /* phase 0: r = b - A x, z = M^-1 r; b.b, r.r, z.r */
+  double pbb = 0.0, prr = 0.0, pzr = 0.0;
+  for (size_t c = t0; c < nc; c += stride) {
+    float rv = 0.0f, zv = 0.0f;
+    if (a.A[c] == CELL_FLUID) {
+      int i, j, k;
+      decode(c, n, i, j, k);
+      float bc = a.b[c];
+      pbb += (double)(bc * bc);
+      float xc = a.x[c];
+      /* the initial matvec reads x, which nobody writes in this phase */
+      float ax = cg_matvec<MODE>(a, c, i, j, k, xc, a.x, a.x, 0.0f, true);
+      rv = bc + -1.0f * ax;
+      prr += (double)(rv * rv);
+      zv = cg_precond<MODE>(a, c, i, j, k, rv);
+      pzr += (double)(zv * rv);
+    }
+    a.r[c] = rv;
+    a.z[c] = zv;
+  }
+  {
+    double t = block_sum_double<CG_BLOCK>(pbb);
+    double u = block_sum_double<CG_BLOCK>(prr);
+    double v = block_sum_double<CG_BLOCK>(pzr);
+    if (threadIdx.x == 0) {
+      a.part[0 * (size_t)nb + blockIdx.x] = t;
+      a.part[1 * (size_t)nb + blockIdx.x] = u;
+      a.part[2 * (size_t)nb + blockIdx.x] = v;
+    }
+  }
+  if (!grid_barrier(a.bar, a.iflags)) return;
+  const double b2 = sum_partials(a.part, 0, nb);
+  double rr = sum_partials(a.part, 1, nb);
+  double azr = sum_partials(a.part, 2, nb);
+  double eps;
+  if (MODE == FLIPGPU_SOLVE_REF) {
+    eps = a.ref_eps;
+    if (a.eps_abs >= 0.0) {
+      eps = a.eps_abs;
+    } else if (a.rel_tol > 0.0) {
+      double target = a.rel_tol * a.rel_tol * b2;
+      while (eps > target && eps > 0.0) eps *= 0.25;
+    }
+  } else {
+    eps = a.rel_tol * a.rel_tol * b2;
+  }
+  int done = 0, iters = 0;
+  double e2 = rr;
+  if (MODE != FLIPGPU_SOLVE_REF && rr <= eps) done = 1;
+  float *so = a.s0, *sn = a.s1;
+  float beta_f = 0.0f;
+  bool first = true;
+  while (!done) {
+    /* phase A: s_new = z + beta*s_old (op), w = A s_new, w.s_new */
+    double pws = 0.0;
+    for (size_t c = t0; c < nc; c += stride) {
+      float snv = 0.0f, wv = 0.0f;
+      if (a.A[c] == CELL_FLUID) {
+        int i, j, k;
+        decode(c, n, i, j, k);
+        float zc = a.z[c];
+        snv = first ? zc : zc + beta_f * so[c];
+        wv = cg_matvec<MODE>(a, c, i, j, k, snv, a.z, so, beta_f, first);
+        pws += (double)(wv * snv);
+      }
+      sn[c] = snv;
+      a.w[c] = wv;
+    }
+    {
+      double t = block_sum_double<CG_BLOCK>(pws);
+      if (threadIdx.x == 0) a.part[3 * (size_t)nb + blockIdx.x] = t;
+    }
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    const double alpha = azr / sum_partials(a.part, 3, nb);
+    const float alpha_f = (float)alpha, nalpha_f = (float)(-alpha);
+    /* phase B: x += alpha s, r -= alpha w, z = M^-1 r; r.r, z.r */
+    prr = 0.0;
+    pzr = 0.0;
+    for (size_t c = t0; c < nc; c += stride) {
+      if (a.A[c] == CELL_FLUID) {
+        int i, j, k;
+        decode(c, n, i, j, k);
+        a.x[c] = a.x[c] + alpha_f * sn[c];
+        float rv = a.r[c] + nalpha_f * a.w[c];
+        a.r[c] = rv;
+        prr += (double)(rv * rv);
+        float zv = cg_precond<MODE>(a, c, i, j, k, rv);
+        a.z[c] = zv;
+        pzr += (double)(zv * rv);
+      } else {
+        a.x[c] = 0.0f;
+        a.r[c] = 0.0f;
+        a.z[c] = 0.0f;
+      }
+    }
+    {
+      double t = block_sum_double<CG_BLOCK>(prr);
+      double u = block_sum_double<CG_BLOCK>(pzr);
+      if (threadIdx.x == 0) {
+        a.part[4 * (size_t)nb + blockIdx.x] = t;
+        a.part[5 * (size_t)nb + blockIdx.x] = u;
+      }
+    }
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    rr = sum_partials(a.part, 4, nb);
+    const double zr = sum_partials(a.part, 5, nb);
+    iters++;
+    e2 = (MODE == FLIPGPU_SOLVE_REF) ? (double)(float)rr : rr;
+    if (e2 <= eps) done = 1;
+    else if (!(e2 == e2)) done = 2;
+    else if (iters >= a.max_iters) done = 3;
+    const double beta = zr / azr;
+    azr = zr;
+    beta_f = (float)beta;
+    first = false;
+    float *t = so;
+    so = sn;
+    sn = t;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.iflags[IF_DONE] = done;
+    a.iflags[IF_ITERS] = iters;
+    a.iflags[IF_NAN] = done == 2;
+    a.scal[SC_ERR2] = e2;
+    a.scal[SC_B2] = b2;
+    a.scal[SC_EPS] = eps;
+  }
+}
+
 } // namespace
+
+static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
+  double sc[SC_COUNT];
+  int host_flags[IF_COUNT];
+  cudaMemcpyAsync(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(host_flags, h->iflags, sizeof(host_flags), cudaMemcpyDeviceToHost, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    snprintf(h->err, sizeof h->err, "solve: %s", cudaGetErrorString(e));
+    return FLIPGPU_ECUDA;
+  }
+  int status = FLIPGPU_OK;
+  if (host_flags[IF_TIMEOUT]) status = FLIPGPU_ETIMEOUT;
+  else if (host_flags[IF_NAN]) status = FLIPGPU_ENAN;
+  else if (host_flags[IF_DONE] == 3) status = FLIPGPU_ENOCONV;
+  if (st) {
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    st->iterations = host_flags[IF_ITERS];
+    st->status = status;
+    st->r2 = sc[SC_ERR2];
+    st->b2 = sc[SC_B2];
+    st->ms = ms;
+  }
+  if (status == FLIPGPU_ETIMEOUT) {
+    snprintf(h->err, sizeof h->err, "solve: a grid barrier wait expired");
+    return status;
+  }
+  if (status == FLIPGPU_ENAN) {
+    snprintf(h->err, sizeof h->err, "solve: non-finite residual");
+    return status;
+  }
+  /* the reference stops silently at its cap */
+  if (status == FLIPGPU_ENOCONV && mode != FLIPGPU_SOLVE_REF) {
+    snprintf(h->err, sizeof h->err, "solve: no convergence in %d iterations", host_flags[IF_ITERS]);
+    return status;
+  }
+  return FLIPGPU_OK;
+}
 
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   const int n = h->n;
@@ -464,6 +788,53 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
                             mode == FLIPGPU_SOLVE_REF ? nullptr : h->diag,
                             precond == FLIPGPU_PRECOND_JACOBI ? h->Pf : nullptr, h->iflags);
   FG_LAUNCHED(h, 1);
+  /* persistent single-launch CG unless the REF preconditioner has an entry
+   * equal to 1.0 (then its neighbour terms act and it runs sequentially) */
+  bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid > 0;
+  if (persistent && mode == FLIPGPU_SOLVE_REF) {
+    int exotic = 0;
+    cudaMemcpyAsync(&exotic, h->iflags + IF_EXOTIC, sizeof(int), cudaMemcpyDeviceToHost, S);
+    cudaStreamSynchronize(S);
+    persistent = exotic == 0;
+  }
+  if (persistent) {
+    CgArgs a;
+    a.s = sa;
+    a.nc = nc;
+    a.A = h->A;
+    a.L = h->L;
+    a.b = h->div;
+    a.x = h->press;
+    a.r = h->r;
+    a.z = h->z;
+    a.s0 = h->s;
+    a.s1 = h->s1;
+    a.w = h->w;
+    a.P = h->P;
+    a.diag = h->diag;
+    a.Pf = h->Pf;
+    a.part = h->partial;
+    a.bar = h->bar;
+    a.iflags = h->iflags;
+    a.scal = h->scal;
+    a.eps_abs = h->prm.eps_abs;
+    a.rel_tol = h->prm.rel_tol;
+    a.ref_eps = ref_eps;
+    a.max_iters = max_iters;
+    cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
+    void *kargs[] = {&a};
+    cudaError_t e = cudaLaunchCooperativeKernel(
+        mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
+                                  : (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
+        dim3(h->cg_grid), dim3(CG_BLOCK), kargs, 0, S);
+    FG_LAUNCHED(h, 1);
+    if (e != cudaSuccess) {
+      snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
+      return FLIPGPU_ECUDA;
+    }
+    cudaEventRecord(h->ev1, S);
+    return finish_stats(h, st, mode);
+  }
   if (mode == FLIPGPU_SOLVE_REF) {
     k_build_ref_seq<<<1, 1, 0, S>>>(n, h->A, h->P, nullptr, h->iflags, h->L, h->prm.subcell);
     FG_LAUNCHED(h, 1);
@@ -566,4 +937,22 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     return status;
   }
   return FLIPGPU_OK;
+}
+
+int cg_grid_size(int *out) {
+  int dev = 0, sms = 0, per_sm_ref = 0, per_sm_fast = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  if (!coop) {
+    *out = 0;
+    return 0;
+  }
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ref, k_cg<FLIPGPU_SOLVE_REF>, CG_BLOCK, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_fast, k_cg<FLIPGPU_SOLVE_FAST>, CG_BLOCK, 0);
+  int per_sm = per_sm_ref < per_sm_fast ? per_sm_ref : per_sm_fast;
+  if (per_sm > 4) per_sm = 4;
+  *out = sms * per_sm;
+  return 0;
 }
