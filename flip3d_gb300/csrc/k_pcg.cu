@@ -489,19 +489,35 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags) {
   return ok != 0;
 }
 
-/* Sum of the nb partials of slot k, identical in every block (fixed order). */
-__device__ __forceinline__ double sum_partials(const double *part, int k, unsigned nb) {
-  __shared__ double res;
-  if (threadIdx.x < 32) {
-    double v = 0.0;
-    for (unsigned i = threadIdx.x; i < nb; i += 32) v += __ldcg(part + (size_t)k * nb + i);
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (threadIdx.x == 0) res = v;
+/* Sums of the nb partials of slots k0 and k1 (k1 < 0: none), identical in
+ * every block: each thread loads its strided share (one L2 round trip), then
+ * a fixed shuffle/shared-memory tree. */
+__device__ __forceinline__ void sum_partials(const double *part, int k0, int k1, unsigned nb,
+                                             double &out0, double &out1) {
+  __shared__ double w0[CG_BLOCK / 32], w1[CG_BLOCK / 32];
+  double v0 = 0.0, v1 = 0.0;
+  for (unsigned i = threadIdx.x; i < nb; i += CG_BLOCK) {
+    v0 += __ldcg(part + (size_t)k0 * nb + i);
+    if (k1 >= 0) v1 += __ldcg(part + (size_t)k1 * nb + i);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    w0[wid] = v0;
+    w1[wid] = v1;
   }
   __syncthreads();
-  double r = res;
+  double a0 = 0.0, a1 = 0.0;
+  for (int i = 0; i < CG_BLOCK / 32; i++) {
+    a0 += w0[i];
+    a1 += w1[i];
+  }
   __syncthreads();
-  return r;
+  out0 = a0;
+  out1 = a1;
 }
 
 template <int MODE>
@@ -616,9 +632,9 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
     }
   }
   if (!grid_barrier(a.bar, a.iflags)) return;
-  const double b2 = sum_partials(a.part, 0, nb);
-  double rr = sum_partials(a.part, 1, nb);
-  double azr = sum_partials(a.part, 2, nb);
+  double b2, rr, azr, unused;
+  sum_partials(a.part, 0, 1, nb, b2, rr);
+  sum_partials(a.part, 2, -1, nb, azr, unused);
   double eps;
   if (MODE == FLIPGPU_SOLVE_REF) {
     eps = a.ref_eps;
@@ -658,7 +674,9 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
       if (threadIdx.x == 0) a.part[3 * (size_t)nb + blockIdx.x] = t;
     }
     if (!grid_barrier(a.bar, a.iflags)) return;
-    const double alpha = azr / sum_partials(a.part, 3, nb);
+    double ws;
+    sum_partials(a.part, 3, -1, nb, ws, unused);
+    const double alpha = azr / ws;
     const float alpha_f = (float)alpha, nalpha_f = (float)(-alpha);
     /* phase B: x += alpha s, r -= alpha w, z = M^-1 r; r.r, z.r */
     prr = 0.0;
@@ -689,8 +707,8 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
       }
     }
     if (!grid_barrier(a.bar, a.iflags)) return;
-    rr = sum_partials(a.part, 4, nb);
-    const double zr = sum_partials(a.part, 5, nb);
+    double zr;
+    sum_partials(a.part, 4, 5, nb, rr, zr);
     iters++;
     e2 = (MODE == FLIPGPU_SOLVE_REF) ? (double)(float)rr : rr;
     if (e2 <= eps) done = 1;
