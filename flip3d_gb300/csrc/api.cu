@@ -52,6 +52,12 @@ float smallest_float_ge(double d) {
   if ((double)f < d) f = nextafterf(f, INFINITY);
   return f;
 }
+/* 1/x when x is an exact power of two (the reciprocal is then exact), else 0 */
+float pow2_rcp(float x) {
+  int e;
+  float m = frexpf(x, &e);
+  return (x > 0.0f && m == 0.5f) ? ldexpf(1.0f, 1 - e) : 0.0f;
+}
 void split(double v, float &hi, float &lo) {
   hi = (float)v;
   lo = (float)(v - (double)hi);
@@ -207,11 +213,13 @@ SimConst make_const(const FlipGpu *h) {
   c.density = p.density;
   float kh = (float)(4.0 * (double)p.density / n);
   c.kd_hh = kh * kh;
+  c.kd_rcp = pow2_rcp(c.kd_hh);
   c.max_dens = h->max_dens;
   const float RE = (float)1.4;
   c.re_p2g_hh = RE * RE;
   c.re_corr = (float)((double)p.density / n);
   c.re_corr_hh = c.re_corr * c.re_corr;
+  c.corr_rcp = pow2_rcp(c.re_corr_hh);
   c.re_repo = (float)(1.0 / n);
   c.re_repo_hh = c.re_repo * c.re_repo;
   c.r2_floor = smallest_float_ge(1.0e-5);
@@ -226,6 +234,7 @@ SimConst make_const(const FlipGpu *h) {
   c.corr_near_thr = largest_float_le(0.1 * (double)c.re_corr);
   double re2 = (double)c.re_corr * (double)c.re_corr;
   c.corr_cut2 = smallest_float_ge(re2 * (1.0 + 1.0 / 256.0));
+  c.corr_reach = smallest_float_ge((double)c.re_corr * (1.0 + 1.0 / 256.0));
   c.dt = p.dt;
   c.dt_f = (float)p.dt;
   split(p.dt, c.dt_h, c.dt_l);
@@ -335,8 +344,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
     delete h;
     return FLIPGPU_ECUDA;
   }
-  if (cg_grid_size(&h->cg_grid) != 0) h->cg_grid = 0;
-  if (h->cg_grid * 6 > 8192) h->cg_grid = 8192 / 6;
+  if (cg_grid_size(h->cg_grid) != 0) h->cg_grid[0] = h->cg_grid[1] = h->cg_grid[2] = 0;
   *out = h;
   return FLIPGPU_OK;
 }

@@ -71,4 +71,63 @@ __device__ __forceinline__ uint32_t block_sum_u32(uint32_t v) {
   return r;
 }
 
+/* Double-float accumulator: hi + lo carries about 44+ significant bits with
+ * FP32 instructions only (Knuth TwoSum; products split exactly by FMA). Used
+ * for dot products, where per-element FP64 is GB300's bottleneck. */
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_zero() { return FF{0.0f, 0.0f}; }
+
+/* acc += b (b a float) */
+__device__ __forceinline__ void ff_add(FF &a, float b) {
+  float s, e;
+  refmath::two_sum(a.hi, b, s, e);
+  a.hi = s;
+  a.lo += e;
+}
+
+/* acc += x*y with the product kept exact */
+__device__ __forceinline__ void ff_add_prod(FF &a, float x, float y) {
+  float p = x * y;
+  float pe = fmaf(x, y, -p);
+  ff_add(a, p);
+  a.lo += pe;
+}
+
+__device__ __forceinline__ FF ff_merge(FF a, FF b) {
+  float s, e;
+  refmath::two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  float hi = s + e;
+  float lo = e - (hi - s);
+  return FF{hi, lo};
+}
+
+__device__ __forceinline__ FF ff_shfl_down(FF v, int o) {
+  return FF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+}
+
+/* Block sum in a fixed tree; the result is valid in every thread. */
+template <int BLOCK> __device__ __forceinline__ FF block_sum_ff(FF v) {
+  __shared__ FF warp_part[BLOCK / 32];
+  __shared__ FF total;
+  for (int o = 16; o > 0; o >>= 1) v = ff_merge(v, ff_shfl_down(v, o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_part[wid] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    FF t = warp_part[0];
+    for (int i = 1; i < BLOCK / 32; i++) t = ff_merge(t, warp_part[i]);
+    total = t;
+  }
+  __syncthreads();
+  FF r = total;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double ff_to_double(FF v) { return (double)v.hi + (double)v.lo; }
+
 #endif

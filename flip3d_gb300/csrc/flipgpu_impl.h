@@ -27,6 +27,8 @@ struct SimConst {
   float h;            /* (float)(1.0/n): cell width (src/flip3D.cpp:809) */
   float density;      /* DENSITY */
   float kd_hh;        /* density kernel radius^2: h*h of (float)(4*DENSITY/N) */
+  float kd_rcp;       /* 1/kd_hh when kd_hh is a power of two, else 0 */
+  float corr_rcp;     /* 1/re_corr_hh when it is a power of two, else 0 */
   float max_dens;
   float re_p2g_hh;    /* RE*RE for P2G (src/mapper.cpp:14) */
   float re_corr;      /* DENSITY/N (src/flip3D.cpp:1242) */
@@ -42,6 +44,7 @@ struct SimConst {
   float push_re_thr;  /* largest float < push_re */
   float corr_near_thr;/* largest float <= 0.1*re (src/corrector.cpp:68) */
   float corr_cut2;    /* squared distance beyond which the spring weight is 0 */
+  float corr_reach;   /* re*(1+2^-8): cell-range reach of the corrector */
   float dt_f;         /* (float)DT, the corrector's dt */
   double dt;
   float dt_h, dt_l;   /* DT split into floats */
@@ -102,7 +105,7 @@ struct FlipGpu {
   double *scal;       /* device scalars of the CG recurrence */
   int *iflags;        /* device flags/counters */
   unsigned *bar;      /* grid barrier of the persistent CG: count, generation */
-  int cg_grid;        /* blocks of the cooperative CG launch (0 = unavailable) */
+  int cg_grid[3];     /* cooperative CG grids: REF, FAST, FAST quads (0 = unavailable) */
   int npartial;
 
   /* reposition */

@@ -93,7 +93,7 @@ k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restric
     float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) == CELL_WALL) return;
     float d2 = hypot2_ref(Q.x - P.x, Q.y - P.y, Q.z - P.z);
-    wsum += smooth_ref(d2, c.kd_hh);
+    wsum += c.kd_rcp != 0.0f ? smooth_ref_pow2(d2, c.kd_rcp) : smooth_ref(d2, c.kd_hh);
   });
   float d = wsum / c.max_dens;
   dens[p] = d;
@@ -403,65 +403,100 @@ __global__ void k_repo_resample(SimConst c, const int *__restrict__ counts,
 
 /* ------------------------------------------------------ corrector */
 
-/* Spring displacement (src/corrector.cpp:54-100): writes the moved position
- * to the canonical arrays (neighbours are read from the sorted snapshot). A
- * neighbour whose float squared distance exceeds corr_cut2 has weight
- * exactly 0 (its distance is at least re*(1+2^-9)) and adds nothing. */
+/* Cells that can hold a particle within `reach` (world units) of p along one
+ * axis, intersected with the reference's neighbourhood [c0-1, c0+1]. A
+ * particle q lies in cell clamp(floor(n*q), 0, n-1), so one within reach lies
+ * in clamp(floor(n(p-reach')), 0, n-1) .. clamp(floor(n(p+reach')), 0, n-1);
+ * reach' carries a 2^-8 margin against rounding. */
+__device__ __forceinline__ void reach_range(float p, float reach_m, float fn, int n, int c0,
+                                            int &lo, int &hi) {
+  int a = min(max((int)floorf(fn * (p - reach_m)), 0), n - 1);
+  int b = min(max((int)floorf(fn * (p + reach_m)), 0), n - 1);
+  lo = max(c0 - 1, a);
+  hi = min(c0 + 1, b);
+}
+
+constexpr int NEAR_CAP = 24; /* near-list batch per thread */
+
+/* Spring displacement (src/corrector.cpp:54-100). Two passes per batch: a
+ * cheap test collects the neighbours within re*(1+2^-8) into a per-thread
+ * list (all other neighbours have weight exactly 0 and add nothing), then
+ * the exact arithmetic runs over the list in the same order. Writes the
+ * moved position to the canonical arrays; neighbours come from the sorted
+ * snapshot. */
 __global__ void __launch_bounds__(BLK)
 k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
          const float4 *__restrict__ spos, const float *__restrict__ nx,
          const float *__restrict__ ny, const float *__restrict__ nz, float *__restrict__ px,
          float *__restrict__ py, float *__restrict__ pz) {
+  __shared__ uint32_t near_list[NEAR_CAP][BLK];
   int a = blockIdx.x * BLK + threadIdx.x;
-  if (a >= c.np) return;
-  float4 P = spos[a];
-  if (unpack_type(P.w) != CELL_FLUID) return;
+  bool active = a < c.np;
+  float4 P = active ? spos[a] : make_float4(0, 0, 0, 0);
+  if (!active || unpack_type(P.w) != CELL_FLUID) return;
   uint32_t p = perm[a];
   const float re = c.re_corr;
   int x = cell_clamp_macro(P.x, c.fn), y = cell_clamp_macro(P.y, c.fn),
       z = cell_clamp_macro(P.z, c.fn);
+  int i0, i1, j0, j1, k0, k1;
+  reach_range(P.x, c.corr_reach, c.fn, c.n, x, i0, i1);
+  reach_range(P.y, c.corr_reach, c.fn, c.n, y, j0, j1);
+  reach_range(P.z, c.corr_reach, c.fn, c.n, z, k0, k1);
   float spring[3] = {0.0f, 0.0f, 0.0f};
-  visit_cells(c.n, cs, x - 1, x + 1, y - 1, y + 1, z - 1, z + 1, [&](uint32_t b) {
+  int cnt = 0;
+  auto flush = [&]() {
+    for (int t = 0; t < cnt; t++) {
+      uint32_t b = near_list[t][threadIdx.x];
+      float4 Q = __ldg(spos + b);
+      float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+      float dist = length_ref(dx, dy, dz);
+      float w = 50.0f * (c.corr_rcp != 0.0f ? smooth_ref_pow2(dist * dist, c.corr_rcp)
+                                            : smooth_ref(dist * dist, c.re_corr_hh));
+      if (dist > c.corr_near_thr) {
+        spring[0] += w * dx / dist * re;
+        spring[1] += w * dy / dist * re;
+        spring[2] += w * dz / dist * re;
+      } else if (unpack_type(Q.w) == CELL_FLUID) {
+        uint32_t o = perm[b];
+        for (int q = 0; q < 3; q++) {
+          uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)c.step, q),
+                                   (uint64_t)p, (uint64_t)o);
+          spring[q] = (float)((double)spring[q] + 0.01 * (double)re / (double)c.dt_f *
+                                                      (double)(int)(r % 101) / 100.0);
+        }
+      } else {
+        uint32_t o = perm[b];
+        float nn[3] = {nx[o], ny[o], nz[o]};
+        for (int q = 0; q < 3; q++)
+          spring[q] = (float)((double)spring[q] +
+                              0.05 * (double)re / (double)c.dt_f * (double)nn[q]);
+      }
+    }
+    cnt = 0;
+  };
+  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     if (b == (uint32_t)a) return;
     float4 Q = __ldg(spos + b);
-    float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-    if (hypot2_ref(dx, dy, dz) > c.corr_cut2) return;
-    float dist = length_ref(dx, dy, dz);
-    float w = 50.0f * smooth_ref(dist * dist, c.re_corr_hh);
-    if (dist > c.corr_near_thr) {
-      spring[0] += w * dx / dist * re;
-      spring[1] += w * dy / dist * re;
-      spring[2] += w * dz / dist * re;
-    } else if (unpack_type(Q.w) == CELL_FLUID) {
-      uint32_t o = perm[b];
-      for (int q = 0; q < 3; q++) {
-        uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)c.step, q),
-                                 (uint64_t)p, (uint64_t)o);
-        spring[q] = (float)((double)spring[q] + 0.01 * (double)re / (double)c.dt_f *
-                                                    (double)(int)(r % 101) / 100.0);
-      }
-    } else {
-      uint32_t o = perm[b];
-      float nn[3] = {nx[o], ny[o], nz[o]};
-      for (int q = 0; q < 3; q++)
-        spring[q] = (float)((double)spring[q] +
-                            0.05 * (double)re / (double)c.dt_f * (double)nn[q]);
-    }
+    if (hypot2_ref(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
+    near_list[cnt][threadIdx.x] = b;
+    if (++cnt == NEAR_CAP) flush();
   });
+  flush();
   px[p] = P.x + c.dt_f * spring[0];
   py[p] = P.y + c.dt_f * spring[1];
   pz[p] = P.z + c.dt_f * spring[2];
 }
 
 /* Velocity resample at the moved position (src/corrector.cpp:91-114 with
- * resample at :15-47), then the commit (the position was already
- * written). */
+ * resample at :15-47): the same reach restriction and near list, with the
+ * sharp kernel's exact support test r2 < re^2. */
 __global__ void __launch_bounds__(BLK)
 k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
            const float4 *__restrict__ spos, const float4 *__restrict__ svel,
            const float *__restrict__ px, const float *__restrict__ py,
            const float *__restrict__ pz, float *__restrict__ vx, float *__restrict__ vy,
            float *__restrict__ vz) {
+  __shared__ uint32_t near_list[NEAR_CAP][BLK];
   int a = blockIdx.x * BLK + threadIdx.x;
   if (a >= c.np) return;
   if (unpack_type(spos[a].w) != CELL_FLUID) return;
@@ -469,20 +504,36 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
   float T[3] = {px[p], py[p], pz[p]};
   int ci = cell_clamp(T[0], c.fn, c.n), cj = cell_clamp(T[1], c.fn, c.n),
       ck = cell_clamp(T[2], c.fn, c.n);
+  int i0, i1, j0, j1, k0, k1;
+  reach_range(T[0], c.corr_reach, c.fn, c.n, ci, i0, i1);
+  reach_range(T[1], c.corr_reach, c.fn, c.n, cj, j0, j1);
+  reach_range(T[2], c.corr_reach, c.fn, c.n, ck, k0, k1);
   float u[3] = {0.0f, 0.0f, 0.0f};
   float wsum = 0.0f;
-  visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+  int cnt = 0;
+  auto flush = [&]() {
+    for (int t = 0; t < cnt; t++) {
+      uint32_t b = near_list[t][threadIdx.x];
+      float4 Q = __ldg(spos + b);
+      float d2 = hypot2_ref(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
+      float w = sharp_ref(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
+      float4 V = __ldg(svel + b);
+      u[0] += w * V.x;
+      u[1] += w * V.y;
+      u[2] += w * V.z;
+      wsum += w;
+    }
+    cnt = 0;
+  };
+  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) != CELL_FLUID) return;
     float d2 = hypot2_ref(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
     if (!(d2 < c.re_corr_hh)) return;
-    float w = sharp_ref(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
-    float4 V = __ldg(svel + b);
-    u[0] += w * V.x;
-    u[1] += w * V.y;
-    u[2] += w * V.z;
-    wsum += w;
+    near_list[cnt][threadIdx.x] = b;
+    if (++cnt == NEAR_CAP) flush();
   });
+  flush();
   if (wsum != 0.0f) {
     vx[p] = u[0] / wsum;
     vy[p] = u[1] / wsum;

@@ -451,7 +451,7 @@ struct CgArgs {
   const double *P;
   const float *diag;
   const float *Pf;
-  double *part;
+  float2 *part;
   unsigned *bar;
   int *iflags;
   double *scal;
@@ -489,35 +489,35 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags) {
   return ok != 0;
 }
 
-/* Sums of the nb partials of slots k0 and k1 (k1 < 0: none), identical in
- * every block: each thread loads its strided share (one L2 round trip), then
- * a fixed shuffle/shared-memory tree. */
-__device__ __forceinline__ void sum_partials(const double *part, int k0, int k1, unsigned nb,
+/* Sums of the nb float-pair partials of slots k0 and k1 (k1 < 0: none),
+ * identical in every block: strided loads, then a fixed merge tree. */
+__device__ __forceinline__ void sum_partials(const float2 *part, int k0, int k1, unsigned nb,
                                              double &out0, double &out1) {
-  __shared__ double w0[CG_BLOCK / 32], w1[CG_BLOCK / 32];
-  double v0 = 0.0, v1 = 0.0;
+  FF v0 = ff_zero(), v1 = ff_zero();
   for (unsigned i = threadIdx.x; i < nb; i += CG_BLOCK) {
-    v0 += __ldcg(part + (size_t)k0 * nb + i);
-    if (k1 >= 0) v1 += __ldcg(part + (size_t)k1 * nb + i);
+    float2 a = __ldcg(part + (size_t)k0 * nb + i);
+    v0 = ff_merge(v0, FF{a.x, a.y});
+    if (k1 >= 0) {
+      float2 b = __ldcg(part + (size_t)k1 * nb + i);
+      v1 = ff_merge(v1, FF{b.x, b.y});
+    }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    v0 += __shfl_down_sync(0xffffffffu, v0, o);
-    v1 += __shfl_down_sync(0xffffffffu, v1, o);
-  }
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) {
-    w0[wid] = v0;
-    w1[wid] = v1;
-  }
-  __syncthreads();
-  double a0 = 0.0, a1 = 0.0;
-  for (int i = 0; i < CG_BLOCK / 32; i++) {
-    a0 += w0[i];
-    a1 += w1[i];
-  }
-  __syncthreads();
-  out0 = a0;
-  out1 = a1;
+  out0 = ff_to_double(block_sum_ff<CG_BLOCK>(v0));
+  out1 = k1 >= 0 ? ff_to_double(block_sum_ff<CG_BLOCK>(v1)) : 0.0;
+}
+
+/* Dot-product term: REF mode sums the float-rounded product, as
+ * product() does (src/solver.cpp:51); FAST mode keeps the product exact. */
+template <int MODE> __device__ __forceinline__ void dot_acc(FF &acc, float x, float y) {
+  if (MODE == FLIPGPU_SOLVE_REF)
+    ff_add(acc, x * y);
+  else
+    ff_add_prod(acc, x, y);
+}
+
+__device__ __forceinline__ void store_partial(float2 *part, int k, unsigned nb, FF v) {
+  FF t = block_sum_ff<CG_BLOCK>(v);
+  if (threadIdx.x == 0) part[(size_t)k * nb + blockIdx.x] = make_float2(t.hi, t.lo);
 }
 
 template <int MODE>
@@ -602,35 +602,28 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
   const size_t nc = a.nc;
 
   /* phase 0: r = b - A x, z = M^-1 r; b.b, r.r, z.r */
-  double pbb = 0.0, prr = 0.0, pzr = 0.0;
+  FF pbb = ff_zero(), prr = ff_zero(), pzr = ff_zero();
   for (size_t c = t0; c < nc; c += stride) {
     float rv = 0.0f, zv = 0.0f;
     if (a.A[c] == CELL_FLUID) {
       int i, j, k;
       decode(c, n, i, j, k);
       float bc = a.b[c];
-      pbb += (double)(bc * bc);
+      dot_acc<MODE>(pbb, bc, bc);
       float xc = a.x[c];
       /* the initial matvec reads x, which nobody writes in this phase */
       float ax = cg_matvec<MODE>(a, c, i, j, k, xc, a.x, a.x, 0.0f, true);
       rv = bc + -1.0f * ax;
-      prr += (double)(rv * rv);
+      dot_acc<MODE>(prr, rv, rv);
       zv = cg_precond<MODE>(a, c, i, j, k, rv);
-      pzr += (double)(zv * rv);
+      dot_acc<MODE>(pzr, zv, rv);
     }
     a.r[c] = rv;
     a.z[c] = zv;
   }
-  {
-    double t = block_sum_double<CG_BLOCK>(pbb);
-    double u = block_sum_double<CG_BLOCK>(prr);
-    double v = block_sum_double<CG_BLOCK>(pzr);
-    if (threadIdx.x == 0) {
-      a.part[0 * (size_t)nb + blockIdx.x] = t;
-      a.part[1 * (size_t)nb + blockIdx.x] = u;
-      a.part[2 * (size_t)nb + blockIdx.x] = v;
-    }
-  }
+  store_partial(a.part, 0, nb, pbb);
+  store_partial(a.part, 1, nb, prr);
+  store_partial(a.part, 2, nb, pzr);
   if (!grid_barrier(a.bar, a.iflags)) return;
   double b2, rr, azr, unused;
   sum_partials(a.part, 0, 1, nb, b2, rr);
@@ -655,7 +648,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
   bool first = true;
   while (!done) {
     /* phase A: s_new = z + beta*s_old (op), w = A s_new, w.s_new */
-    double pws = 0.0;
+    FF pws = ff_zero();
     for (size_t c = t0; c < nc; c += stride) {
       float snv = 0.0f, wv = 0.0f;
       if (a.A[c] == CELL_FLUID) {
@@ -664,23 +657,20 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
         float zc = a.z[c];
         snv = first ? zc : zc + beta_f * so[c];
         wv = cg_matvec<MODE>(a, c, i, j, k, snv, a.z, so, beta_f, first);
-        pws += (double)(wv * snv);
+        dot_acc<MODE>(pws, wv, snv);
       }
       sn[c] = snv;
       a.w[c] = wv;
     }
-    {
-      double t = block_sum_double<CG_BLOCK>(pws);
-      if (threadIdx.x == 0) a.part[3 * (size_t)nb + blockIdx.x] = t;
-    }
+    store_partial(a.part, 3, nb, pws);
     if (!grid_barrier(a.bar, a.iflags)) return;
     double ws;
     sum_partials(a.part, 3, -1, nb, ws, unused);
     const double alpha = azr / ws;
     const float alpha_f = (float)alpha, nalpha_f = (float)(-alpha);
     /* phase B: x += alpha s, r -= alpha w, z = M^-1 r; r.r, z.r */
-    prr = 0.0;
-    pzr = 0.0;
+    prr = ff_zero();
+    pzr = ff_zero();
     for (size_t c = t0; c < nc; c += stride) {
       if (a.A[c] == CELL_FLUID) {
         int i, j, k;
@@ -688,24 +678,18 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
         a.x[c] = a.x[c] + alpha_f * sn[c];
         float rv = a.r[c] + nalpha_f * a.w[c];
         a.r[c] = rv;
-        prr += (double)(rv * rv);
+        dot_acc<MODE>(prr, rv, rv);
         float zv = cg_precond<MODE>(a, c, i, j, k, rv);
         a.z[c] = zv;
-        pzr += (double)(zv * rv);
+        dot_acc<MODE>(pzr, zv, rv);
       } else {
         a.x[c] = 0.0f;
         a.r[c] = 0.0f;
         a.z[c] = 0.0f;
       }
     }
-    {
-      double t = block_sum_double<CG_BLOCK>(prr);
-      double u = block_sum_double<CG_BLOCK>(pzr);
-      if (threadIdx.x == 0) {
-        a.part[4 * (size_t)nb + blockIdx.x] = t;
-        a.part[5 * (size_t)nb + blockIdx.x] = u;
-      }
-    }
+    store_partial(a.part, 4, nb, prr);
+    store_partial(a.part, 5, nb, pzr);
     if (!grid_barrier(a.bar, a.iflags)) return;
     double zr;
     sum_partials(a.part, 4, 5, nb, rr, zr);
@@ -717,6 +701,274 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
     const double beta = zr / azr;
     azr = zr;
     beta_f = (float)beta;
+    first = false;
+    float *t = so;
+    so = sn;
+    sn = t;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.iflags[IF_DONE] = done;
+    a.iflags[IF_ITERS] = iters;
+    a.iflags[IF_NAN] = done == 2;
+    a.scal[SC_ERR2] = e2;
+    a.scal[SC_B2] = b2;
+    a.scal[SC_EPS] = eps;
+  }
+}
+
+/* FAST-mode CG on quads of 4 consecutive k-cells (n % 4 == 0): 16-byte
+ * loads, every neighbour load of a quad issued together, k-neighbours passed
+ * between lanes by shuffles (a warp's lanes hold consecutive quads of a
+ * k-row), quads without fluid skipped after phase 0 (their vectors stay 0).
+ * Warps walk tiles of 32 quads so that shuffles always see a full warp. */
+struct QuadNb {
+  float4 sn;      /* s_new at the neighbour quad (0 where not FLUID) */
+};
+
+__device__ __forceinline__ bool fl(unsigned char a) { return a == CELL_FLUID; }
+
+__device__ __forceinline__ float4 quad_snew(uchar4 A4, float4 z4, float4 so4, float beta,
+                                            bool first) {
+  float4 r;
+  r.x = fl(A4.x) ? (first ? z4.x : z4.x + beta * so4.x) : 0.0f;
+  r.y = fl(A4.y) ? (first ? z4.y : z4.y + beta * so4.y) : 0.0f;
+  r.z = fl(A4.z) ? (first ? z4.z : z4.z + beta * so4.z) : 0.0f;
+  r.w = fl(A4.w) ? (first ? z4.w : z4.w + beta * so4.w) : 0.0f;
+  return r;
+}
+
+/* s_new of the quad and of its i/j neighbours, then w = A s_new. src_z is z
+ * (or x in phase 0 with first=true). Returns sn4 and w4. Every lane must
+ * call it (shuffles). */
+__device__ __forceinline__ void quad_matvec(const CgArgs &a, size_t q, bool valid, int qrow,
+                                            size_t qplane, int i, int j, int kq,
+                                            const float *src_z, const float *so, float beta,
+                                            bool first, float4 &sn4, float4 &w4,
+                                            uchar4 &A4) {
+  const int n = a.s.n;
+  const uchar4 *A4p = reinterpret_cast<const uchar4 *>(a.A);
+  const float4 *z4p = reinterpret_cast<const float4 *>(src_z);
+  const float4 *so4p = reinterpret_cast<const float4 *>(so);
+  A4 = valid ? A4p[q] : make_uchar4(0, 0, 0, 0);
+  const bool any = fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w);
+  sn4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (any) {
+    float4 z4 = __ldcg(z4p + q);
+    float4 so4 = first ? z4 : __ldcg(so4p + q);
+    sn4 = quad_snew(A4, z4, so4, beta, first);
+  }
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  float left = __shfl_up_sync(FULL, sn4.w, 1);
+  int left_fl = __shfl_up_sync(FULL, (int)fl(A4.w), 1);
+  float right = __shfl_down_sync(FULL, sn4.x, 1);
+  int right_fl = __shfl_down_sync(FULL, (int)fl(A4.x), 1);
+  w4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!any) return;
+  const size_t c0 = 4 * q;
+  const int k0 = 4 * kq;
+  /* k-1 of the first cell and k+1 of the last */
+  if (k0 == 0) {
+    left_fl = 0;
+  } else if (lane == 0) {
+    unsigned char al = a.A[c0 - 1];
+    left_fl = fl(al);
+    if (left_fl) {
+      float zl = __ldcg(src_z + c0 - 1);
+      left = first ? zl : zl + beta * __ldcg(so + c0 - 1);
+    }
+  }
+  if (k0 + 4 >= n) {
+    right_fl = 0;
+  } else if (lane == 31) {
+    unsigned char ar = a.A[c0 + 4];
+    right_fl = fl(ar);
+    if (right_fl) {
+      float zr = __ldcg(src_z + c0 + 4);
+      right = first ? zr : zr + beta * __ldcg(so + c0 + 4);
+    }
+  }
+  (void)qrow;
+  /* i/j neighbours: issue all loads first */
+  const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
+  const long off[4] = {(long)qplane, -(long)qplane, (long)qrow, -(long)qrow};
+  uchar4 An[4];
+  float4 zn[4], son[4];
+#pragma unroll
+  for (int d = 0; d < 4; d++) {
+    if (has[d]) {
+      size_t qq = (size_t)((long)q + off[d]);
+      An[d] = A4p[qq];
+      zn[d] = __ldcg(z4p + qq);
+      son[d] = first ? zn[d] : __ldcg(so4p + qq);
+    } else {
+      An[d] = make_uchar4(0, 0, 0, 0);
+      zn[d] = son[d] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  const float4 d4 = __ldg(reinterpret_cast<const float4 *>(a.diag) + q);
+  float acc[4] = {d4.x * sn4.x, d4.y * sn4.y, d4.z * sn4.z, d4.w * sn4.w};
+#pragma unroll
+  for (int d = 0; d < 4; d++) {
+    float4 v = quad_snew(An[d], zn[d], son[d], beta, first);
+    acc[0] -= v.x;
+    acc[1] -= v.y;
+    acc[2] -= v.z;
+    acc[3] -= v.w;
+  }
+  const float snv[4] = {sn4.x, sn4.y, sn4.z, sn4.w};
+  const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+  /* k neighbours inside the quad and across it */
+  acc[0] -= (fv[1] ? snv[1] : 0.0f) + (left_fl ? left : 0.0f);
+  acc[1] -= (fv[0] ? snv[0] : 0.0f) + (fv[2] ? snv[2] : 0.0f);
+  acc[2] -= (fv[1] ? snv[1] : 0.0f) + (fv[3] ? snv[3] : 0.0f);
+  acc[3] -= (fv[2] ? snv[2] : 0.0f) + (right_fl ? right : 0.0f);
+  const float s = a.s.inv_h2_f;
+  w4 = make_float4(fv[0] ? acc[0] * s : 0.0f, fv[1] ? acc[1] * s : 0.0f,
+                   fv[2] ? acc[2] * s : 0.0f, fv[3] ? acc[3] * s : 0.0f);
+}
+
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_quad(CgArgs a) {
+  const unsigned nb = gridDim.x;
+  const int n = a.s.n;
+  const int qrow = n / 4;
+  const size_t qplane = (size_t)qrow * n;
+  const size_t nq = a.nc / 4;
+  const size_t warps = (size_t)nb * (CG_BLOCK / 32);
+  const size_t wid = (size_t)blockIdx.x * (CG_BLOCK / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  float4 *x4 = reinterpret_cast<float4 *>(a.x);
+  float4 *r4 = reinterpret_cast<float4 *>(a.r);
+  float4 *z4 = reinterpret_cast<float4 *>(a.z);
+  float4 *w4p = reinterpret_cast<float4 *>(a.w);
+  const float4 *b4 = reinterpret_cast<const float4 *>(a.b);
+  const float4 *pf4 = reinterpret_cast<const float4 *>(a.Pf);
+  auto decode_q = [&](size_t q, int &i, int &j, int &kq) {
+    kq = (int)(q % qrow);
+    j = (int)((q / qrow) % n);
+    i = (int)(q / qplane);
+  };
+  auto acc4 = [](FF &f, float4 u, float4 v) {
+    ff_add_prod(f, u.x, v.x);
+    ff_add_prod(f, u.y, v.y);
+    ff_add_prod(f, u.z, v.z);
+    ff_add_prod(f, u.w, v.w);
+  };
+
+  /* phase 0: r = b - A x, z = M^-1 r (zeros outside FLUID); b.b, r.r, z.r */
+  FF pbb = ff_zero(), prr = ff_zero(), pzr = ff_zero();
+  for (size_t base = wid * 32; base < nq; base += warps * 32) {
+    size_t q = base + lane;
+    bool valid = q < nq;
+    int i = 0, j = 0, kq = 0;
+    if (valid) decode_q(q, i, j, kq);
+    float4 xs, ax;
+    uchar4 A4;
+    quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.x, a.x, 0.0f, true, xs, ax, A4);
+    if (!valid) continue;
+    float4 bv = b4[q];
+    const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+    float bb[4] = {bv.x, bv.y, bv.z, bv.w}, av[4] = {ax.x, ax.y, ax.z, ax.w};
+    float rv[4], zv[4], xv[4];
+    float4 pf = (fv[0] || fv[1] || fv[2] || fv[3]) ? pf4[q] : make_float4(0, 0, 0, 0);
+    float pfv[4] = {pf.x, pf.y, pf.z, pf.w};
+    float4 xo = x4[q];
+    float xov[4] = {xo.x, xo.y, xo.z, xo.w};
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      if (fv[t]) {
+        ff_add_prod(pbb, bb[t], bb[t]);
+        rv[t] = bb[t] - av[t];
+        zv[t] = rv[t] * pfv[t];
+        ff_add_prod(prr, rv[t], rv[t]);
+        ff_add_prod(pzr, zv[t], rv[t]);
+        xv[t] = xov[t];
+      } else {
+        rv[t] = zv[t] = xv[t] = 0.0f;
+      }
+    }
+    r4[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    z4[q] = make_float4(zv[0], zv[1], zv[2], zv[3]);
+    x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
+  }
+  store_partial(a.part, 0, nb, pbb);
+  store_partial(a.part, 1, nb, prr);
+  store_partial(a.part, 2, nb, pzr);
+  if (!grid_barrier(a.bar, a.iflags)) return;
+  double b2, rr, azr, unused;
+  sum_partials(a.part, 0, 1, nb, b2, rr);
+  sum_partials(a.part, 2, -1, nb, azr, unused);
+  const double eps = a.rel_tol * a.rel_tol * b2;
+  int done = rr <= eps ? 1 : 0, iters = 0;
+  double e2 = rr;
+  float *so = a.s0, *sn = a.s1;
+  float beta_f = 0.0f;
+  bool first = true;
+  while (!done) {
+    /* phase A: s_new = z + beta*s_old, w = A s_new; w.s_new */
+    FF pws = ff_zero();
+    for (size_t base = wid * 32; base < nq; base += warps * 32) {
+      size_t q = base + lane;
+      bool valid = q < nq;
+      int i = 0, j = 0, kq = 0;
+      if (valid) decode_q(q, i, j, kq);
+      float4 sn4, wv;
+      uchar4 A4;
+      quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.z, so, beta_f, first,
+                  sn4, wv, A4);
+      if (!valid || !(fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w))) continue;
+      reinterpret_cast<float4 *>(sn)[q] = sn4;
+      w4p[q] = wv;
+      acc4(pws, wv, sn4);
+    }
+    store_partial(a.part, 3, nb, pws);
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    double ws;
+    sum_partials(a.part, 3, -1, nb, ws, unused);
+    const double alpha = azr / ws;
+    const float alpha_f = (float)alpha;
+    /* phase B: x += alpha s, r -= alpha w, z = M^-1 r; r.r, z.r */
+    prr = ff_zero();
+    pzr = ff_zero();
+    for (size_t base = wid * 32; base < nq; base += warps * 32) {
+      size_t q = base + lane;
+      if (q >= nq) continue;
+      uchar4 A4 = reinterpret_cast<const uchar4 *>(a.A)[q];
+      const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+      if (!(fv[0] || fv[1] || fv[2] || fv[3])) continue;
+      float4 xv = x4[q], sv = reinterpret_cast<const float4 *>(sn)[q], rv = r4[q], wv = w4p[q],
+             pf = pf4[q];
+      float X[4] = {xv.x, xv.y, xv.z, xv.w}, S[4] = {sv.x, sv.y, sv.z, sv.w};
+      float R[4] = {rv.x, rv.y, rv.z, rv.w}, W[4] = {wv.x, wv.y, wv.z, wv.w};
+      float PF[4] = {pf.x, pf.y, pf.z, pf.w}, Z[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        if (fv[t]) {
+          X[t] = fmaf(alpha_f, S[t], X[t]);
+          R[t] = fmaf(-alpha_f, W[t], R[t]);
+          Z[t] = R[t] * PF[t];
+          ff_add_prod(prr, R[t], R[t]);
+          ff_add_prod(pzr, Z[t], R[t]);
+        } else {
+          Z[t] = 0.0f;
+        }
+      }
+      x4[q] = make_float4(X[0], X[1], X[2], X[3]);
+      r4[q] = make_float4(R[0], R[1], R[2], R[3]);
+      z4[q] = make_float4(Z[0], Z[1], Z[2], Z[3]);
+    }
+    store_partial(a.part, 4, nb, prr);
+    store_partial(a.part, 5, nb, pzr);
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    double zr;
+    sum_partials(a.part, 4, 5, nb, rr, zr);
+    iters++;
+    e2 = rr;
+    if (e2 <= eps) done = 1;
+    else if (!(e2 == e2)) done = 2;
+    else if (iters >= a.max_iters) done = 3;
+    beta_f = (float)(zr / azr);
+    azr = zr;
     first = false;
     float *t = so;
     so = sn;
@@ -808,7 +1060,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   FG_LAUNCHED(h, 1);
   /* persistent single-launch CG unless the REF preconditioner has an entry
    * equal to 1.0 (then its neighbour terms act and it runs sequentially) */
-  bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid > 0;
+  bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid[0] > 0;
   if (persistent && mode == FLIPGPU_SOLVE_REF) {
     int exotic = 0;
     cudaMemcpyAsync(&exotic, h->iflags + IF_EXOTIC, sizeof(int), cudaMemcpyDeviceToHost, S);
@@ -831,7 +1083,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.P = h->P;
     a.diag = h->diag;
     a.Pf = h->Pf;
-    a.part = h->partial;
+    a.part = (float2 *)h->partial;
     a.bar = h->bar;
     a.iflags = h->iflags;
     a.scal = h->scal;
@@ -841,10 +1093,14 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.max_iters = max_iters;
     cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
     void *kargs[] = {&a};
-    cudaError_t e = cudaLaunchCooperativeKernel(
-        mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
-                                  : (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
-        dim3(h->cg_grid), dim3(CG_BLOCK), kargs, 0, S);
+    const void *kern = mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
+                                                 : (const void *)k_cg<FLIPGPU_SOLVE_FAST>;
+    int grid = h->cg_grid[mode == FLIPGPU_SOLVE_REF ? 0 : 1];
+    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0) {
+      kern = (const void *)k_cg_quad;
+      grid = h->cg_grid[2];
+    }
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, 0, S);
     FG_LAUNCHED(h, 1);
     if (e != cudaSuccess) {
       snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
@@ -957,20 +1213,22 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   return FLIPGPU_OK;
 }
 
+/* Cooperative grid of each CG variant: SMs x resident blocks (at most 4). */
 int cg_grid_size(int *out) {
-  int dev = 0, sms = 0, per_sm_ref = 0, per_sm_fast = 0;
+  int dev = 0, sms = 0, coop = 0;
+  out[0] = out[1] = out[2] = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  if (!coop) {
-    *out = 0;
-    return 0;
+  if (!coop) return 0;
+  const void *k[3] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>, (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
+                      (const void *)k_cg_quad};
+  for (int v = 0; v < 3; v++) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], CG_BLOCK, 0);
+    if (per_sm > 4) per_sm = 4;
+    out[v] = sms * per_sm;
+    if (out[v] * 6 > 8192) out[v] = 8192 / 6;
   }
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_ref, k_cg<FLIPGPU_SOLVE_REF>, CG_BLOCK, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_fast, k_cg<FLIPGPU_SOLVE_FAST>, CG_BLOCK, 0);
-  int per_sm = per_sm_ref < per_sm_fast ? per_sm_ref : per_sm_fast;
-  if (per_sm > 4) per_sm = 4;
-  *out = sms * per_sm;
   return 0;
 }

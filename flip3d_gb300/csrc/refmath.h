@@ -114,6 +114,13 @@ RM_FN float smooth_ref(float r2, float hh) {
   return fmaxf(1.0f - q, 0.0f);
 }
 
+/* smooth_ref with hh a power of two (rcp = 1/hh exactly): the quotient is
+ * an exact scaling, so a multiply gives the division's result bit for bit. */
+RM_FN float smooth_ref_pow2(float r2, float rcp) {
+  float q = r2 * rcp;
+  return fmaxf(1.0f - q, 0.0f);
+}
+
 /* sharp_kernel (src/kernel.cpp:8-10): fmax(hh/fmax(r2,1e-5) - 1.0, 0.0) in
  * double, rounded to float. For r2 >= hh the result is 0. r2 below 1e-5
  * (r2_floor is the smallest float above 1e-5) takes the constant branch

@@ -144,10 +144,12 @@ def test_solve_ref_mode_matches_reference(gpu, name, tag, rel):
     assert np.mean(p == ref) > 0.9
 
 
-def test_solve_fast_mode_converges_to_fp64(gpu, orc):
-    """FAST mode (FP32 matvec, FP64 dots) to rel-res 1e-6 against an FP64
-    IC(0) solve run to 1e-12 on the oracle."""
-    g = np.load(f"{GOLD}/solver_n16.npz")
+@pytest.mark.parametrize("name", ["solver_n16", "solver_n13"])
+def test_solve_fast_mode_converges_to_fp64(gpu, orc, name):
+    """FAST mode (FP32 matvec and Jacobi, double-float dot products) to
+    rel-res 1e-6 against an FP64 IC(0) solve run to 1e-12 on the oracle.
+    n=16 runs the quad-vectorised kernel, n=13 the per-cell one."""
+    g = np.load(f"{GOLD}/{name}.npz")
     n = int(g["n"])
     sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
                    precond=gpu.PRECOND_JACOBI)
@@ -207,3 +209,29 @@ def test_step_deterministic(gpu):
         outs.append(sim.get_particles())
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+
+
+def test_fast_step_close_to_reference_step(gpu, orc):
+    """One FAST-mode step (Jacobi PCG to rel-res 1e-6, FP32) against the
+    reference step on the oracle: both solves meet the same relative residual,
+    so particle states agree to the solver tolerance."""
+    sc = scenes.dam_break(32, seed=2)
+    n = sc.n
+    md = orc.max_density(n)
+    osim = orc.Sim(sc, orc.params(n, orc.PRECOND_REF, rel_tol=1e-6, seed=4), md)
+    gsim = make_sim(gpu, n, sc.count, rel_tol=1e-6, seed=4, solve_mode=gpu.SOLVE_FAST,
+                    precond=gpu.PRECOND_JACOBI)
+    gsim.set_scene(sc)
+    gsim.set_max_density(md)
+    for _ in range(2):
+        osim.step()
+        st = gsim.step()
+        assert st.status == 0
+    opos, ovel, _, otyp = osim.get()
+    gpos, gvel, _, _ = gsim.get_particles()
+    fl = otyp == 1
+    vscale = float(np.abs(ovel[fl]).max())
+    print("fast vs ref: max dpos", np.abs(gpos - opos).max(), "max dvel",
+          np.abs(gvel[fl] - ovel[fl]).max(), "vscale", vscale)
+    assert np.abs(gpos - opos).max() <= 2e-5
+    assert np.abs(gvel[fl] - ovel[fl]).max() <= 2e-3 * max(vscale, 1.0)
