@@ -71,5 +71,29 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+SHIM_LIB = os.path.join(HERE, "libflip3d_shim.so")
+
+
+def build_shim(force: bool = False) -> str:
+    """libflip3d_shim.so: the reference's sorter/mapper/solver/corrector call
+    surface on top of libflipgpu.so (host C++, g++)."""
+    lib = build(force=force)
+    src = os.path.join(HERE, "shim", "shim.cpp")
+    deps = [src] + [os.path.join(HERE, "shim", f) for f in os.listdir(os.path.join(HERE, "shim"))
+                    if f.endswith(".h")]
+    if (not force and os.path.exists(SHIM_LIB)
+            and all(os.path.getmtime(d) <= os.path.getmtime(SHIM_LIB) for d in deps + [lib])):
+        return SHIM_LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", SHIM_LIB + ".tmp", src,
+           "-I", os.path.join(HERE, "shim", "compat"), "-L", HERE, "-lflipgpu",
+           "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"shim build failed:\n{res.stderr}")
+    os.replace(SHIM_LIB + ".tmp", SHIM_LIB)
+    return SHIM_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_shim(force="--force" in sys.argv))

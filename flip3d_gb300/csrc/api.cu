@@ -361,6 +361,14 @@ int flipgpu_destroy(FlipGpu *h) {
   return FLIPGPU_OK;
 }
 
+int flipgpu_set_params(FlipGpu *h, const FlipGpuParams *p) {
+  if (!h || !p) return FLIPGPU_EINVAL;
+  if (p->n != h->prm.n || p->max_particles != h->prm.max_particles)
+    return fail(h, FLIPGPU_EINVAL, "set_params: n and max_particles are fixed per handle");
+  h->prm = *p;
+  return FLIPGPU_OK;
+}
+
 int flipgpu_set_stream(FlipGpu *h, void *stream) {
   if (!h) return FLIPGPU_EINVAL;
   h->stream = stream ? (cudaStream_t)stream : h->own_stream;
@@ -555,6 +563,43 @@ int flipgpu_g2p(FlipGpu *h) {
   CK(h, launch_g2p(h));
   if (h->cells_valid) CK(h, launch_payload(h, 0));
   return FLIPGPU_OK;
+}
+
+/* Point buffers: device pointers are used directly; host ones are staged
+ * through h->stage (3*cap floats) in chunks. */
+static int point_query(FlipGpu *h, int count, const float *pts, float *io, int on_device,
+                       int what, float re) {
+  if (!h || count < 0 || (count > 0 && (!pts || !io))) return FLIPGPU_EINVAL;
+  if (what == 1 && !h->cells_valid) return fail(h, FLIPGPU_EINVAL, "resample: no cell lists");
+  if (on_device) {
+    CK(h, what == 0 ? launch_fetch_points(h, count, pts, io)
+                    : launch_resample_points(h, count, pts, io, re));
+    return FLIPGPU_OK;
+  }
+  const int chunk = h->cap > 0 ? (h->cap > 1 ? h->cap / 2 : 1) : 0;
+  if (chunk == 0) return fail(h, FLIPGPU_EINVAL, "no staging capacity");
+  float *dp = h->stage, *dio = h->stage + 3 * (size_t)chunk;
+  for (int off = 0; off < count; off += chunk) {
+    int m = count - off < chunk ? count - off : chunk;
+    size_t bytes = (size_t)m * 3 * sizeof(float);
+    CK(h, cudaMemcpyAsync(dp, pts + 3 * (size_t)off, bytes, cudaMemcpyHostToDevice, h->stream));
+    if (what == 1)
+      CK(h, cudaMemcpyAsync(dio, io + 3 * (size_t)off, bytes, cudaMemcpyHostToDevice, h->stream));
+    CK(h, what == 0 ? launch_fetch_points(h, m, dp, dio)
+                    : launch_resample_points(h, m, dp, dio, re));
+    CK(h, cudaMemcpyAsync(io + 3 * (size_t)off, dio, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+  }
+  return FLIPGPU_OK;
+}
+
+int flipgpu_fetch_velocity(FlipGpu *h, int count, const float *pts, float *out, int on_device) {
+  return point_query(h, count, pts, out, on_device, 0, 0.0f);
+}
+
+int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel, float re,
+                     int on_device) {
+  return point_query(h, count, pts, vel, on_device, 1, re);
 }
 
 int flipgpu_solve(FlipGpu *h, FlipGpuSolveStats *st) {

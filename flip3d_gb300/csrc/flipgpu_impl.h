@@ -165,6 +165,9 @@ cudaError_t launch_flip_blend(FlipGpu *h);
 cudaError_t launch_advect(FlipGpu *h);
 cudaError_t launch_reposition(FlipGpu *h, int *stuck_host);
 cudaError_t launch_correct(FlipGpu *h);
+cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *out);
+cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, float *vel,
+                                   float re);
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
 

@@ -163,8 +163,9 @@ k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__
 
 /* ----------------------------------------------------- mapG2P / FLIP */
 
-/* mapper::mapG2P for the fluid particles (wall velocities are never read
- * by any stage). */
+/* mapper::mapG2P (src/mapper.cpp:90-94) for every particle, walls included,
+ * as the reference does (the step itself skips walls: no stage reads their
+ * velocity). */
 __global__ void __launch_bounds__(BLK)
 k_g2p(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
       const float *__restrict__ pz, const uint8_t *__restrict__ type,
@@ -172,7 +173,8 @@ k_g2p(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
       const float *__restrict__ u2, float *__restrict__ vx, float *__restrict__ vy,
       float *__restrict__ vz) {
   int p = blockIdx.x * BLK + threadIdx.x;
-  if (p >= c.np || type[p] != CELL_FLUID) return;
+  if (p >= c.np) return;
+  (void)type;
   float v[3];
   fetch_velocity(c.n, c.fn, u0, u1, u2, px[p], py[p], pz[p], v);
   vx[p] = v[0];
@@ -541,7 +543,75 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
   }
 }
 
+/* mapper::fetchVelocity at arbitrary points (AoS in and out). */
+__global__ void k_fetch_points(SimConst c, int count, const float *__restrict__ pts,
+                               const float *__restrict__ u0, const float *__restrict__ u1,
+                               const float *__restrict__ u2, float *__restrict__ out) {
+  int t = blockIdx.x * BLK + threadIdx.x;
+  if (t >= count) return;
+  float v[3];
+  fetch_velocity(c.n, c.fn, u0, u1, u2, pts[3 * (size_t)t], pts[3 * (size_t)t + 1],
+                 pts[3 * (size_t)t + 2], v);
+  out[3 * (size_t)t] = v[0];
+  out[3 * (size_t)t + 1] = v[1];
+  out[3 * (size_t)t + 2] = v[2];
+}
+
+/* corrector::resample (src/corrector.cpp:15-47) at arbitrary points; each
+ * point only reads the sorted snapshot, so points are independent. */
+__global__ void k_resample_points(SimConst c, int count, const float *__restrict__ pts,
+                                  float *__restrict__ vel, float re_hh, float small,
+                                  const uint32_t *__restrict__ cs,
+                                  const float4 *__restrict__ spos,
+                                  const float4 *__restrict__ svel) {
+  int t = blockIdx.x * BLK + threadIdx.x;
+  if (t >= count) return;
+  float P[3] = {pts[3 * (size_t)t], pts[3 * (size_t)t + 1], pts[3 * (size_t)t + 2]};
+  int ci = cell_clamp(P[0], c.fn, c.n), cj = cell_clamp(P[1], c.fn, c.n),
+      ck = cell_clamp(P[2], c.fn, c.n);
+  float u[3] = {0.0f, 0.0f, 0.0f};
+  float wsum = 0.0f;
+  visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+    float4 Q = __ldg(spos + b);
+    if (unpack_type(Q.w) != CELL_FLUID) return;
+    float d2 = hypot2_ref(P[0] - Q.x, P[1] - Q.y, P[2] - Q.z);
+    if (!(d2 < re_hh)) return;
+    float w = sharp_ref(d2, re_hh, c.r2_floor, small);
+    float4 V = __ldg(svel + b);
+    u[0] += w * V.x;
+    u[1] += w * V.y;
+    u[2] += w * V.z;
+    wsum += w;
+  });
+  if (wsum != 0.0f) {
+    vel[3 * (size_t)t] = u[0] / wsum;
+    vel[3 * (size_t)t + 1] = u[1] / wsum;
+    vel[3 * (size_t)t + 2] = u[2] / wsum;
+  }
+}
+
 } // namespace
+
+cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *out) {
+  if (count == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  k_fetch_points<<<grid_for(count, BLK), BLK, 0, h->stream>>>(c, count, pts, h->u[0], h->u[1],
+                                                              h->u[2], out);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, float *vel,
+                                   float re) {
+  if (count == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  float hh = re * re;
+  float small = (float)fmax((double)hh / 1.0e-5 - 1.0, 0.0);
+  k_resample_points<<<grid_for(count, BLK), BLK, 0, h->stream>>>(
+      c, count, pts, vel, hh, small, h->cell_start, h->spos, h->svel);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;

@@ -81,6 +81,10 @@ SIGNATURES = {
     "flipgpu_get_profile": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_sort_cells_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
+    "flipgpu_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
+    "flipgpu_fetch_velocity": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_resample": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float,
+                                   C.c_int]),
 }
 
 STAGES = ["sort", "density", "mark_water", "p2g", "divergence", "solve", "gradient",
@@ -228,6 +232,22 @@ class Simulation:
         self._ck(self.lib.flipgpu_get_particles(self.h, C.c_void_p(pos_ptr),
                                                 C.c_void_p(vel_ptr), None, None, 0),
                  "get_particles")
+
+    def fetch_velocity(self, pts):
+        """mapper::fetchVelocity at each point of pts [m,3]."""
+        pts = _c(pts, np.float32)
+        out = np.zeros_like(pts)
+        self._ck(self.lib.flipgpu_fetch_velocity(self.h, pts.shape[0], _ptr(pts), _ptr(out), 0),
+                 "fetch_velocity")
+        return out
+
+    def resample(self, pts, vel, re):
+        """corrector::resample at each point (vel: fallback values)."""
+        pts = _c(pts, np.float32)
+        out = _c(vel, np.float32).copy()
+        self._ck(self.lib.flipgpu_resample(self.h, pts.shape[0], _ptr(pts), _ptr(out),
+                                           C.c_float(re), 0), "resample")
+        return out
 
     def set_profiling(self, on=True):
         self._ck(self.lib.flipgpu_set_profiling(self.h, int(on)), "set_profiling")

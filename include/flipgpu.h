@@ -94,6 +94,9 @@ void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles);
 int flipgpu_create(const FlipGpuParams *p, FlipGpu **out);
 int flipgpu_destroy(FlipGpu *h);
 const char *flipgpu_last_error(const FlipGpu *h);
+/* Change the run parameters of a handle (everything except n and
+ * max_particles, which must match). solver::setSubcell maps onto this. */
+int flipgpu_set_params(FlipGpu *h, const FlipGpuParams *p);
 /* Use an external stream (a cudaStream_t); NULL restores the handle's own. */
 int flipgpu_set_stream(FlipGpu *h, void *stream);
 int flipgpu_sync(FlipGpu *h);
@@ -136,9 +139,18 @@ int flipgpu_mark_water(FlipGpu *h);
 int flipgpu_add_force(FlipGpu *h);
 /* mapper::mapP2G (src/mapper.cpp:17-88) into the face grids. */
 int flipgpu_p2g(FlipGpu *h);
-/* mapper::mapG2P (src/mapper.cpp:90-94): particle velocity = trilinear
- * sample of the face grids (fluid particles). */
+/* mapper::mapG2P (src/mapper.cpp:90-94): every particle's velocity = the
+ * trilinear sample of the face grids at its position. */
 int flipgpu_g2p(FlipGpu *h);
+/* mapper::fetchVelocity (src/mapper.cpp:108-112) at count points: trilinear
+ * samples of the handle's face grids. pts/out are float[count][3]. */
+int flipgpu_fetch_velocity(FlipGpu *h, int count, const float *pts, float *out,
+                           int on_device);
+/* corrector::resample (src/corrector.cpp:15-47) at count points with kernel
+ * radius re against the current cell lists (flipgpu_sort first): vel holds
+ * the fallback velocity on input and the resampled one on output. */
+int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel,
+                     float re, int on_device);
 /* solver::solve (src/solver.cpp:224-241) on the handle's A, L, pressure
  * (initial guess, overwritten) and divergence (negated, as the reference
  * does). */

@@ -65,6 +65,7 @@ def lib():
         L.orc_matvec.argtypes = [C.c_int, C.c_int, u8p, f32p, f32p, f32p]
         L.orc_correct.argtypes = [C.c_int, C.c_int, f32p, f32p, u8p, f32p, u32p, u32p,
                                   C.c_float, C.c_float, C.c_uint64, C.c_int64]
+        L.orc_resample.argtypes = [C.c_int, f32p, f32p, u8p, u32p, u32p, f32p, f32p, C.c_float]
         L.orc_sim_create.argtypes = [C.POINTER(OrcParams), C.c_int, f32p, f32p, u8p, f32p,
                                      C.c_float]
         L.orc_sim_create.restype = C.c_void_p
@@ -166,6 +167,15 @@ def correct(n, pos, vel, typ, nrm, cs, perm, dt, re, seed, step):
     lib().orc_correct(n, pos.shape[0], pos, vel, _c(typ, np.uint8), _c(nrm, np.float32),
                       cs, perm, np.float32(dt), np.float32(re), seed, step)
     return pos, vel
+
+
+def resample(n, pos, vel, typ, cs, perm, p, u, re):
+    """corrector::resample at one point; u is the fallback velocity."""
+    out = _c(u, np.float32).copy()
+    lib().orc_resample(n, _c(pos, np.float32), _c(vel, np.float32), _c(typ, np.uint8),
+                       _c(cs, np.uint32), _c(perm, np.uint32), _c(p, np.float32), out,
+                       np.float32(re))
+    return out
 
 
 def max_density(n, density_param=0.5):
