@@ -468,7 +468,7 @@ int flipgpu_get_grid(FlipGpu *h, float *u0, float *u1, float *u2, uint8_t *A, fl
 
 int flipgpu_get_cells(FlipGpu *h, uint32_t *cell_start, uint32_t *perm, int on_device) {
   if (!h) return FLIPGPU_EINVAL;
-  if (!h->cells_valid) return fail(h, FLIPGPU_EINVAL, "no cell lists: call flipgpu_sort first");
+  if (!h->lists_exist) return fail(h, FLIPGPU_EINVAL, "no cell lists: call flipgpu_sort first");
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   if (cell_start)
     CK(h, cudaMemcpyAsync(cell_start, h->cell_start, (h->nc + 1) * sizeof(uint32_t), kind, h->stream));
@@ -570,7 +570,12 @@ int flipgpu_g2p(FlipGpu *h) {
 static int point_query(FlipGpu *h, int count, const float *pts, float *io, int on_device,
                        int what, float re) {
   if (!h || count < 0 || (count > 0 && (!pts || !io))) return FLIPGPU_EINVAL;
-  if (what == 1 && !h->cells_valid) return fail(h, FLIPGPU_EINVAL, "resample: no cell lists");
+  if (what == 1) {
+    if (!h->lists_exist) return fail(h, FLIPGPU_EINVAL, "resample: no cell lists");
+    /* the lists of the last sort over the particles' current data, as the
+     * reference's sorter keeps particle pointers */
+    CK(h, launch_payload(h, 0));
+  }
   if (on_device) {
     CK(h, what == 0 ? launch_fetch_points(h, count, pts, io)
                     : launch_resample_points(h, count, pts, io, re));

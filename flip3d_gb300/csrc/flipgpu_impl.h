@@ -83,7 +83,8 @@ struct FlipGpu {
   float4 *spg;        /* clamp(n*pos, 0, n), w = type (P2G) */
   float4 *svel;       /* velocity, w unused */
   float *sdens;
-  bool cells_valid;
+  bool cells_valid;   /* lists match the current positions */
+  bool lists_exist;   /* some sort has run (lists of the last sort) */
 
   /* static wall lists (walls never move) */
   int nwall;

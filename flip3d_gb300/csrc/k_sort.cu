@@ -230,5 +230,6 @@ cudaError_t launch_sort(FlipGpu *h, int apply_gravity) {
   if (e != cudaSuccess) return e;
   e = launch_payload(h, apply_gravity);
   h->cells_valid = true;
+  h->lists_exist = true;
   return e;
 }

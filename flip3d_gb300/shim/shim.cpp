@@ -291,9 +291,15 @@ void corrector::setRandomKey(uint64_t seed, int64_t step) {
   g_step = step;
 }
 
+/* The reference reads the neighbours' current data through the sorter's
+ * particle pointers (a reposition loop updates velocities between calls), so
+ * the current records of the sorted particles are uploaded first. */
 void corrector::resample(sorter *sort, FLOAT p[3], FLOAT u[3], FLOAT re) {
   FlipShimCells &s = *sort->shim();
   if (!s.ctx.h) return;
+  Soa cur;
+  pack(s.parts, cur);
+  CHECK(s.ctx.h, flipgpu_put_state(s.ctx.h, cur.pos.data(), cur.vel.data(), 0));
   CHECK(s.ctx.h, flipgpu_resample(s.ctx.h, 1, p, u, re, 0));
 }
 

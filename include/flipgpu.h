@@ -117,6 +117,7 @@ int flipgpu_set_grid(FlipGpu *h, const float *u0, const float *u1,
                      const float *press, const float *div, int on_device);
 int flipgpu_get_grid(FlipGpu *h, float *u0, float *u1, float *u2, uint8_t *A,
                      float *L, float *press, float *div, int on_device);
+/* The cell lists of the last sort. */
 int flipgpu_get_cells(FlipGpu *h, uint32_t *cell_start, uint32_t *perm,
                       int on_device);
 
@@ -147,8 +148,10 @@ int flipgpu_g2p(FlipGpu *h);
 int flipgpu_fetch_velocity(FlipGpu *h, int count, const float *pts, float *out,
                            int on_device);
 /* corrector::resample (src/corrector.cpp:15-47) at count points with kernel
- * radius re against the current cell lists (flipgpu_sort first): vel holds
- * the fallback velocity on input and the resampled one on output. */
+ * radius re: the cell lists of the last sort over the particles' current
+ * positions and velocities (the reference's sorter keeps particle pointers,
+ * so it reads current data through old lists). vel holds the fallback
+ * velocity on input and the resampled one on output. */
 int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel,
                      float re, int on_device);
 /* solver::solve (src/solver.cpp:224-241) on the handle's A, L, pressure

@@ -91,8 +91,10 @@ def test_shim_drives_the_gpu_like_the_reference(tmp_path):
     fl = typ == 1
     assert np.array_equal(cpos, g["corr_pos"])
     assert np.array_equal(cvel[fl], g["corr_vel"][fl])
-    # resample at q[0] against the lists of the positions before the move
+    # resample at q[0]: the lists of the positions before the move over the
+    # particles' current (corrected) data, as the reference's sorter does
     ru = take(np.float32, 3)
-    rr = orc.resample(n, pos, vel, typ, cs, perm, q[0], np.zeros(3, np.float32), 1.0 / n)
+    rr = orc.resample(n, g["corr_pos"], g["corr_vel"], typ, cs, perm, q[0],
+                      np.zeros(3, np.float32), 1.0 / n)
     assert np.array_equal(ru, rr)
     assert off == len(raw)
