@@ -170,7 +170,8 @@ void free_all(FlipGpu *h) {
                   h->div, h->r, h->z, h->s, h->s1, h->w, h->bar, h->P, h->Pf, h->diag,
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
-                  h->water_idx, h->stage};
+                  h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
+                  h->ticket, h->brick_part};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -325,7 +326,24 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->scal, SC_COUNT) AL(h->iflags, IF_COUNT) AL(h->flag, cap) AL(h->scan_a, scan_n)
   AL(h->scan_b, scan_n) AL(h->scan_tmp, h->scan_cap) AL(h->stuck_idx, cap)
   AL(h->water_idx, nc) AL(h->stage, 3 * cap)
+  h->nbx = (p->n + 7) / 8;
+  h->nbricks = h->nbx * h->nbx * h->nbx;
+  AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
+  AL(h->ticket, 1) AL(h->brick_part, h->nbricks)
 #undef AL
+  {
+    /* bricks by increasing i+j+k: every brick's dependencies come earlier */
+    std::vector<unsigned> order;
+    const int nb = h->nbx;
+    for (int d = 0; d <= 3 * (nb - 1); d++)
+      for (int i = 0; i < nb; i++)
+        for (int j = 0; j < nb; j++) {
+          int k = d - i - j;
+          if (k >= 0 && k < nb) order.push_back((unsigned)((i * nb + j) * nb + k));
+        }
+    cudaMemcpy(h->brick_order, order.data(), order.size() * sizeof(unsigned),
+               cudaMemcpyHostToDevice);
+  }
   for (int c = 0; c < 3; c++) {
     cudaMemsetAsync(h->u[c], 0, nf * sizeof(float), h->stream);
     cudaMemsetAsync(h->us[c], 0, nf * sizeof(float), h->stream);
@@ -344,7 +362,8 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
     delete h;
     return FLIPGPU_ECUDA;
   }
-  if (cg_grid_size(h->cg_grid) != 0) h->cg_grid[0] = h->cg_grid[1] = h->cg_grid[2] = 0;
+  if (cg_grid_size(h->cg_grid) != 0)
+    h->cg_grid[0] = h->cg_grid[1] = h->cg_grid[2] = h->cg_grid[3] = 0;
   *out = h;
   return FLIPGPU_OK;
 }

@@ -106,7 +106,10 @@ struct FlipGpu {
   double *scal;       /* device scalars of the CG recurrence */
   int *iflags;        /* device flags/counters */
   unsigned *bar;      /* grid barrier of the persistent CG: count, generation */
-  int cg_grid[3];     /* cooperative CG grids: REF, FAST, FAST quads (0 = unavailable) */
+  int cg_grid[4];     /* cooperative CG grids: REF, FAST, FAST quads, FAST IC (0 = none) */
+  int nbx, nbricks;   /* 8^3 bricks of the IC wavefront */
+  unsigned *brick_order, *fflag, *bflag, *ticket;
+  float2 *brick_part;
   int npartial;
 
   /* reposition */

@@ -457,9 +457,19 @@ struct CgArgs {
   double *scal;
   double eps_abs, rel_tol, ref_eps;
   int max_iters;
+  /* IC(0)/MIC(0) wavefront */
+  float mic_tau;
+  float *Pic;                  /* factor: 1/sqrt(e) per FLUID cell */
+  int nbx;                     /* bricks per axis */
+  int nbricks;
+  const unsigned *brick_order; /* bricks by increasing i+j+k of the brick */
+  unsigned *fflag, *bflag;     /* epoch of the last forward / backward sweep done */
+  unsigned *ticket;
+  float2 *brick_part;          /* per-brick z.r partials */
 };
 
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags) {
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags,
+                                             unsigned *reset_ticket = nullptr) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -468,6 +478,8 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags) {
     __threadfence();
     unsigned arrived = atomicAdd(bar, 1u);
     if (arrived == gridDim.x - 1) {
+      /* every block is past its task loop: the ticket counter can restart */
+      if (reset_ticket) atomicExch(reset_ticket, 0u);
       atomicExch(bar, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
@@ -984,7 +996,349 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_quad(CgArgs a) {
   }
 }
 
+
+/* ------------------------------------------- IC(0)/MIC(0) as wavefronts */
+
+/* The lexicographic incomplete-Cholesky factor of the reference's
+ * buildPreconditioner (src/solver.cpp:125-139), with the neighbour test on
+ * the cell flag instead of the value, plus the MIC(0) modification weighted
+ * by tau; and its triangular solves (src/solver.cpp:141-180). A cell depends
+ * on its -x/-y/-z neighbours (forward) or +x/+y/+z neighbours (backward), so
+ * cells on one plane i+j+k are independent. The grid is cut into 8^3 bricks;
+ * a brick depends on the three bricks before it along the axes. Bricks are
+ * handed to warps by an atomic ticket in wavefront order; a warp waits (bounded)
+ * for its three predecessors' epoch flags, loads the brick and its halo into
+ * shared memory, runs the 22 intra-brick planes separated by __syncwarp, writes
+ * back and publishes its flag. Tickets are taken in an order where every
+ * dependency has a smaller ticket, so a waiting warp only waits for warps
+ * that already run. */
+constexpr int BRK = 8;
+constexpr int BRK3 = BRK * BRK * BRK;
+constexpr int HB = BRK + 2;
+constexpr int HB3 = HB * HB * HB;
+constexpr int NPLANES = 3 * BRK - 2;
+constexpr int WARPS_PER_CTA = CG_BLOCK / 32;
+constexpr unsigned long long FLAG_SPIN_LIMIT = 1ull << 24;
+
+struct BrickPlanes {
+  unsigned short cell[BRK3];       /* (i<<6)|(j<<3)|k sorted by i+j+k */
+  unsigned short start[NPLANES + 1];
+};
+__constant__ BrickPlanes c_planes;
+
+struct BrickSmem {
+  float v[HB3];           /* r -> q (forward), q -> z (backward), diag -> P (build) */
+  float p[HB3];           /* factor */
+  unsigned char fl[HB3];  /* FLUID flags */
+};
+
+__device__ __forceinline__ int hidx(int i, int j, int k) { return ((i + 1) * HB + (j + 1)) * HB + (k + 1); }
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+/* every lane waits (bounded) until flag >= epoch */
+__device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, int *iflags) {
+  unsigned long long spins = 0;
+  while (ld_acquire(flag) < epoch) {
+    if (++spins > FLAG_SPIN_LIMIT) {
+      atomicExch(iflags + IF_TIMEOUT, 1);
+      return;
+    }
+    __nanosleep(64);
+  }
+}
+
+/* kind: 0 build the factor, 1 forward solve, 2 backward solve */
+__device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, unsigned epoch_f,
+                           unsigned epoch_b, const float *r, float *qz) {
+  const int lane = threadIdx.x & 31;
+  const int n = a.s.n, nbx = a.nbx;
+  const int BI = brick / (nbx * nbx), BJ = (brick / nbx) % nbx, BK = brick % nbx;
+  const int i0 = BI * BRK, j0 = BJ * BRK, k0 = BK * BRK;
+  const uint8_t *A = a.A;
+  auto cidx = [&](int i, int j, int k) { return ((size_t)i * n + j) * n + k; };
+  auto inside = [&](int i, int j, int k) {
+    return i >= 0 && i < n && j >= 0 && j < n && k >= 0 && k < n;
+  };
+  /* own cells, independent of other bricks */
+  for (int t = lane; t < BRK3; t += 32) {
+    int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
+    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
+    int h = hidx(bi, bj, bk);
+    if (!inside(i, j, k)) {
+      sm.fl[h] = 0;
+      sm.v[h] = 0.0f;
+      sm.p[h] = 0.0f;
+      continue;
+    }
+    size_t c = cidx(i, j, k);
+    unsigned char f = A[c] == CELL_FLUID;
+    sm.fl[h] = f;
+    if (kind == 0) {
+      sm.v[h] = f ? a.diag[c] : 0.0f;
+    } else if (kind == 1) {
+      sm.v[h] = f ? __ldcg(r + c) : 0.0f;
+      sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
+    } else {
+      sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
+    }
+  }
+  /* dependencies */
+  const int dir = kind == 2 ? 1 : -1;
+  const int nbI = BI + dir, nbJ = BJ + dir, nbK = BK + dir;
+  const unsigned *flags = kind == 2 ? a.bflag : a.fflag;
+  const unsigned ep = kind == 2 ? epoch_b : epoch_f;
+  if (nbI >= 0 && nbI < nbx) wait_flag(flags + (nbI * nbx + BJ) * nbx + BK, ep, a.iflags);
+  if (nbJ >= 0 && nbJ < nbx) wait_flag(flags + (BI * nbx + nbJ) * nbx + BK, ep, a.iflags);
+  if (nbK >= 0 && nbK < nbx) wait_flag(flags + (BI * nbx + BJ) * nbx + nbK, ep, a.iflags);
+  if (kind == 2) {
+    /* the forward solve of this brick wrote q */
+    wait_flag(a.fflag + brick, epoch_f, a.iflags);
+    for (int t = lane; t < BRK3; t += 32) {
+      int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
+      int i = i0 + bi, j = j0 + bj, k = k0 + bk;
+      int h = hidx(bi, bj, bk);
+      sm.v[h] = (inside(i, j, k) && sm.fl[h]) ? __ldcg(qz + cidx(i, j, k)) : 0.0f;
+    }
+  }
+  /* halo faces: -1 (build/forward) or +1 (backward) along each axis */
+  const int hf = kind == 2 ? BRK : -1;
+  for (int t = lane; t < 3 * BRK * BRK; t += 32) {
+    int face = t / (BRK * BRK), u = (t / BRK) % BRK, w = t % BRK;
+    /* face 0: (hf,u,w), face 1: (u,hf,w), face 2: (u,w,hf) */
+    int bi = face == 0 ? hf : u, bj = face == 1 ? hf : (face == 0 ? u : w),
+        bk = face == 2 ? hf : w;
+    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
+    int h = hidx(bi, bj, bk);
+    if (!inside(i, j, k)) {
+      sm.fl[h] = 0;
+      sm.v[h] = 0.0f;
+      sm.p[h] = 0.0f;
+      continue;
+    }
+    size_t c = cidx(i, j, k);
+    unsigned char f = A[c] == CELL_FLUID;
+    sm.fl[h] = f;
+    sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
+    sm.v[h] = (f && kind != 0) ? __ldcg(qz + c) : 0.0f;
+  }
+  __syncwarp();
+  const float tau = a.mic_tau;
+  for (int pl = 0; pl < NPLANES; pl++) {
+    const int d = kind == 2 ? NPLANES - 1 - pl : pl;
+    for (int e = c_planes.start[d] + lane; e < c_planes.start[d + 1]; e += 32) {
+      unsigned cc = c_planes.cell[e];
+      int bi = cc >> 6, bj = (cc >> 3) & 7, bk = cc & 7;
+      int h = hidx(bi, bj, bk);
+      if (!sm.fl[h]) continue;
+      const int hm[3] = {hidx(bi - 1, bj, bk), hidx(bi, bj - 1, bk), hidx(bi, bj, bk - 1)};
+      const int hp[3] = {hidx(bi + 1, bj, bk), hidx(bi, bj + 1, bk), hidx(bi, bj, bk + 1)};
+      if (kind == 0) {
+        float diag = sm.v[h];
+        float ev = diag;
+        for (int ax = 0; ax < 3; ax++) {
+          if (!sm.fl[hm[ax]]) continue;
+          float pm = sm.p[hm[ax]];
+          ev -= pm * pm;
+          if (tau != 0.0f) {
+            /* the two other plus-side couplings of that neighbour */
+            int mi = i0 + bi - (ax == 0), mj = j0 + bj - (ax == 1), mk = k0 + bk - (ax == 2);
+            int cnt = 0;
+            for (int ax2 = 0; ax2 < 3; ax2++) {
+              if (ax2 == ax) continue;
+              int qi = mi + (ax2 == 0), qj = mj + (ax2 == 1), qk = mk + (ax2 == 2);
+              if (inside(qi, qj, qk) && __ldg(A + cidx(qi, qj, qk)) == CELL_FLUID) cnt++;
+            }
+            ev -= tau * (float)cnt * pm * pm;
+          }
+        }
+        if (ev < 0.25f * diag) ev = diag;
+        sm.p[h] = 1.0f / sqrtf(ev);
+      } else if (kind == 1) {
+        float t = sm.v[h];
+        for (int ax = 0; ax < 3; ax++)
+          if (sm.fl[hm[ax]]) t += sm.p[hm[ax]] * sm.v[hm[ax]];
+        sm.v[h] = t * sm.p[h];
+      } else {
+        float t = 0.0f;
+        for (int ax = 0; ax < 3; ax++)
+          if (sm.fl[hp[ax]]) t += sm.v[hp[ax]];
+        sm.v[h] = (sm.v[h] + sm.p[h] * t) * sm.p[h];
+      }
+    }
+    __syncwarp();
+  }
+  /* write back, per-brick z.r for the backward solve, publish */
+  FF zr = ff_zero();
+  for (int t = lane; t < BRK3; t += 32) {
+    int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
+    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
+    int h = hidx(bi, bj, bk);
+    if (!inside(i, j, k)) continue;
+    size_t c = cidx(i, j, k);
+    if (kind == 0) {
+      a.Pic[c] = sm.fl[h] ? sm.p[h] : 0.0f;
+    } else {
+      qz[c] = sm.v[h];
+      if (kind == 2 && sm.fl[h]) ff_add_prod(zr, sm.v[h], __ldcg(r + c));
+    }
+  }
+  if (kind == 2) {
+    for (int o = 16; o > 0; o >>= 1) zr = ff_merge(zr, ff_shfl_down(zr, o));
+    if (lane == 0) a.brick_part[brick] = make_float2(zr.hi, zr.lo);
+  }
+  __threadfence();
+  __syncwarp();
+  if (lane == 0) st_release((kind == 2 ? a.bflag : a.fflag) + brick, kind == 2 ? epoch_b : epoch_f);
+}
+
+/* Run one factor build (tasks = nbricks) or one forward+backward apply
+ * (tasks = 2*nbricks) over the ticket counter. */
+__device__ void wavefront(const CgArgs &a, BrickSmem *sm_all, bool build, unsigned epoch_f,
+                          unsigned epoch_b, const float *r, float *qz) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BrickSmem &sm = sm_all[warp];
+  const unsigned tasks = build ? (unsigned)a.nbricks : 2u * (unsigned)a.nbricks;
+  while (true) {
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(a.ticket, 1u);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= tasks) break;
+    if (*(volatile int *)(a.iflags + IF_TIMEOUT)) break;
+    if (t < (unsigned)a.nbricks)
+      brick_task(a, sm, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
+    else
+      brick_task(a, sm, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r, qz);
+  }
+}
+
+/* Sum of the per-brick partials in brick order (identical in every block). */
+__device__ __forceinline__ double sum_brick_parts(const CgArgs &a) {
+  FF v = ff_zero();
+  for (int b = threadIdx.x; b < a.nbricks; b += CG_BLOCK) {
+    float2 p = __ldcg(a.brick_part + b);
+    v = ff_merge(v, FF{p.x, p.y});
+  }
+  return ff_to_double(block_sum_ff<CG_BLOCK>(v));
+}
+
+/* FAST-mode PCG with the wavefront IC(0)/MIC(0) preconditioner. */
+__global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
+  extern __shared__ unsigned char dyn[];
+  BrickSmem *sm = reinterpret_cast<BrickSmem *>(dyn);
+  const unsigned nb = gridDim.x;
+  const size_t stride = (size_t)nb * CG_BLOCK;
+  const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
+  const int n = a.s.n;
+  const size_t nc = a.nc;
+  constexpr int M = FLIPGPU_SOLVE_FAST;
+  unsigned apply = 0; /* preconditioner applications so far */
+
+  /* factor (forward-type sweep, epoch 1) */
+  wavefront(a, sm, true, 1u, 0u, nullptr, nullptr);
+  if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
+  /* r = b - A x; b.b, r.r */
+  FF pbb = ff_zero(), prr = ff_zero();
+  for (size_t c = t0; c < nc; c += stride) {
+    float rv = 0.0f;
+    if (a.A[c] == CELL_FLUID) {
+      int i, j, k;
+      decode(c, n, i, j, k);
+      float bc = a.b[c];
+      ff_add_prod(pbb, bc, bc);
+      float ax = cg_matvec<M>(a, c, i, j, k, a.x[c], a.x, a.x, 0.0f, true);
+      rv = bc - ax;
+      ff_add_prod(prr, rv, rv);
+    } else {
+      a.x[c] = 0.0f;
+    }
+    a.r[c] = rv;
+  }
+  store_partial(a.part, 0, nb, pbb);
+  store_partial(a.part, 1, nb, prr);
+  if (!grid_barrier(a.bar, a.iflags)) return;
+  double b2, rr, unused;
+  sum_partials(a.part, 0, 1, nb, b2, rr);
+  const double eps = a.rel_tol * a.rel_tol * b2;
+  int done = rr <= eps ? 1 : 0, iters = 0;
+  double e2 = rr, azr = 0.0;
+  if (!done) {
+    apply++;
+    wavefront(a, sm, false, apply + 1, apply, a.r, a.z);
+    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
+    azr = sum_brick_parts(a);
+  }
+  float *so = a.s0, *sn = a.s1;
+  float beta_f = 0.0f;
+  bool first = true;
+  while (!done) {
+    /* phase A: s = z + beta s, w = A s; w.s */
+    FF pws = ff_zero();
+    for (size_t c = t0; c < nc; c += stride) {
+      if (a.A[c] != CELL_FLUID) continue;
+      int i, j, k;
+      decode(c, n, i, j, k);
+      float zc = __ldcg(a.z + c);
+      float snv = first ? zc : zc + beta_f * so[c];
+      float wv = cg_matvec<M>(a, c, i, j, k, snv, a.z, so, beta_f, first);
+      ff_add_prod(pws, wv, snv);
+      sn[c] = snv;
+      a.w[c] = wv;
+    }
+    store_partial(a.part, 3, nb, pws);
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    double ws;
+    sum_partials(a.part, 3, -1, nb, ws, unused);
+    const float alpha_f = (float)(azr / ws);
+    /* phase B: x += alpha s, r -= alpha w; r.r */
+    FF prr2 = ff_zero();
+    for (size_t c = t0; c < nc; c += stride) {
+      if (a.A[c] != CELL_FLUID) continue;
+      a.x[c] = fmaf(alpha_f, sn[c], a.x[c]);
+      float rv = fmaf(-alpha_f, a.w[c], a.r[c]);
+      a.r[c] = rv;
+      ff_add_prod(prr2, rv, rv);
+    }
+    store_partial(a.part, 4, nb, prr2);
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    sum_partials(a.part, 4, -1, nb, rr, unused);
+    iters++;
+    e2 = rr;
+    if (e2 <= eps) { done = 1; break; }
+    if (!(e2 == e2)) { done = 2; break; }
+    if (iters >= a.max_iters) { done = 3; break; }
+    /* z = M^-1 r by the two wavefront sweeps; z.r per brick */
+    apply++;
+    wavefront(a, sm, false, apply + 1, apply, a.r, a.z);
+    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
+    const double zr = sum_brick_parts(a);
+    beta_f = (float)(zr / azr);
+    azr = zr;
+    first = false;
+    float *t = so;
+    so = sn;
+    sn = t;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.iflags[IF_DONE] = done;
+    a.iflags[IF_ITERS] = iters;
+    a.iflags[IF_NAN] = done == 2;
+    a.scal[SC_ERR2] = e2;
+    a.scal[SC_B2] = b2;
+    a.scal[SC_EPS] = eps;
+  }
+}
+
 } // namespace
+
+size_t ic_smem_bytes();
 
 static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   double sc[SC_COUNT];
@@ -1061,6 +1415,11 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   /* persistent single-launch CG unless the REF preconditioner has an entry
    * equal to 1.0 (then its neighbour terms act and it runs sequentially) */
   bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid[0] > 0;
+  if (precond == FLIPGPU_PRECOND_IC && (mode != FLIPGPU_SOLVE_FAST || h->cg_grid[3] <= 0)) {
+    snprintf(h->err, sizeof h->err, "solve: the IC preconditioner needs FAST mode and a "
+                                    "cooperative launch");
+    return FLIPGPU_EINVAL;
+  }
   if (persistent && mode == FLIPGPU_SOLVE_REF) {
     int exotic = 0;
     cudaMemcpyAsync(&exotic, h->iflags + IF_EXOTIC, sizeof(int), cudaMemcpyDeviceToHost, S);
@@ -1091,16 +1450,34 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.rel_tol = h->prm.rel_tol;
     a.ref_eps = ref_eps;
     a.max_iters = max_iters;
+    a.mic_tau = (float)h->prm.mic_tau;
+    a.Pic = h->Pf;
+    a.nbx = h->nbx;
+    a.nbricks = h->nbricks;
+    a.brick_order = h->brick_order;
+    a.fflag = h->fflag;
+    a.bflag = h->bflag;
+    a.ticket = h->ticket;
+    a.brick_part = h->brick_part;
     cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
     void *kargs[] = {&a};
     const void *kern = mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
                                                  : (const void *)k_cg<FLIPGPU_SOLVE_FAST>;
     int grid = h->cg_grid[mode == FLIPGPU_SOLVE_REF ? 0 : 1];
+    size_t smem = 0;
     if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0) {
       kern = (const void *)k_cg_quad;
       grid = h->cg_grid[2];
     }
-    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, 0, S);
+    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_IC) {
+      kern = (const void *)k_cg_ic;
+      grid = h->cg_grid[3];
+      smem = ic_smem_bytes();
+      cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
+      cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
+      cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
+    }
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, smem, S);
     FG_LAUNCHED(h, 1);
     if (e != cudaSuccess) {
       snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
@@ -1213,19 +1590,47 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   return FLIPGPU_OK;
 }
 
+size_t ic_smem_bytes() { return sizeof(BrickSmem) * WARPS_PER_CTA; }
+
+/* Intra-brick plane lists, uploaded once per device. */
+int ic_init_device() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (done[dev]) return 0;
+  BrickPlanes bp;
+  int e = 0;
+  for (int d = 0; d < NPLANES; d++) {
+    bp.start[d] = (unsigned short)e;
+    for (int i = 0; i < BRK; i++)
+      for (int j = 0; j < BRK; j++)
+        for (int k = 0; k < BRK; k++)
+          if (i + j + k == d) bp.cell[e++] = (unsigned short)((i << 6) | (j << 3) | k);
+  }
+  bp.start[NPLANES] = (unsigned short)e;
+  if (cudaMemcpyToSymbol(c_planes, &bp, sizeof bp) != cudaSuccess) return -1;
+  if (cudaFuncSetAttribute(k_cg_ic, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)ic_smem_bytes()) != cudaSuccess)
+    return -1;
+  done[dev] = true;
+  return 0;
+}
+
 /* Cooperative grid of each CG variant: SMs x resident blocks (at most 4). */
 int cg_grid_size(int *out) {
   int dev = 0, sms = 0, coop = 0;
-  out[0] = out[1] = out[2] = 0;
+  out[0] = out[1] = out[2] = out[3] = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   if (!coop) return 0;
-  const void *k[3] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>, (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
-                      (const void *)k_cg_quad};
-  for (int v = 0; v < 3; v++) {
+  if (ic_init_device() != 0) return -1;
+  const void *k[4] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>, (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
+                      (const void *)k_cg_quad, (const void *)k_cg_ic};
+  for (int v = 0; v < 4; v++) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], CG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], CG_BLOCK,
+                                                  v == 3 ? ic_smem_bytes() : 0);
     if (per_sm > 4) per_sm = 4;
     out[v] = sms * per_sm;
     if (out[v] * 6 > 8192) out[v] = 8192 / 6;

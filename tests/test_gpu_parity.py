@@ -258,3 +258,51 @@ def test_fast_step_close_to_reference_step(gpu, orc):
           np.abs(gvel[fl] - ovel[fl]).max(), "vscale", vscale)
     assert np.abs(gpos - opos).max() <= 2e-5
     assert np.abs(gvel[fl] - ovel[fl]).max() <= 2e-3 * max(vscale, 1.0)
+
+
+@pytest.mark.parametrize("tau", [0.0, 0.97])
+@pytest.mark.parametrize("name", ["solver_n16", "solver_n13"])
+def test_solve_ic_wavefront_matches_fp64_factor(gpu, orc, name, tau):
+    """IC(0) (tau=0) / MIC(0) (tau=0.97) applied as brick wavefronts in FP32
+    against the oracle's sequential FP64 factor: same solution to rel-res
+    1e-6, and iteration counts within 15% of the FP64 run (a wrong factor or
+    sweep order shows up as a different count or no convergence)."""
+    g = np.load(f"{GOLD}/{name}.npz")
+    n = int(g["n"])
+    sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                   precond=gpu.PRECOND_IC, mic_tau=tau)
+    sim.set_grid(A=g["A"], L=g["L"], press=np.zeros(n ** 3, np.float32), div=g["b"])
+    st = sim.solve()
+    assert st.status == 0
+    assert st.r2 <= 1e-12 * st.b2 * (1 + 1e-9)
+    _, _, _, p, _ = sim.get_grid()
+    prm = orc.params(n, orc.PRECOND_IC, rel_tol=1e-6, mic_tau=tau)
+    x6, _, it6, _, _ = orc.solve(prm, g["A"], g["L"], np.zeros(n ** 3, np.float32), g["b"])
+    prm = orc.params(n, orc.PRECOND_IC, rel_tol=1e-12, mic_tau=tau)
+    x, _, _, _, _ = orc.solve(prm, g["A"], g["L"], np.zeros(n ** 3, np.float32), g["b"])
+    fl = g["A"] == 1
+    err = np.linalg.norm((p - x)[fl]) / np.linalg.norm(x[fl])
+    assert err < 1e-4, err
+    assert abs(st.iterations - it6) <= max(2, 0.15 * it6), (st.iterations, it6)
+
+
+def test_solve_mic_on_a_dam_break(gpu, orc):
+    """MIC(0) wavefront on a realistic N=32 system (several bricks per axis)."""
+    sc = scenes.dam_break(32, seed=1)
+    n = sc.n
+    cs, perm = orc.sort(n, sc.pos)
+    dens = orc.density(n, sc.pos, sc.type, cs, perm, orc.max_density(n))
+    A = orc.mark_water(n, sc.type, dens, cs, perm)
+    L = orc.levelset(n, sc.type, dens, cs, perm)
+    b = np.where(A == 1, np.random.default_rng(1).normal(0, 1, n ** 3), 0).astype(np.float32)
+    prm = orc.params(n, orc.PRECOND_IC, rel_tol=1e-6, mic_tau=0.97)
+    x6, _, it6, _, _ = orc.solve(prm, A, L, np.zeros(n ** 3, np.float32), b)
+    sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                   precond=gpu.PRECOND_IC, mic_tau=0.97)
+    sim.set_grid(A=A, L=L, press=np.zeros(n ** 3, np.float32), div=b)
+    st = sim.solve()
+    assert st.status == 0
+    _, _, _, p, _ = sim.get_grid()
+    fl = A == 1
+    assert np.linalg.norm((p - x6)[fl]) / np.linalg.norm(x6[fl]) < 1e-4
+    assert abs(st.iterations - it6) <= max(2, 0.15 * it6), (st.iterations, it6)
