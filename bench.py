@@ -183,7 +183,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128)
-    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "ref"])
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "mic", "ref"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -203,9 +203,11 @@ def main():
         dist.init_process_group("nccl")
     sc = scenes.dam_break(args.n, seed=rank)
     P = sc.count
-    pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "ref": gpu.PRECOND_REF}[args.precond]
+    pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "mic": gpu.PRECOND_IC,
+           "ref": gpu.PRECOND_REF}[args.precond]
     mode = gpu.SOLVE_REF if args.precond == "ref" else gpu.SOLVE_FAST
-    prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1)
+    prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1,
+                             mic_tau=0.97 if args.precond == "mic" else 0.0)
     sim = gpu.Simulation(prm)
     sim.set_scene(sc)
     sim.calibrate_max_density()
