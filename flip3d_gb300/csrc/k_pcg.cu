@@ -1051,7 +1051,7 @@ __device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, 
       atomicExch(iflags + IF_TIMEOUT, 1);
       return;
     }
-    __nanosleep(64);
+    __nanosleep(20);
   }
 }
 
@@ -1067,27 +1067,42 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, 
   auto inside = [&](int i, int j, int k) {
     return i >= 0 && i < n && j >= 0 && j < n && k >= 0 && k < n;
   };
-  /* own cells, independent of other bricks */
-  for (int t = lane; t < BRK3; t += 32) {
+  /* All loads of a phase are issued unconditionally and together (the
+   * fluid mask is applied afterwards), so a phase costs one L2 round trip
+   * instead of one per cell. */
+  constexpr int OWN = BRK3 / 32;       /* own cells per lane */
+  constexpr int HALO = 3 * BRK * BRK / 32; /* halo cells per lane */
+  auto own_cell = [&](int u, int &h, size_t &c, bool &in) {
+    int t = lane + 32 * u;
     int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
-    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
-    int h = hidx(bi, bj, bk);
-    if (!inside(i, j, k)) {
-      sm.fl[h] = 0;
-      sm.v[h] = 0.0f;
-      sm.p[h] = 0.0f;
-      continue;
+    h = hidx(bi, bj, bk);
+    in = inside(i0 + bi, j0 + bj, k0 + bk);
+    c = in ? cidx(i0 + bi, j0 + bj, k0 + bk) : 0;
+  };
+  /* own cells, independent of other bricks */
+  {
+    unsigned char fa[OWN];
+    float va[OWN], pa[OWN];
+#pragma unroll
+    for (int u = 0; u < OWN; u++) {
+      int h;
+      size_t c;
+      bool in;
+      own_cell(u, h, c, in);
+      fa[u] = in ? A[c] : (unsigned char)CELL_AIR;
+      va[u] = !in ? 0.0f : (kind == 0 ? __ldg(a.diag + c) : (kind == 1 ? __ldcg(r + c) : 0.0f));
+      pa[u] = (in && kind != 0) ? __ldcg(a.Pic + c) : 0.0f;
     }
-    size_t c = cidx(i, j, k);
-    unsigned char f = A[c] == CELL_FLUID;
-    sm.fl[h] = f;
-    if (kind == 0) {
-      sm.v[h] = f ? a.diag[c] : 0.0f;
-    } else if (kind == 1) {
-      sm.v[h] = f ? __ldcg(r + c) : 0.0f;
-      sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
-    } else {
-      sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < OWN; u++) {
+      int h;
+      size_t c;
+      bool in;
+      own_cell(u, h, c, in);
+      unsigned char f = fa[u] == CELL_FLUID;
+      sm.fl[h] = f;
+      sm.v[h] = f ? va[u] : 0.0f;
+      sm.p[h] = f ? pa[u] : 0.0f;
     }
   }
   /* dependencies */
@@ -1095,39 +1110,58 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, 
   const int nbI = BI + dir, nbJ = BJ + dir, nbK = BK + dir;
   const unsigned *flags = kind == 2 ? a.bflag : a.fflag;
   const unsigned ep = kind == 2 ? epoch_b : epoch_f;
-  if (nbI >= 0 && nbI < nbx) wait_flag(flags + (nbI * nbx + BJ) * nbx + BK, ep, a.iflags);
-  if (nbJ >= 0 && nbJ < nbx) wait_flag(flags + (BI * nbx + nbJ) * nbx + BK, ep, a.iflags);
-  if (nbK >= 0 && nbK < nbx) wait_flag(flags + (BI * nbx + BJ) * nbx + nbK, ep, a.iflags);
   if (kind == 2) {
     /* the forward solve of this brick wrote q */
     wait_flag(a.fflag + brick, epoch_f, a.iflags);
-    for (int t = lane; t < BRK3; t += 32) {
-      int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
-      int i = i0 + bi, j = j0 + bj, k = k0 + bk;
-      int h = hidx(bi, bj, bk);
-      sm.v[h] = (inside(i, j, k) && sm.fl[h]) ? __ldcg(qz + cidx(i, j, k)) : 0.0f;
+    float qa[OWN];
+#pragma unroll
+    for (int u = 0; u < OWN; u++) {
+      int h;
+      size_t c;
+      bool in;
+      own_cell(u, h, c, in);
+      qa[u] = in ? __ldcg(qz + c) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < OWN; u++) {
+      int h;
+      size_t c;
+      bool in;
+      own_cell(u, h, c, in);
+      sm.v[h] = sm.fl[h] ? qa[u] : 0.0f;
     }
   }
+  if (nbI >= 0 && nbI < nbx) wait_flag(flags + (nbI * nbx + BJ) * nbx + BK, ep, a.iflags);
+  if (nbJ >= 0 && nbJ < nbx) wait_flag(flags + (BI * nbx + nbJ) * nbx + BK, ep, a.iflags);
+  if (nbK >= 0 && nbK < nbx) wait_flag(flags + (BI * nbx + BJ) * nbx + nbK, ep, a.iflags);
   /* halo faces: -1 (build/forward) or +1 (backward) along each axis */
   const int hf = kind == 2 ? BRK : -1;
-  for (int t = lane; t < 3 * BRK * BRK; t += 32) {
-    int face = t / (BRK * BRK), u = (t / BRK) % BRK, w = t % BRK;
-    /* face 0: (hf,u,w), face 1: (u,hf,w), face 2: (u,w,hf) */
-    int bi = face == 0 ? hf : u, bj = face == 1 ? hf : (face == 0 ? u : w),
-        bk = face == 2 ? hf : w;
-    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
-    int h = hidx(bi, bj, bk);
-    if (!inside(i, j, k)) {
-      sm.fl[h] = 0;
-      sm.v[h] = 0.0f;
-      sm.p[h] = 0.0f;
-      continue;
+  {
+    unsigned char fa[HALO];
+    float va[HALO], pa[HALO];
+    int ha[HALO];
+#pragma unroll
+    for (int u = 0; u < HALO; u++) {
+      int t = lane + 32 * u;
+      int face = t / (BRK * BRK), uu = (t / BRK) % BRK, w = t % BRK;
+      /* face 0: (hf,uu,w), face 1: (uu,hf,w), face 2: (uu,w,hf) */
+      int bi = face == 0 ? hf : uu, bj = face == 1 ? hf : (face == 0 ? uu : w),
+          bk = face == 2 ? hf : w;
+      int i = i0 + bi, j = j0 + bj, k = k0 + bk;
+      ha[u] = hidx(bi, bj, bk);
+      bool in = inside(i, j, k);
+      size_t c = in ? cidx(i, j, k) : 0;
+      fa[u] = in ? A[c] : (unsigned char)CELL_AIR;
+      pa[u] = in ? __ldcg(a.Pic + c) : 0.0f;
+      va[u] = (in && kind != 0) ? __ldcg(qz + c) : 0.0f;
     }
-    size_t c = cidx(i, j, k);
-    unsigned char f = A[c] == CELL_FLUID;
-    sm.fl[h] = f;
-    sm.p[h] = f ? __ldcg(a.Pic + c) : 0.0f;
-    sm.v[h] = (f && kind != 0) ? __ldcg(qz + c) : 0.0f;
+#pragma unroll
+    for (int u = 0; u < HALO; u++) {
+      unsigned char f = fa[u] == CELL_FLUID;
+      sm.fl[ha[u]] = f;
+      sm.p[ha[u]] = f ? pa[u] : 0.0f;
+      sm.v[ha[u]] = f ? va[u] : 0.0f;
+    }
   }
   __syncwarp();
   const float tau = a.mic_tau;
