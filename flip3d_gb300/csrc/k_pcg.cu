@@ -1043,21 +1043,27 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-/* every lane waits (bounded) until flag >= epoch */
+/* Lane 0 waits (bounded) until flag >= epoch with acquire loads; the warp
+ * barrier and fence then order the other lanes' loads after it. */
 __device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, int *iflags) {
-  unsigned long long spins = 0;
-  while (ld_acquire(flag) < epoch) {
-    if (++spins > FLAG_SPIN_LIMIT) {
-      atomicExch(iflags + IF_TIMEOUT, 1);
-      return;
+  if ((threadIdx.x & 31) == 0) {
+    unsigned long long spins = 0;
+    while (ld_acquire(flag) < epoch) {
+      if (++spins > FLAG_SPIN_LIMIT) {
+        atomicExch(iflags + IF_TIMEOUT, 1);
+        break;
+      }
+      __nanosleep(64);
     }
-    __nanosleep(20);
   }
+  __syncwarp();
+  __threadfence();
 }
 
 /* kind: 0 build the factor, 1 forward solve, 2 backward solve */
-__device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, unsigned epoch_f,
-                           unsigned epoch_b, const float *r, float *qz) {
+__device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl_tab, int brick,
+                           int kind, unsigned epoch_f, unsigned epoch_b, const float *r,
+                           float *qz) {
   const int lane = threadIdx.x & 31;
   const int n = a.s.n, nbx = a.nbx;
   const int BI = brick / (nbx * nbx), BJ = (brick / nbx) % nbx, BK = brick % nbx;
@@ -1167,8 +1173,8 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, 
   const float tau = a.mic_tau;
   for (int pl = 0; pl < NPLANES; pl++) {
     const int d = kind == 2 ? NPLANES - 1 - pl : pl;
-    for (int e = c_planes.start[d] + lane; e < c_planes.start[d + 1]; e += 32) {
-      unsigned cc = c_planes.cell[e];
+    for (int e = pl_tab.start[d] + lane; e < pl_tab.start[d + 1]; e += 32) {
+      unsigned cc = pl_tab.cell[e];
       int bi = cc >> 6, bj = (cc >> 3) & 7, bk = cc & 7;
       int h = hidx(bi, bj, bk);
       if (!sm.fl[h]) continue;
@@ -1235,8 +1241,9 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, int brick, int kind, 
 
 /* Run one factor build (tasks = nbricks) or one forward+backward apply
  * (tasks = 2*nbricks) over the ticket counter. */
-__device__ void wavefront(const CgArgs &a, BrickSmem *sm_all, bool build, unsigned epoch_f,
-                          unsigned epoch_b, const float *r, float *qz) {
+__device__ void wavefront(const CgArgs &a, BrickSmem *sm_all, const BrickPlanes &pl_tab,
+                          bool build, unsigned epoch_f, unsigned epoch_b, const float *r,
+                          float *qz) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BrickSmem &sm = sm_all[warp];
   const unsigned tasks = build ? (unsigned)a.nbricks : 2u * (unsigned)a.nbricks;
@@ -1247,9 +1254,10 @@ __device__ void wavefront(const CgArgs &a, BrickSmem *sm_all, bool build, unsign
     if (t >= tasks) break;
     if (*(volatile int *)(a.iflags + IF_TIMEOUT)) break;
     if (t < (unsigned)a.nbricks)
-      brick_task(a, sm, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
+      brick_task(a, sm, pl_tab, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
     else
-      brick_task(a, sm, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r, qz);
+      brick_task(a, sm, pl_tab, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r,
+                 qz);
   }
 }
 
@@ -1267,6 +1275,11 @@ __device__ __forceinline__ double sum_brick_parts(const CgArgs &a) {
 __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   extern __shared__ unsigned char dyn[];
   BrickSmem *sm = reinterpret_cast<BrickSmem *>(dyn);
+  /* the intra-brick plane table, read with lane-varying indices */
+  __shared__ BrickPlanes pl_tab;
+  for (int i = threadIdx.x; i < BRK3; i += CG_BLOCK) pl_tab.cell[i] = c_planes.cell[i];
+  for (int i = threadIdx.x; i <= NPLANES; i += CG_BLOCK) pl_tab.start[i] = c_planes.start[i];
+  __syncthreads();
   const unsigned nb = gridDim.x;
   const size_t stride = (size_t)nb * CG_BLOCK;
   const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
@@ -1276,7 +1289,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   unsigned apply = 0; /* preconditioner applications so far */
 
   /* factor (forward-type sweep, epoch 1) */
-  wavefront(a, sm, true, 1u, 0u, nullptr, nullptr);
+  wavefront(a, sm, pl_tab, true, 1u, 0u, nullptr, nullptr);
   if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
   /* r = b - A x; b.b, r.r */
   FF pbb = ff_zero(), prr = ff_zero();
@@ -1305,7 +1318,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   double e2 = rr, azr = 0.0;
   if (!done) {
     apply++;
-    wavefront(a, sm, false, apply + 1, apply, a.r, a.z);
+    wavefront(a, sm, pl_tab, false, apply + 1, apply, a.r, a.z);
     if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
     azr = sum_brick_parts(a);
   }
@@ -1350,7 +1363,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
     if (iters >= a.max_iters) { done = 3; break; }
     /* z = M^-1 r by the two wavefront sweeps; z.r per brick */
     apply++;
-    wavefront(a, sm, false, apply + 1, apply, a.r, a.z);
+    wavefront(a, sm, pl_tab, false, apply + 1, apply, a.r, a.z);
     if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
     const double zr = sum_brick_parts(a);
     beta_f = (float)(zr / azr);
