@@ -171,7 +171,7 @@ void free_all(FlipGpu *h) {
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
-                  h->ticket, h->brick_part};
+                  h->ticket, h->brick_part, h->repo_draw, h->repo_res, h->repo_old};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -326,6 +326,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->scal, SC_COUNT) AL(h->iflags, IF_COUNT) AL(h->flag, cap) AL(h->scan_a, scan_n)
   AL(h->scan_b, scan_n) AL(h->scan_tmp, h->scan_cap) AL(h->stuck_idx, cap)
   AL(h->water_idx, nc) AL(h->stage, 3 * cap)
+  AL(h->repo_draw, cap) AL(h->repo_res, cap) AL(h->repo_old, cap)
   h->nbx = (p->n + 7) / 8;
   h->nbricks = h->nbx * h->nbx * h->nbx;
   AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
@@ -364,6 +365,12 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   }
   if (cg_grid_size(h->cg_grid) != 0)
     h->cg_grid[0] = h->cg_grid[1] = h->cg_grid[2] = h->cg_grid[3] = 0;
+  if (particles_init_device() != 0) {
+    free_all(h);
+    cudaStreamDestroy(h->own_stream);
+    delete h;
+    return FLIPGPU_ECUDA;
+  }
   *out = h;
   return FLIPGPU_OK;
 }

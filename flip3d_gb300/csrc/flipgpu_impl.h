@@ -116,6 +116,8 @@ struct FlipGpu {
   uint8_t *flag;      /* per particle / per cell */
   uint32_t *scan_a, *scan_b, *scan_tmp;
   uint32_t *stuck_idx, *water_idx;
+  uint32_t *repo_draw;       /* shuffle draws when the list exceeds shared memory */
+  float4 *repo_res, *repo_old; /* per stuck particle: resampled / previous velocity */
   size_t scan_cap;
 
   float *stage;       /* AoS staging for downloads */
@@ -174,6 +176,7 @@ cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, floa
                                    float re);
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
+int particles_init_device();
 
 /* device-wide exclusive scan of n uint32 (in may equal out) */
 cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,

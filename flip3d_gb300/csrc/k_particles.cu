@@ -17,6 +17,7 @@ using namespace refmath;
 namespace {
 
 constexpr int BLK = 256;
+constexpr int REPO_GRID = 152 * 4; /* grid-stride launches over the stuck list */
 
 /* Visit the slots of cells [i0,i1]x[j0,j1]x[k0,k1] (clipped to the grid) in
  * the reference's order; f(slot). */
@@ -320,28 +321,55 @@ __global__ void k_compact(size_t n, const uint32_t *__restrict__ flag,
 
 /* reposition (src/flip3D.cpp:405-441): deep-water cells in order, repeated
  * until there are as many as stuck particles, shuffled with the keyed
- * Fisher-Yates, then each stuck particle placed at a keyed spot in its
- * cell. One thread: the shuffle is sequential and the lists are short. */
-__global__ void k_repo_place(SimConst c, const int *__restrict__ counts,
-                             const uint32_t *__restrict__ stuck_idx,
-                             const uint32_t *__restrict__ water_idx,
-                             uint32_t *__restrict__ waters, float *__restrict__ px,
-                             float *__restrict__ py, float *__restrict__ pz) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+ * Fisher-Yates (my_rand_shuffle, src/utility.cpp:28-30). The draws are
+ * independent and computed in parallel; the swaps are sequential and run on
+ * one thread over shared memory (REPO_SMEM entries; longer lists swap in
+ * global memory). */
+constexpr int REPO_SMEM = 16384;
+constexpr int REPO_THREADS = 1024;
+
+__global__ void __launch_bounds__(REPO_THREADS)
+    k_repo_shuffle(SimConst c, const int *__restrict__ counts,
+                   const uint32_t *__restrict__ water_idx, uint32_t *__restrict__ waters,
+                   uint32_t *__restrict__ draws) {
+  extern __shared__ uint32_t sm[];
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
   if (m == 0 || w == 0) return;
-  for (int q = 0; q < m; q++) waters[q] = water_idx[q % w];
-  for (int q = m - 1; q >= 1; q--) {
+  const bool in_smem = m <= REPO_SMEM;
+  uint32_t *wv = in_smem ? sm : waters;
+  uint32_t *dj = in_smem ? sm + REPO_SMEM : draws;
+  for (int q = threadIdx.x; q < m; q += blockDim.x) {
+    wv[q] = water_idx[q % w];
     uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_SHUFFLE, (uint64_t)c.step, 0),
                              (uint64_t)q, 0);
-    int j = (int)(r % (uint32_t)(q + 1));
-    uint32_t t = waters[q];
-    waters[q] = waters[j];
-    waters[j] = t;
+    dj[q] = r % (uint32_t)(q + 1);
   }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = m - 1; q >= 1; q--) {
+      uint32_t j = dj[q];
+      uint32_t t = wv[q];
+      wv[q] = wv[j];
+      wv[j] = t;
+    }
+  }
+  __syncthreads();
+  if (in_smem)
+    for (int q = threadIdx.x; q < m; q += blockDim.x) waters[q] = wv[q];
+}
+
+/* Each stuck particle q placed at a keyed spot in cell waters[q]
+ * (src/flip3D.cpp:435-441); also records q in rank[particle]. */
+__global__ void k_repo_place(SimConst c, const int *__restrict__ counts,
+                             const uint32_t *__restrict__ stuck_idx,
+                             const uint32_t *__restrict__ waters, uint32_t *__restrict__ rank,
+                             float *__restrict__ px, float *__restrict__ py,
+                             float *__restrict__ pz) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
   const int n = c.n;
   const double h = (double)c.re_repo;
-  for (int q = 0; q < m; q++) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
     uint32_t cell = waters[q];
     int cc[3] = {(int)(cell / ((uint32_t)n * n)), (int)((cell / n) % n), (int)(cell % n)};
     float out[3];
@@ -355,51 +383,127 @@ __global__ void k_repo_place(SimConst c, const int *__restrict__ counts,
     px[p] = out[0];
     py[p] = out[1];
     pz[p] = out[2];
+    rank[p] = (uint32_t)q;
   }
 }
 
-/* corrector::resample (src/corrector.cpp:15-47) at particle position p for
- * the repositioned particles, in order, one thread: a later particle sees
- * the already-resampled velocity of an earlier one, as in the reference's
- * loop (src/flip3D.cpp:445-450). Neighbour velocities come from the
- * canonical arrays for that reason. */
-__global__ void k_repo_resample(SimConst c, const int *__restrict__ counts,
-                                const uint32_t *__restrict__ stuck_idx,
-                                const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
-                                const float4 *__restrict__ spos, const float *__restrict__ px,
-                                const float *__restrict__ py, const float *__restrict__ pz,
-                                float *__restrict__ vx, float *__restrict__ vy,
-                                float *__restrict__ vz) {
+/* corrector::resample (src/corrector.cpp:15-47) at the position of stuck
+ * particle q. The reference resamples the stuck particles one after another
+ * (src/flip3D.cpp:445-450), so particle q sees the new velocity of every
+ * stuck particle q' < q and the old velocity of every q' >= q. `vel_of`
+ * supplies a neighbour's velocity under that rule; `dep` is set when a
+ * contributing neighbour is a stuck particle q' < q. */
+template <class V>
+__device__ __forceinline__ float3 repo_resample_one(const SimConst &c, float3 P, uint32_t q,
+                                                    const uint32_t *__restrict__ cs,
+                                                    const uint32_t *__restrict__ perm,
+                                                    const float4 *__restrict__ spos,
+                                                    const uint8_t *__restrict__ stuck,
+                                                    const uint32_t *__restrict__ rank,
+                                                    bool &dep, V vel_of) {
+  int ci = cell_clamp(P.x, c.fn, c.n), cj = cell_clamp(P.y, c.fn, c.n),
+      ck = cell_clamp(P.z, c.fn, c.n);
+  float u[3] = {0.0f, 0.0f, 0.0f};
+  float wsum = 0.0f;
+  visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
+    float4 Q = spos[b];
+    if (unpack_type(Q.w) != CELL_FLUID) return;
+    float d2 = hypot2_ref(P.x - Q.x, P.y - Q.y, P.z - Q.z);
+    if (!(d2 < c.re_repo_hh)) return; /* weight exactly 0 */
+    float wt = sharp_ref(d2, c.re_repo_hh, c.r2_floor, c.sharp_small_repo);
+    uint32_t o = perm[b];
+    bool is_stuck = stuck[o] != 0;
+    uint32_t ro = is_stuck ? rank[o] : 0xffffffffu;
+    if (is_stuck && ro < q) dep = true;
+    float3 v = vel_of(o, is_stuck, ro);
+    u[0] += wt * v.x;
+    u[1] += wt * v.y;
+    u[2] += wt * v.z;
+    wsum += wt;
+  });
+  if (wsum != 0.0f) {
+    u[0] /= wsum;
+    u[1] /= wsum;
+    u[2] /= wsum;
+  }
+  return make_float3(u[0], u[1], u[2]);
+}
+
+/* All stuck particles in parallel with the velocities before the
+ * resample; a particle with no earlier stuck neighbour gets its final value
+ * here (res.w = 0), the others are redone in order by k_repo_ordered
+ * (res.w = 1). old[q] keeps the velocity before the resample. */
+__global__ void k_repo_gather(SimConst c, const int *__restrict__ counts,
+                              const uint32_t *__restrict__ stuck_idx,
+                              const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                              const float4 *__restrict__ spos, const uint8_t *__restrict__ stuck,
+                              const uint32_t *__restrict__ rank, const float *__restrict__ px,
+                              const float *__restrict__ py, const float *__restrict__ pz,
+                              const float *__restrict__ vx, const float *__restrict__ vy,
+                              const float *__restrict__ vz, float4 *__restrict__ res,
+                              float4 *__restrict__ old) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    uint32_t p = stuck_idx[q];
+    float3 P = make_float3(px[p], py[p], pz[p]);
+    bool dep = false;
+    float3 u = repo_resample_one(c, P, (uint32_t)q, cs, perm, spos, stuck, rank, dep,
+                                 [&](uint32_t o, bool, uint32_t) {
+                                   return make_float3(vx[o], vy[o], vz[o]);
+                                 });
+    res[q] = make_float4(u.x, u.y, u.z, dep ? 1.0f : 0.0f);
+    old[q] = make_float4(vx[p], vy[p], vz[p], 0.0f);
+  }
+}
+
+__global__ void k_repo_commit(const int *__restrict__ counts,
+                              const uint32_t *__restrict__ stuck_idx,
+                              const float4 *__restrict__ res, float *__restrict__ vx,
+                              float *__restrict__ vy, float *__restrict__ vz) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    float4 r = res[q];
+    if (r.w != 0.0f) continue;
+    uint32_t p = stuck_idx[q];
+    vx[p] = r.x;
+    vy[p] = r.y;
+    vz[p] = r.z;
+  }
+}
+
+/* The dependent particles in increasing q, one thread: neighbours that are
+ * stuck particles q' < q are read with their new velocity (already
+ * committed), q' >= q with the old one. */
+__global__ void k_repo_ordered(SimConst c, const int *__restrict__ counts,
+                               const uint32_t *__restrict__ stuck_idx,
+                               const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                               const float4 *__restrict__ spos, const uint8_t *__restrict__ stuck,
+                               const uint32_t *__restrict__ rank, const float *__restrict__ px,
+                               const float *__restrict__ py, const float *__restrict__ pz,
+                               float *__restrict__ vx, float *__restrict__ vy,
+                               float *__restrict__ vz, const float4 *__restrict__ res,
+                               const float4 *__restrict__ old) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
-  if (m == 0 || w == 0) return;
+  if (w == 0) return;
   for (int q = 0; q < m; q++) {
+    if (res[q].w == 0.0f) continue;
     uint32_t p = stuck_idx[q];
-    float P[3] = {px[p], py[p], pz[p]};
-    int ci = cell_clamp(P[0], c.fn, c.n), cj = cell_clamp(P[1], c.fn, c.n),
-        ck = cell_clamp(P[2], c.fn, c.n);
-    float u[3] = {0.0f, 0.0f, 0.0f};
-    float wsum = 0.0f;
-    visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
-      float4 Q = spos[b];
-      if (unpack_type(Q.w) != CELL_FLUID) return;
-      float d2 = hypot2_ref(P[0] - Q.x, P[1] - Q.y, P[2] - Q.z);
-      if (!(d2 < c.re_repo_hh)) return;
-      float wt = sharp_ref(d2, c.re_repo_hh, c.r2_floor, c.sharp_small_repo);
-      uint32_t o = perm[b];
-      u[0] += wt * vx[o];
-      u[1] += wt * vy[o];
-      u[2] += wt * vz[o];
-      wsum += wt;
-    });
-    if (wsum != 0.0f) {
-      u[0] /= wsum;
-      u[1] /= wsum;
-      u[2] /= wsum;
-    }
-    vx[p] = u[0];
-    vy[p] = u[1];
-    vz[p] = u[2];
+    float3 P = make_float3(px[p], py[p], pz[p]);
+    bool dep = false;
+    float3 u = repo_resample_one(c, P, (uint32_t)q, cs, perm, spos, stuck, rank, dep,
+                                 [&](uint32_t o, bool is_stuck, uint32_t ro) {
+                                   if (is_stuck && ro >= (uint32_t)q) {
+                                     float4 v = old[ro];
+                                     return make_float3(v.x, v.y, v.z);
+                                   }
+                                   return make_float3(vx[o], vy[o], vz[o]);
+                                 });
+    vx[p] = u.x;
+    vy[p] = u.y;
+    vz[p] = u.z;
   }
 }
 
@@ -678,15 +782,24 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
   if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->nc)) != cudaSuccess) return e;
   k_compact<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->nc, h->scan_a, h->scan_b,
                                                          h->water_idx, h->iflags + IF_NWATER);
-  k_repo_place<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->water_idx, h->scan_b,
-                                        h->px, h->py, h->pz);
+  k_repo_shuffle<<<1, REPO_THREADS, 2 * REPO_SMEM * sizeof(uint32_t), h->stream>>>(
+      c, h->iflags, h->water_idx, h->scan_b, h->repo_draw);
+  k_repo_place<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->scan_b,
+                                                 h->scan_a, h->px, h->py, h->pz);
   FG_LAUNCHED(h, 2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   /* sorter::sort (src/flip3D.cpp:443), shared with the corrector's sort. */
   if ((e = launch_sort(h, 0)) != cudaSuccess) return e;
-  k_repo_resample<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start, h->perm,
-                                           h->spos, h->px, h->py, h->pz, h->vx, h->vy, h->vz);
-  FG_LAUNCHED(h, 1);
+  k_repo_gather<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start,
+                                                  h->perm, h->spos, h->flag, h->scan_a, h->px,
+                                                  h->py, h->pz, h->vx, h->vy, h->vz,
+                                                  h->repo_res, h->repo_old);
+  k_repo_commit<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->stuck_idx, h->repo_res, h->vx,
+                                                  h->vy, h->vz);
+  k_repo_ordered<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start, h->perm,
+                                          h->spos, h->flag, h->scan_a, h->px, h->py, h->pz,
+                                          h->vx, h->vy, h->vz, h->repo_res, h->repo_old);
+  FG_LAUNCHED(h, 3);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   /* refresh the sorted velocities of the resampled particles */
   if ((e = launch_payload(h, 0)) != cudaSuccess) return e;
@@ -711,4 +824,16 @@ cudaError_t launch_correct(FlipGpu *h) {
                                                           h->vy, h->vz);
   FG_LAUNCHED(h, 2);
   return cudaGetLastError();
+}
+
+int particles_init_device() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (done[dev]) return 0;
+  if (cudaFuncSetAttribute(k_repo_shuffle, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(2 * REPO_SMEM * sizeof(uint32_t))) != cudaSuccess)
+    return -1;
+  done[dev] = true;
+  return 0;
 }

@@ -129,10 +129,20 @@ RM_FN float sharp_ref(float r2, float hh, float r2_floor, float small) {
   if (!(r2 < hh)) return 0.0f;
   if (r2 < r2_floor) return small;
   float q = hh / r2;                  /* correctly rounded quotient */
-  /* Near the support edge q - 1 cancels and the reference's own double
-   * rounding of hh/r2 (2^-53 of q) reaches 2^-12 of a float ulp of the
-   * result; evaluate its expression there. */
-  if (q < 1.00390625f) return (float)((double)hh / (double)r2 - 1.0);
+  /* Near the support edge (q < 1 + 2^-8) q - 1 cancels: there hh - r2 is
+   * exact (Sterbenz), so D/r2 rounds the exact value once. The reference
+   * rounds hh/r2 to double first, which can move a result lying within about
+   * 2^-12 ulp of a tie; those go to its double expression. */
+  if (q < 1.00390625f) {
+    float D = hh - r2;
+    float X = D / r2;
+    float R = fmaf(-X, r2, D);        /* exact remainder */
+    float t = R / r2;
+    float gapx = from_bits(bits_of(X) + 1) - X;
+    if (fabsf(fabsf(t) - 0.5f * gapx) <= gapx * 0x1p-10f || X == 0.0f)
+      return (float)((double)hh / (double)r2 - 1.0);
+    return X;
+  }
   float rem = fmaf(-q, r2, hh);       /* hh - q*r2, exact */
   float t, e;
   two_sum(q, -1.0f, t, e);            /* t + e == q - 1 exactly */

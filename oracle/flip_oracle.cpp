@@ -24,6 +24,7 @@
  */
 #include "flip_oracle.h"
 #include "../include/flip_rng.h"
+#include "../include/flip_mc_table.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1140,6 +1141,26 @@ extern "C" void orc_sim_get_grid(const OrcSim *s, float *u0, float *u1, float *u
   if (press) std::memcpy(press, s->press.data(), s->press.size() * sizeof(float));
 }
 
+/* Overwrite particle or grid state (null pointers leave a field as it is);
+ * stage-level tests start both implementations from one state. */
+extern "C" void orc_sim_put(OrcSim *s, const float *pos, const float *vel,
+                            const float *dens) {
+  if (pos) std::memcpy(s->pos.data(), pos, s->pos.size() * sizeof(float));
+  if (vel) std::memcpy(s->vel.data(), vel, s->vel.size() * sizeof(float));
+  if (dens) std::memcpy(s->dens.data(), dens, s->dens.size() * sizeof(float));
+}
+
+extern "C" void orc_sim_put_grid(OrcSim *s, const float *u0, const float *u1,
+                                 const float *u2, const uint8_t *A, const float *L,
+                                 const float *press) {
+  const float *src[3] = {u0, u1, u2};
+  for (int c = 0; c < 3; c++)
+    if (src[c]) std::memcpy(s->u[c].data(), src[c], s->u[c].size() * sizeof(float));
+  if (A) std::memcpy(s->A.data(), A, s->A.size());
+  if (L) std::memcpy(s->L.data(), L, s->L.size() * sizeof(float));
+  if (press) std::memcpy(s->press.data(), press, s->press.size() * sizeof(float));
+}
+
 extern "C" int orc_sim_last_stuck(const OrcSim *s) { return s->last_stuck; }
 extern "C" double orc_sim_last_r2(const OrcSim *s) { return s->last_r2; }
 extern "C" void orc_sim_set_step(OrcSim *s, int64_t step) { s->step = step; }
@@ -1177,3 +1198,221 @@ extern "C" float orc_max_density(int n, float density) {
   for (int p = 0; p < np; p++) md = (float)std::fmax((double)md, (double)dens[p]);
   return md;
 }
+
+/* ================================================================ mesher */
+
+namespace {
+
+/* implicit_func (src/implicit.cpp:14-27) over the 5^3 cells around p
+ * (src/implicit.cpp:29-38). The value only depends on the set of
+ * neighbours: a min over fluid distances, or the wall constant if any wall
+ * particle is closer than density/gn. */
+double implicit_at(const Cells &cells, const float *pos, const uint8_t *type,
+                   const float p[3], float density) {
+  const int gn = cells.gn;
+  const int ci = cell_clamp(p[0], gn), cj = cell_clamp(p[1], gn), ck = cell_clamp(p[2], gn);
+  double phi = 8.0 * (double)density / gn;
+  const float wall_r = density / (float)gn;
+  bool wall = false;
+  cells.visit(ci - 2, ci + 2, cj - 2, cj + 2, ck - 2, ck + 2, [&](uint32_t q) {
+    if (wall) return;
+    float d = length(pos + 3 * (size_t)q, p);
+    if (type[q] == ORC_WALL) {
+      if (d < wall_r) wall = true;
+      return;
+    }
+    if ((double)d < phi) phi = d;
+  });
+  if (wall) return 4.5 * (double)density / gn;
+  return phi - (double)wall_r;
+}
+
+inline bool is_normal(double x) { return std::isnormal(x); }
+
+} // namespace
+
+struct OrcMesh {
+  int mg;
+  std::vector<float> phi;     /* (mg)^3, x fastest */
+  std::vector<double> vert, nrm;
+  std::vector<int32_t> faces;
+  int64_t ntris;
+};
+
+extern "C" void orc_implicit(int n, const float *pos, const uint8_t *type,
+                             const uint32_t *cs, const uint32_t *perm, float density,
+                             int m, const float *pts, double *out) {
+  Cells cells{n, cs, perm};
+  for (int i = 0; i < m; i++) out[i] = implicit_at(cells, pos, type, pts + 3 * i, density);
+}
+
+/* generateMesh (src/mesher.cpp:137-195): field, marching cubes
+ * (src/rchandra/CIsoSurface.cpp:331-780), long-edge face filter, connections
+ * and two smoothing passes. Marching cubes is restated without its maps:
+ * every cut grid edge gets one vertex, numbered in increasing edge id
+ * 3*node + axis (node = (z*(n+1) + y)*(n+1) + x); triangles come cell by
+ * cell with x outermost and z innermost, each cell's in table order. */
+extern "C" OrcMesh *orc_mesh(int n, const float *pos, const uint8_t *type,
+                             const uint32_t *cs, const uint32_t *perm, float density) {
+  OrcMesh *M = new OrcMesh;
+  const int mg = n + 1, C = n;
+  M->mg = mg;
+  const size_t nn = (size_t)mg * mg * mg;
+  M->phi.resize(nn);
+  Cells cells{n, cs, perm};
+  /* density field (src/mesher.cpp:142-153) */
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int i = 0; i < mg; i++)
+    for (int j = 0; j < mg; j++)
+      for (int k = 0; k < mg; k++) {
+        const double h = 1.0 / (double)(mg - 1);
+        float p[3] = {(float)(i * h), (float)(j * h), (float)(k * h)};
+        double value = implicit_at(cells, pos, type, p, density);
+        if (i == 0 || i == mg - 1 || j == 0 || j == mg - 1 || k == 0 || k == mg - 1)
+          value = std::fmax(value, 0.01);
+        M->phi[((size_t)mg * mg) * k + (size_t)mg * j + i] = (float)(-value);
+      }
+  const float *F = M->phi.data();
+  auto node = [&](int x, int y, int z) { return ((size_t)z * mg + y) * mg + x; };
+  auto inside = [&](size_t v) { return F[v] < 0.0f; };
+  const float L = (float)(1.0 / (double)(mg - 1));
+  /* vertices: one per cut edge in increasing edge id */
+  std::vector<int32_t> vid(3 * nn, -1);
+  std::vector<float> V;
+  for (int z = 0; z <= C; z++)
+    for (int y = 0; y <= C; y++)
+      for (int x = 0; x <= C; x++) {
+        const size_t b = node(x, y, z);
+        for (int a = 0; a < 3; a++) {
+          int fx = x + (a == 0), fy = y + (a == 1), fz = z + (a == 2);
+          if (fx > C || fy > C || fz > C) continue;
+          const size_t f = node(fx, fy, fz);
+          if (inside(b) == inside(f)) continue;
+          /* The cell that owns the edge interpolates it: from the far node
+           * to the base node for x edges below the top y row and for y edges
+           * on the last x column, from the base node otherwise
+           * (CalculateIntersection, src/rchandra/CIsoSurface.cpp:580-680). */
+          bool rev = (a == 0 && y < C) || (a == 1 && x == C);
+          int v1[3] = {x, y, z}, v2[3] = {fx, fy, fz};
+          if (rev) std::swap(v1, v2);
+          float val1 = F[node(v1[0], v1[1], v1[2])], val2 = F[node(v2[0], v2[1], v2[2])];
+          float mu = (0.0f - val1) / (val2 - val1);
+          vid[3 * b + a] = (int32_t)(V.size() / 3);
+          for (int d = 0; d < 3; d++) {
+            float p1 = (float)(unsigned)v1[d] * L, p2 = (float)(unsigned)v2[d] * L;
+            V.push_back(p1 + mu * (p2 - p1));
+          }
+        }
+      }
+  const size_t nv = V.size() / 3;
+  /* triangles */
+  signed char tri[256][16];
+  unsigned char tcount[256];
+  flip_mc_decode(tri, tcount);
+  std::vector<int32_t> T;
+  for (int x = 0; x < C; x++)
+    for (int y = 0; y < C; y++)
+      for (int z = 0; z < C; z++) {
+        unsigned idx = 0;
+        for (int c = 0; c < 8; c++)
+          if (inside(node(x + FLIP_MC_CORNER[c][0], y + FLIP_MC_CORNER[c][1],
+                          z + FLIP_MC_CORNER[c][2])))
+            idx |= 1u << c;
+        for (int t = 0; t < 3 * tcount[idx]; t++) {
+          const unsigned char *e = FLIP_MC_EDGE_NODE[tri[idx][t]];
+          T.push_back(vid[3 * node(x + e[0], y + e[1], z + e[2]) + e[3]]);
+        }
+      }
+  const size_t nt = T.size() / 3;
+  M->ntris = (int64_t)nt;
+  /* CalculateNormals (src/rchandra/CIsoSurface.cpp:740-778): all triangles */
+  std::vector<float> Nf(3 * nv, 0.0f);
+  for (size_t t = 0; t < nt; t++) {
+    const float *p0 = &V[3 * (size_t)T[3 * t]], *p1 = &V[3 * (size_t)T[3 * t + 1]],
+                *p2 = &V[3 * (size_t)T[3 * t + 2]];
+    float a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+    float b[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+    float nr[3] = {a[2] * b[1] - a[1] * b[2], a[0] * b[2] - a[2] * b[0],
+                   a[1] * b[0] - a[0] * b[1]};
+    for (int q = 0; q < 3; q++)
+      for (int d = 0; d < 3; d++) Nf[3 * (size_t)T[3 * t + q] + d] += nr[d];
+  }
+  for (size_t v = 0; v < nv; v++) {
+    float *x = &Nf[3 * v];
+    float len = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    x[0] /= len;
+    x[1] /= len;
+    x[2] /= len;
+  }
+  /* faces with every edge shorter than 0.1 (src/mesher.cpp:166-183) */
+  const double maxlen2 = 0.1 * 0.1;
+  for (size_t t = 0; t < nt; t++) {
+    const float *p0 = &V[3 * (size_t)T[3 * t]], *p1 = &V[3 * (size_t)T[3 * t + 1]],
+                *p2 = &V[3 * (size_t)T[3 * t + 2]];
+    if (length2(p0, p1) < maxlen2 && length2(p1, p2) < maxlen2 && length2(p0, p2) < maxlen2)
+      for (int q = 0; q < 3; q++) M->faces.push_back(T[3 * t + q]);
+  }
+  /* buildConnection (src/mesher.cpp:89-101) */
+  std::vector<std::vector<int32_t>> conn(nv);
+  for (size_t f = 0; f < M->faces.size(); f += 3) {
+    int32_t a = M->faces[f], b = M->faces[f + 1], c = M->faces[f + 2];
+    conn[a].push_back(b), conn[a].push_back(c);
+    conn[b].push_back(a), conn[b].push_back(c);
+    conn[c].push_back(a), conn[c].push_back(b);
+  }
+  /* smoothMesh(..., 2, 1, 1) (src/mesher.cpp:13-87) */
+  std::vector<double> &X = M->vert, &Y = M->nrm;
+  X.assign(V.begin(), V.end());
+  Y.assign(Nf.begin(), Nf.end());
+  std::vector<double> cx(3 * nv, 0.0), cy(3 * nv, 0.0);
+  for (int it = 0; it < 2; it++) {
+#pragma omp parallel for schedule(static)
+    for (long vi = 0; vi < (long)nv; vi++) {
+      float wsum = 0.0f;
+      double v[3] = {0.0, 0.0, 0.0}, vn[3] = {0.0, 0.0, 0.0};
+      auto add = [&](size_t u) {
+        for (int d = 0; d < 3; d++)
+          if (!is_normal(X[3 * u + d]) || !is_normal(Y[3 * u + d])) return;
+        for (int d = 0; d < 3; d++) {
+          v[d] += 1.0 * X[3 * u + d];
+          vn[d] += 1.0 * Y[3 * u + d];
+        }
+        wsum += 1.0f;
+      };
+      add((size_t)vi);
+      for (int32_t u : conn[vi]) add((size_t)u);
+      float len = hypotf((float)vn[0], hypotf((float)vn[1], (float)vn[2]));
+      for (int d = 0; d < 3; d++) {
+        if (wsum != 0.0f) cx[3 * vi + d] = v[d] / (double)wsum;
+        if (len != 0.0f) cy[3 * vi + d] = vn[d] / len;
+      }
+    }
+    X = cx;
+    Y = cy;
+  }
+  return M;
+}
+
+/* The mesh write_mesh makes after a step (src/flip3D.cpp:999-1004): the
+ * lists of the last sort over the current positions. */
+extern "C" OrcMesh *orc_sim_mesh(const OrcSim *s) {
+  return orc_mesh(s->prm.n, s->pos.data(), s->type.data(), s->cs.data(), s->perm.data(),
+                  s->prm.density);
+}
+
+extern "C" void orc_mesh_counts(const OrcMesh *m, int64_t *nverts, int64_t *nfaces,
+                                int64_t *ntris) {
+  if (nverts) *nverts = (int64_t)(m->vert.size() / 3);
+  if (nfaces) *nfaces = (int64_t)(m->faces.size() / 3);
+  if (ntris) *ntris = m->ntris;
+}
+
+extern "C" void orc_mesh_get(const OrcMesh *m, double *vertices, double *normals,
+                             int32_t *faces, float *phi) {
+  if (vertices) std::memcpy(vertices, m->vert.data(), m->vert.size() * sizeof(double));
+  if (normals) std::memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(double));
+  if (faces) std::memcpy(faces, m->faces.data(), m->faces.size() * sizeof(int32_t));
+  if (phi) std::memcpy(phi, m->phi.data(), m->phi.size() * sizeof(float));
+}
+
+extern "C" void orc_mesh_free(OrcMesh *m) { delete m; }

@@ -128,10 +128,31 @@ void orc_sim_get(const OrcSim *s, float *pos, float *vel, float *dens,
                  uint8_t *type);
 void orc_sim_get_grid(const OrcSim *s, float *u0, float *u1, float *u2,
                       uint8_t *A, float *L, float *press);
+void orc_sim_put(OrcSim *s, const float *pos, const float *vel, const float *dens);
+void orc_sim_put_grid(OrcSim *s, const float *u0, const float *u1, const float *u2,
+                      const uint8_t *A, const float *L, const float *press);
 int orc_sim_last_stuck(const OrcSim *s);
 double orc_sim_last_r2(const OrcSim *s);
 void orc_sim_set_step(OrcSim *s, int64_t step);
 void orc_sim_set_threads(int nthreads);
+
+/* implicit::implicit_func (src/implicit.cpp:14-38) at m points. */
+void orc_implicit(int n, const float *pos, const uint8_t *type, const uint32_t *cs,
+                  const uint32_t *perm, float density, int m, const float *pts,
+                  double *out);
+
+/* mesher::generateMesh (src/mesher.cpp:137-195) with mg = n+1 on the cell
+ * lists cs/perm over positions pos. The result stays in an OrcMesh until
+ * orc_mesh_free; phi is the field it meshed, (n+1)^3 floats in the
+ * reference's layout (x fastest). */
+typedef struct OrcMesh OrcMesh;
+OrcMesh *orc_mesh(int n, const float *pos, const uint8_t *type, const uint32_t *cs,
+                  const uint32_t *perm, float density);
+void orc_mesh_counts(const OrcMesh *m, int64_t *nverts, int64_t *nfaces, int64_t *ntris);
+void orc_mesh_get(const OrcMesh *m, double *vertices, double *normals, int32_t *faces,
+                  float *phi);
+void orc_mesh_free(OrcMesh *m);
+OrcMesh *orc_sim_mesh(const OrcSim *s);
 
 /* Max-density calibration (src/flip3D.cpp:689-709). */
 float orc_max_density(int n, float density);

@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 PRECOND_NONE, PRECOND_REF, PRECOND_IC = 0, 1, 2
 
@@ -75,12 +77,23 @@ def lib():
         L.orc_sim_stage.argtypes = [C.c_void_p, C.c_int]
         L.orc_sim_get.argtypes = [C.c_void_p, f32p, f32p, f32p, u8p]
         L.orc_sim_get_grid.argtypes = [C.c_void_p, f32p, f32p, f32p, u8p, f32p, f32p]
+        L.orc_sim_put.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_sim_put_grid.argtypes = [C.c_void_p] + [C.c_void_p] * 6
         L.orc_sim_last_stuck.argtypes = [C.c_void_p]
         L.orc_sim_last_stuck.restype = C.c_int
         L.orc_sim_last_r2.argtypes = [C.c_void_p]
         L.orc_sim_last_r2.restype = C.c_double
         L.orc_sim_set_step.argtypes = [C.c_void_p, C.c_int64]
         L.orc_sim_set_threads.argtypes = [C.c_int]
+        L.orc_implicit.argtypes = [C.c_int, f32p, u8p, u32p, u32p, C.c_float, C.c_int, f32p,
+                                   f64p]
+        L.orc_mesh.argtypes = [C.c_int, f32p, u8p, u32p, u32p, C.c_float]
+        L.orc_mesh.restype = C.c_void_p
+        L.orc_sim_mesh.argtypes = [C.c_void_p]
+        L.orc_sim_mesh.restype = C.c_void_p
+        L.orc_mesh_counts.argtypes = [C.c_void_p] + [C.POINTER(C.c_int64)] * 3
+        L.orc_mesh_get.argtypes = [C.c_void_p, f64p, f64p, i32p, f32p]
+        L.orc_mesh_free.argtypes = [C.c_void_p]
         L.orc_max_density.argtypes = [C.c_int, C.c_float]
         L.orc_max_density.restype = C.c_float
         _lib = L
@@ -178,6 +191,36 @@ def resample(n, pos, vel, typ, cs, perm, p, u, re):
     return out
 
 
+def implicit(n, pos, typ, cs, perm, pts, density=0.5):
+    """implicit::implicit_func at each point of pts [m,3]."""
+    pts = _c(pts, np.float32)
+    out = np.zeros(pts.shape[0], np.float64)
+    lib().orc_implicit(n, _c(pos, np.float32), _c(typ, np.uint8), _c(cs, np.uint32),
+                       _c(perm, np.uint32), np.float32(density), pts.shape[0], pts, out)
+    return out
+
+
+def _take_mesh(h, n):
+    L = lib()
+    nv, nf, nt = C.c_int64(), C.c_int64(), C.c_int64()
+    L.orc_mesh_counts(h, C.byref(nv), C.byref(nf), C.byref(nt))
+    out = {"vertices": np.zeros(3 * nv.value, np.float64),
+           "normals": np.zeros(3 * nv.value, np.float64),
+           "faces": np.zeros(3 * nf.value, np.int32),
+           "phi": np.zeros((n + 1) ** 3, np.float32), "triangles": nt.value}
+    L.orc_mesh_get(h, out["vertices"], out["normals"], out["faces"], out["phi"])
+    L.orc_mesh_free(h)
+    return out
+
+
+def mesh(n, pos, typ, cs, perm, density=0.5):
+    """mesher::generateMesh with mg = n+1: dict of vertices, normals (flat
+    float64), faces (flat int32), phi ((n+1)^3, x fastest), triangles."""
+    h = lib().orc_mesh(n, _c(pos, np.float32), _c(typ, np.uint8), _c(cs, np.uint32),
+                       _c(perm, np.uint32), np.float32(density))
+    return _take_mesh(h, n)
+
+
 def max_density(n, density_param=0.5):
     return float(lib().orc_max_density(n, np.float32(density_param)))
 
@@ -223,6 +266,20 @@ class Sim:
         p = np.zeros(n ** 3, np.float32)
         lib().orc_sim_get_grid(self._h, u[0], u[1], u[2], A, L, p)
         return u, A, L, p
+
+    def put(self, pos=None, vel=None, dens=None):
+        keep = [None if a is None else _c(a, np.float32) for a in (pos, vel, dens)]
+        lib().orc_sim_put(self._h, *[None if a is None else a.ctypes.data for a in keep])
+
+    def put_grid(self, u=None, A=None, L=None, press=None):
+        u = [None] * 3 if u is None else list(u)
+        keep = [None if a is None else _c(a, np.float32) for a in u]
+        keep.append(None if A is None else _c(A, np.uint8))
+        keep += [None if a is None else _c(a, np.float32) for a in (L, press)]
+        lib().orc_sim_put_grid(self._h, *[None if a is None else a.ctypes.data for a in keep])
+
+    def mesh(self):
+        return _take_mesh(lib().orc_sim_mesh(self._h), self.n)
 
     @property
     def stuck(self):

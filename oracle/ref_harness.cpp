@@ -35,6 +35,7 @@ extern "C" int flipref_place_rand(void);
 #define rand() flipref_place_rand()
 #include "flip3D.cpp"
 #undef rand
+#include "implicit.h"
 
 #include <sys/stat.h>
 #include <unistd.h>
@@ -340,6 +341,53 @@ extern "C" void fr_sim_stage(int stage) {
 }
 
 extern "C" int fr_sim_stuck(void) { return gNumStuck; }
+
+/* ---------------------------------------------------------------- mesher */
+
+/* implicit::implicit_func at m points on freshly sorted particles. */
+extern "C" void fr_implicit(int n, int np, const float *pos, const uint8_t *type,
+                            float density, int m, const float *pts, double *out) {
+  make_pool(np, pos, NULL, type, NULL, NULL);
+  std::vector<particle *> v;
+  pool_vector(v);
+  sorter s(n);
+  s.sort(v);
+  for (int i = 0; i < m; i++) {
+    FLOAT p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+    out[i] = implicit::implicit_func(&s, p, density);
+  }
+}
+
+/* mesher::generateMesh keeps buffers sized by its first call (one grid size
+ * per process). The result stays here until the next call. */
+static std::vector<double> g_mesh_v, g_mesh_n;
+static std::vector<int> g_mesh_f;
+
+extern "C" void fr_mesh(int n, int np, const float *pos, const uint8_t *type,
+                        float density, int64_t *counts) {
+  make_pool(np, pos, NULL, type, NULL, NULL);
+  std::vector<particle *> v;
+  pool_vector(v);
+  sorter s(n);
+  s.sort(v);
+  mesher::generateMesh(NULL, &s, v, density, n + 1, g_mesh_v, g_mesh_n, g_mesh_f);
+  counts[0] = (int64_t)(g_mesh_v.size() / 3);
+  counts[1] = (int64_t)(g_mesh_f.size() / 3);
+}
+
+/* The mesh write_mesh makes after a driver step (src/flip3D.cpp:999-1004):
+ * the driver's current lists and positions. */
+extern "C" void fr_sim_mesh(int64_t *counts) {
+  mesher::generateMesh(A, sort, particles, DENSITY, N + 1, g_mesh_v, g_mesh_n, g_mesh_f);
+  counts[0] = (int64_t)(g_mesh_v.size() / 3);
+  counts[1] = (int64_t)(g_mesh_f.size() / 3);
+}
+
+extern "C" void fr_mesh_get(double *vert, double *nrm, int32_t *faces) {
+  memcpy(vert, g_mesh_v.data(), g_mesh_v.size() * sizeof(double));
+  memcpy(nrm, g_mesh_n.data(), g_mesh_n.size() * sizeof(double));
+  for (size_t i = 0; i < g_mesh_f.size(); i++) faces[i] = g_mesh_f[i];
+}
 
 extern "C" void fr_sim_get(float *pos, float *vel, float *dens, uint8_t *type) {
   for (int q = 0; q < g_pool_n; q++) {

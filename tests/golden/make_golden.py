@@ -59,6 +59,13 @@ def load_ref():
     L.fr_sim_get_grid.argtypes = [f32p, f32p, f32p, u8p, f32p, f32p]
     L.fr_sim_stuck.restype = C.c_int
     L.fr_max_density.restype = C.c_float
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+    i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+    L.fr_implicit.argtypes = [C.c_int, C.c_int, f32p, u8p, C.c_float, C.c_int, f32p, f64p]
+    L.fr_mesh.argtypes = [C.c_int, C.c_int, f32p, u8p, C.c_float, i64p]
+    L.fr_sim_mesh.argtypes = [i64p]
+    L.fr_mesh_get.argtypes = [f64p, f64p, i32p]
     L.fr_grid_n.restype = C.c_int
     return L
 
@@ -178,6 +185,56 @@ def task_driver(out: str, steps: int = 10, rel_tol: float = 1e-6):
     np.savez_compressed(out, **rec)
 
 
+def _mesh_arrays(L, counts):
+    nv, nf = int(counts[0]), int(counts[1])
+    v = np.zeros(3 * nv, np.float64)
+    nr = np.zeros(3 * nv, np.float64)
+    f = np.zeros(3 * nf, np.int32)
+    L.fr_mesh_get(v, nr, f)
+    return v, nr, f
+
+
+def task_mesh(out: str, n: int):
+    """generateMesh (mg = n+1) and implicit_func on the scrambled scene."""
+    L = load_ref()
+    sc = component_scene(n)
+    P = sc.count
+    rng = np.random.default_rng(SEED + 4)
+    pts = rng.uniform(-0.1, 1.1, size=(3000, 3)).astype(np.float32)
+    pts[:1000] = sc.pos[rng.choice(P, 1000, replace=False)] + \
+        rng.normal(0, 0.3 / n, size=(1000, 3)).astype(np.float32)
+    phi = np.zeros(pts.shape[0], np.float64)
+    L.fr_implicit(n, P, sc.pos, sc.type, np.float32(0.5), pts.shape[0], pts, phi)
+    counts = np.zeros(2, np.int64)
+    L.fr_mesh(n, P, sc.pos, sc.type, np.float32(0.5), counts)
+    v, nr, f = _mesh_arrays(L, counts)
+    np.savez_compressed(out, n=n, pos=sc.pos, type=sc.type, pts=pts, phi=phi, vertices=v,
+                        normals=nr, faces=f)
+
+
+def task_mesh_driver(out: str, steps: int = 3):
+    """The mesh write_mesh makes after `steps` driver steps at N=32: digests
+    and subsets (the oracle rebuilds the state by running its own steps)."""
+    L = load_ref()
+    n = L.fr_grid_n()
+    sc = scenes.pool_sphere(n, seed=0)
+    md = L.fr_max_density()
+    L.fr_sim_setup(sc.count, sc.pos, sc.vel, sc.type, sc.nrm, md, SEED, 1e-6)
+    for _ in range(steps):
+        for st in range(5):
+            L.fr_sim_stage(st)
+    counts = np.zeros(2, np.int64)
+    L.fr_sim_mesh(counts)
+    v, nr, f = _mesh_arrays(L, counts)
+    rng = np.random.default_rng(SEED + 5)
+    sv = np.sort(rng.choice(v.shape[0], min(3000, v.shape[0]), replace=False))
+    sf = np.sort(rng.choice(f.shape[0], min(3000, f.shape[0]), replace=False))
+    np.savez_compressed(out, n=n, steps=steps, seed=SEED, rel_tol=1e-6, counts=counts,
+                        vertices_sha=digest(v), normals_sha=digest(nr), faces_sha=digest(f),
+                        vsub=sv, vertices_sub=v[sv], normals_sub=nr[sv], fsub=sf,
+                        faces_sub=f[sf])
+
+
 TASKS = {
     "components_n16": lambda out: task_components(out, 16),
     "components_n13": lambda out: task_components(out, 13),
@@ -185,6 +242,9 @@ TASKS = {
     "solver_n13": lambda out: task_solver(out, 13),
     "driver_n32": lambda out: task_driver(out, 10, 1e-6),
     "driver_n32_abs": lambda out: task_driver(out, 5, 0.0),
+    "mesh_n16": lambda out: task_mesh(out, 16),
+    "mesh_n13": lambda out: task_mesh(out, 13),
+    "mesh_driver_n32": lambda out: task_mesh_driver(out, 3),
 }
 
 

@@ -306,3 +306,46 @@ def test_solve_mic_on_a_dam_break(gpu, orc):
     fl = A == 1
     assert np.linalg.norm((p - x6)[fl]) / np.linalg.norm(x6[fl]) < 1e-4
     assert abs(st.iterations - it6) <= max(2, 0.15 * it6), (st.iterations, it6)
+
+
+def _forced_reposition_state(orc, sc, seed):
+    """A state where the fluid particles of one wall slab are stuck and the
+    only deep-water cell is the centre of a 3^3 fluid block, so every stuck
+    particle is re-seeded into the same cell and most of them resample next
+    to an earlier one (the ordered path of reposition)."""
+    n = sc.n
+    prm = orc.params(n, orc.PRECOND_REF, rel_tol=1e-6, seed=seed)
+    o = orc.Sim(sc, prm)
+    o.set_step(5)
+    o.stage(0)
+    A = np.zeros((n, n, n), np.uint8)
+    A[0], A[-1], A[:, 0], A[:, -1], A[:, :, 0], A[:, :, -1] = 2, 2, 2, 2, 2, 2
+    A[5, 1:5, 1:n - 1] = 2
+    A[10:13, 2:5, 6:9] = 1
+    rng = np.random.default_rng(seed)
+    pos, vel, dens, typ = o.get()
+    vel = rng.normal(0.0, 1.0, size=vel.shape).astype(np.float32)
+    vel[typ != 1] = 0.0
+    nf = (n + 1) * n * n
+    u = [np.zeros(nf, np.float32) for _ in range(3)]
+    zeros = np.zeros(n ** 3, np.float32)
+    o.put(vel=vel)
+    o.put_grid(u, A.ravel(), zeros, zeros)
+    return o, pos, vel, dens, typ, u, A.ravel(), zeros
+
+
+def test_reposition_ordered_resample_matches_oracle(gpu, orc):
+    sc = scenes.pool_sphere(16, seed=4)
+    o, pos, vel, dens, typ, u, A, zeros = _forced_reposition_state(orc, sc, 7)
+    g = make_sim(gpu, sc.n, sc.count, seed=7)
+    g.set_particles(pos, typ, vel, sc.nrm, dens)
+    g.set_grid(u, A, zeros, zeros, zeros)
+    g.set_step(5)
+    stuck = g.advect()
+    o.stage(3)
+    assert stuck == o.stuck == 448
+    opos, ovel, _, _ = o.get()
+    gpos, gvel, _, _ = g.get_particles()
+    assert np.array_equal(gpos, opos)
+    fl = typ == 1
+    assert np.array_equal(gvel[fl], ovel[fl])

@@ -112,3 +112,39 @@ def test_driver_steps(name):
         sim.step()
         if k in (2, 5, steps):
             check(f"step{k}")
+
+
+@pytest.mark.parametrize("name", ["mesh_n16", "mesh_n13"])
+def test_mesh_and_implicit(name):
+    """implicit::implicit_func and mesher::generateMesh (field, marching
+    cubes, face filter, normals, two smoothing passes) on a scrambled scene."""
+    g = load(name)
+    n = int(g["n"])
+    cs, perm = orc.sort(n, g["pos"])
+    phi = orc.implicit(n, g["pos"], g["type"], cs, perm, g["pts"])
+    assert np.array_equal(phi, g["phi"])
+    m = orc.mesh(n, g["pos"], g["type"], cs, perm)
+    for k in ("vertices", "normals", "faces"):
+        assert np.array_equal(m[k], g[k]), k
+
+
+def test_mesh_after_driver_steps():
+    """The mesh write_mesh exports after three N=32 steps
+    (src/flip3D.cpp:999-1004, 1254-1257): digests of the full arrays."""
+    g = load("mesh_driver_n32")
+    n = int(g["n"])
+    sc = scenes.pool_sphere(n, seed=0)
+    md = orc.max_density(n)
+    prm = orc.params(n, orc.PRECOND_REF, rel_tol=float(g["rel_tol"]), seed=int(g["seed"]))
+    sim = orc.Sim(sc, prm, md)
+    for _ in range(int(g["steps"])):
+        sim.step()
+    m = sim.mesh()
+    assert m["vertices"].shape[0] // 3 == int(g["counts"][0])
+    assert m["faces"].shape[0] // 3 == int(g["counts"][1])
+    assert np.array_equal(m["vertices"][g["vsub"]], g["vertices_sub"])
+    assert np.array_equal(m["normals"][g["vsub"]], g["normals_sub"])
+    assert np.array_equal(m["faces"][g["fsub"]], g["faces_sub"])
+    assert sha(m["vertices"]) == str(g["vertices_sha"])
+    assert sha(m["normals"]) == str(g["normals_sha"])
+    assert sha(m["faces"]) == str(g["faces_sha"])
