@@ -171,7 +171,8 @@ void free_all(FlipGpu *h) {
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
-                  h->ticket, h->brick_part, h->repo_draw, h->repo_res, h->repo_old};
+                  h->ticket, h->brick_part, h->repo_draw, h->repo_res, h->repo_old,
+                  h->repo_cnt, h->repo_start, h->repo_list, h->repo_state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -327,6 +328,8 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->scan_b, scan_n) AL(h->scan_tmp, h->scan_cap) AL(h->stuck_idx, cap)
   AL(h->water_idx, nc) AL(h->stage, 3 * cap)
   AL(h->repo_draw, cap) AL(h->repo_res, cap) AL(h->repo_old, cap)
+  AL(h->repo_cnt, cap + 1) AL(h->repo_start, cap + 1) AL(h->repo_list, cap)
+  AL(h->repo_state, cap)
   h->nbx = (p->n + 7) / 8;
   h->nbricks = h->nbx * h->nbx * h->nbx;
   AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
@@ -378,6 +381,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
 int flipgpu_destroy(FlipGpu *h) {
   if (!h) return FLIPGPU_EINVAL;
   cudaStreamSynchronize(h->stream);
+  mesh_free(h);
   free_all(h);
   cudaEventDestroy(h->ev0);
   cudaEventDestroy(h->ev1);
@@ -636,6 +640,46 @@ int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel, float 
 int flipgpu_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   if (!h) return FLIPGPU_EINVAL;
   return run_solve(h, st);
+}
+
+int flipgpu_implicit(FlipGpu *h, int count, const float *pts, double *out, int on_device) {
+  if (!h || count < 0 || (count > 0 && (!pts || !out))) return FLIPGPU_EINVAL;
+  if (!h->lists_exist) return fail(h, FLIPGPU_EINVAL, "implicit: no cell lists");
+  if (on_device) {
+    CK(h, launch_implicit_points(h, count, pts, out));
+    return FLIPGPU_OK;
+  }
+  /* points (3 floats) and values (1 double) share the staging buffer */
+  const int chunk = (int)(((size_t)h->cap * 3 / 5) & ~(size_t)1);
+  if (chunk <= 0) return fail(h, FLIPGPU_EINVAL, "no staging capacity");
+  float *dp = h->stage;
+  double *dout = reinterpret_cast<double *>(h->stage + 3 * (size_t)chunk);
+  for (int off = 0; off < count; off += chunk) {
+    int m = count - off < chunk ? count - off : chunk;
+    CK(h, cudaMemcpyAsync(dp, pts + 3 * (size_t)off, (size_t)m * 3 * sizeof(float),
+                          cudaMemcpyHostToDevice, h->stream));
+    CK(h, launch_implicit_points(h, m, dp, dout));
+    CK(h, cudaMemcpyAsync(out + off, dout, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+  }
+  return FLIPGPU_OK;
+}
+
+int flipgpu_mesh(FlipGpu *h, int64_t *n_vertices, int64_t *n_faces) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->lists_exist) return fail(h, FLIPGPU_EINVAL, "mesh: no cell lists");
+  int r = mesh_run(h, n_vertices, n_faces);
+  if (r != FLIPGPU_OK) return fail(h, r, "mesh: %s", cudaGetErrorString(cudaGetLastError()));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_mesh(FlipGpu *h, double *vertices, double *normals, int32_t *faces,
+                     float *field) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r = mesh_get(h, vertices, normals, faces, field);
+  if (r != FLIPGPU_OK) return fail(h, r, "get_mesh: no mesh or copy failed");
+  return FLIPGPU_OK;
 }
 
 int flipgpu_project(FlipGpu *h, FlipGpuSolveStats *st) {

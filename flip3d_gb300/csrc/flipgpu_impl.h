@@ -19,6 +19,8 @@
 
 enum { CELL_AIR = 0, CELL_FLUID = 1, CELL_WALL = 2 };
 
+struct MeshBufs; /* mesher buffers (k_mesh.cu) */
+
 /* Per-run constants handed to kernels by value. */
 struct SimConst {
   int n;              /* grid cells per axis */
@@ -116,11 +118,14 @@ struct FlipGpu {
   uint8_t *flag;      /* per particle / per cell */
   uint32_t *scan_a, *scan_b, *scan_tmp;
   uint32_t *stuck_idx, *water_idx;
-  uint32_t *repo_draw;       /* shuffle draws when the list exceeds shared memory */
+  uint32_t *repo_draw;       /* per stuck particle: shuffle draw */
+  uint32_t *repo_cnt, *repo_start, *repo_list; /* shuffle steps listed by position */
   float4 *repo_res, *repo_old; /* per stuck particle: resampled / previous velocity */
+  uint8_t *repo_state;       /* per stuck particle: resample round state */
   size_t scan_cap;
 
   float *stage;       /* AoS staging for downloads */
+  MeshBufs *mesh;     /* mesher buffers, allocated by the first mesh call */
   cudaEvent_t ev0, ev1;
 
   /* per-stage profiling */
@@ -151,6 +156,7 @@ enum {
   IF_NWATER,
   IF_NAN,
   IF_TIMEOUT,
+  IF_REPO_LEFT,
   IF_COUNT
 };
 
@@ -181,6 +187,16 @@ int particles_init_device();
 /* device-wide exclusive scan of n uint32 (in may equal out) */
 cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,
                            size_t n);
+/* the same with caller scratch of tmp_blocks entries (scan_tmp_blocks(n)) */
+cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
+                               uint32_t *tmp, size_t tmp_blocks);
+size_t scan_tmp_blocks(size_t n);
+
+/* mesher (k_mesh.cu) */
+int mesh_run(FlipGpu *h, int64_t *nverts, int64_t *nfaces);
+int mesh_get(FlipGpu *h, double *vertices, double *normals, int32_t *faces, float *phi);
+cudaError_t launch_implicit_points(FlipGpu *h, int count, const float *pts, double *out);
+void mesh_free(FlipGpu *h);
 
 /* kernel-count bookkeeping */
 #define FG_LAUNCHED(h, k) ((h)->launches += (k))

@@ -18,6 +18,7 @@ namespace {
 
 constexpr int BLK = 256;
 constexpr int REPO_GRID = 152 * 4; /* grid-stride launches over the stuck list */
+constexpr int REPO_ROUNDS = 16;    /* parallel resample rounds before the ordered tail */
 
 /* Visit the slots of cells [i0,i1]x[j0,j1]x[k0,k1] (clipped to the grid) in
  * the reference's order; f(slot). */
@@ -319,43 +320,105 @@ __global__ void k_compact(size_t n, const uint32_t *__restrict__ flag,
   if (i == n - 1) *count = (int)(offset[i] + flag[i]);
 }
 
-/* reposition (src/flip3D.cpp:405-441): deep-water cells in order, repeated
- * until there are as many as stuck particles, shuffled with the keyed
- * Fisher-Yates (my_rand_shuffle, src/utility.cpp:28-30). The draws are
- * independent and computed in parallel; the swaps are sequential and run on
- * one thread over shared memory (REPO_SMEM entries; longer lists swap in
- * global memory). */
-constexpr int REPO_SMEM = 16384;
-constexpr int REPO_THREADS = 1024;
-
-__global__ void __launch_bounds__(REPO_THREADS)
-    k_repo_shuffle(SimConst c, const int *__restrict__ counts,
-                   const uint32_t *__restrict__ water_idx, uint32_t *__restrict__ waters,
-                   uint32_t *__restrict__ draws) {
-  extern __shared__ uint32_t sm[];
+/* reposition (src/flip3D.cpp:405-441): the first m deep-water cells in cell
+ * order (repeated when there are fewer), shuffled by my_rand_shuffle
+ * (src/utility.cpp:28-30) — here the keyed Fisher-Yates: for i = m-1 .. 1
+ * swap(a[i], a[j_i]) with j_i = draw(i) % (i+1).
+ *
+ * The swaps run in parallel. Step i is the last to touch position i, so
+ * a[i] ends with whatever position j_i held just before step i; that value
+ * was put there by the most recent earlier step s > i with j_s = j_i (the
+ * smallest such s), which took it from position s just before step s, and
+ * so on back to an untouched original entry. lists[p] holds the steps s with
+ * j_s = p in ascending order; each output follows its chain of lookups. */
+__global__ void k_shuffle_draws(SimConst c, const int *__restrict__ counts,
+                                uint32_t *__restrict__ draw, uint32_t *__restrict__ cnt) {
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
-  if (m == 0 || w == 0) return;
-  const bool in_smem = m <= REPO_SMEM;
-  uint32_t *wv = in_smem ? sm : waters;
-  uint32_t *dj = in_smem ? sm + REPO_SMEM : draws;
-  for (int q = threadIdx.x; q < m; q += blockDim.x) {
-    wv[q] = water_idx[q % w];
+  if (w == 0) return;
+  for (int q = 1 + blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
     uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_SHUFFLE, (uint64_t)c.step, 0),
                              (uint64_t)q, 0);
-    dj[q] = r % (uint32_t)(q + 1);
+    uint32_t j = r % (uint32_t)(q + 1);
+    draw[q] = j;
+    atomicAdd(cnt + j, 1u);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int q = m - 1; q >= 1; q--) {
-      uint32_t j = dj[q];
-      uint32_t t = wv[q];
-      wv[q] = wv[j];
-      wv[j] = t;
+}
+
+__global__ void k_shuffle_fill(const int *__restrict__ counts, const uint32_t *__restrict__ draw,
+                               const uint32_t *__restrict__ start, uint32_t *__restrict__ cnt,
+                               uint32_t *__restrict__ list) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
+  for (int q = 1 + blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    const uint32_t j = draw[q];
+    list[start[j] + atomicSub(cnt + j, 1u) - 1u] = (uint32_t)q;
+  }
+}
+
+/* each list ascending (lists are short: about ln(m/p) entries) */
+__global__ void k_shuffle_sort(const int *__restrict__ counts, const uint32_t *__restrict__ start,
+                               uint32_t *__restrict__ list) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < m; p += gridDim.x * blockDim.x) {
+    const uint32_t s = start[p], e = start[p + 1];
+    for (uint32_t a = s + 1; a < e; a++) {
+      const uint32_t v = list[a];
+      uint32_t b = a;
+      while (b > s && list[b - 1] > v) {
+        list[b] = list[b - 1];
+        b--;
+      }
+      list[b] = v;
     }
   }
-  __syncthreads();
-  if (in_smem)
-    for (int q = threadIdx.x; q < m; q += blockDim.x) waters[q] = wv[q];
+}
+
+/* smallest step s > t with j_s = p, or m when there is none */
+__device__ __forceinline__ uint32_t first_after(const uint32_t *__restrict__ start,
+                                                const uint32_t *__restrict__ list, uint32_t p,
+                                                uint32_t t, uint32_t m) {
+  uint32_t lo = start[p], hi = start[p + 1];
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (list[mid] > t) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo < start[p + 1] ? list[lo] : m;
+}
+
+/* original index of the value position s holds just before step s */
+__device__ __forceinline__ uint32_t held_before(const uint32_t *__restrict__ start,
+                                                const uint32_t *__restrict__ list, uint32_t s,
+                                                uint32_t m) {
+  for (;;) { /* s strictly increases and stays below m */
+    const uint32_t nx = first_after(start, list, s, s, m);
+    if (nx == m) return s;
+    s = nx;
+  }
+}
+
+__global__ void k_shuffle_resolve(const int *__restrict__ counts,
+                                  const uint32_t *__restrict__ draw,
+                                  const uint32_t *__restrict__ start,
+                                  const uint32_t *__restrict__ list,
+                                  const uint32_t *__restrict__ water_idx,
+                                  uint32_t *__restrict__ waters) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0) return;
+  const uint32_t um = (uint32_t)m;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    uint32_t src;
+    const uint32_t ui = (uint32_t)i;
+    const uint32_t p = i == 0 ? 0u : draw[i];
+    if (p == ui) {
+      src = held_before(start, list, ui, um);
+    } else {
+      const uint32_t s = first_after(start, list, p, ui, um);
+      src = s == um ? p : held_before(start, list, s, um);
+    }
+    waters[i] = water_idx[src % (uint32_t)w];
+  }
 }
 
 /* Each stuck particle q placed at a keyed spot in cell waters[q]
@@ -429,10 +492,12 @@ __device__ __forceinline__ float3 repo_resample_one(const SimConst &c, float3 P,
   return make_float3(u[0], u[1], u[2]);
 }
 
-/* All stuck particles in parallel with the velocities before the
- * resample; a particle with no earlier stuck neighbour gets its final value
- * here (res.w = 0), the others are redone in order by k_repo_ordered
- * (res.w = 1). old[q] keeps the velocity before the resample. */
+/* Round 0: every stuck particle with the velocities before the resample.
+ * A particle with no earlier stuck particle among its contributing
+ * neighbours has its final value (state READY); the others stay PENDING for
+ * the later rounds. old[q] keeps the velocity before the resample. */
+enum { RP_PENDING = 0, RP_DONE = 1, RP_READY = 2 };
+
 __global__ void k_repo_gather(SimConst c, const int *__restrict__ counts,
                               const uint32_t *__restrict__ stuck_idx,
                               const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
@@ -441,7 +506,8 @@ __global__ void k_repo_gather(SimConst c, const int *__restrict__ counts,
                               const float *__restrict__ py, const float *__restrict__ pz,
                               const float *__restrict__ vx, const float *__restrict__ vy,
                               const float *__restrict__ vz, float4 *__restrict__ res,
-                              float4 *__restrict__ old) {
+                              float4 *__restrict__ old, uint8_t *__restrict__ state,
+                              int *__restrict__ left) {
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
   if (w == 0) return;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
@@ -452,30 +518,69 @@ __global__ void k_repo_gather(SimConst c, const int *__restrict__ counts,
                                  [&](uint32_t o, bool, uint32_t) {
                                    return make_float3(vx[o], vy[o], vz[o]);
                                  });
-    res[q] = make_float4(u.x, u.y, u.z, dep ? 1.0f : 0.0f);
+    res[q] = make_float4(u.x, u.y, u.z, 0.0f);
     old[q] = make_float4(vx[p], vy[p], vz[p], 0.0f);
+    state[q] = dep ? RP_PENDING : RP_READY;
+    if (dep) atomicAdd(left, 1);
+  }
+}
+
+/* Later rounds: a PENDING particle whose earlier stuck neighbours are all
+ * DONE computes its value — new velocities for stuck q' < q, old ones for
+ * q' > q — and becomes READY. */
+__global__ void k_repo_round(SimConst c, const int *__restrict__ counts,
+                             const uint32_t *__restrict__ stuck_idx,
+                             const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                             const float4 *__restrict__ spos, const uint8_t *__restrict__ stuck,
+                             const uint32_t *__restrict__ rank, const float *__restrict__ px,
+                             const float *__restrict__ py, const float *__restrict__ pz,
+                             const float *__restrict__ vx, const float *__restrict__ vy,
+                             const float *__restrict__ vz, float4 *__restrict__ res,
+                             const float4 *__restrict__ old, uint8_t *__restrict__ state,
+                             const int *__restrict__ left) {
+  const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
+  if (w == 0 || *left == 0) return;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    if (state[q] != RP_PENDING) continue;
+    uint32_t p = stuck_idx[q];
+    float3 P = make_float3(px[p], py[p], pz[p]);
+    bool dep = false, blocked = false;
+    float3 u = repo_resample_one(c, P, (uint32_t)q, cs, perm, spos, stuck, rank, dep,
+                                 [&](uint32_t o, bool is_stuck, uint32_t ro) {
+                                   if (is_stuck && ro >= (uint32_t)q) {
+                                     float4 v = old[ro];
+                                     return make_float3(v.x, v.y, v.z);
+                                   }
+                                   if (is_stuck && state[ro] != RP_DONE) blocked = true;
+                                   return make_float3(vx[o], vy[o], vz[o]);
+                                 });
+    if (blocked) continue;
+    res[q] = make_float4(u.x, u.y, u.z, 0.0f);
+    state[q] = RP_READY;
   }
 }
 
 __global__ void k_repo_commit(const int *__restrict__ counts,
                               const uint32_t *__restrict__ stuck_idx,
-                              const float4 *__restrict__ res, float *__restrict__ vx,
-                              float *__restrict__ vy, float *__restrict__ vz) {
+                              const float4 *__restrict__ res, uint8_t *__restrict__ state,
+                              float *__restrict__ vx, float *__restrict__ vy,
+                              float *__restrict__ vz, int *__restrict__ left, int round) {
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
-  if (w == 0) return;
+  if (w == 0 || (round > 0 && *left == 0)) return;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    if (state[q] != RP_READY) continue;
     float4 r = res[q];
-    if (r.w != 0.0f) continue;
     uint32_t p = stuck_idx[q];
     vx[p] = r.x;
     vy[p] = r.y;
     vz[p] = r.z;
+    state[q] = RP_DONE;
+    if (round > 0) atomicSub(left, 1);
   }
 }
 
-/* The dependent particles in increasing q, one thread: neighbours that are
- * stuck particles q' < q are read with their new velocity (already
- * committed), q' >= q with the old one. */
+/* Whatever is still PENDING after the rounds, in increasing q on one
+ * thread: every earlier stuck particle is final by then. */
 __global__ void k_repo_ordered(SimConst c, const int *__restrict__ counts,
                                const uint32_t *__restrict__ stuck_idx,
                                const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
@@ -483,13 +588,13 @@ __global__ void k_repo_ordered(SimConst c, const int *__restrict__ counts,
                                const uint32_t *__restrict__ rank, const float *__restrict__ px,
                                const float *__restrict__ py, const float *__restrict__ pz,
                                float *__restrict__ vx, float *__restrict__ vy,
-                               float *__restrict__ vz, const float4 *__restrict__ res,
-                               const float4 *__restrict__ old) {
+                               float *__restrict__ vz, const float4 *__restrict__ old,
+                               const uint8_t *__restrict__ state, const int *__restrict__ left) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
-  if (w == 0) return;
+  if (w == 0 || *left == 0) return;
   for (int q = 0; q < m; q++) {
-    if (res[q].w == 0.0f) continue;
+    if (state[q] == RP_DONE) continue;
     uint32_t p = stuck_idx[q];
     float3 P = make_float3(px[p], py[p], pz[p]);
     bool dep = false;
@@ -769,7 +874,11 @@ cudaError_t launch_advect(FlipGpu *h) {
 cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
   SimConst c = make_const(h);
   cudaError_t e;
-  if (h->np > 0) {
+  if (h->np == 0) {
+    if (stuck_host) *stuck_host = 0;
+    return cudaSuccess;
+  }
+  {
     k_u8_to_u32<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, h->flag, h->scan_a);
     FG_LAUNCHED(h, 1);
     if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->np)) != cudaSuccess) return e;
@@ -782,24 +891,48 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
   if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->nc)) != cudaSuccess) return e;
   k_compact<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->nc, h->scan_a, h->scan_b,
                                                          h->water_idx, h->iflags + IF_NWATER);
-  k_repo_shuffle<<<1, REPO_THREADS, 2 * REPO_SMEM * sizeof(uint32_t), h->stream>>>(
-      c, h->iflags, h->water_idx, h->scan_b, h->repo_draw);
+  /* my_rand_shuffle: draws, lists of the steps per position, chains */
+  {
+    const size_t np1 = (size_t)h->np + 1;
+    if ((e = cudaMemsetAsync(h->repo_cnt, 0, np1 * sizeof(uint32_t), h->stream)) != cudaSuccess)
+      return e;
+    k_shuffle_draws<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->repo_draw, h->repo_cnt);
+    FG_LAUNCHED(h, 1);
+    if ((e = scan_exclusive(h, h->repo_cnt, h->repo_start, np1)) != cudaSuccess) return e;
+    k_shuffle_fill<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->repo_draw, h->repo_start,
+                                                     h->repo_cnt, h->repo_list);
+    k_shuffle_sort<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->repo_start, h->repo_list);
+    k_shuffle_resolve<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->repo_draw, h->repo_start,
+                                                        h->repo_list, h->water_idx, h->scan_b);
+    FG_LAUNCHED(h, 3);
+  }
   k_repo_place<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->scan_b,
                                                  h->scan_a, h->px, h->py, h->pz);
-  FG_LAUNCHED(h, 2);
+  FG_LAUNCHED(h, 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   /* sorter::sort (src/flip3D.cpp:443), shared with the corrector's sort. */
   if ((e = launch_sort(h, 0)) != cudaSuccess) return e;
-  k_repo_gather<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start,
-                                                  h->perm, h->spos, h->flag, h->scan_a, h->px,
-                                                  h->py, h->pz, h->vx, h->vy, h->vz,
-                                                  h->repo_res, h->repo_old);
-  k_repo_commit<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->stuck_idx, h->repo_res, h->vx,
-                                                  h->vy, h->vz);
+  /* corrector::resample of each stuck particle in order (src/flip3D.cpp:445-450) */
+  int *left = h->iflags + IF_REPO_LEFT;
+  if ((e = cudaMemsetAsync(left, 0, sizeof(int), h->stream)) != cudaSuccess) return e;
+  k_repo_gather<<<REPO_GRID, BLK, 0, h->stream>>>(
+      c, h->iflags, h->stuck_idx, h->cell_start, h->perm, h->spos, h->flag, h->scan_a, h->px,
+      h->py, h->pz, h->vx, h->vy, h->vz, h->repo_res, h->repo_old, h->repo_state, left);
+  k_repo_commit<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->stuck_idx, h->repo_res,
+                                                  h->repo_state, h->vx, h->vy, h->vz, left, 0);
+  FG_LAUNCHED(h, 2);
+  for (int r = 1; r <= REPO_ROUNDS; r++) {
+    k_repo_round<<<REPO_GRID, BLK, 0, h->stream>>>(
+        c, h->iflags, h->stuck_idx, h->cell_start, h->perm, h->spos, h->flag, h->scan_a, h->px,
+        h->py, h->pz, h->vx, h->vy, h->vz, h->repo_res, h->repo_old, h->repo_state, left);
+    k_repo_commit<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->stuck_idx, h->repo_res,
+                                                    h->repo_state, h->vx, h->vy, h->vz, left, r);
+    FG_LAUNCHED(h, 2);
+  }
   k_repo_ordered<<<1, 32, 0, h->stream>>>(c, h->iflags, h->stuck_idx, h->cell_start, h->perm,
                                           h->spos, h->flag, h->scan_a, h->px, h->py, h->pz,
-                                          h->vx, h->vy, h->vz, h->repo_res, h->repo_old);
-  FG_LAUNCHED(h, 3);
+                                          h->vx, h->vy, h->vz, h->repo_old, h->repo_state, left);
+  FG_LAUNCHED(h, 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   /* refresh the sorted velocities of the resampled particles */
   if ((e = launch_payload(h, 0)) != cudaSuccess) return e;
@@ -826,14 +959,4 @@ cudaError_t launch_correct(FlipGpu *h) {
   return cudaGetLastError();
 }
 
-int particles_init_device() {
-  static bool done[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
-  if (done[dev]) return 0;
-  if (cudaFuncSetAttribute(k_repo_shuffle, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(2 * REPO_SMEM * sizeof(uint32_t))) != cudaSuccess)
-    return -1;
-  done[dev] = true;
-  return 0;
-}
+int particles_init_device() { return 0; }

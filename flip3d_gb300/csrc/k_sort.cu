@@ -187,16 +187,23 @@ __global__ void k_payload(SimConst c, int apply_gravity, const uint32_t *__restr
 
 } // namespace
 
-cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n) {
+cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
+                               uint32_t *tmp, size_t tmp_blocks) {
   if (n == 0) return cudaSuccess;
   size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
-  if (nb > h->scan_cap) return cudaErrorInvalidValue;
-  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, h->scan_tmp);
-  k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(h->scan_tmp, nb);
-  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, h->scan_tmp);
+  if (nb > tmp_blocks) return cudaErrorInvalidValue;
+  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, tmp);
+  k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(tmp, nb);
+  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, tmp);
   FG_LAUNCHED(h, 3);
   return cudaGetLastError();
 }
+
+cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n) {
+  return scan_exclusive_tmp(h, in, out, n, h->scan_tmp, h->scan_cap);
+}
+
+size_t scan_tmp_blocks(size_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
 cudaError_t launch_payload(FlipGpu *h, int apply_gravity) {
   SimConst c = make_const(h);

@@ -83,6 +83,10 @@ SIGNATURES = {
                                              C.c_void_p, C.c_void_p]),
     "flipgpu_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
     "flipgpu_fetch_velocity": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_implicit": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_mesh": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "flipgpu_get_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "flipgpu_resample": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_float,
                                    C.c_int]),
 }
@@ -286,6 +290,30 @@ class Simulation:
         st = SolveStats()
         self._ck(fn(self.h, C.byref(st)), what)
         return st
+
+    def implicit(self, pts):
+        """implicit::implicit_func at each point of pts [m,3] (float64)."""
+        pts = _c(pts, np.float32)
+        out = np.zeros(pts.shape[0], np.float64)
+        self._ck(self.lib.flipgpu_implicit(self.h, pts.shape[0], _ptr(pts), _ptr(out), 0),
+                 "implicit")
+        return out
+
+    def mesh(self, field=False):
+        """mesher::generateMesh on the lists of the last sort: dict of
+        vertices, normals (float64 [nv,3]), faces (int32 [nf,3]) and, with
+        field=True, the meshed field ((n+1)^3 float32, x fastest)."""
+        nv, nf = C.c_int64(), C.c_int64()
+        self._ck(self.lib.flipgpu_mesh(self.h, C.byref(nv), C.byref(nf)), "mesh")
+        out = {"vertices": np.zeros((nv.value, 3), np.float64),
+               "normals": np.zeros((nv.value, 3), np.float64),
+               "faces": np.zeros((nf.value, 3), np.int32)}
+        if field:
+            out["field"] = np.zeros((self.n + 1) ** 3, np.float32)
+        self._ck(self.lib.flipgpu_get_mesh(self.h, _ptr(out["vertices"]), _ptr(out["normals"]),
+                                           _ptr(out["faces"]),
+                                           _ptr(out["field"]) if field else None), "get_mesh")
+        return out
 
     def solve(self):
         return self._stats_call(self.lib.flipgpu_solve, "solve")

@@ -1,6 +1,7 @@
 /*
  * shim.cpp — the reference's sorter / mapper / solver / corrector call
- * surface (src/sorter.h, src/mapper.h, src/solver.h, src/corrector.h) on top
+ * surface (src/sorter.h, src/mapper.h, src/solver.h, src/corrector.h,
+ * src/mesher.h, src/implicit.h) on top
  * of the C ABI of libflipgpu, so a driver written against those functions
  * (src/flip3D.cpp) runs them on the GPU. Each call converts the driver's
  * particle records and jagged T*** grids (alloc3D, k contiguous) to the
@@ -17,7 +18,9 @@
 
 #include "../../include/flipgpu.h"
 #include "corrector.h"
+#include "implicit.h"
 #include "mapper.h"
+#include "mesher.h"
 #include "solver.h"
 #include "sorter.h"
 
@@ -331,4 +334,55 @@ void corrector::correct(sorter *sort, std::vector<particle *> &particles, FLOAT 
       particles[q]->u[k] = vel[3 * q + k];
     }
   }
+}
+
+/* ----------------------------------------------------------------- mesher */
+
+/* The handle's density parameter and the particles' current positions (the
+ * reference reads them through the sorter's pointers) before a field query. */
+static void prepare_field(FlipShimCells &s, int gn, FLOAT density) {
+  if (g_density != density) {
+    g_density = density;
+    FlipGpuParams p = params_for(gn, s.ctx.cap);
+    CHECK(s.ctx.h, flipgpu_set_params(s.ctx.h, &p));
+  }
+  Soa cur;
+  pack(s.parts, cur);
+  CHECK(s.ctx.h, flipgpu_put_state(s.ctx.h, cur.pos.data(), cur.vel.data(), 0));
+}
+
+double implicit::implicit_func(sorter *sort, FLOAT p[3], FLOAT density) {
+  FlipShimCells &s = *sort->shim();
+  const int gn = sort->getCellSize();
+  if (!s.ctx.h) return 8.0 * density / gn - (double)(density / gn); /* no particles */
+  prepare_field(s, gn, density);
+  double out = 0.0;
+  CHECK(s.ctx.h, flipgpu_implicit(s.ctx.h, 1, p, &out, 0));
+  return out;
+}
+
+void mesher::generateMesh(char ***A, sorter *sort, std::vector<particle *> &particles,
+                          FLOAT density, int mg, std::vector<double> &vertices,
+                          std::vector<double> &normals, std::vector<int> &faces) {
+  (void)A;
+  (void)particles;
+  FlipShimCells &s = *sort->shim();
+  const int gn = sort->getCellSize();
+  vertices.clear();
+  normals.clear();
+  faces.clear();
+  if (mg != gn + 1) {
+    fprintf(stderr, "flip3d shim: generateMesh needs mg = grid size + 1 (%d), got %d\n", gn + 1,
+            mg);
+    abort();
+  }
+  if (!s.ctx.h) return;
+  prepare_field(s, gn, density);
+  int64_t nv = 0, nf = 0;
+  CHECK(s.ctx.h, flipgpu_mesh(s.ctx.h, &nv, &nf));
+  vertices.resize(3 * (size_t)nv);
+  normals.resize(3 * (size_t)nv);
+  std::vector<int32_t> f(3 * (size_t)nf);
+  CHECK(s.ctx.h, flipgpu_get_mesh(s.ctx.h, vertices.data(), normals.data(), f.data(), nullptr));
+  faces.assign(f.begin(), f.end());
 }

@@ -154,6 +154,26 @@ int flipgpu_fetch_velocity(FlipGpu *h, int count, const float *pts, float *out,
  * velocity on input and the resampled one on output. */
 int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel,
                      float re, int on_device);
+/* implicit::implicit_func (src/implicit.cpp:14-38) at count points (float
+ * [count][3]): distance to the nearest non-wall particle within the 5^3
+ * cells around the point, capped at 8*density/n, minus density/n; the wall
+ * value 4.5*density/n when a wall particle is closer than density/n. Reads
+ * the lists of the last sort over current positions. out is double[count]. */
+int flipgpu_implicit(FlipGpu *h, int count, const float *pts, double *out,
+                     int on_device);
+/* mesher::generateMesh (src/mesher.cpp:137-195) with mg = n+1, the way
+ * write_mesh calls it after a step (src/flip3D.cpp:999-1004): the lists of
+ * the last sort over current positions; the reference's A argument is
+ * unused there and has no counterpart. Computes the mesh on the device and
+ * returns its vertex and face counts; flipgpu_get_mesh copies it out. */
+int flipgpu_mesh(FlipGpu *h, int64_t *n_vertices, int64_t *n_faces);
+/* The last mesh: vertices and normals double[n_vertices][3], faces
+ * int32[n_faces][3] (vertex indices), and optionally the field it meshed,
+ * float[(n+1)^3] in the reference's dense_grid layout (x fastest, node
+ * (x,y,z) at (z*(n+1) + y)*(n+1) + x, value = -implicit_func). Any pointer
+ * may be NULL. */
+int flipgpu_get_mesh(FlipGpu *h, double *vertices, double *normals,
+                     int32_t *faces, float *field);
 /* solver::solve (src/solver.cpp:224-241) on the handle's A, L, pressure
  * (initial guess, overwritten) and divergence (negated, as the reference
  * does). */

@@ -13,7 +13,9 @@
 #include <vector>
 
 #include "corrector.h"
+#include "implicit.h"
 #include "mapper.h"
+#include "mesher.h"
 #include "solver.h"
 #include "sorter.h"
 
@@ -154,6 +156,17 @@ int main(int argc, char **argv) {
   FLOAT ru[3] = {0.0f, 0.0f, 0.0f};
   corrector::resample(&s, &q[0], ru, (FLOAT)(1.0 / n));
   wr(out, ru, 3);
+  /* implicit field and the mesh write_mesh makes, on the same lists */
+  double phi = implicit::implicit_func(&s, &q[0], 0.5f);
+  wr(out, &phi, 1);
+  std::vector<double> mv, mn;
+  std::vector<int> mf;
+  mesher::generateMesh(A, &s, ps, 0.5f, n + 1, mv, mn, mf);
+  long long counts[2] = {(long long)(mv.size() / 3), (long long)(mf.size() / 3)};
+  wr(out, counts, 2);
+  wr(out, mv.data(), mv.size());
+  wr(out, mn.data(), mn.size());
+  wr(out, mf.data(), mf.size());
   fclose(out);
   return 0;
 }

@@ -308,11 +308,14 @@ def test_solve_mic_on_a_dam_break(gpu, orc):
     assert abs(st.iterations - it6) <= max(2, 0.15 * it6), (st.iterations, it6)
 
 
-def _forced_reposition_state(orc, sc, seed):
-    """A state where the fluid particles of one wall slab are stuck and the
-    only deep-water cell is the centre of a 3^3 fluid block, so every stuck
-    particle is re-seeded into the same cell and most of them resample next
-    to an earlier one (the ordered path of reposition)."""
+def _forced_reposition_state(orc, sc, seed, wide=False):
+    """A state where the fluid particles of one wall slab are stuck. Narrow:
+    the only deep-water cell is the centre of a 3^3 fluid block, so every
+    stuck particle is re-seeded into the same cell and each resamples next to
+    all earlier ones (past the parallel rounds into the ordered tail). Wide:
+    the rest of the box is fluid, so the stuck particles fill the first deep
+    cells one per cell, a compact block where neighbours depend on each
+    other in random order (the parallel rounds)."""
     n = sc.n
     prm = orc.params(n, orc.PRECOND_REF, rel_tol=1e-6, seed=seed)
     o = orc.Sim(sc, prm)
@@ -321,7 +324,12 @@ def _forced_reposition_state(orc, sc, seed):
     A = np.zeros((n, n, n), np.uint8)
     A[0], A[-1], A[:, 0], A[:, -1], A[:, :, 0], A[:, :, -1] = 2, 2, 2, 2, 2, 2
     A[5, 1:5, 1:n - 1] = 2
-    A[10:13, 2:5, 6:9] = 1
+    if wide:
+        A[1:5, 1:n - 1, 1:n - 1] = 1
+        A[6:n - 1, 1:n - 1, 1:n - 1] = 1
+        A[5, 5:n - 1, 1:n - 1] = 1
+    else:
+        A[10:13, 2:5, 6:9] = 1
     rng = np.random.default_rng(seed)
     pos, vel, dens, typ = o.get()
     vel = rng.normal(0.0, 1.0, size=vel.shape).astype(np.float32)
@@ -334,9 +342,10 @@ def _forced_reposition_state(orc, sc, seed):
     return o, pos, vel, dens, typ, u, A.ravel(), zeros
 
 
-def test_reposition_ordered_resample_matches_oracle(gpu, orc):
+@pytest.mark.parametrize("wide", [False, True])
+def test_reposition_ordered_resample_matches_oracle(gpu, orc, wide):
     sc = scenes.pool_sphere(16, seed=4)
-    o, pos, vel, dens, typ, u, A, zeros = _forced_reposition_state(orc, sc, 7)
+    o, pos, vel, dens, typ, u, A, zeros = _forced_reposition_state(orc, sc, 7, wide)
     g = make_sim(gpu, sc.n, sc.count, seed=7)
     g.set_particles(pos, typ, vel, sc.nrm, dens)
     g.set_grid(u, A, zeros, zeros, zeros)
@@ -349,3 +358,70 @@ def test_reposition_ordered_resample_matches_oracle(gpu, orc):
     assert np.array_equal(gpos, opos)
     fl = typ == 1
     assert np.array_equal(gvel[fl], ovel[fl])
+
+
+@pytest.mark.parametrize("name", ["mesh_n16", "mesh_n13"])
+def test_mesh_matches_reference(gpu, orc, name):
+    """mesher::generateMesh and implicit::implicit_func against the
+    reference's own output on a scrambled scene (bit for bit)."""
+    g = np.load(f"{GOLD}/{name}.npz")
+    n = int(g["n"])
+    sim = make_sim(gpu, n, g["pos"].shape[0])
+    sim.set_particles(g["pos"], g["type"])
+    sim.sort()
+    assert np.array_equal(sim.implicit(g["pts"]), g["phi"])
+    m = sim.mesh(field=True)
+    cs, perm = orc.sort(n, g["pos"])
+    om = orc.mesh(n, g["pos"], g["type"], cs, perm)
+    assert np.array_equal(m["field"], om["phi"])
+    assert np.array_equal(m["vertices"].ravel(), g["vertices"])
+    assert np.array_equal(m["faces"].ravel(), g["faces"])
+    assert np.array_equal(m["normals"].ravel(), g["normals"])
+
+
+def test_mesh_after_steps_matches_oracle(gpu, orc):
+    """The mesh write_mesh exports after a step: the corrector's lists over
+    post-correction positions, computed on the GPU state and by the oracle
+    on that same state."""
+    sc = scenes.pool_sphere(32, seed=0)
+    sim = make_sim(gpu, sc.n, sc.count, rel_tol=1e-6, seed=3)
+    sim.set_scene(sc)
+    sim.calibrate_max_density()
+    for _ in range(2):
+        sim.step()
+    pos, vel, dens, typ = sim.get_particles()
+    cs, perm = sim.get_cells()
+    m = sim.mesh()
+    om = orc.mesh(sc.n, pos, typ, cs, perm)
+    assert m["vertices"].shape[0] > 1000
+    assert np.array_equal(m["vertices"].ravel(), om["vertices"])
+    assert np.array_equal(m["faces"].ravel(), om["faces"])
+    assert np.array_equal(m["normals"].ravel(), om["normals"])
+
+
+def test_mesh_on_stale_lists_matches_oracle(gpu, orc):
+    """The reference's sorter keeps particle pointers, so a mesh made after
+    particles moved reads new positions through old lists. Particles here
+    move up to 1.5 cells (a few far away) after the sort."""
+    g = np.load(f"{GOLD}/mesh_n16.npz")
+    n = int(g["n"])
+    pos, typ = g["pos"], g["type"]
+    sim = make_sim(gpu, n, pos.shape[0])
+    sim.set_particles(pos, typ)
+    sim.sort()
+    cs, perm = sim.get_cells()
+    rng = np.random.default_rng(11)
+    moved = pos.copy()
+    fl = typ == 1
+    moved[fl] += rng.uniform(-1.5 / n, 1.5 / n, size=(fl.sum(), 3)).astype(np.float32)
+    far = rng.choice(np.nonzero(fl)[0], 20, replace=False)
+    moved[far] = rng.uniform(0.0, 1.0, size=(20, 3)).astype(np.float32)
+    sim.put_state(moved, np.zeros_like(moved))
+    pts = g["pts"]
+    assert np.array_equal(sim.implicit(pts), orc.implicit(n, moved, typ, cs, perm, pts))
+    m = sim.mesh(field=True)
+    om = orc.mesh(n, moved, typ, cs, perm)
+    assert np.array_equal(m["field"], om["phi"])
+    assert np.array_equal(m["vertices"].ravel(), om["vertices"])
+    assert np.array_equal(m["faces"].ravel(), om["faces"])
+    assert np.array_equal(m["normals"].ravel(), om["normals"])

@@ -97,4 +97,12 @@ def test_shim_drives_the_gpu_like_the_reference(tmp_path):
     rr = orc.resample(n, g["corr_pos"], g["corr_vel"], typ, cs, perm, q[0],
                       np.zeros(3, np.float32), 1.0 / n)
     assert np.array_equal(ru, rr)
+    phi = take(np.float64, 1)
+    assert np.array_equal(phi, orc.implicit(n, g["corr_pos"], typ, cs, perm, q[:1]))
+    nv, nfc = (int(v) for v in take(np.int64, 2))
+    mv, mn = take(np.float64, 3 * nv), take(np.float64, 3 * nv)
+    mf = take(np.int32, 3 * nfc)
+    om = orc.mesh(n, g["corr_pos"], typ, cs, perm)
+    assert np.array_equal(mv, om["vertices"]) and np.array_equal(mn, om["normals"])
+    assert np.array_equal(mf, om["faces"])
     assert off == len(raw)

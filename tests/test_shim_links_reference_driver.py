@@ -1,6 +1,7 @@
 """An unmodified copy of the reference driver (src/flip3D.cpp, src/main.cpp)
 compiles and links against the GPU shim in place of the reference's
-sorter/mapper/solver/corrector sources. Needs the reference tree; skipped
+sorter/mapper/solver/corrector/mesher/implicit sources (and the marching
+cubes they use). Needs the reference tree; skipped
 where it is absent. Builds only (running needs a GPU)."""
 import os
 import subprocess
@@ -18,7 +19,7 @@ def test_reference_driver_links_against_shim(tmp_path):
     here = os.path.join(ROOT, "flip3d_gb300")
     shim = os.path.join(here, "shim")
     force = []
-    for h in ("sorter.h", "mapper.h", "solver.h", "corrector.h"):
+    for h in ("sorter.h", "mapper.h", "solver.h", "corrector.h", "mesher.h", "implicit.h"):
         force += ["-include", os.path.join(shim, h)]
     common = ["-O1", "-w", "-fopenmp", "-I", REF, "-I", os.path.join(REF, "rchandra"),
               "-include", "cmath", "-include", "limits", "-include", "vector", "-include", "map"]
@@ -29,8 +30,7 @@ def test_reference_driver_links_against_shim(tmp_path):
         subprocess.check_call(["g++", *common, *force, "-c", os.path.join(REF, src), "-o", o])
         objs.append(o)
     # the reference's files that stay on the host (not the replaced hot path)
-    for src in ("utility.cpp", "kernel.cpp", "exporter.cpp", "write_bmp.cpp", "implicit.cpp",
-                "mesher.cpp", "rchandra/CIsoSurface.cpp", "rchandra/Vectors.cpp"):
+    for src in ("utility.cpp", "kernel.cpp", "exporter.cpp", "write_bmp.cpp"):
         o = str(tmp_path / (os.path.basename(src) + ".o"))
         subprocess.check_call(["g++", *common, "-include", "algorithm", *force, "-c",
                                os.path.join(REF, src), "-o", o])
