@@ -32,8 +32,23 @@ sys.path.insert(0, ROOT)
 METRIC = "learned-warm-start vs plain MIC-PCG ms/solve @ rel-res 1e-6; particle-steps/s"
 UNIT = "particle-steps/s"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-TRAFFIC = os.path.join(ROOT, "profiles", "traffic.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "traffic.txt")
 FALLBACK_HBM = 6800.0
+
+
+def measured_traffic(stage, n):
+    """DRAM bytes per launch of the stage's dominant kernel from the ncu
+    summary in profiles/ (None when that stage/grid was not captured)."""
+    try:
+        with open(TRAFFIC) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 3 and not line.startswith("#") and parts[0] == stage \
+                        and int(parts[1]) == n:
+                    return int(parts[2])
+    except OSError:
+        pass
+    return None
 
 
 def hbm_peak():
@@ -260,12 +275,7 @@ def main():
     nbytes = stage_bytes(dom, P, args.n, it_prof)
     peak, peak_kind = hbm_peak()
     achieved = nbytes / (dom_ms / 1e3) / 1e9
-    traffic = None
-    try:
-        with open(TRAFFIC) as f:
-            traffic = json.load(f).get(dom)
-    except Exception:
-        pass
+    traffic = measured_traffic(dom, args.n)
 
     # end to end through the C ABI with pinned host buffers
     hpos = torch.empty((P, 3), dtype=torch.float32, pin_memory=True)
@@ -291,6 +301,13 @@ def main():
         e2e_s = float(t.item())
     e2e = total_particles * args.steps / e2e_s
 
+    # mesher::generateMesh on the last step's lists (device only, not in `value`)
+    sim.mesh_counts()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mesh_v, mesh_f = sim.mesh_counts()
+    mesh_ms = (time.perf_counter() - t0) * 1e3
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores, steps, dt = cpu_step_rate(scenes.dam_break(args.n, seed=0))
@@ -311,6 +328,9 @@ def main():
             "solve": {"ms_per_solve": statistics.mean(solve_ms), "iters": statistics.mean(iters),
                       "kind": f"plain PCG ({args.precond})"},
             "stages_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof.items()},
+            "mesh": {"ms": mesh_ms, "vertices": mesh_v, "faces": mesh_f,
+                     "note": "mesher::generateMesh after the last step, host-timed, "
+                             "not part of value"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind, "algorithmic_bytes": nbytes,

@@ -299,6 +299,12 @@ class Simulation:
                  "implicit")
         return out
 
+    def mesh_counts(self):
+        """Build the mesh on the device only; returns (vertices, faces)."""
+        nv, nf = C.c_int64(), C.c_int64()
+        self._ck(self.lib.flipgpu_mesh(self.h, C.byref(nv), C.byref(nf)), "mesh")
+        return nv.value, nf.value
+
     def mesh(self, field=False):
         """mesher::generateMesh on the lists of the last sort: dict of
         vertices, normals (float64 [nv,3]), faces (int32 [nf,3]) and, with
