@@ -36,6 +36,57 @@ TRAFFIC = os.path.join(ROOT, "profiles", "traffic.txt")
 FALLBACK_HBM = 6800.0
 
 
+WEIGHTS = os.path.join(ROOT, "flip3d_gb300", "unet_weights.bin")
+
+
+def solver_comparison(gpu, sim, prm, n, systems=3):
+    """ms per solve and CG iterations to rel-res 1e-6 on pressure systems
+    captured from the next steps of the run, each solved from the same
+    previous-step guess by: plain Jacobi PCG, plain MIC(0) PCG, and both with
+    the learned warm start (trained weights in flip3d_gb300/)."""
+    sim.set_capture(True)
+    caught = []
+    for _ in range(systems):
+        sim.step()
+        caught.append(sim.solve_system())
+    sim.set_capture(False)
+    net = None
+    if os.path.exists(WEIGHTS) and n % 8 == 0:
+        net = gpu.UNet(seed=0)
+        net.load(WEIGHTS)
+    variants = [("plain_jacobi", gpu.PRECOND_JACOBI, 0.0, None),
+                ("plain_mic", gpu.PRECOND_IC, 0.97, None)]
+    if net is not None:
+        variants += [("learned_jacobi", gpu.PRECOND_JACOBI, 0.0, net),
+                     ("learned_mic", gpu.PRECOND_IC, 0.97, net)]
+    out = {}
+    for name, pre, tau, w in variants:
+        p = gpu.Params.from_buffer_copy(prm)
+        p.precond, p.mic_tau, p.solve_mode = pre, tau, gpu.SOLVE_FAST
+        sim.set_params(p)
+        sim.set_warm_start(w)
+        ms, it, wms = [], [], []
+        for A, L, b, x0, _, _ in caught:
+            for rep in range(2):  # the first solve of a variant warms it up
+                sim.set_grid(A=A, L=L, press=x0, div=-b)
+                st = sim.solve()
+            ms.append(st.ms)
+            it.append(st.iterations)
+            wms.append(st.warm_ms)
+        out[name] = {"ms_per_solve": statistics.mean(ms), "iters": statistics.mean(it)}
+        if w is not None:
+            out[name]["warm_start_ms"] = statistics.mean(wms)
+    sim.set_warm_start(None)
+    sim.set_params(prm)
+    if "learned_jacobi" in out:
+        out["learned_vs_plain_mic"] = out["learned_jacobi"]["ms_per_solve"] / \
+            out["plain_mic"]["ms_per_solve"]
+        out["learned_vs_plain_jacobi"] = out["learned_jacobi"]["ms_per_solve"] / \
+            out["plain_jacobi"]["ms_per_solve"]
+    out["systems"] = systems
+    return out
+
+
 def measured_traffic(stage, n):
     """DRAM bytes per launch of the stage's dominant kernel from the ncu
     summary in profiles/ (None when that stage/grid was not captured)."""
@@ -301,6 +352,9 @@ def main():
         e2e_s = float(t.item())
     e2e = total_particles * args.steps / e2e_s
 
+    # the metric's solver comparison on systems of this run (not in `value`)
+    solve_cmp = solver_comparison(gpu, sim, prm, args.n)
+
     # mesher::generateMesh on the last step's lists (device only, not in `value`)
     sim.mesh_counts()
     torch.cuda.synchronize()
@@ -327,6 +381,7 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "solve": {"ms_per_solve": statistics.mean(solve_ms), "iters": statistics.mean(iters),
                       "kind": f"plain PCG ({args.precond})"},
+            "solver_comparison": solve_cmp,
             "stages_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof.items()},
             "mesh": {"ms": mesh_ms, "vertices": mesh_v, "faces": mesh_f,
                      "note": "mesher::generateMesh after the last step, host-timed, "

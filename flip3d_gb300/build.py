@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflipgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["api.cu", "k_sort.cu", "k_particles.cu", "k_grid.cu", "k_pcg.cu", "k_mesh.cu",
+SOURCES = ["api.cu", "k_sort.cu", "k_particles.cu", "k_grid.cu", "k_pcg.cu", "k_mesh.cu", "k_unet.cu",
            "noalloc_sort.cu"]
 FLAGS = {name: ["-fmad=false"] for name in SOURCES}
 

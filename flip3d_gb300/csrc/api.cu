@@ -382,6 +382,17 @@ int flipgpu_destroy(FlipGpu *h) {
   if (!h) return FLIPGPU_EINVAL;
   cudaStreamSynchronize(h->stream);
   mesh_free(h);
+  if (h->wdelta) {
+    cudaFree(h->wdelta);
+    cudaFree(h->wpart);
+    cudaEventDestroy(h->wev[0]);
+    cudaEventDestroy(h->wev[1]);
+  }
+  if (h->cap_b) {
+    cudaFree(h->cap_b);
+    cudaFree(h->cap_x0);
+    cudaFree(h->cap_r0);
+  }
   free_all(h);
   cudaEventDestroy(h->ev0);
   cudaEventDestroy(h->ev1);
@@ -663,6 +674,40 @@ int flipgpu_implicit(FlipGpu *h, int count, const float *pts, double *out, int o
                           h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
   }
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_warm_start(FlipGpu *h, FlipUNet *u) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (u && h->n % 8 != 0)
+    return fail(h, FLIPGPU_EINVAL, "warm start needs a grid that is a multiple of 8 cells");
+  h->warm = u;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_capture(FlipGpu *h, int on) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (on && !h->cap_b) {
+    CK(h, cudaMalloc(&h->cap_b, h->nc * sizeof(float)));
+    CK(h, cudaMalloc(&h->cap_x0, h->nc * sizeof(float)));
+    CK(h, cudaMalloc(&h->cap_r0, h->nc * sizeof(float)));
+  }
+  h->capture = on ? 1 : 0;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_solve_system(FlipGpu *h, uint8_t *A, float *L, float *b, float *x0, float *r0,
+                             float *x, int on_device) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->cap_b) return fail(h, FLIPGPU_EINVAL, "get_solve_system: capture is off");
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (A) CK(h, cudaMemcpyAsync(A, h->A, h->nc, k, h->stream));
+  if (L) CK(h, cudaMemcpyAsync(L, h->L, h->nc * sizeof(float), k, h->stream));
+  if (b) CK(h, cudaMemcpyAsync(b, h->cap_b, h->nc * sizeof(float), k, h->stream));
+  if (x0) CK(h, cudaMemcpyAsync(x0, h->cap_x0, h->nc * sizeof(float), k, h->stream));
+  if (r0) CK(h, cudaMemcpyAsync(r0, h->cap_r0, h->nc * sizeof(float), k, h->stream));
+  if (x) CK(h, cudaMemcpyAsync(x, h->press, h->nc * sizeof(float), k, h->stream));
+  if (!on_device) CK(h, cudaStreamSynchronize(h->stream));
   return FLIPGPU_OK;
 }
 

@@ -126,6 +126,15 @@ struct FlipGpu {
 
   float *stage;       /* AoS staging for downloads */
   MeshBufs *mesh;     /* mesher buffers, allocated by the first mesh call */
+
+  /* learned warm start (k_unet.cu) */
+  FlipUNet *warm;     /* network, or null for the previous-step guess */
+  float *wdelta;      /* correction, A*correction, A*x0 (3 n^3) */
+  double *wpart;
+  cudaEvent_t wev[2];
+  /* capture of the last solve's system for training data */
+  int capture;
+  float *cap_b, *cap_x0, *cap_r0;
   cudaEvent_t ev0, ev1;
 
   /* per-stage profiling */
@@ -191,6 +200,12 @@ cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,
 cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
                                uint32_t *tmp, size_t tmp_blocks);
 size_t scan_tmp_blocks(size_t n);
+
+/* learned warm start (k_unet.cu): x0 += g*d before CG; out3 = {r0.r0 of
+ * the previous-step guess, of the new guess, g} */
+int warm_start_apply(FlipGpu *h, float inv_h2_f, double *out3, float *ms);
+/* r = b - A x with the FAST-mode matrix (diag set by the solver's setup) */
+cudaError_t launch_residual(FlipGpu *h, float inv_h2_f, const float *x, float *r);
 
 /* mesher (k_mesh.cu) */
 int mesh_run(FlipGpu *h, int64_t *nverts, int64_t *nfaces);

@@ -1459,6 +1459,29 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
                             mode == FLIPGPU_SOLVE_REF ? nullptr : h->diag,
                             precond == FLIPGPU_PRECOND_JACOBI ? h->Pf : nullptr, h->iflags);
   FG_LAUNCHED(h, 1);
+  /* the system as posed (b negated as the reference does), for training data */
+  if (h->capture && h->cap_b) {
+    cudaMemcpyAsync(h->cap_b, h->div, nc * sizeof(float), cudaMemcpyDeviceToDevice, S);
+    cudaMemcpyAsync(h->cap_x0, h->press, nc * sizeof(float), cudaMemcpyDeviceToDevice, S);
+    if (mode == FLIPGPU_SOLVE_FAST) launch_residual(h, sa.inv_h2_f, h->press, h->cap_r0);
+    else cudaMemsetAsync(h->cap_r0, 0, nc * sizeof(float), S);
+  }
+  /* learned warm start: x0 += g d before CG (FAST mode) */
+  double wres[3] = {0.0, 0.0, 0.0};
+  float wms = 0.0f;
+  const int warm = h->warm && mode == FLIPGPU_SOLVE_FAST;
+  if (warm) {
+    int wr = warm_start_apply(h, sa.inv_h2_f, wres, &wms);
+    if (wr != FLIPGPU_OK) return wr;
+  }
+  auto warm_stats = [&](FlipGpuSolveStats *o) {
+    if (!o) return;
+    o->warm = warm;
+    o->r2_prev = wres[0];
+    o->r2_guess = warm ? wres[1] : 0.0;
+    o->gamma = wres[2];
+    o->warm_ms = wms;
+  };
   /* persistent single-launch CG unless the REF preconditioner has an entry
    * equal to 1.0 (then its neighbour terms act and it runs sequentially) */
   bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid[0] > 0;
@@ -1531,7 +1554,9 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       return FLIPGPU_ECUDA;
     }
     cudaEventRecord(h->ev1, S);
-    return finish_stats(h, st, mode);
+    int rc = finish_stats(h, st, mode);
+    warm_stats(st);
+    return rc;
   }
   if (mode == FLIPGPU_SOLVE_REF) {
     k_build_ref_seq<<<1, 1, 0, S>>>(n, h->A, h->P, nullptr, h->iflags, h->L, h->prm.subcell);
@@ -1623,6 +1648,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     st->r2 = sc[SC_ERR2];
     st->b2 = sc[SC_B2];
     st->ms = ms;
+    warm_stats(st);
   }
   /* The reference stops silently at its cap; only non-finite residuals are
    * errors in REF mode. */

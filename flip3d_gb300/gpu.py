@@ -35,7 +35,9 @@ class Params(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
-                ("b2", C.c_double), ("ms", C.c_double)]
+                ("b2", C.c_double), ("ms", C.c_double), ("warm", C.c_int),
+                ("r2_prev", C.c_double), ("r2_guess", C.c_double), ("gamma", C.c_double),
+                ("warm_ms", C.c_double)]
 
 
 class FlipGpuError(RuntimeError):
@@ -83,6 +85,21 @@ SIGNATURES = {
                                              C.c_void_p, C.c_void_p]),
     "flipgpu_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
     "flipgpu_fetch_velocity": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipunet_param_count": (C.c_int64, []),
+    "flipunet_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
+    "flipunet_destroy": (C.c_int, [C.c_void_p]),
+    "flipunet_last_error": (C.c_char_p, [C.c_void_p]),
+    "flipunet_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipunet_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipunet_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipunet_predict": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5),
+    "flipunet_gradients": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5 +
+                           [C.POINTER(C.c_double), C.c_void_p]),
+    "flipunet_train_step": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5 +
+                            [C.c_float, C.POINTER(C.c_double)]),
+    "flipgpu_set_warm_start": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipgpu_set_capture": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipgpu_get_solve_system": (C.c_int, [C.c_void_p] + [C.c_void_p] * 6 + [C.c_int]),
     "flipgpu_implicit": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_mesh": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "flipgpu_get_mesh": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -299,6 +316,36 @@ class Simulation:
                  "implicit")
         return out
 
+    def set_params(self, params: Params):
+        """Change run parameters (n and max_particles must stay)."""
+        self._ck(self.lib.flipgpu_set_params(self.h, C.byref(params)), "set_params")
+        self.params = params
+
+    def set_warm_start(self, net):
+        """Attach a UNet (or None) to this simulation's FAST-mode solves."""
+        self._warm = net
+        self._ck(self.lib.flipgpu_set_warm_start(self.h, net.h if net is not None else None),
+                 "set_warm_start")
+
+    def set_capture(self, on=True):
+        self._ck(self.lib.flipgpu_set_capture(self.h, 1 if on else 0), "set_capture")
+
+    def solve_system(self, dev=None):
+        """The last solve's (A, L, b, x0, r0, x): numpy arrays, or copies into
+        the device buffers dev = (A, L, b, x0, r0, x) given as raw addresses
+        (None skips one)."""
+        if dev is not None:
+            self._ck(self.lib.flipgpu_get_solve_system(
+                self.h, *[C.c_void_p(a) if a is not None else None for a in dev], 1),
+                "get_solve_system")
+            return None
+        nc = self.n ** 3
+        A = np.zeros(nc, np.uint8)
+        L, b, x0, r0, x = (np.zeros(nc, np.float32) for _ in range(5))
+        self._ck(self.lib.flipgpu_get_solve_system(self.h, _ptr(A), _ptr(L), _ptr(b), _ptr(x0),
+                                                   _ptr(r0), _ptr(x), 0), "get_solve_system")
+        return A, L, b, x0, r0, x
+
     def mesh_counts(self):
         """Build the mesh on the device only; returns (vertices, faces)."""
         nv, nf = C.c_int64(), C.c_int64()
@@ -340,3 +387,66 @@ class Simulation:
 
     def step(self):
         return self._stats_call(self.lib.flipgpu_step, "step")
+
+
+class UNet:
+    """The learned warm start's network (libflipgpu's flipunet_* calls).
+    Array arguments of predict/gradients/train_step are raw device addresses
+    (e.g. torch tensors' data_ptr()) of batch systems of n^3 cells."""
+
+    def __init__(self, seed=0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.flipunet_create(seed, C.byref(h))
+        if rc != 0:
+            raise FlipGpuError(f"flipunet_create failed ({rc})")
+        self.h = h
+        self.nparam = int(self.lib.flipunet_param_count())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.flipunet_destroy(self.h)
+            self.h = None
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            msg = self.lib.flipunet_last_error(self.h)
+            raise FlipGpuError(f"{what}: {msg.decode() if msg else rc}")
+
+    def set_stream(self, stream_handle):
+        self._ck(self.lib.flipunet_set_stream(self.h, C.c_void_p(stream_handle)), "set_stream")
+
+    def params(self):
+        p = np.zeros(self.nparam, np.float32)
+        self._ck(self.lib.flipunet_get_params(self.h, _ptr(p)), "get_params")
+        return p
+
+    def set_params(self, p):
+        p = _c(p, np.float32)
+        assert p.shape[0] == self.nparam
+        self._ck(self.lib.flipunet_set_params(self.h, _ptr(p)), "set_params")
+
+    def save(self, path):
+        self.params().tofile(path)
+
+    def load(self, path):
+        self.set_params(np.fromfile(path, np.float32))
+
+    def predict(self, n, batch, A, b, x0, r0, delta):
+        self._ck(self.lib.flipunet_predict(self.h, n, batch, *[C.c_void_p(a) for a in
+                                                             (A, b, x0, r0, delta)]), "predict")
+
+    def gradients(self, n, batch, A, b, x0, r0, x):
+        loss = C.c_double()
+        g = np.zeros(self.nparam, np.float32)
+        self._ck(self.lib.flipunet_gradients(self.h, n, batch,
+                                             *[C.c_void_p(a) for a in (A, b, x0, r0, x)],
+                                             C.byref(loss), _ptr(g)), "gradients")
+        return loss.value, g
+
+    def train_step(self, n, batch, A, b, x0, r0, x, lr):
+        loss = C.c_double()
+        self._ck(self.lib.flipunet_train_step(self.h, n, batch,
+                                              *[C.c_void_p(a) for a in (A, b, x0, r0, x)],
+                                              C.c_float(lr), C.byref(loss)), "train_step")
+        return loss.value

@@ -83,8 +83,15 @@ typedef struct FlipGpuSolveStats {
   int status;         /* FLIPGPU_OK / ENOCONV / ENAN */
   double r2;          /* final r.r */
   double b2;          /* b.b */
-  double ms;          /* device time of the solve (CUDA events) */
+  double ms;          /* device time of the solve (CUDA events), warm start included */
+  int warm;           /* 1 when a learned warm start ran before CG */
+  double r2_prev;     /* warm start: r.r of the previous-step guess */
+  double r2_guess;    /* warm start: r.r of the guess CG started from */
+  double gamma;       /* warm start: step taken along the network's correction */
+  double warm_ms;     /* warm start: device time of network + step */
 } FlipGpuSolveStats;
+
+typedef struct FlipUNet FlipUNet;
 
 typedef struct FlipGpu FlipGpu;
 
@@ -237,6 +244,54 @@ int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max);
 int flipgpu_sort_cells_noalloc(int n, int count, const float *pos,
                                uint32_t *cell_start, uint32_t *perm,
                                void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference; the reference starts
+ * CG from the previous step's pressure, src/flip3D.cpp:679 and
+ * src/solver.cpp:224).
+ *
+ * A 3D U-Net (4 levels, 16/32/48/64 channels, BF16 activations, FP32
+ * accumulation, tensor-core implicit-GEMM convolutions) maps (liquid mask,
+ * b, previous pressure x0 and its residual r0 = b - A x0) to a correction d
+ * (an approximation of A^-1 r0). With a network attached, a
+ * FAST-mode solve starts from x0 + g d, where g = d.r0 / d.Ad minimises the
+ * A-norm error along d (so the guess is never worse than x0 in that norm)
+ * and CG still runs to the same relative residual. Grids must be a multiple
+ * of 8 cells per axis. All array arguments of the flipunet_* calls are
+ * device pointers to batch systems of n^3 cells each, concatenated. */
+int64_t flipunet_param_count(void);
+int flipunet_create(uint64_t seed, FlipUNet **out);
+int flipunet_destroy(FlipUNet *u);
+const char *flipunet_last_error(const FlipUNet *u);
+int flipunet_set_stream(FlipUNet *u, void *stream);
+/* FP32 master parameters (host arrays of flipunet_param_count() floats);
+ * setting them resets the optimiser state. */
+int flipunet_get_params(FlipUNet *u, float *params);
+int flipunet_set_params(FlipUNet *u, const float *params);
+/* delta = the correction for systems (A, b, x0, r0), zero off the liquid. */
+int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
+                     const float *x0, const float *r0, float *delta);
+/* Mean squared error over liquid cells between the network output and
+ * (x - x0)/s (s = RMS of r0 over the liquid times h^2), its gradient (host
+ * array, may be NULL) and no update. */
+int flipunet_gradients(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
+                       const float *x0, const float *r0, const float *x, double *loss,
+                       float *grad);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on that loss. */
+int flipunet_train_step(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
+                        const float *x0, const float *r0, const float *x, float lr,
+                        double *loss);
+/* Attach a network to a simulation's FAST-mode solves (NULL detaches). */
+int flipgpu_set_warm_start(FlipGpu *h, FlipUNet *u);
+/* Keep a copy of each solve's system: flipgpu_get_solve_system returns A,
+ * L (the levelset of the subcell diagonal), b (the solver's right-hand side,
+ * already negated as solver::solve does), x0 (the initial guess before any
+ * warm start), r0 = b - A x0 (FAST mode) and x (the solution) of the last
+ * solve. Any pointer may be NULL. To solve such a system again,
+ * set_grid(A, L, press = x0, div = -b). */
+int flipgpu_set_capture(FlipGpu *h, int on);
+int flipgpu_get_solve_system(FlipGpu *h, uint8_t *A, float *L, float *b, float *x0, float *r0,
+                             float *x, int on_device);
 
 #ifdef __cplusplus
 }

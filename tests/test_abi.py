@@ -9,13 +9,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "flipgpu.h")).read()
-    return sorted(set(re.findall(r"\b(flipgpu_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(flip(?:gpu|unet)_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_declares_the_entry_points():
     names = declared_symbols()
     for must in ("flipgpu_create", "flipgpu_sort", "flipgpu_p2g", "flipgpu_g2p",
-                 "flipgpu_solve", "flipgpu_correct", "flipgpu_step"):
+                 "flipgpu_solve", "flipgpu_correct", "flipgpu_step", "flipgpu_mesh",
+                 "flipgpu_implicit", "flipunet_train_step", "flipgpu_set_warm_start"):
         assert must in names
 
 

@@ -1,0 +1,160 @@
+"""The learned warm start: the CUDA U-Net's forward pass, loss and
+gradients against the FP64 CPU restatement (oracle/unet_oracle.py), Adam
+training, and its effect on the pressure solve.
+
+Tolerances: activations and gradients are BF16 on the GPU (8-bit
+mantissa); the oracle rounds to BF16 at the same points, so what remains is
+FP32 accumulation order and the BF16 rounding flips it causes, which grow
+as gradients travel back through the layers. The network output must agree
+to 3 % relative L2, the loss to 1 %, every parameter tensor's gradient to
+6 % and their median to 2 %."""
+import numpy as np
+import pytest
+
+from flip3d_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from flip3d_gb300 import gpu as g
+    g.load()
+    return g
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    return t
+
+
+def systems(gpu, n, seeds, steps=3):
+    """Real solver systems (A, L, b, x0, r0, x) from short runs of random scenes."""
+    out = []
+    for s in seeds:
+        sc = scenes.random_scene(n, s)
+        sim = gpu.Simulation(gpu.default_params(n, sc.count, rel_tol=1e-6,
+                                                solve_mode=gpu.SOLVE_FAST,
+                                                precond=gpu.PRECOND_JACOBI, seed=s))
+        sim.set_scene(sc)
+        sim.calibrate_max_density()
+        sim.set_capture(True)
+        for _ in range(steps):
+            sim.step()
+        out.append(sim.solve_system())
+    return out
+
+
+def to_dev(torch, arrs, dtype):
+    return torch.tensor(np.stack(arrs), dtype=dtype, device="cuda").contiguous()
+
+
+def test_unet_forward_and_gradients_match_cpu_oracle(gpu, torch):
+    from oracle import unet_oracle as U
+    n, seeds = 16, [3, 4]
+    sy = systems(gpu, n, seeds)
+    A = to_dev(torch, [s[0] for s in sy], torch.uint8)
+    b, x0, r0, x = (to_dev(torch, [s[k] for s in sy], torch.float32) for k in (2, 3, 4, 5))
+    net = gpu.UNet(seed=5)
+    p = net.params()
+    rng = np.random.default_rng(1)
+    woff, boff, hoff, total = U.layout()
+    for l, (cin, cout, _) in enumerate(U.CONVS):  # non-zero biases: live ReLUs everywhere
+        p[boff[l]:boff[l] + cout] = rng.normal(0.0, 0.05, cout)
+    p[hoff:hoff + 16] = rng.normal(0.0, 0.3, 16)
+    net.set_params(p)
+    delta = torch.zeros(len(seeds), n ** 3, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    net.predict(n, len(seeds), A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(),
+                delta.data_ptr())
+    torch.cuda.synchronize()
+    loss, g = net.gradients(n, len(seeds), A.data_ptr(), b.data_ptr(), x0.data_ptr(),
+                            r0.data_ptr(), x.data_ptr())
+    shp = (len(seeds), n, n, n)
+    An, bn, x0n, r0n, xn = (t.cpu().numpy().reshape(shp) for t in (A, b, x0, r0, x))
+    oloss, og, t = U.loss_and_grads(p.astype(np.float64), An, bn, x0n, r0n, xn,
+                                    round_bf16=True)
+    _, sx, fl = U.features(An, bn, x0n, r0n)
+    want = np.where(fl, t["O"] * sx[:, None, None, None], 0.0)
+    got = delta.cpu().numpy().reshape(shp)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel < 3e-2, rel
+    assert abs(loss - oloss) <= 1e-2 * abs(oloss), (loss, oloss)
+    errs = []
+    for l, (cin, cout, _) in enumerate(U.CONVS):
+        for name, (a, m) in (("W", (woff[l], 27 * cin * cout)), ("b", (boff[l], cout))):
+            ref = og[a:a + m]
+            errs.append((np.linalg.norm(g[a:a + m] - ref) / max(np.linalg.norm(ref), 1e-30),
+                         l, name))
+    errs.append((np.linalg.norm(g[hoff:] - og[hoff:]) / np.linalg.norm(og[hoff:]), -1, "head"))
+    print("gradient relative errors:", [(l, nm, round(float(e), 4)) for e, l, nm in errs])
+    assert max(e for e, _, _ in errs) < 6e-2, max(errs)
+    assert np.median([e for e, _, _ in errs]) < 2e-2
+
+
+def test_unet_training_reduces_the_loss(gpu, torch):
+    n = 16
+    sy = systems(gpu, n, [7, 8, 9, 10])
+    A = to_dev(torch, [s[0] for s in sy], torch.uint8)
+    b, x0, r0, x = (to_dev(torch, [s[k] for s in sy], torch.float32) for k in (2, 3, 4, 5))
+    net = gpu.UNet(seed=1)
+    losses = [net.train_step(n, 4, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(),
+                             x.data_ptr(), 1e-3) for _ in range(40)]
+    assert np.all(np.isfinite(losses))
+    assert losses[-1] < 0.5 * losses[0], losses[::8]
+
+
+def test_unet_training_is_deterministic(gpu, torch):
+    n = 16
+    sy = systems(gpu, n, [11, 12])
+    A = to_dev(torch, [s[0] for s in sy], torch.uint8)
+    b, x0, r0, x = (to_dev(torch, [s[k] for s in sy], torch.float32) for k in (2, 3, 4, 5))
+    ps = []
+    for _ in range(2):
+        net = gpu.UNet(seed=2)
+        for _ in range(3):
+            net.train_step(n, 2, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(),
+                           x.data_ptr(), 1e-3)
+        ps.append(net.params())
+    assert np.array_equal(ps[0], ps[1])
+
+
+def test_warm_start_is_never_worse_and_keeps_the_answer(gpu):
+    """Even an untrained network cannot make the starting residual worse in
+    the A-norm sense (the step along its correction is optimal and may be
+    zero), and the solve still reaches the same relative residual."""
+    n = 32
+    sc = scenes.random_scene(n, 21)
+    sim = gpu.Simulation(gpu.default_params(n, sc.count, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                                            precond=gpu.PRECOND_JACOBI, seed=21))
+    sim.set_scene(sc)
+    sim.calibrate_max_density()
+    net = gpu.UNet(seed=3)
+    sim.set_warm_start(net)
+    for _ in range(4):
+        st = sim.step()
+        assert st.status == 0 and st.warm == 1
+        assert st.r2 <= 1e-12 * st.b2 * (1 + 1e-6)
+        assert st.warm_ms > 0
+
+
+def test_trained_warm_start_on_heldout_scenes(gpu, torch):
+    """A short training run on N=32 scenes, evaluated on held-out seeds: the
+    training loss falls, the prediction error of the correction falls, and
+    the solve from the learned start takes no more CG iterations than from
+    the previous-step guess (the start is A-norm optimal along the
+    correction, so it cannot be worse than the previous-step guess in the
+    norm CG minimises)."""
+    from flip3d_gb300 import train_unet as T
+    n = 32
+    data = T.collect(n, range(100, 106), steps=24, every=3)
+    held = T.collect(n, range(900, 902), steps=24, every=3)
+    net = gpu.UNet(seed=0)
+    before = T.evaluate(net, held, n)
+    hist = T.train(net, data, n, epochs=12, batch=8, lr=1e-3)
+    res = T.evaluate(net, held, n)
+    print(before, res, hist[0], hist[-1])
+    assert hist[-1] < hist[0]
+    assert res["pred_rel_err"] < before["pred_rel_err"]
+    assert res["learned_iters"] <= res["plain_iters"] + 1.0
