@@ -101,6 +101,7 @@ struct FlipGpu {
 
   /* solver */
   float *r, *z, *s, *s1, *w;
+  float *w1, *pdir;   /* single-reduction CG: second w buffer, directions */
   double *P;          /* REF preconditioner diagonal (double, as the reference) */
   float *Pf;          /* FP32 preconditioner diagonal / IC factor */
   float *diag;        /* FP32 matvec diagonal (FAST mode) */
@@ -154,6 +155,7 @@ enum {
   SC_B2,
   SC_DOT,        /* scratch result of the last dot */
   SC_ERR2_0,
+  SC_TRUE2,      /* FP64 r.r of b - A x after a FAST solve */
   SC_COUNT
 };
 /* Device int slots (FlipGpu::iflags). */

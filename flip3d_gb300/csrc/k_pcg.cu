@@ -448,6 +448,7 @@ struct CgArgs {
   const float *L;
   const float *b;
   float *x, *r, *z, *s0, *s1, *w;
+  float *w1, *p;               /* single-reduction CG: second w buffer, directions */
   const double *P;
   const float *diag;
   const float *Pf;
@@ -997,6 +998,304 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_quad(CgArgs a) {
 }
 
 
+/* FAST-mode Jacobi PCG with one grid-wide reduction per iteration
+ * (Chronopoulos-Gear): with u = M^-1 r and w = A u,
+ *   p = u + beta p,  s = w + beta s  (s = A p),  x += alpha p,  r -= alpha s,
+ *   gamma = r.u, delta = w.u,  beta' = gamma'/gamma,
+ *   alpha' = gamma' / (delta' - beta' gamma' / alpha),
+ * and the new w = A u' needs u' = M^-1 (r - alpha (w + beta s_old)) at the
+ * neighbours, which every thread recomputes from the previous iteration's
+ * r, w, s (kept in ping-pong buffers), so one sweep and one barrier make an
+ * iteration. Quads of 4 k-cells per thread as in k_cg_quad; partial sums
+ * alternate between two slot sets so that a slow reader of one iteration's
+ * sums never sees the next iteration's. */
+struct Cg1Nb {
+  uchar4 A;
+  float4 pf, r, w, s;
+};
+
+__device__ __forceinline__ float4 cg1_unext(uchar4 A4, float4 pf, float4 r, float4 w, float4 s,
+                                            float alpha, float beta, bool first) {
+  auto one = [&](unsigned char a, float pfv, float rv, float wv, float sv) {
+    if (!fl(a)) return 0.0f;
+    const float sn = first ? wv : wv + beta * sv;
+    return pfv * (rv - alpha * sn);
+  };
+  return make_float4(one(A4.x, pf.x, r.x, w.x, s.x), one(A4.y, pf.y, r.y, w.y, s.y),
+                     one(A4.z, pf.z, r.z, w.z, s.z), one(A4.w, pf.w, r.w, w.w, s.w));
+}
+
+__device__ __forceinline__ float cg1_unext1(const CgArgs &a, size_t c, const float *R,
+                                            const float *W, const float *S, float alpha,
+                                            float beta, bool first, int &isfl) {
+  isfl = fl(a.A[c]);
+  if (!isfl) return 0.0f;
+  const float wv = __ldcg(W + c);
+  const float sn = first ? wv : wv + beta * __ldcg(S + c);
+  return a.Pf[c] * (__ldcg(R + c) - alpha * sn);
+}
+
+__global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
+  const unsigned nb = gridDim.x;
+  const int n = a.s.n;
+  const int qrow = n / 4;
+  const size_t qplane = (size_t)qrow * n;
+  const size_t nq = a.nc / 4;
+  const size_t warps = (size_t)nb * (CG_BLOCK / 32);
+  const size_t wid = (size_t)blockIdx.x * (CG_BLOCK / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  float4 *x4 = reinterpret_cast<float4 *>(a.x);
+  float4 *p4 = reinterpret_cast<float4 *>(a.p);
+  const float4 *b4 = reinterpret_cast<const float4 *>(a.b);
+  const float4 *pf4 = reinterpret_cast<const float4 *>(a.Pf);
+  const float4 *d4p = reinterpret_cast<const float4 *>(a.diag);
+  const uchar4 *A4p = reinterpret_cast<const uchar4 *>(a.A);
+  float *R[2] = {a.r, a.z}, *W[2] = {a.w, a.w1}, *S[2] = {a.s0, a.s1};
+  auto decode_q = [&](size_t q, int &i, int &j, int &kq) {
+    kq = (int)(q % qrow);
+    j = (int)((q / qrow) % n);
+    i = (int)(q / qplane);
+  };
+  const float hs = a.s.inv_h2_f;
+
+  /* phase 0a: r = b - A x on the liquid; b.b, r.r */
+  FF pbb = ff_zero(), prr = ff_zero();
+  for (size_t base = wid * 32; base < nq; base += warps * 32) {
+    size_t q = base + lane;
+    bool valid = q < nq;
+    int i = 0, j = 0, kq = 0;
+    if (valid) decode_q(q, i, j, kq);
+    float4 xs, ax;
+    uchar4 A4;
+    quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.x, a.x, 0.0f, true, xs, ax, A4);
+    if (!valid) continue;
+    const float4 bv = b4[q];
+    const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+    const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, av[4] = {ax.x, ax.y, ax.z, ax.w};
+    const float4 xo = x4[q];
+    const float xov[4] = {xo.x, xo.y, xo.z, xo.w};
+    float rv[4], xv[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      if (fv[t]) {
+        ff_add_prod(pbb, bb[t], bb[t]);
+        rv[t] = bb[t] - av[t];
+        ff_add_prod(prr, rv[t], rv[t]);
+        xv[t] = xov[t];
+      } else {
+        rv[t] = xv[t] = 0.0f;
+      }
+    }
+    reinterpret_cast<float4 *>(R[0])[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
+  }
+  store_partial(a.part, 0, nb, pbb);
+  store_partial(a.part, 1, nb, prr);
+  if (!grid_barrier(a.bar, a.iflags)) return;
+  double b2, rr;
+  sum_partials(a.part, 0, 1, nb, b2, rr);
+  const double eps = a.rel_tol * a.rel_tol * b2;
+  int done = rr <= eps ? 1 : 0, iters = 0;
+  double e2 = rr;
+
+  /* the sweep: for the quads of this warp, from R[cur], W[cur], S[cur]
+   * (and the directions) at step (alpha, beta, first) to R/W/S[cur^1];
+   * init: only w = A M^-1 r (alpha = 0, no s, no updates) */
+  auto sweep = [&](int cur, float alpha, float beta, bool first, bool init, FF &pg, FF &pd,
+                   FF &pr) {
+    const float *Ro = R[cur], *Wo = W[cur], *So = S[cur];
+    float *Rn = R[cur ^ 1], *Wn = W[cur ^ 1], *Sn = S[cur ^ 1];
+    for (size_t base = wid * 32; base < nq; base += warps * 32) {
+      const size_t q = base + lane;
+      const bool valid = q < nq;
+      int i = 0, j = 0, kq = 0;
+      if (valid) decode_q(q, i, j, kq);
+      const size_t qs = valid ? q : 0;
+      const uchar4 A4 = valid ? A4p[qs] : make_uchar4(0, 0, 0, 0);
+      const bool any = fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w);
+      float4 pf = make_float4(0, 0, 0, 0), r = pf, w = pf, so = pf, un = pf, sn = pf, rn = pf;
+      if (any) {
+        pf = pf4[qs];
+        r = __ldcg(reinterpret_cast<const float4 *>(Ro) + qs);
+        if (!init) {
+          w = __ldcg(reinterpret_cast<const float4 *>(Wo) + qs);
+          if (!first) so = __ldcg(reinterpret_cast<const float4 *>(So) + qs);
+        }
+        if (init) {
+          un = make_float4(fl(A4.x) ? pf.x * r.x : 0.0f, fl(A4.y) ? pf.y * r.y : 0.0f,
+                           fl(A4.z) ? pf.z * r.z : 0.0f, fl(A4.w) ? pf.w * r.w : 0.0f);
+        } else {
+          un = cg1_unext(A4, pf, r, w, so, alpha, beta, first);
+        }
+      }
+      /* k neighbours across quads */
+      float left = __shfl_up_sync(FULL, un.w, 1);
+      int left_fl = __shfl_up_sync(FULL, (int)fl(A4.w), 1);
+      float right = __shfl_down_sync(FULL, un.x, 1);
+      int right_fl = __shfl_down_sync(FULL, (int)fl(A4.x), 1);
+      if (!valid || !any) continue;
+      const size_t c0 = 4 * q;
+      const int k0 = 4 * kq;
+      if (k0 == 0) {
+        left_fl = 0;
+      } else if (lane == 0) {
+        left = init ? (fl(a.A[c0 - 1]) ? a.Pf[c0 - 1] * __ldcg(Ro + c0 - 1) : 0.0f)
+                    : cg1_unext1(a, c0 - 1, Ro, Wo, So, alpha, beta, first, left_fl);
+        left_fl = fl(a.A[c0 - 1]);
+      }
+      if (k0 + 4 >= n) {
+        right_fl = 0;
+      } else if (lane == 31) {
+        right = init ? (fl(a.A[c0 + 4]) ? a.Pf[c0 + 4] * __ldcg(Ro + c0 + 4) : 0.0f)
+                     : cg1_unext1(a, c0 + 4, Ro, Wo, So, alpha, beta, first, right_fl);
+        right_fl = fl(a.A[c0 + 4]);
+      }
+      /* i/j neighbour quads, two at a time (loads of a pair issued together) */
+      const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
+      const long off[4] = {(long)qplane, -(long)qplane, (long)qrow, -(long)qrow};
+      const float4 dg = __ldg(d4p + q);
+      float acc[4] = {dg.x * un.x, dg.y * un.y, dg.z * un.z, dg.w * un.w};
+#pragma unroll
+      for (int h2 = 0; h2 < 4; h2 += 2) {
+        Cg1Nb nbq[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const int d = h2 + e;
+          const float4 zero = make_float4(0, 0, 0, 0);
+          nbq[e].A = make_uchar4(0, 0, 0, 0);
+          nbq[e].pf = nbq[e].r = nbq[e].w = nbq[e].s = zero;
+          if (has[d]) {
+            const size_t qq = (size_t)((long)q + off[d]);
+            nbq[e].A = A4p[qq];
+            nbq[e].pf = pf4[qq];
+            nbq[e].r = __ldcg(reinterpret_cast<const float4 *>(Ro) + qq);
+            if (!init) {
+              nbq[e].w = __ldcg(reinterpret_cast<const float4 *>(Wo) + qq);
+              if (!first) nbq[e].s = __ldcg(reinterpret_cast<const float4 *>(So) + qq);
+            }
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          float4 v;
+          if (init) {
+            v = make_float4(fl(nbq[e].A.x) ? nbq[e].pf.x * nbq[e].r.x : 0.0f,
+                            fl(nbq[e].A.y) ? nbq[e].pf.y * nbq[e].r.y : 0.0f,
+                            fl(nbq[e].A.z) ? nbq[e].pf.z * nbq[e].r.z : 0.0f,
+                            fl(nbq[e].A.w) ? nbq[e].pf.w * nbq[e].r.w : 0.0f);
+          } else {
+            v = cg1_unext(nbq[e].A, nbq[e].pf, nbq[e].r, nbq[e].w, nbq[e].s, alpha, beta, first);
+          }
+          acc[0] -= v.x;
+          acc[1] -= v.y;
+          acc[2] -= v.z;
+          acc[3] -= v.w;
+        }
+      }
+      const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+      const float uv[4] = {un.x, un.y, un.z, un.w};
+      acc[0] -= (fv[1] ? uv[1] : 0.0f) + (left_fl ? left : 0.0f);
+      acc[1] -= (fv[0] ? uv[0] : 0.0f) + (fv[2] ? uv[2] : 0.0f);
+      acc[2] -= (fv[1] ? uv[1] : 0.0f) + (fv[3] ? uv[3] : 0.0f);
+      acc[3] -= (fv[2] ? uv[2] : 0.0f) + (right_fl ? right : 0.0f);
+      float wn[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) wn[t] = fv[t] ? acc[t] * hs : 0.0f;
+      reinterpret_cast<float4 *>(Wn)[q] = make_float4(wn[0], wn[1], wn[2], wn[3]);
+      if (init) {
+#pragma unroll
+        for (int t = 0; t < 4; t++)
+          if (fv[t]) {
+            const float rt = t == 0 ? r.x : t == 1 ? r.y : t == 2 ? r.z : r.w;
+            ff_add_prod(pg, rt, uv[t]);
+            ff_add_prod(pd, wn[t], uv[t]);
+          }
+        /* R[cur^1] mirrors R[cur] so the first sweep reads the same r */
+        reinterpret_cast<float4 *>(Rn)[q] = r;
+        continue;
+      }
+      /* own updates: p, s, x, r */
+      const float4 w4 = w, s4 = so;
+      const float4 po = first ? make_float4(0, 0, 0, 0) : p4[q];
+      const float4 xo = x4[q];
+      const float Wv[4] = {w4.x, w4.y, w4.z, w4.w}, Sv[4] = {s4.x, s4.y, s4.z, s4.w};
+      const float Pv[4] = {po.x, po.y, po.z, po.w}, Xv[4] = {xo.x, xo.y, xo.z, xo.w};
+      const float Rv[4] = {r.x, r.y, r.z, r.w}, PF[4] = {pf.x, pf.y, pf.z, pf.w};
+      float pn[4], snn[4], xn[4], rnn[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        if (fv[t]) {
+          const float u = PF[t] * Rv[t];
+          pn[t] = first ? u : u + beta * Pv[t];
+          snn[t] = first ? Wv[t] : Wv[t] + beta * Sv[t];
+          xn[t] = Xv[t] + alpha * pn[t];
+          rnn[t] = Rv[t] - alpha * snn[t];
+          ff_add_prod(pg, rnn[t], uv[t]);
+          ff_add_prod(pd, wn[t], uv[t]);
+          ff_add_prod(pr, rnn[t], rnn[t]);
+        } else {
+          pn[t] = snn[t] = xn[t] = rnn[t] = 0.0f;
+        }
+      }
+      p4[q] = make_float4(pn[0], pn[1], pn[2], pn[3]);
+      x4[q] = make_float4(xn[0], xn[1], xn[2], xn[3]);
+      reinterpret_cast<float4 *>(Sn)[q] = make_float4(snn[0], snn[1], snn[2], snn[3]);
+      reinterpret_cast<float4 *>(Rn)[q] = make_float4(rnn[0], rnn[1], rnn[2], rnn[3]);
+      (void)sn;
+      (void)rn;
+    }
+  };
+
+  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u */
+  FF pg = ff_zero(), pd = ff_zero(), pr = ff_zero();
+  sweep(0, 0.0f, 0.0f, true, true, pg, pd, pr);
+  store_partial(a.part, 2, nb, pg);
+  store_partial(a.part, 3, nb, pd);
+  if (!grid_barrier(a.bar, a.iflags)) return;
+  double gamma, delta;
+  sum_partials(a.part, 2, 3, nb, gamma, delta);
+  double alpha = gamma / delta, beta = 0.0;
+  if (!(alpha == alpha) || !(delta > 0.0)) done = done ? done : 2;
+  int cur = 1; /* R[1] = r0, W[1] = w0 */
+  bool first = true;
+  int set = 0;
+  while (!done) {
+    FF g2 = ff_zero(), d2 = ff_zero(), r2 = ff_zero();
+    sweep(cur, (float)alpha, (float)beta, first, false, g2, d2, r2);
+    const int k0 = set ? 3 : 0;
+    store_partial(a.part, k0, nb, g2);
+    store_partial(a.part, k0 + 1, nb, d2);
+    store_partial(a.part, k0 + 2, nb, r2);
+    if (!grid_barrier(a.bar, a.iflags)) return;
+    double gn, dn, rn, unused;
+    sum_partials(a.part, k0, k0 + 1, nb, gn, dn);
+    sum_partials(a.part, k0 + 2, -1, nb, rn, unused);
+    set ^= 1;
+    cur ^= 1;
+    first = false;
+    iters++;
+    e2 = rn;
+    if (e2 <= eps) done = 1;
+    else if (!(e2 == e2)) done = 2;
+    else if (iters >= a.max_iters) done = 3;
+    const double bnext = gn / gamma;
+    const double den = dn - bnext * gn / alpha;
+    alpha = gn / den;
+    beta = bnext;
+    gamma = gn;
+    if (!done && !(alpha == alpha && den > 0.0)) done = 2;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.iflags[IF_DONE] = done;
+    a.iflags[IF_ITERS] = iters;
+    a.iflags[IF_NAN] = done == 2;
+    a.scal[SC_ERR2] = e2;
+    a.scal[SC_B2] = b2;
+    a.scal[SC_EPS] = eps;
+  }
+}
+
 /* ------------------------------------------- IC(0)/MIC(0) as wavefronts */
 
 /* The lexicographic incomplete-Cholesky factor of the reference's
@@ -1387,6 +1686,48 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
 
 size_t ic_smem_bytes();
 
+/* FP64 r.r of the true residual b - A x of the FAST-mode matrix (the FP32
+ * coefficients, evaluated in double): the check of the outer refinement. */
+__global__ void __launch_bounds__(BLK) k_true_r2(SolveArgs s, const uint8_t *__restrict__ A,
+                                                 const float *__restrict__ diag,
+                                                 const float *__restrict__ b,
+                                                 const float *__restrict__ x,
+                                                 double *__restrict__ part) {
+  __shared__ double sh[BLK];
+  const int n = s.n;
+  const size_t nc = (size_t)n * n * n;
+  double acc2 = 0.0;
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK) {
+    if (A[c] != CELL_FLUID) continue;
+    int i, j, k;
+    decode(c, n, i, j, k);
+    double acc = (double)diag[c] * (double)x[c];
+    const size_t sj = n, si = (size_t)n * n;
+    if (i + 1 < n && A[c + si] == CELL_FLUID) acc -= (double)x[c + si];
+    if (i > 0 && A[c - si] == CELL_FLUID) acc -= (double)x[c - si];
+    if (j + 1 < n && A[c + sj] == CELL_FLUID) acc -= (double)x[c + sj];
+    if (j > 0 && A[c - sj] == CELL_FLUID) acc -= (double)x[c - sj];
+    if (k + 1 < n && A[c + 1] == CELL_FLUID) acc -= (double)x[c + 1];
+    if (k > 0 && A[c - 1] == CELL_FLUID) acc -= (double)x[c - 1];
+    const double r = (double)b[c] - acc * (double)s.inv_h2_f;
+    acc2 += r * r;
+  }
+  sh[threadIdx.x] = acc2;
+  __syncthreads();
+  for (int w = BLK / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_true_r2_sum(int nb, const double *__restrict__ part, double *__restrict__ scal) {
+  if (threadIdx.x || blockIdx.x) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; b++) s += part[b];
+  scal[SC_TRUE2] = s;
+}
+
 static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   double sc[SC_COUNT];
   int host_flags[IF_COUNT];
@@ -1509,6 +1850,8 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.s0 = h->s;
     a.s1 = h->s1;
     a.w = h->w;
+    a.w1 = h->w1;
+    a.p = h->pdir;
     a.P = h->P;
     a.diag = h->diag;
     a.Pf = h->Pf;
@@ -1536,7 +1879,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     int grid = h->cg_grid[mode == FLIPGPU_SOLVE_REF ? 0 : 1];
     size_t smem = 0;
     if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0) {
-      kern = (const void *)k_cg_quad;
+      kern = (const void *)k_cg_cg1;
       grid = h->cg_grid[2];
     }
     if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_IC) {
@@ -1547,14 +1890,51 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
       cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
     }
-    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, smem, S);
-    FG_LAUNCHED(h, 1);
-    if (e != cudaSuccess) {
-      snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
-      return FLIPGPU_ECUDA;
+    /* FAST mode: after CG meets the tolerance on its recursive residual,
+     * the true residual is recomputed in FP64; while it misses the
+     * tolerance CG restarts from x (at most refine_steps times) */
+    const int passes = mode == FLIPGPU_SOLVE_FAST ? 1 + (h->prm.refine_steps > 0 ? h->prm.refine_steps : 0) : 1;
+    int total_iters = 0, rc = FLIPGPU_OK;
+    double last_true2 = 0.0;
+    for (int pass = 0; pass < passes; pass++) {
+      if (pass > 0) {
+        cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
+        if (precond == FLIPGPU_PRECOND_IC) {
+          cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
+          cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
+          cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
+        }
+      }
+      cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, smem, S);
+      FG_LAUNCHED(h, 1);
+      if (e != cudaSuccess) {
+        snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
+        return FLIPGPU_ECUDA;
+      }
+      if (mode == FLIPGPU_SOLVE_FAST) {
+        k_true_r2<<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press, h->partial);
+        k_true_r2_sum<<<1, 32, 0, S>>>(RED_BLOCKS, h->partial, h->scal);
+        FG_LAUNCHED(h, 2);
+      }
+      cudaEventRecord(h->ev1, S);
+      FlipGpuSolveStats one;
+      rc = finish_stats(h, &one, mode);
+      total_iters += one.iterations;
+      if (st) {
+        *st = one;
+        st->iterations = total_iters;
+      }
+      if (rc != FLIPGPU_OK || mode != FLIPGPU_SOLVE_FAST) break;
+      double true2 = 0.0;
+      cudaMemcpy(&true2, h->scal + SC_TRUE2, sizeof(double), cudaMemcpyDeviceToHost);
+      if (st) st->r2_true = true2;
+      /* stop when the true residual meets the tolerance, or when a restart
+       * no longer helps: with x stored in FP32 the true residual levels off
+       * near the FP32 rounding of A x */
+      if (true2 <= h->prm.rel_tol * h->prm.rel_tol * one.b2) break;
+      if (pass > 0 && true2 > 0.25 * last_true2) break;
+      last_true2 = true2;
     }
-    cudaEventRecord(h->ev1, S);
-    int rc = finish_stats(h, st, mode);
     warm_stats(st);
     return rc;
   }
@@ -1699,7 +2079,7 @@ int cg_grid_size(int *out) {
   if (!coop) return 0;
   if (ic_init_device() != 0) return -1;
   const void *k[4] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>, (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
-                      (const void *)k_cg_quad, (const void *)k_cg_ic};
+                      (const void *)k_cg_cg1, (const void *)k_cg_ic};
   for (int v = 0; v < 4; v++) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], CG_BLOCK,

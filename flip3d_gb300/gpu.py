@@ -37,7 +37,7 @@ class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
                 ("b2", C.c_double), ("ms", C.c_double), ("warm", C.c_int),
                 ("r2_prev", C.c_double), ("r2_guess", C.c_double), ("gamma", C.c_double),
-                ("warm_ms", C.c_double)]
+                ("warm_ms", C.c_double), ("r2_true", C.c_double)]
 
 
 class FlipGpuError(RuntimeError):

@@ -75,7 +75,13 @@ typedef struct FlipGpuParams {
                          most rel_tol^2*b.b; 0 keeps the reference's own */
   double eps_abs;     /* REF mode: explicit absolute r.r bound if >= 0 */
   int max_iters;      /* CG iteration cap; <=0: n^3 like the reference */
-  int refine_steps;   /* FAST mode: outer FP64 refinement passes (0 = off) */
+  int refine_steps;   /* FAST mode: after CG stops, the true residual b - A x
+                         is recomputed in FP64 (stats r2_true); while it
+                         misses rel_tol and the last restart cut it at least
+                         4x, CG restarts from x, at most refine_steps times.
+                         Default 0: with x in FP32 the true residual levels
+                         off near the FP32 rounding of A x (about 1e-4 of
+                         ||b|| at n=128), where restarts cannot help. */
 } FlipGpuParams;
 
 typedef struct FlipGpuSolveStats {
@@ -89,6 +95,8 @@ typedef struct FlipGpuSolveStats {
   double r2_guess;    /* warm start: r.r of the guess CG started from */
   double gamma;       /* warm start: step taken along the network's correction */
   double warm_ms;     /* warm start: device time of network + step */
+  double r2_true;     /* FAST mode: FP64 r.r of b - A x at the end (the
+                         recursive r2 is what CG's stop test saw) */
 } FlipGpuSolveStats;
 
 typedef struct FlipUNet FlipUNet;
