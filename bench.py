@@ -216,7 +216,7 @@ def run_reference(args):
         return
     from flip3d_gb300 import scenes
     from oracle import pyoracle as orc
-    sc = scenes.dam_break(args.n, seed=0)
+    sc = getattr(scenes, args.scene)(args.n, seed=0)
     cores = os.cpu_count() or 1
     orc.set_threads(cores)
     prm = orc.params(sc.n, orc.PRECOND_REF, rel_tol=1e-6, seed=1)
@@ -232,11 +232,11 @@ def run_reference(args):
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": f"dam_break N={args.n} ({sc.count} particles)",
+           "config": {"workload": f"{args.scene} N={args.n} ({sc.count} particles)",
                       "particles": sc.count, "grid": args.n, "solver": "reference PCG",
                       "rel_res": 1e-6},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"{args.steps} full steps of dam_break N={args.n}"},
+                            "sample": f"{args.steps} full steps of {args.scene} N={args.n}"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -250,6 +250,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "mic", "ref"])
+    ap.add_argument("--scene", default="dam_break", choices=["dam_break", "sphere_into_pool"],
+                    help="dam_break (column x<0.4, y<0.8) or sphere_into_pool (pool 0.25, "
+                         "sphere r 0.15 falling at 2 m/s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -267,7 +270,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    sc = scenes.dam_break(args.n, seed=rank)
+    sc = getattr(scenes, args.scene)(args.n, seed=rank)
     P = sc.count
     pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "mic": gpu.PRECOND_IC,
            "ref": gpu.PRECOND_REF}[args.precond]
@@ -366,9 +369,9 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        rate, cores, steps, dt = cpu_step_rate(scenes.dam_break(args.n, seed=0))
+        rate, cores, steps, dt = cpu_step_rate(getattr(scenes, args.scene)(args.n, seed=0))
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{steps} full step(s) of dam_break N={args.n} ({P} particles), "
+               "sample": f"{steps} full step(s) of {args.scene} N={args.n} ({P} particles), "
                          f"{dt:.1f} s"}
 
     if rank == 0:
@@ -377,7 +380,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"dam_break N={args.n}, 8 particles/cell, rel-res 1e-6",
+            "config": {"workload": f"{args.scene} N={args.n}, 8 particles/cell, rel-res 1e-6",
                        "particles": P, "grid": args.n, "solver": f"FP32 PCG {args.precond}, FP64 dots",
                        "l2": "inputs larger than L2 (state ~0.6 GB per step)",
                        "parallelism": f"replicas x{world}"},

@@ -239,6 +239,8 @@ SimConst make_const(const FlipGpu *h) {
   c.corr_reach = smallest_float_ge((double)c.re_corr * (1.0 + 1.0 / 256.0));
   c.dt = p.dt;
   c.dt_f = (float)p.dt;
+  c.kick_fluid = 0.01 * (double)c.re_corr / (double)c.dt_f;
+  c.kick_wall = 0.05 * (double)c.re_corr / (double)c.dt_f;
   split(p.dt, c.dt_h, c.dt_l);
   c.grav = -p.dt * p.gravity;
   split(c.grav, c.grav_h, c.grav_l);

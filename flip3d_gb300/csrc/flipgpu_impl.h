@@ -48,6 +48,8 @@ struct SimConst {
   float corr_cut2;    /* squared distance beyond which the spring weight is 0 */
   float corr_reach;   /* re*(1+2^-8): cell-range reach of the corrector */
   float dt_f;         /* (float)DT, the corrector's dt */
+  double kick_fluid;  /* 0.01*re/dt (src/corrector.cpp:75) */
+  double kick_wall;   /* 0.05*re/dt (src/corrector.cpp:80) */
   double dt;
   float dt_h, dt_l;   /* DT split into floats */
   double grav;        /* -DT*GRAVITY */

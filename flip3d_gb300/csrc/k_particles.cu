@@ -629,6 +629,16 @@ __device__ __forceinline__ void reach_range(float p, float reach_m, float fn, in
 
 constexpr int NEAR_CAP = 24; /* near-list batch per thread */
 
+/* The corrector's kicks (src/corrector.cpp:74-81) in the reference's double
+ * arithmetic, out of line (rare branches; see refmath.h on FP64 hoisting).
+ * k = 0.01*re/dt or 0.05*re/dt, precomputed on the host. */
+__device__ __noinline__ float kick_add(float s, double k, int draw) {
+  return (float)((double)s + k * (double)draw / 100.0);
+}
+__device__ __noinline__ float wall_kick_add(float s, double k, float nrm) {
+  return (float)((double)s + k * (double)nrm);
+}
+
 /* Spring displacement (src/corrector.cpp:54-100). Two passes per batch: a
  * cheap test collects the neighbours within re*(1+2^-8) into a per-thread
  * list (all other neighbours have weight exactly 0 and add nothing), then
@@ -672,15 +682,12 @@ k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict
         for (int q = 0; q < 3; q++) {
           uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)c.step, q),
                                    (uint64_t)p, (uint64_t)o);
-          spring[q] = (float)((double)spring[q] + 0.01 * (double)re / (double)c.dt_f *
-                                                      (double)(int)(r % 101) / 100.0);
+          spring[q] = kick_add(spring[q], c.kick_fluid, (int)(r % 101));
         }
       } else {
         uint32_t o = perm[b];
         float nn[3] = {nx[o], ny[o], nz[o]};
-        for (int q = 0; q < 3; q++)
-          spring[q] = (float)((double)spring[q] +
-                              0.05 * (double)re / (double)c.dt_f * (double)nn[q]);
+        for (int q = 0; q < 3; q++) spring[q] = wall_kick_add(spring[q], c.kick_wall, nn[q]);
       }
     }
     cnt = 0;

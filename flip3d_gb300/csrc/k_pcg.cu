@@ -1247,7 +1247,12 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
     }
   };
 
-  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u */
+  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u.
+   * The scalar recurrences run in FP64 on thread 0 of each block only (the
+   * sums are identical in every block) and reach the block as floats
+   * through shared memory: FP64 division is slow on this GPU. */
+  __shared__ float s_alpha, s_beta;
+  __shared__ int s_done;
   FF pg = ff_zero(), pd = ff_zero(), pr = ff_zero();
   sweep(0, 0.0f, 0.0f, true, true, pg, pd, pr);
   store_partial(a.part, 2, nb, pg);
@@ -1255,14 +1260,22 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
   if (!grid_barrier(a.bar, a.iflags)) return;
   double gamma, delta;
   sum_partials(a.part, 2, 3, nb, gamma, delta);
-  double alpha = gamma / delta, beta = 0.0;
-  if (!(alpha == alpha) || !(delta > 0.0)) done = done ? done : 2;
+  double alpha = 0.0, beta = 0.0;
+  if (threadIdx.x == 0) {
+    alpha = gamma / delta;
+    if (!(alpha == alpha) || !(delta > 0.0)) done = done ? done : 2;
+    s_alpha = (float)alpha;
+    s_done = done;
+  }
+  __syncthreads();
+  float alpha_f = s_alpha, beta_f = 0.0f;
+  done = s_done;
   int cur = 1; /* R[1] = r0, W[1] = w0 */
   bool first = true;
   int set = 0;
   while (!done) {
     FF g2 = ff_zero(), d2 = ff_zero(), r2 = ff_zero();
-    sweep(cur, (float)alpha, (float)beta, first, false, g2, d2, r2);
+    sweep(cur, alpha_f, beta_f, first, false, g2, d2, r2);
     const int k0 = set ? 3 : 0;
     store_partial(a.part, k0, nb, g2);
     store_partial(a.part, k0 + 1, nb, d2);
@@ -1275,16 +1288,25 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
     cur ^= 1;
     first = false;
     iters++;
-    e2 = rn;
-    if (e2 <= eps) done = 1;
-    else if (!(e2 == e2)) done = 2;
-    else if (iters >= a.max_iters) done = 3;
-    const double bnext = gn / gamma;
-    const double den = dn - bnext * gn / alpha;
-    alpha = gn / den;
-    beta = bnext;
-    gamma = gn;
-    if (!done && !(alpha == alpha && den > 0.0)) done = 2;
+    if (threadIdx.x == 0) {
+      e2 = rn;
+      if (e2 <= eps) done = 1;
+      else if (!(e2 == e2)) done = 2;
+      else if (iters >= a.max_iters) done = 3;
+      const double bnext = gn / gamma;
+      const double den = dn - bnext * gn / alpha;
+      alpha = gn / den;
+      beta = bnext;
+      gamma = gn;
+      if (!done && !(alpha == alpha && den > 0.0)) done = 2;
+      s_alpha = (float)alpha;
+      s_beta = (float)beta;
+      s_done = done;
+    }
+    __syncthreads();
+    alpha_f = s_alpha;
+    beta_f = s_beta;
+    done = s_done;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.iflags[IF_DONE] = done;
@@ -1642,7 +1664,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
     if (!grid_barrier(a.bar, a.iflags)) return;
     double ws;
     sum_partials(a.part, 3, -1, nb, ws, unused);
-    const float alpha_f = (float)(azr / ws);
+    __shared__ float s_bcast;
+    if (threadIdx.x == 0) s_bcast = (float)(azr / ws); /* one FP64 division per block */
+    __syncthreads();
+    const float alpha_f = s_bcast;
     /* phase B: x += alpha s, r -= alpha w; r.r */
     FF prr2 = ff_zero();
     for (size_t c = t0; c < nc; c += stride) {
@@ -1665,7 +1690,10 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
     wavefront(a, sm, pl_tab, false, apply + 1, apply, a.r, a.z);
     if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
     const double zr = sum_brick_parts(a);
-    beta_f = (float)(zr / azr);
+    __syncthreads();
+    if (threadIdx.x == 0) s_bcast = (float)(zr / azr);
+    __syncthreads();
+    beta_f = s_bcast;
     azr = zr;
     first = false;
     float *t = so;

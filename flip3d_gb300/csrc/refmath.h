@@ -24,12 +24,34 @@
 
 #if defined(__CUDACC__)
 #define RM_FN __host__ __device__ __forceinline__
+/* The double-precision fallbacks are out of line: inlined, the compiler may
+ * hoist their float-to-double conversions onto the common path, and every
+ * FP64 instruction costs the time of dozens of FP32 ones on this GPU. */
+#define RM_COLD static __host__ __device__ __noinline__
 #else
 #include <cmath>
 #define RM_FN static inline
+#define RM_COLD static
 #endif
 
 namespace refmath {
+
+/* ---- double expressions of the reference, taken only when the FP32
+ * error-free evaluation cannot decide the rounding ---- */
+RM_COLD float hypot_d(float a, float b) {
+  return (float)sqrt((double)a * (double)a + (double)b * (double)b);
+}
+RM_COLD float sharp_d(float hh, float r2) { return (float)((double)hh / (double)r2 - 1.0); }
+RM_COLD float add_d(float a, double b) { return (float)((double)a + b); }
+RM_COLD float blend_d(float x, float y, double c1, double c2) {
+  double a = c1 * (double)x;
+  double b = c2 * (double)y;
+  return (float)(a + b);
+}
+RM_COLD float axpy_d(float p, float v, double c) {
+  double d = c * (double)v;
+  return (float)((double)p + d);
+}
 
 /* s + e == a + b exactly (Knuth TwoSum). */
 RM_FN void two_sum(float a, float b, float &s, float &e) {
@@ -91,8 +113,7 @@ RM_FN float hypot_ref(float a, float b) {
   float corr = d * (0.5f / r);         /* sqrt(s + lo) - r to ~2^-24 rel */
   float out, t;
   two_sum(r, corr, out, t);
-  if (near_tie(out, t))
-    return (float)sqrt((double)a * (double)a + (double)b * (double)b);
+  if (near_tie(out, t)) return hypot_d(a, b);
   return out;
 }
 
@@ -139,8 +160,7 @@ RM_FN float sharp_ref(float r2, float hh, float r2_floor, float small) {
     float R = fmaf(-X, r2, D);        /* exact remainder */
     float t = R / r2;
     float gapx = from_bits(bits_of(X) + 1) - X;
-    if (fabsf(fabsf(t) - 0.5f * gapx) <= gapx * 0x1p-10f || X == 0.0f)
-      return (float)((double)hh / (double)r2 - 1.0);
+    if (fabsf(fabsf(t) - 0.5f * gapx) <= gapx * 0x1p-10f || X == 0.0f) return sharp_d(hh, r2);
     return X;
   }
   float rem = fmaf(-q, r2, hh);       /* hh - q*r2, exact */
@@ -151,7 +171,7 @@ RM_FN float sharp_ref(float r2, float hh, float r2_floor, float small) {
   float c = c1 + rem2 / r2;           /* ... to double-float accuracy */
   float out, r;
   two_sum(t, e + c, out, r);
-  if (near_tie(out, r)) return (float)((double)hh / (double)r2 - 1.0);
+  if (near_tie(out, r)) return sharp_d(hh, r2);
   return out;
 }
 
@@ -167,8 +187,7 @@ RM_FN float add_fd(float a, float b_hi, float b_lo, double b) {
   float s, e, out, t;
   two_sum(a, b_hi, s, e);
   two_sum(s, e + b_lo, out, t);
-  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(a), fabsf(b_hi))))
-    return (float)((double)a + b);
+  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(a), fabsf(b_hi)))) return add_d(a, b);
   return out;
 }
 
@@ -187,11 +206,7 @@ RM_FN float blend_ref(float x, float y, float c1h, float c1l, float c2h,
   mul_fd(y, c2h, c2l, p2, e2);
   two_sum(p1, p2, s, es);
   two_sum(s, es + (e1 + e2), out, t);
-  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(p1), fabsf(p2)))) {
-    double a = c1 * (double)x;
-    double b = c2 * (double)y;
-    return (float)(a + b);
-  }
+  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(p1), fabsf(p2)))) return blend_d(x, y, c1, c2);
   return out;
 }
 
@@ -202,10 +217,7 @@ RM_FN float axpy_fd(float p, float v, float ch, float cl, double c) {
   mul_fd(v, ch, cl, m, me);
   two_sum(p, m, s, es);
   two_sum(s, es + me, out, t);
-  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(p), fabsf(m)))) {
-    double d = c * (double)v;
-    return (float)((double)p + d);
-  }
+  if (near_tie(out, t) || cancelled(out, fmaxf(fabsf(p), fabsf(m)))) return axpy_d(p, v, c);
   return out;
 }
 
