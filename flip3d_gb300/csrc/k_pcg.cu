@@ -998,6 +998,50 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_quad(CgArgs a) {
 }
 
 
+/* K per-thread partial sums reduced over the block into
+ * part[(k0+q)*nb + blockIdx.x] with one __syncthreads (warp shuffle trees,
+ * then thread q merges the warps' value q in a fixed order). */
+template <int K>
+__device__ __forceinline__ void store_partials(float2 *part, int k0, unsigned nb, FF (&v)[K]) {
+  __shared__ FF wp[K][CG_BLOCK / 32];
+#pragma unroll
+  for (int q = 0; q < K; q++)
+    for (int o = 16; o > 0; o >>= 1) v[q] = ff_merge(v[q], ff_shfl_down(v[q], o));
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < K; q++) wp[q][wid] = v[q];
+  __syncthreads();
+  if (threadIdx.x < K) {
+    FF t = wp[threadIdx.x][0];
+    for (int i = 1; i < CG_BLOCK / 32; i++) t = ff_merge(t, wp[threadIdx.x][i]);
+    part[(size_t)(k0 + threadIdx.x) * nb + blockIdx.x] = make_float2(t.hi, t.lo);
+  }
+}
+
+/* Sums over the nb block partials of slots k0..k0+K-1, by warp 0 (lane-
+ * strided merges, then a shuffle tree: the same order in every block);
+ * valid in thread 0. */
+template <int K>
+__device__ __forceinline__ void warp_sum_partials(const float2 *part, int k0, unsigned nb,
+                                                  double (&out)[K]) {
+  const int lane = threadIdx.x & 31;
+  FF v[K];
+#pragma unroll
+  for (int q = 0; q < K; q++) v[q] = ff_zero();
+  for (unsigned i = lane; i < nb; i += 32)
+#pragma unroll
+    for (int q = 0; q < K; q++) {
+      const float2 a = __ldcg(part + (size_t)(k0 + q) * nb + i);
+      v[q] = ff_merge(v[q], FF{a.x, a.y});
+    }
+#pragma unroll
+  for (int q = 0; q < K; q++) {
+    for (int o = 16; o > 0; o >>= 1) v[q] = ff_merge(v[q], ff_shfl_down(v[q], o));
+    out[q] = ff_to_double(v[q]);
+  }
+}
+
 /* FAST-mode Jacobi PCG with one grid-wide reduction per iteration
  * (Chronopoulos-Gear): with u = M^-1 r and w = A u,
  *   p = u + beta p,  s = w + beta s  (s = A p),  x += alpha p,  r -= alpha s,
@@ -1090,14 +1134,29 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
     reinterpret_cast<float4 *>(R[0])[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
     x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
   }
-  store_partial(a.part, 0, nb, pbb);
-  store_partial(a.part, 1, nb, prr);
+  __shared__ float s_alpha, s_beta;
+  __shared__ int s_done;
+  {
+    FF v[2] = {pbb, prr};
+    store_partials<2>(a.part, 0, nb, v);
+  }
   if (!grid_barrier(a.bar, a.iflags)) return;
-  double b2, rr;
-  sum_partials(a.part, 0, 1, nb, b2, rr);
-  const double eps = a.rel_tol * a.rel_tol * b2;
-  int done = rr <= eps ? 1 : 0, iters = 0;
-  double e2 = rr;
+  /* the FP64 scalar work runs on thread 0 of each block (the sums are the
+   * same in every block) and reaches the others through shared memory */
+  double b2 = 0.0, eps = 0.0, e2 = 0.0;
+  int done = 0, iters = 0;
+  if (threadIdx.x < 32) {
+    double t[2];
+    warp_sum_partials<2>(a.part, 0, nb, t);
+    if (threadIdx.x == 0) {
+      b2 = t[0];
+      e2 = t[1];
+      eps = a.rel_tol * a.rel_tol * b2;
+      s_done = e2 <= eps ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  done = s_done;
 
   /* the sweep: for the quads of this warp, from R[cur], W[cur], S[cur]
    * (and the directions) at step (alpha, beta, first) to R/W/S[cur^1];
@@ -1247,25 +1306,25 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
     }
   };
 
-  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u.
-   * The scalar recurrences run in FP64 on thread 0 of each block only (the
-   * sums are identical in every block) and reach the block as floats
-   * through shared memory: FP64 division is slow on this GPU. */
-  __shared__ float s_alpha, s_beta;
-  __shared__ int s_done;
+  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u */
   FF pg = ff_zero(), pd = ff_zero(), pr = ff_zero();
   sweep(0, 0.0f, 0.0f, true, true, pg, pd, pr);
-  store_partial(a.part, 2, nb, pg);
-  store_partial(a.part, 3, nb, pd);
+  {
+    FF v[2] = {pg, pd};
+    store_partials<2>(a.part, 2, nb, v);
+  }
   if (!grid_barrier(a.bar, a.iflags)) return;
-  double gamma, delta;
-  sum_partials(a.part, 2, 3, nb, gamma, delta);
-  double alpha = 0.0, beta = 0.0;
-  if (threadIdx.x == 0) {
-    alpha = gamma / delta;
-    if (!(alpha == alpha) || !(delta > 0.0)) done = done ? done : 2;
-    s_alpha = (float)alpha;
-    s_done = done;
+  double gamma = 0.0, alpha = 0.0, beta = 0.0;
+  if (threadIdx.x < 32) {
+    double t[2];
+    warp_sum_partials<2>(a.part, 2, nb, t);
+    if (threadIdx.x == 0) {
+      gamma = t[0];
+      alpha = gamma / t[1];
+      if (!(alpha == alpha) || !(t[1] > 0.0)) done = done ? done : 2;
+      s_alpha = (float)alpha;
+      s_done = done;
+    }
   }
   __syncthreads();
   float alpha_f = s_alpha, beta_f = 0.0f;
@@ -1274,34 +1333,34 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
   bool first = true;
   int set = 0;
   while (!done) {
-    FF g2 = ff_zero(), d2 = ff_zero(), r2 = ff_zero();
-    sweep(cur, alpha_f, beta_f, first, false, g2, d2, r2);
+    FF v[3] = {ff_zero(), ff_zero(), ff_zero()};
+    sweep(cur, alpha_f, beta_f, first, false, v[0], v[1], v[2]);
     const int k0 = set ? 3 : 0;
-    store_partial(a.part, k0, nb, g2);
-    store_partial(a.part, k0 + 1, nb, d2);
-    store_partial(a.part, k0 + 2, nb, r2);
+    store_partials<3>(a.part, k0, nb, v);
     if (!grid_barrier(a.bar, a.iflags)) return;
-    double gn, dn, rn, unused;
-    sum_partials(a.part, k0, k0 + 1, nb, gn, dn);
-    sum_partials(a.part, k0 + 2, -1, nb, rn, unused);
     set ^= 1;
     cur ^= 1;
     first = false;
     iters++;
-    if (threadIdx.x == 0) {
-      e2 = rn;
-      if (e2 <= eps) done = 1;
-      else if (!(e2 == e2)) done = 2;
-      else if (iters >= a.max_iters) done = 3;
-      const double bnext = gn / gamma;
-      const double den = dn - bnext * gn / alpha;
-      alpha = gn / den;
-      beta = bnext;
-      gamma = gn;
-      if (!done && !(alpha == alpha && den > 0.0)) done = 2;
-      s_alpha = (float)alpha;
-      s_beta = (float)beta;
-      s_done = done;
+    if (threadIdx.x < 32) {
+      double t[3];
+      warp_sum_partials<3>(a.part, k0, nb, t);
+      if (threadIdx.x == 0) {
+        const double gn = t[0], dn = t[1];
+        e2 = t[2];
+        if (e2 <= eps) done = 1;
+        else if (!(e2 == e2)) done = 2;
+        else if (iters >= a.max_iters) done = 3;
+        const double bnext = gn / gamma;
+        const double den = dn - bnext * gn / alpha;
+        alpha = gn / den;
+        beta = bnext;
+        gamma = gn;
+        if (!done && !(alpha == alpha && den > 0.0)) done = 2;
+        s_alpha = (float)alpha;
+        s_beta = (float)beta;
+        s_done = done;
+      }
     }
     __syncthreads();
     alpha_f = s_alpha;
