@@ -171,7 +171,7 @@ void free_all(FlipGpu *h) {
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
-                  h->ticket, h->brick_part, h->repo_draw, h->repo_res, h->repo_old,
+                  h->ticket, h->brick_part, h->dstep, h->repo_draw, h->repo_res, h->repo_old,
                   h->repo_cnt, h->repo_start, h->repo_list, h->repo_state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -254,6 +254,7 @@ SimConst make_const(const FlipGpu *h) {
   split(c.l0, c.l0h, c.l0l);
   c.seed = p.seed;
   c.step = h->step;
+  c.dstep = h->dstep;
   return c;
 }
 
@@ -335,7 +336,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   h->nbx = (p->n + 7) / 8;
   h->nbricks = h->nbx * h->nbx * h->nbx;
   AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
-  AL(h->ticket, 1) AL(h->brick_part, h->nbricks)
+  AL(h->ticket, 1) AL(h->brick_part, h->nbricks) AL(h->dstep, 1)
 #undef AL
   {
     /* bricks by increasing i+j+k: every brick's dependencies come earlier */
@@ -362,6 +363,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   cudaMemsetAsync(h->iflags, 0, IF_COUNT * sizeof(int), h->stream);
   cudaMemsetAsync(h->s, 0, nc * sizeof(float), h->stream);
   cudaMemsetAsync(h->s1, 0, nc * sizeof(float), h->stream);
+  cudaMemsetAsync(h->dstep, 0, sizeof(int64_t), h->stream);
   e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     free_all(h);
@@ -383,6 +385,8 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
 int flipgpu_destroy(FlipGpu *h) {
   if (!h) return FLIPGPU_EINVAL;
   cudaStreamSynchronize(h->stream);
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  if (h->graph) cudaGraphDestroy(h->graph);
   mesh_free(h);
   if (h->wdelta) {
     cudaFree(h->wdelta);
@@ -427,6 +431,8 @@ int flipgpu_sync(FlipGpu *h) {
 int flipgpu_set_step(FlipGpu *h, int64_t step) {
   if (!h) return FLIPGPU_EINVAL;
   h->step = step;
+  CK(h, cudaMemcpyAsync(h->dstep, &h->step, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
   return FLIPGPU_OK;
 }
 
@@ -785,9 +791,15 @@ int flipgpu_correct(FlipGpu *h) {
   return FLIPGPU_OK;
 }
 
-int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
-  if (!h) return FLIPGPU_EINVAL;
+static __global__ void k_step_inc(int64_t *dstep) { *dstep += 1; }
+
+/* simulateStep (src/flip3D.cpp:1194-1264) minus the preview, pouring and
+ * file output. With async_mode set nothing in it waits for the device, so it
+ * can be recorded into a CUDA graph. */
+static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
   h->step++;
+  k_step_inc<<<1, 1, 0, h->stream>>>(h->dstep);
+  FG_LAUNCHED(h, 1);
   StageClock clk(h);
   /* sort + add_ExtForce fused into the payload, then computeDensity */
   clk.mark(FLIPGPU_STAGE_SORT);
@@ -808,6 +820,131 @@ int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
   clk.mark(FLIPGPU_NSTAGES);
   clk.flush();
   h->cells_valid = false;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  return step_body(h, st);
+}
+
+static int async_ok(FlipGpu *h) {
+  if (h->prm.solve_mode != FLIPGPU_SOLVE_FAST)
+    return fail(h, FLIPGPU_EINVAL, "asynchronous steps need the FAST solver");
+  if (h->warm) return fail(h, FLIPGPU_EINVAL, "asynchronous steps run without a warm start");
+  if (h->prof_on) return fail(h, FLIPGPU_EINVAL, "asynchronous steps run without profiling");
+  return FLIPGPU_OK;
+}
+
+int flipgpu_step_async(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r = async_ok(h);
+  if (r != FLIPGPU_OK) return r;
+  h->async_mode = 1;
+  r = step_body(h, nullptr);
+  h->async_mode = 0;
+  return r;
+}
+
+int flipgpu_capture_step(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r = async_ok(h);
+  if (r != FLIPGPU_OK) return r;
+  if (h->graph_exec) {
+    cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+  }
+  if (h->graph) {
+    cudaGraphDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  const int64_t step0 = h->step, launches0 = h->launches;
+  CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeRelaxed));
+  h->async_mode = 1;
+  r = step_body(h, nullptr);
+  h->async_mode = 0;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  h->step = step0; /* recording ran nothing */
+  h->graph_launches = h->launches - launches0;
+  h->launches = launches0;
+  if (r != FLIPGPU_OK) {
+    if (g) cudaGraphDestroy(g);
+    return r;
+  }
+  if (e != cudaSuccess) return fail(h, FLIPGPU_ECUDA, "capture_step: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return fail(h, FLIPGPU_ECUDA, "capture_step: instantiate: %s", cudaGetErrorString(e));
+  }
+  h->graph = g;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_step_graph(FlipGpu *h) {
+  if (!h) return FLIPGPU_EINVAL;
+  if (!h->graph_exec) return fail(h, FLIPGPU_EINVAL, "step_graph: no captured step");
+  h->step++;
+  h->launches += h->graph_launches;
+  CK(h, cudaGraphLaunch(h->graph_exec, h->stream));
+  h->cells_valid = false;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_last_solve_stats(FlipGpu *h, FlipGpuSolveStats *st) {
+  if (!h || !st) return FLIPGPU_EINVAL;
+  return read_solve_stats(h, st);
+}
+
+/* ----------------------------------------------------------------- batches */
+
+struct FlipBatch {
+  std::vector<FlipGpu *> sims;
+  bool graphs = false;
+};
+
+int flipbatch_create(FlipBatch **out) {
+  if (!out) return FLIPGPU_EINVAL;
+  *out = new (std::nothrow) FlipBatch();
+  return *out ? FLIPGPU_OK : FLIPGPU_ENOMEM;
+}
+
+int flipbatch_destroy(FlipBatch *b) {
+  if (!b) return FLIPGPU_EINVAL;
+  delete b;
+  return FLIPGPU_OK;
+}
+
+int flipbatch_add(FlipBatch *b, FlipGpu *h) {
+  if (!b || !h) return FLIPGPU_EINVAL;
+  b->sims.push_back(h);
+  return FLIPGPU_OK;
+}
+
+int flipbatch_capture(FlipBatch *b) {
+  if (!b) return FLIPGPU_EINVAL;
+  for (FlipGpu *h : b->sims) {
+    int r = flipgpu_capture_step(h);
+    if (r != FLIPGPU_OK) return r;
+  }
+  b->graphs = true;
+  return FLIPGPU_OK;
+}
+
+int flipbatch_step(FlipBatch *b) {
+  if (!b) return FLIPGPU_EINVAL;
+  for (FlipGpu *h : b->sims) {
+    int r = b->graphs ? flipgpu_step_graph(h) : flipgpu_step_async(h);
+    if (r != FLIPGPU_OK) return r;
+  }
+  return FLIPGPU_OK;
+}
+
+int flipbatch_sync(FlipBatch *b) {
+  if (!b) return FLIPGPU_EINVAL;
+  for (FlipGpu *h : b->sims) CK(h, cudaStreamSynchronize(h->stream));
   return FLIPGPU_OK;
 }
 

@@ -60,6 +60,7 @@ struct SimConst {
   float l0h, l0l;
   uint64_t seed;
   int64_t step;
+  const int64_t *dstep; /* the step counter in device memory (graph replays advance it) */
 };
 
 struct FlipGpu {
@@ -73,6 +74,11 @@ struct FlipGpu {
   cudaStream_t own_stream;
   float max_dens;
   int64_t step;
+  int64_t *dstep;     /* device copy of step, advanced by a kernel each step */
+  int async_mode;     /* the step being recorded or run needs no host sync */
+  cudaGraph_t graph;
+  cudaGraphExec_t graph_exec;
+  int64_t graph_launches; /* kernels in the captured step */
   int64_t launches;
   char err[512];
 
@@ -194,6 +200,9 @@ cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *
 cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, float *vel,
                                    float re);
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
+/* stats of the last solve read from the device (for steps run without a
+ * host sync) */
+int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
 int particles_init_device();
 

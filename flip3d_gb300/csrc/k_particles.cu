@@ -336,7 +336,7 @@ __global__ void k_shuffle_draws(SimConst c, const int *__restrict__ counts,
   const int m = counts[IF_NSTUCK], w = counts[IF_NWATER];
   if (w == 0) return;
   for (int q = 1 + blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
-    uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_SHUFFLE, (uint64_t)c.step, 0),
+    uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_SHUFFLE, (uint64_t)*c.dstep, 0),
                              (uint64_t)q, 0);
     uint32_t j = r % (uint32_t)(q + 1);
     draw[q] = j;
@@ -437,7 +437,7 @@ __global__ void k_repo_place(SimConst c, const int *__restrict__ counts,
     int cc[3] = {(int)(cell / ((uint32_t)n * n)), (int)((cell / n) % n), (int)(cell % n)};
     float out[3];
     for (int d = 0; d < 3; d++) {
-      uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_PLACE, (uint64_t)c.step, 0),
+      uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_PLACE, (uint64_t)*c.dstep, 0),
                                (uint64_t)(3 * q + d), 0);
       double frac = 0.5 * (double)(int)(r % 101) / 100;
       out[d] = (float)(h * ((double)cc[d] + 0.25 + frac));
@@ -680,7 +680,7 @@ k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict
       } else if (unpack_type(Q.w) == CELL_FLUID) {
         uint32_t o = perm[b];
         for (int q = 0; q < 3; q++) {
-          uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)c.step, q),
+          uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)*c.dstep, q),
                                    (uint64_t)p, (uint64_t)o);
           spring[q] = kick_add(spring[q], c.kick_fluid, (int)(r % 101));
         }

@@ -1815,6 +1815,24 @@ __global__ void k_true_r2_sum(int nb, const double *__restrict__ part, double *_
   scal[SC_TRUE2] = s;
 }
 
+int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st) {
+  double sc[SC_COUNT];
+  int fl[IF_COUNT];
+  cudaMemcpyAsync(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost, h->stream);
+  cudaMemcpyAsync(fl, h->iflags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return FLIPGPU_ECUDA;
+  *st = FlipGpuSolveStats();
+  st->iterations = fl[IF_ITERS];
+  st->status = fl[IF_TIMEOUT] ? FLIPGPU_ETIMEOUT
+               : fl[IF_NAN]   ? FLIPGPU_ENAN
+               : fl[IF_DONE] == 3 ? FLIPGPU_ENOCONV
+                                  : FLIPGPU_OK;
+  st->r2 = sc[SC_ERR2];
+  st->b2 = sc[SC_B2];
+  st->r2_true = sc[SC_TRUE2];
+  return FLIPGPU_OK;
+}
+
 static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   double sc[SC_COUNT];
   int host_flags[IF_COUNT];
@@ -1879,7 +1897,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
                                  h->prm.eps_abs, h->prm.rel_tol, ref_eps, max_iters);
     FG_LAUNCHED(h, 1);
   };
-  cudaEventRecord(h->ev0, S);
+  if (!h->async_mode) cudaEventRecord(h->ev0, S);
   cudaMemsetAsync(h->iflags, 0, IF_COUNT * sizeof(int), S);
   /* setup: flip b, preconditioner / diagonal */
   k_setup<<<G, BLK, 0, S>>>(sa, mode, h->A, h->L, h->div,
@@ -1969,6 +1987,14 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       kern = (const void *)k_cg_cg1;
       grid = h->cg_grid[2];
     }
+    /* no more blocks than the grid has work for (about two quads or eight
+     * cells per thread): small grids keep short barriers and leave the rest
+     * of the GPU to other simulations */
+    if (precond != FLIPGPU_PRECOND_IC) {
+      const size_t per_block = (size_t)CG_BLOCK * 8;
+      const size_t want = (nc + per_block - 1) / per_block;
+      if (want < (size_t)grid) grid = want > 0 ? (int)want : 1;
+    }
     if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_IC) {
       kern = (const void *)k_cg_ic;
       grid = h->cg_grid[3];
@@ -2003,6 +2029,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
         k_true_r2_sum<<<1, 32, 0, S>>>(RED_BLOCKS, h->partial, h->scal);
         FG_LAUNCHED(h, 2);
       }
+      if (h->async_mode) break; /* stats stay on the device (read_solve_stats) */
       cudaEventRecord(h->ev1, S);
       FlipGpuSolveStats one;
       rc = finish_stats(h, &one, mode);

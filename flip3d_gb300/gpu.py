@@ -85,6 +85,16 @@ SIGNATURES = {
                                              C.c_void_p, C.c_void_p]),
     "flipgpu_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
     "flipgpu_fetch_velocity": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_step_async": (C.c_int, [C.c_void_p]),
+    "flipgpu_capture_step": (C.c_int, [C.c_void_p]),
+    "flipgpu_step_graph": (C.c_int, [C.c_void_p]),
+    "flipgpu_last_solve_stats": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipbatch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "flipbatch_destroy": (C.c_int, [C.c_void_p]),
+    "flipbatch_add": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipbatch_capture": (C.c_int, [C.c_void_p]),
+    "flipbatch_step": (C.c_int, [C.c_void_p]),
+    "flipbatch_sync": (C.c_int, [C.c_void_p]),
     "flipunet_param_count": (C.c_int64, []),
     "flipunet_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     "flipunet_destroy": (C.c_int, [C.c_void_p]),
@@ -321,6 +331,22 @@ class Simulation:
         self._ck(self.lib.flipgpu_set_params(self.h, C.byref(params)), "set_params")
         self.params = params
 
+    def step_async(self):
+        """One step with no host synchronisation (FAST solver)."""
+        self._ck(self.lib.flipgpu_step_async(self.h), "step_async")
+
+    def capture_step(self):
+        """Record one step as a CUDA graph; step_graph replays it."""
+        self._ck(self.lib.flipgpu_capture_step(self.h), "capture_step")
+
+    def step_graph(self):
+        self._ck(self.lib.flipgpu_step_graph(self.h), "step_graph")
+
+    def last_solve_stats(self):
+        st = SolveStats()
+        self._ck(self.lib.flipgpu_last_solve_stats(self.h, C.byref(st)), "last_solve_stats")
+        return st
+
     def set_warm_start(self, net):
         """Attach a UNet (or None) to this simulation's FAST-mode solves."""
         self._warm = net
@@ -450,3 +476,43 @@ class UNet:
                                               *[C.c_void_p(a) for a in (A, b, x0, r0, x)],
                                               C.c_float(lr), C.byref(loss)), "train_step")
         return loss.value
+
+
+class Batch:
+    """Independent simulations advanced together (flipbatch_*): every
+    member's step runs on its own stream without host waits, optionally
+    replayed from CUDA graphs."""
+
+    def __init__(self, sims=()):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.flipbatch_create(C.byref(h))
+        if rc != OK:
+            raise FlipGpuError(f"flipbatch_create failed ({rc})")
+        self.h = h
+        self.sims = []
+        for s in sims:
+            self.add(s)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.flipbatch_destroy(self.h)
+            self.h = None
+
+    def _ck(self, rc, what):
+        if rc != OK:
+            errs = [s.lib.flipgpu_last_error(s.h).decode() for s in self.sims]
+            raise FlipGpuError(f"{what} failed ({rc}): {[e for e in errs if e][:3]}")
+
+    def add(self, sim):
+        self._ck(self.lib.flipbatch_add(self.h, sim.h), "add")
+        self.sims.append(sim)
+
+    def capture(self):
+        self._ck(self.lib.flipbatch_capture(self.h), "capture")
+
+    def step(self):
+        self._ck(self.lib.flipbatch_step(self.h), "step")
+
+    def sync(self):
+        self._ck(self.lib.flipbatch_sync(self.h), "sync")

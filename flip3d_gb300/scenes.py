@@ -226,6 +226,24 @@ def random_scene(n: int, seed: int) -> Scene:
     return build(n, objs, seed, name=f"random_n{n}_s{seed}")
 
 
+BATCH_SIZES = (24, 32, 48, 64, 96)
+
+
+def batch_scene(seed: int) -> Scene:
+    """One scene of the batched workload: N uniform from {24,32,48,64,96},
+    pool depth U(0.1, 0.4), a sphere of radius U(0.08, 0.2) above it (falling
+    from rest)."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.choice(BATCH_SIZES))
+    wall = 1.0 / n
+    depth = float(rng.uniform(0.1, 0.4))
+    r = float(rng.uniform(0.08, 0.2))
+    cx, cz = (float(v) for v in rng.uniform(0.2 + r / 2, 0.8 - r / 2, size=2))
+    cy = float(min(1.0 - wall - r - 0.02, depth + r + rng.uniform(0.05, 0.3)))
+    return build(n, [Box((wall, wall, wall), (1 - wall, depth, 1 - wall)),
+                     Sphere((cx, cy, cz), r)], seed, name=f"batch_s{seed}_n{n}")
+
+
 def calibration_lattice(n: int, density: float = 0.5) -> np.ndarray:
     """The 10^3 lattice whose peak density normalises ``dens``
     (src/flip3D.cpp:689-699)."""

@@ -254,6 +254,34 @@ int flipgpu_sort_cells_noalloc(int n, int count, const float *pos,
                                void *stream);
 
 /* ---------------------------------------------------------------------------
+ * Steps without host synchronisation, CUDA graphs and batches of scenes (no
+ * counterpart in the reference, which runs one scene per process).
+ *
+ * flipgpu_step_async is flipgpu_step with nothing waiting for the device
+ * (FAST solver only; no warm start, no profiling): the solve's statistics
+ * stay on the device until flipgpu_last_solve_stats reads them.
+ * flipgpu_capture_step records one such step as a CUDA graph (the step
+ * counter that keys the random draws lives on the device, so replays
+ * advance it) and flipgpu_step_graph replays it. */
+int flipgpu_step_async(FlipGpu *h);
+int flipgpu_capture_step(FlipGpu *h);
+int flipgpu_step_graph(FlipGpu *h);
+int flipgpu_last_solve_stats(FlipGpu *h, FlipGpuSolveStats *stats);
+
+/* A batch advances independent simulations together: each handle keeps its
+ * own stream, so the steps of different scenes overlap on the GPU and the
+ * host does not wait between them. The batch does not own the handles. */
+typedef struct FlipBatch FlipBatch;
+int flipbatch_create(FlipBatch **out);
+int flipbatch_destroy(FlipBatch *b);
+int flipbatch_add(FlipBatch *b, FlipGpu *h);
+/* record every member's step as a graph; later flipbatch_step calls replay */
+int flipbatch_capture(FlipBatch *b);
+/* one step of every member (graphs if captured, else asynchronous steps) */
+int flipbatch_step(FlipBatch *b);
+int flipbatch_sync(FlipBatch *b);
+
+/* ---------------------------------------------------------------------------
  * Learned warm start (no counterpart in the reference; the reference starts
  * CG from the previous step's pressure, src/flip3D.cpp:679 and
  * src/solver.cpp:224).

@@ -9,7 +9,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "flipgpu.h")).read()
-    return sorted(set(re.findall(r"\b(flip(?:gpu|unet)_[a-z0-9_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(flip(?:gpu|unet|batch)_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_declares_the_entry_points():
