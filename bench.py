@@ -319,6 +319,8 @@ def main():
                     help="dam_break (column x<0.4, y<0.8) or sphere_into_pool (pool 0.25, "
                          "sphere r 0.15 falling at 2 m/s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solver-comparison", action="store_true",
+                    help="skip the plain/MIC/learned solver comparison (profiling runs)")
     ap.add_argument("--batch-scenes", type=int, default=0,
                     help="run the batched workload instead: this many independent scenes "
                          "with N uniform from {24,32,48,64,96}, stepped together (captured "
@@ -430,7 +432,7 @@ def main():
     e2e = total_particles * args.steps / e2e_s
 
     # the metric's solver comparison on systems of this run (not in `value`)
-    solve_cmp = solver_comparison(gpu, sim, prm, args.n)
+    solve_cmp = None if args.no_solver_comparison else solver_comparison(gpu, sim, prm, args.n)
 
     # mesher::generateMesh on the last step's lists (device only, not in `value`)
     sim.mesh_counts()

@@ -1808,11 +1808,16 @@ __global__ void __launch_bounds__(BLK) k_true_r2(SolveArgs s, const uint8_t *__r
   if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-__global__ void k_true_r2_sum(int nb, const double *__restrict__ part, double *__restrict__ scal) {
-  if (threadIdx.x || blockIdx.x) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; b++) s += part[b];
-  scal[SC_TRUE2] = s;
+/* one block of RED_BLOCKS threads: a fixed tree over the block partials */
+__global__ void k_true_r2_sum(const double *__restrict__ part, double *__restrict__ scal) {
+  __shared__ double sh[RED_BLOCKS];
+  sh[threadIdx.x] = part[threadIdx.x];
+  __syncthreads();
+  for (int w = RED_BLOCKS / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) scal[SC_TRUE2] = sh[0];
 }
 
 int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st) {
@@ -2026,7 +2031,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       }
       if (mode == FLIPGPU_SOLVE_FAST) {
         k_true_r2<<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press, h->partial);
-        k_true_r2_sum<<<1, 32, 0, S>>>(RED_BLOCKS, h->partial, h->scal);
+        k_true_r2_sum<<<1, RED_BLOCKS, 0, S>>>(h->partial, h->scal);
         FG_LAUNCHED(h, 2);
       }
       if (h->async_mode) break; /* stats stay on the device (read_solve_stats) */

@@ -321,14 +321,20 @@ __global__ void k_sample_sums(size_t n3, const uint8_t *__restrict__ A, const fl
  * scale[4s + 0..3] = {s_b, s_r, s_x, s_t} */
 __global__ void k_sample_scale(int batch, int n, const double *__restrict__ part,
                                float *__restrict__ scale, double *__restrict__ count) {
-  const int s = threadIdx.x;
-  if (s >= batch) return;
-  double t[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int k = 0; k < RB; k++)
-    for (int q = 0; q < 4; q++) t[q] += part[4 * (s * RB + k) + q];
-  const double c = t[3];
+  /* block s: a fixed tree over the RB block partials of sample s */
+  __shared__ double sh[RB][4];
+  const int s = blockIdx.x;
+  for (int q = 0; q < 4; q++) sh[threadIdx.x][q] = part[4 * (s * RB + threadIdx.x) + q];
+  __syncthreads();
+  for (int w = RB / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 4; q++) sh[threadIdx.x][q] += sh[threadIdx.x + w][q];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double c = sh[0][3];
   double rms[3];
-  for (int q = 0; q < 3; q++) rms[q] = (c > 0.0 && t[q] > 0.0) ? sqrt(t[q] / c) : 1.0;
+  for (int q = 0; q < 3; q++) rms[q] = (c > 0.0 && sh[0][q] > 0.0) ? sqrt(sh[0][q] / c) : 1.0;
   scale[4 * s + 0] = (float)rms[0];
   scale[4 * s + 1] = (float)rms[1];
   scale[4 * s + 2] = (float)rms[2];
@@ -846,7 +852,7 @@ int prepare_inputs(FlipUNet *u, int n, int batch, const uint8_t *A, const float 
                    const float *x0, const float *r0) {
   const size_t n3 = (size_t)n * n * n;
   k_sample_sums<<<dim3(RB, batch), EBLK, 0, u->stream>>>(n3, A, b, r0, x0, u->red);
-  k_sample_scale<<<1, 64, 0, u->stream>>>(batch, n, u->red, u->scale, u->count);
+  k_sample_scale<<<batch, RB, 0, u->stream>>>(batch, n, u->red, u->scale, u->count);
   k_features<<<(unsigned)((n3 * batch + EBLK - 1) / EBLK), EBLK, 0, u->stream>>>(
       n3, batch, A, b, r0, x0, u->scale, u->X0);
   UCK(cudaGetLastError());
