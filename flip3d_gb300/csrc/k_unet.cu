@@ -184,6 +184,192 @@ __global__ void __launch_bounds__(CTHREADS, 1)
     }
 }
 
+/* ------------------------------------------------ tcgen05 convolution */
+
+/* The same convolution for grids whose k-lines are multiples of 128 cells,
+ * on the 5th-generation tensor cores: one CTA of 4 warps computes 128
+ * consecutive cells of a k-line (M = 128) for all Cout (N = Cout) with the
+ * FP32 accumulator in tensor memory. Operands sit in shared memory in the
+ * K-major, unswizzled core-matrix layout (8 rows x 16 bytes):
+ *   A: the 3x3 input k-lines around the output line (130 cells with the
+ *      k halo), one 16-byte plane per 8 channels, cells 16 bytes apart, so
+ *      the operand of tap (dz, dy, dx) and 16-channel chunk c is a descriptor
+ *      starting at cell dx of line (dz, dy) (SBO 128 B between 8-cell groups,
+ *      LBO = one plane between the two 8-channel halves);
+ *   B: all 27 x Cin x Cout weights, loaded once per CTA (persistent CTAs
+ *      loop over lines).
+ * One thread issues the 27 x Cin/16 MMAs (K = 16 each) and commits them to
+ * an mbarrier; every wait is bounded (an expired wait sets *err and the CTA
+ * stops after freeing its tensor memory). */
+constexpr int TC_M = 128;
+constexpr int TC_ROWS = TC_M + 2;              /* cells per staged line */
+constexpr int TC_PLANE = TC_ROWS * 16;         /* bytes per 8-channel plane */
+constexpr int TC_THREADS = 128;
+constexpr unsigned TC_SPIN = 1u << 22;
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+  for (unsigned spin = 0; spin < TC_SPIN; spin++) {
+    uint32_t done;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                 "selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(addr), "r"(parity)
+                 : "memory");
+    if (done) return true;
+    if (spin > 32) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
+               "%12,%13,%14,%15}, [%16];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                 "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                 "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
+}
+
+/* operands + mbarrier/TMEM slot, plus a margin that keeps every operand
+ * descriptor's reach inside the allocation whatever its strides */
+size_t tc_smem(int cin, int cout) {
+  return (size_t)9 * (cin / 8) * TC_PLANE + (size_t)27 * cin * cout * 2 + 64 + 40960;
+}
+constexpr int TC_SMEM_MAX = 220 * 1024;
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_conv3_tc(int n, int cin, int cout, int batch, const bf16 *__restrict__ X,
+               const uint4 *__restrict__ Wtc, const float *__restrict__ bias,
+               bf16 *__restrict__ Y, int relu, int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  const int q8 = cin / 8;
+  unsigned char *halo = smraw;
+  unsigned char *wsm = smraw + (size_t)9 * q8 * TC_PLANE;
+  const size_t wbytes = (size_t)27 * cin * cout * 2;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(wsm + wbytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(wsm + wbytes + 8);
+  int *fail = reinterpret_cast<int *>(wsm + wbytes + 16);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = cout <= 32 ? 32u : 64u;
+  /* weights, once */
+  for (size_t o = threadIdx.x; o < wbytes / 16; o += TC_THREADS)
+    reinterpret_cast<uint4 *>(wsm)[o] = Wtc[o];
+  if (threadIdx.x == 0) {
+    *fail = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)));
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tslot;
+  const size_t n3 = (size_t)n * n * n;
+  const int segs = n / TC_M;
+  const size_t items = (size_t)batch * n * n * segs;
+  /* instruction descriptor: D f32, A/B bf16, both K-major, N = cout, M = 128 */
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(cout >> 3) << 17) |
+                         ((uint32_t)(TC_M >> 4) << 24);
+  const uint32_t halo_s = smem_u32(halo), w_s = smem_u32(wsm);
+  uint32_t parity = 0;
+  for (size_t item = blockIdx.x; item < items; item += gridDim.x) {
+    const int seg = (int)(item % segs);
+    const int j = (int)((item / segs) % n), i = (int)((item / segs / n) % n);
+    const size_t s = item / ((size_t)segs * n * n);
+    const int k0 = seg * TC_M;
+    __syncthreads(); /* the previous line's accumulator has been read */
+    /* stage the 3x3 lines with the k halo, plane layout */
+    for (int idx = threadIdx.x; idx < 9 * TC_ROWS * q8; idx += TC_THREADS) {
+      const int kc = idx % q8, row = (idx / q8) % TC_ROWS, L = idx / (q8 * TC_ROWS);
+      const int gi = i + L / 3 - 1, gj = j + L % 3 - 1, gk = k0 + row - 1;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (gi >= 0 && gi < n && gj >= 0 && gj < n && gk >= 0 && gk < n)
+        v = *reinterpret_cast<const uint4 *>(X + (s * n3 + ((size_t)gi * n + gj) * n + gk) * cin +
+                                             kc * 8);
+      *reinterpret_cast<uint4 *>(halo + ((size_t)(L * q8 + kc) * TC_ROWS + row) * 16) = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const int nch = cin / 16;
+      uint32_t acc = 0;
+      for (int tap = 0; tap < 27; tap++) {
+        const int L = tap / 3, dx = tap % 3; /* tap = (dz*3 + dy)*3 + dx, line L = dz*3 + dy */
+        for (int c = 0; c < nch; c++) {
+          const uint64_t ad = umma_desc(halo_s + ((uint32_t)(L * q8 + 2 * c) * TC_ROWS + dx) * 16,
+                                        TC_PLANE, 128);
+          const uint64_t bd =
+              umma_desc(w_s + (uint32_t)(tap * nch + c) * (uint32_t)cout * 32u,
+                        (uint32_t)(cout / 8) * 128u, 128);
+          asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                       "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          acc = 1;
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::
+                       "r"(smem_u32(mbar)));
+    }
+    const bool ok = mbar_wait(smem_u32(mbar), parity);
+    parity ^= 1u;
+    if (!ok) atomicExch(fail, 1);
+    __syncthreads();
+    if (*(volatile int *)fail) break;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    /* epilogue: warp w holds cells 32w..32w+31 of the line */
+    const int m = warp * 32 + lane;
+    bf16 *yrow = Y + (s * n3 + ((size_t)i * n + j) * n + k0 + m) * cout;
+    for (int c0 = 0; c0 < cout; c0 += 16) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+      __align__(16) bf16 o[16];
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        float t = v[q] + (bias ? bias[c0 + q] : 0.0f);
+        if (relu) t = fmaxf(t, 0.0f);
+        o[q] = __float2bfloat16(t);
+      }
+      reinterpret_cast<uint4 *>(yrow + c0)[0] = reinterpret_cast<uint4 *>(o)[0];
+      reinterpret_cast<uint4 *>(yrow + c0)[1] = reinterpret_cast<uint4 *>(o)[1];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  }
+  __syncthreads();
+  if (*(volatile int *)fail && threadIdx.x == 0) atomicExch(err, 1);
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols));
+  }
+}
+
+/* W[tap][ci][co] (FP32) into the B operand layout of k_conv3_tc: for k-step
+ * (tap, 16-channel chunk c) a block of cout*32 bytes holding two K-halves of
+ * cout/8 core matrices (8 output channels x 8 input channels, rows 16 B). */
+__global__ void k_pack_tc(int cin, int cout, const float *__restrict__ W, bf16 *__restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= 27 * cin * cout) return;
+  const int co = idx % cout, ci = (idx / cout) % cin, tap = idx / (cout * cin);
+  const int c = ci / 16, kk = ci % 16, h = kk / 8, col = kk % 8, g = co / 8, r = co % 8;
+  const size_t byte = ((size_t)(tap * (cin / 16) + c) * cout * 32) +
+                      (size_t)(h * (cout / 8) + g) * 128 + r * 16 + col * 2;
+  out[byte / 2] = __float2bfloat16(W[idx]);
+}
+
 /* Weight gradient of one tap over one chunk of cells:
  * part[chunk][tap][ci][co] = sum_{v in chunk} X[v + off(tap)][ci] dZ[v][co],
  * and for the centre tap the bias gradient part_b[chunk][co] = sum dZ[v][co].
@@ -703,6 +889,9 @@ struct FlipUNet {
   int64_t woff[NCONV], boff[NCONV], hoff = 0; /* offsets in the parameter vector */
   float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
   uint2 *ffrag[NCONV] = {}, *bfrag[NCONV] = {};
+  bf16 *tcw[NCONV] = {};  /* weights in the tcgen05 B-operand layout */
+  int tc = 0;             /* forward convolutions on tcgen05 where they fit */
+  int *tc_err = nullptr;
   int64_t adam_t = 0;
   bool frags_fresh = false;
   /* workspace */
@@ -752,7 +941,8 @@ int unet_init_device() {
   if (cudaFuncSetAttribute(k_conv3<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
       cudaFuncSetAttribute(k_conv3<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
       cudaFuncSetAttribute(k_conv3<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
-      cudaFuncSetAttribute(k_conv3<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big))
+      cudaFuncSetAttribute(k_conv3<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
+      cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX))
     return -1;
   done[dev] = true;
   return 0;
@@ -772,6 +962,32 @@ cudaError_t conv(FlipUNet *u, int n, int batch, int cin, int cout, const bf16 *X
   default: k_conv3<16><<<grid, CTHREADS, smem, u->stream>>>(n, cin, cout, X, frag, bias, Y, relu); break;
   }
   return cudaGetLastError();
+}
+
+bool tc_fits(int n, int cin, int cout) {
+  return n % TC_M == 0 && cin % 16 == 0 && cout % 16 == 0 && cout <= 64 &&
+         tc_smem(cin, cout) <= (size_t)TC_SMEM_MAX;
+}
+
+cudaError_t conv_tc(FlipUNet *u, int n, int batch, int cin, int cout, const bf16 *X,
+                    const bf16 *Wtc, const float *bias, bf16 *Y, int relu) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t items = (size_t)batch * n * n * (n / TC_M);
+  const unsigned grid = (unsigned)(items < (size_t)sms ? items : (size_t)sms);
+  k_conv3_tc<<<grid, TC_THREADS, tc_smem(cin, cout), u->stream>>>(
+      n, cin, cout, batch, X, reinterpret_cast<const uint4 *>(Wtc), bias, Y, relu, u->tc_err);
+  return cudaGetLastError();
+}
+
+/* forward convolution l: tcgen05 where it fits, mma.sync otherwise */
+cudaError_t conv_fwd(FlipUNet *u, int l, int n, int batch, const bf16 *X, bf16 *Y) {
+  const int cin = kConv[l].cin, cout = kConv[l].cout;
+  const float *bias = u->P + u->boff[l];
+  if (u->tc && tc_fits(n, cin, cout))
+    return conv_tc(u, n, batch, cin, cout, X, u->tcw[l], bias, Y, 1);
+  return conv(u, n, batch, cin, cout, X, u->ffrag[l], bias, Y, 1);
 }
 
 int lvl_n(int n, int level) { return n >> level; }
@@ -841,6 +1057,9 @@ int refresh_frags(FlipUNet *u) {
     const int nf = 27 * (cin / 16) * (cout / 8) * 32, nb = 27 * (cout / 16) * (cin / 8) * 32;
     k_pack<<<(nf + nb + EBLK - 1) / EBLK, EBLK, 0, u->stream>>>(cin, cout, u->P + u->woff[l],
                                                                u->ffrag[l], u->bfrag[l]);
+    if (u->tcw[l])
+      k_pack_tc<<<(27 * cin * cout + EBLK - 1) / EBLK, EBLK, 0, u->stream>>>(
+          cin, cout, u->P + u->woff[l], u->tcw[l]);
   }
   UCK(cudaGetLastError());
   u->frags_fresh = true;
@@ -863,30 +1082,28 @@ unsigned eg(size_t count) { return (unsigned)((count + EBLK - 1) / EBLK); }
 
 int forward(FlipUNet *u, int n, int batch) {
   const int B = batch;
-  auto W = [&](int l) { return u->ffrag[l]; };
-  auto b = [&](int l) { return u->P + u->boff[l]; };
   const int n1 = n / 2, n2 = n / 4, n3l = n / 8;
   const size_t V0 = (size_t)n * n * n, V1 = V0 / 8, V2 = V1 / 8, V3 = V2 / 8;
-  UCK(conv(u, n, B, 16, 16, u->X0, W(0), b(0), u->A0, 1));
-  UCK(conv(u, n, B, 16, 16, u->A0, W(1), b(1), u->E0, 1));
+  UCK(conv_fwd(u, 0, n, B, u->X0, u->A0));
+  UCK(conv_fwd(u, 1, n, B, u->A0, u->E0));
   k_pool<<<eg(V1 * B * 8), EBLK, 0, u->stream>>>(n1, 16, B, u->E0, u->P1);
-  UCK(conv(u, n1, B, 16, 32, u->P1, W(2), b(2), u->A1, 1));
-  UCK(conv(u, n1, B, 32, 32, u->A1, W(3), b(3), u->E1, 1));
+  UCK(conv_fwd(u, 2, n1, B, u->P1, u->A1));
+  UCK(conv_fwd(u, 3, n1, B, u->A1, u->E1));
   k_pool<<<eg(V2 * B * 16), EBLK, 0, u->stream>>>(n2, 32, B, u->E1, u->P2);
-  UCK(conv(u, n2, B, 32, 48, u->P2, W(4), b(4), u->A2, 1));
-  UCK(conv(u, n2, B, 48, 48, u->A2, W(5), b(5), u->E2, 1));
+  UCK(conv_fwd(u, 4, n2, B, u->P2, u->A2));
+  UCK(conv_fwd(u, 5, n2, B, u->A2, u->E2));
   k_pool<<<eg(V3 * B * 24), EBLK, 0, u->stream>>>(n3l, 48, B, u->E2, u->P3);
-  UCK(conv(u, n3l, B, 48, 64, u->P3, W(6), b(6), u->A3, 1));
-  UCK(conv(u, n3l, B, 64, 64, u->A3, W(7), b(7), u->E3, 1));
+  UCK(conv_fwd(u, 6, n3l, B, u->P3, u->A3));
+  UCK(conv_fwd(u, 7, n3l, B, u->A3, u->E3));
   k_up_cat<<<eg(V2 * B * 14), EBLK, 0, u->stream>>>(n2, 64, 48, B, u->E3, u->E2, u->U2);
-  UCK(conv(u, n2, B, 112, 48, u->U2, W(8), b(8), u->B2, 1));
-  UCK(conv(u, n2, B, 48, 48, u->B2, W(9), b(9), u->D2, 1));
+  UCK(conv_fwd(u, 8, n2, B, u->U2, u->B2));
+  UCK(conv_fwd(u, 9, n2, B, u->B2, u->D2));
   k_up_cat<<<eg(V1 * B * 10), EBLK, 0, u->stream>>>(n1, 48, 32, B, u->D2, u->E1, u->U1);
-  UCK(conv(u, n1, B, 80, 32, u->U1, W(10), b(10), u->B1, 1));
-  UCK(conv(u, n1, B, 32, 32, u->B1, W(11), b(11), u->D1, 1));
+  UCK(conv_fwd(u, 10, n1, B, u->U1, u->B1));
+  UCK(conv_fwd(u, 11, n1, B, u->B1, u->D1));
   k_up_cat<<<eg(V0 * B * 6), EBLK, 0, u->stream>>>(n, 32, 16, B, u->D1, u->E0, u->U0);
-  UCK(conv(u, n, B, 48, 16, u->U0, W(12), b(12), u->B0, 1));
-  UCK(conv(u, n, B, 16, 16, u->B0, W(13), b(13), u->D0, 1));
+  UCK(conv_fwd(u, 12, n, B, u->U0, u->B0));
+  UCK(conv_fwd(u, 13, n, B, u->B0, u->D0));
   k_head<<<eg(V0 * B), EBLK, 0, u->stream>>>(V0 * B, u->D0, u->P + u->hoff, u->O);
   UCK(cudaGetLastError());
   return FLIPGPU_OK;
@@ -1038,7 +1255,9 @@ int flipunet_destroy(FlipUNet *u) {
   for (int l = 0; l < NCONV; l++) {
     if (u->ffrag[l]) cudaFree(u->ffrag[l]);
     if (u->bfrag[l]) cudaFree(u->bfrag[l]);
+    if (u->tcw[l]) cudaFree(u->tcw[l]);
   }
+  if (u->tc_err) cudaFree(u->tc_err);
   delete u;
   return FLIPGPU_OK;
 }
@@ -1066,10 +1285,15 @@ int flipunet_create(uint64_t seed, FlipUNet **out) {
   for (int l = 0; l < NCONV; l++) {
     const size_t nf = 27 * (kConv[l].cin / 16) * (kConv[l].cout / 8) * 32;
     const size_t nb = 27 * (kConv[l].cout / 16) * (kConv[l].cin / 8) * 32;
-    if (ualloc(u->ffrag[l], nf) || ualloc(u->bfrag[l], nb)) {
+    if (ualloc(u->ffrag[l], nf) || ualloc(u->bfrag[l], nb) ||
+        ualloc(u->tcw[l], (size_t)27 * kConv[l].cin * kConv[l].cout)) {
       flipunet_destroy(u);
       return FLIPGPU_ENOMEM;
     }
+  }
+  if (ualloc(u->tc_err, 1) || cudaMemset(u->tc_err, 0, sizeof(int)) != cudaSuccess) {
+    flipunet_destroy(u);
+    return FLIPGPU_ENOMEM;
   }
   std::vector<float> p;
   init_params(u, seed, p);
@@ -1127,6 +1351,22 @@ int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const floa
   const size_t n3 = (size_t)n * n * n;
   k_delta_out<<<eg(n3 * batch), EBLK, 0, u->stream>>>(n3, batch, A, u->O, u->scale, delta);
   UCK(cudaGetLastError());
+  if (u->tc) {
+    int e = 0;
+    UCK(cudaMemcpyAsync(&e, u->tc_err, sizeof(int), cudaMemcpyDeviceToHost, u->stream));
+    UCK(cudaStreamSynchronize(u->stream));
+    if (e) {
+      snprintf(u->err, sizeof u->err, "tcgen05 convolution: a bounded wait expired");
+      return FLIPGPU_ETIMEOUT;
+    }
+  }
+  return FLIPGPU_OK;
+}
+
+int flipunet_set_tensor_path(FlipUNet *u, int tcgen05) {
+  if (!u) return FLIPGPU_EINVAL;
+  u->tc = tcgen05 ? 1 : 0;
+  u->frags_fresh = false;
   return FLIPGPU_OK;
 }
 

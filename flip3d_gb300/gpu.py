@@ -100,6 +100,7 @@ SIGNATURES = {
     "flipunet_destroy": (C.c_int, [C.c_void_p]),
     "flipunet_last_error": (C.c_char_p, [C.c_void_p]),
     "flipunet_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "flipunet_set_tensor_path": (C.c_int, [C.c_void_p, C.c_int]),
     "flipunet_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipunet_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipunet_predict": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5),
@@ -441,6 +442,10 @@ class UNet:
 
     def set_stream(self, stream_handle):
         self._ck(self.lib.flipunet_set_stream(self.h, C.c_void_p(stream_handle)), "set_stream")
+
+    def set_tensor_path(self, tcgen05: bool):
+        """Forward convolutions on tcgen05 where they fit (True) or mma.sync."""
+        self._ck(self.lib.flipunet_set_tensor_path(self.h, 1 if tcgen05 else 0), "set_tensor_path")
 
     def params(self):
         p = np.zeros(self.nparam, np.float32)

@@ -304,6 +304,10 @@ int flipunet_set_stream(FlipUNet *u, void *stream);
  * setting them resets the optimiser state. */
 int flipunet_get_params(FlipUNet *u, float *params);
 int flipunet_set_params(FlipUNet *u, const float *params);
+/* Forward convolutions on the tcgen05 tensor cores (TMEM accumulators) for
+ * the levels whose k-lines are multiples of 128 cells (1), or everywhere on
+ * the mma.sync path (0, the default). Training always uses mma.sync. */
+int flipunet_set_tensor_path(FlipUNet *u, int tcgen05);
 /* delta = the correction for systems (A, b, x0, r0), zero off the liquid. */
 int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
                      const float *x0, const float *r0, float *delta);

@@ -158,3 +158,34 @@ def test_trained_warm_start_on_heldout_scenes(gpu, torch):
     assert hist[-1] < hist[0]
     assert res["pred_rel_err"] < before["pred_rel_err"]
     assert res["learned_iters"] <= res["plain_iters"] + 1.0
+
+
+def test_tcgen05_forward_matches_mma_sync(gpu, torch):
+    """The tcgen05 (TMEM accumulator) convolutions of the 128-cell k-line
+    levels give the network output of the mma.sync path: the same BF16
+    products summed in FP32, in another order."""
+    n = 128
+    rng = np.random.default_rng(5)
+    A = torch.tensor((rng.random(n ** 3) < 0.7).astype(np.uint8), device="cuda")
+    b, x0, r0 = (torch.tensor(rng.normal(0, 1, n ** 3).astype(np.float32), device="cuda")
+                 for _ in range(3))
+    net = gpu.UNet(seed=4)
+    p = net.params()
+    from oracle import unet_oracle as U
+    _, boff, hoff, _ = U.layout()
+    for l, (cin, cout, _) in enumerate(U.CONVS):
+        p[boff[l]:boff[l] + cout] = rng.normal(0.0, 0.05, cout)
+    p[hoff:hoff + 16] = rng.normal(0.0, 0.3, 16)
+    net.set_params(p)
+    outs = []
+    for tc in (False, True):
+        net.set_tensor_path(tc)
+        d = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        net.predict(n, 1, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(), d.data_ptr())
+        torch.cuda.synchronize()
+        outs.append(d.cpu().numpy())
+    rel = np.linalg.norm(outs[1] - outs[0]) / np.linalg.norm(outs[0])
+    print("tcgen05 vs mma.sync relative difference", rel)
+    assert np.isfinite(outs[1]).all()
+    assert rel < 1e-2, rel
