@@ -16,12 +16,14 @@
  * x-major like the solver's grids); weights are FP32 masters with BF16
  * copies laid out as tensor-core fragments.
  *
- * Every 3x3x3 convolution — forward, backward-data (the same kernel on
- * flipped, transposed weights) and weight gradient — is an implicit GEMM on
- * the tensor cores (mma.sync m16n8k16 BF16 -> FP32): a block stages a
- * 4x8x8-cell output tile's input halo in shared memory and each warp
- * accumulates 32 cells x up to 64 output channels over 27 taps x Cin/16
- * chunks, loading A fragments with ldmatrix. Weight gradients reduce over
+ * Every 3x3x3 convolution is an implicit GEMM on the tensor cores. The
+ * forward convolutions run on tcgen05 with TMEM accumulators
+ * (k_conv_tc.cu). Backward-data (the same convolution on flipped, transposed
+ * weights), weight gradients and the mma.sync forward path (selectable for
+ * comparison) use mma.sync m16n8k16 BF16 -> FP32: a block stages a 4x8x8-cell
+ * output tile's input halo in shared memory and each warp accumulates 32
+ * cells x up to 64 output channels over 27 taps x Cin/16 chunks, loading A
+ * fragments with ldmatrix. Weight gradients reduce over
  * cells in fixed-size chunks whose partial sums are added in a fixed order,
  * so training is deterministic. Adam updates the FP32 masters.
  */
@@ -32,6 +34,7 @@
 #include <cstring>
 #include <vector>
 
+#include "conv_tc.h"
 #include "devcommon.cuh"
 #include "flipgpu_impl.h"
 
@@ -182,192 +185,6 @@ __global__ void __launch_bounds__(CTHREADS, 1)
         *reinterpret_cast<__nv_bfloat162 *>(yrow + co) = __floats2bfloat162_rn(v0, v1);
       }
     }
-}
-
-/* ------------------------------------------------ tcgen05 convolution */
-
-/* The same convolution for grids whose k-lines are multiples of 128 cells,
- * on the 5th-generation tensor cores: one CTA of 4 warps computes 128
- * consecutive cells of a k-line (M = 128) for all Cout (N = Cout) with the
- * FP32 accumulator in tensor memory. Operands sit in shared memory in the
- * K-major, unswizzled core-matrix layout (8 rows x 16 bytes):
- *   A: the 3x3 input k-lines around the output line (130 cells with the
- *      k halo), one 16-byte plane per 8 channels, cells 16 bytes apart, so
- *      the operand of tap (dz, dy, dx) and 16-channel chunk c is a descriptor
- *      starting at cell dx of line (dz, dy) (SBO 128 B between 8-cell groups,
- *      LBO = one plane between the two 8-channel halves);
- *   B: all 27 x Cin x Cout weights, loaded once per CTA (persistent CTAs
- *      loop over lines).
- * One thread issues the 27 x Cin/16 MMAs (K = 16 each) and commits them to
- * an mbarrier; every wait is bounded (an expired wait sets *err and the CTA
- * stops after freeing its tensor memory). */
-constexpr int TC_M = 128;
-constexpr int TC_ROWS = TC_M + 2;              /* cells per staged line */
-constexpr int TC_PLANE = TC_ROWS * 16;         /* bytes per 8-channel plane */
-constexpr int TC_THREADS = 128;
-constexpr unsigned TC_SPIN = 1u << 22;
-
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-  for (unsigned spin = 0; spin < TC_SPIN; spin++) {
-    uint32_t done;
-    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                 "selp.u32 %0, 1, 0, p;\n}\n"
-                 : "=r"(done)
-                 : "r"(addr), "r"(parity)
-                 : "memory");
-    if (done) return true;
-    if (spin > 32) __nanosleep(64);
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,"
-               "%12,%13,%14,%15}, [%16];\n"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                 "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-                 "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
-}
-
-/* operands + mbarrier/TMEM slot, plus a margin that keeps every operand
- * descriptor's reach inside the allocation whatever its strides */
-size_t tc_smem(int cin, int cout) {
-  return (size_t)9 * (cin / 8) * TC_PLANE + (size_t)27 * cin * cout * 2 + 64 + 40960;
-}
-constexpr int TC_SMEM_MAX = 220 * 1024;
-
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_conv3_tc(int n, int cin, int cout, int batch, const bf16 *__restrict__ X,
-               const uint4 *__restrict__ Wtc, const float *__restrict__ bias,
-               bf16 *__restrict__ Y, int relu, int *__restrict__ err) {
-  extern __shared__ __align__(128) unsigned char smraw[];
-  const int q8 = cin / 8;
-  unsigned char *halo = smraw;
-  unsigned char *wsm = smraw + (size_t)9 * q8 * TC_PLANE;
-  const size_t wbytes = (size_t)27 * cin * cout * 2;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(wsm + wbytes);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(wsm + wbytes + 8);
-  int *fail = reinterpret_cast<int *>(wsm + wbytes + 16);
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t ncols = cout <= 32 ? 32u : 64u;
-  /* weights, once */
-  for (size_t o = threadIdx.x; o < wbytes / 16; o += TC_THREADS)
-    reinterpret_cast<uint4 *>(wsm)[o] = Wtc[o];
-  if (threadIdx.x == 0) {
-    *fail = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar)));
-  }
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
-                     smem_u32(tslot)),
-                 "r"(ncols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
-  }
-  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = *tslot;
-  const size_t n3 = (size_t)n * n * n;
-  const int segs = n / TC_M;
-  const size_t items = (size_t)batch * n * n * segs;
-  /* instruction descriptor: D f32, A/B bf16, both K-major, N = cout, M = 128 */
-  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(cout >> 3) << 17) |
-                         ((uint32_t)(TC_M >> 4) << 24);
-  const uint32_t halo_s = smem_u32(halo), w_s = smem_u32(wsm);
-  uint32_t parity = 0;
-  for (size_t item = blockIdx.x; item < items; item += gridDim.x) {
-    const int seg = (int)(item % segs);
-    const int j = (int)((item / segs) % n), i = (int)((item / segs / n) % n);
-    const size_t s = item / ((size_t)segs * n * n);
-    const int k0 = seg * TC_M;
-    __syncthreads(); /* the previous line's accumulator has been read */
-    /* stage the 3x3 lines with the k halo, plane layout */
-    for (int idx = threadIdx.x; idx < 9 * TC_ROWS * q8; idx += TC_THREADS) {
-      const int kc = idx % q8, row = (idx / q8) % TC_ROWS, L = idx / (q8 * TC_ROWS);
-      const int gi = i + L / 3 - 1, gj = j + L % 3 - 1, gk = k0 + row - 1;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (gi >= 0 && gi < n && gj >= 0 && gj < n && gk >= 0 && gk < n)
-        v = *reinterpret_cast<const uint4 *>(X + (s * n3 + ((size_t)gi * n + gj) * n + gk) * cin +
-                                             kc * 8);
-      *reinterpret_cast<uint4 *>(halo + ((size_t)(L * q8 + kc) * TC_ROWS + row) * 16) = v;
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const int nch = cin / 16;
-      uint32_t acc = 0;
-      for (int tap = 0; tap < 27; tap++) {
-        const int L = tap / 3, dx = tap % 3; /* tap = (dz*3 + dy)*3 + dx, line L = dz*3 + dy */
-        for (int c = 0; c < nch; c++) {
-          const uint64_t ad = umma_desc(halo_s + ((uint32_t)(L * q8 + 2 * c) * TC_ROWS + dx) * 16,
-                                        TC_PLANE, 128);
-          const uint64_t bd =
-              umma_desc(w_s + (uint32_t)(tap * nch + c) * (uint32_t)cout * 32u,
-                        (uint32_t)(cout / 8) * 128u, 128);
-          asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                       "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-          acc = 1;
-        }
-      }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::
-                       "r"(smem_u32(mbar)));
-    }
-    const bool ok = mbar_wait(smem_u32(mbar), parity);
-    parity ^= 1u;
-    if (!ok) atomicExch(fail, 1);
-    __syncthreads();
-    if (*(volatile int *)fail) break;
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    /* epilogue: warp w holds cells 32w..32w+31 of the line */
-    const int m = warp * 32 + lane;
-    bf16 *yrow = Y + (s * n3 + ((size_t)i * n + j) * n + k0 + m) * cout;
-    for (int c0 = 0; c0 < cout; c0 += 16) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      __align__(16) bf16 o[16];
-#pragma unroll
-      for (int q = 0; q < 16; q++) {
-        float t = v[q] + (bias ? bias[c0 + q] : 0.0f);
-        if (relu) t = fmaxf(t, 0.0f);
-        o[q] = __float2bfloat16(t);
-      }
-      reinterpret_cast<uint4 *>(yrow + c0)[0] = reinterpret_cast<uint4 *>(o)[0];
-      reinterpret_cast<uint4 *>(yrow + c0)[1] = reinterpret_cast<uint4 *>(o)[1];
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  }
-  __syncthreads();
-  if (*(volatile int *)fail && threadIdx.x == 0) atomicExch(err, 1);
-  if (warp == 0) {
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(ncols));
-  }
-}
-
-/* W[tap][ci][co] (FP32) into the B operand layout of k_conv3_tc: for k-step
- * (tap, 16-channel chunk c) a block of cout*32 bytes holding two K-halves of
- * cout/8 core matrices (8 output channels x 8 input channels, rows 16 B). */
-__global__ void k_pack_tc(int cin, int cout, const float *__restrict__ W, bf16 *__restrict__ out) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= 27 * cin * cout) return;
-  const int co = idx % cout, ci = (idx / cout) % cin, tap = idx / (cout * cin);
-  const int c = ci / 16, kk = ci % 16, h = kk / 8, col = kk % 8, g = co / 8, r = co % 8;
-  const size_t byte = ((size_t)(tap * (cin / 16) + c) * cout * 32) +
-                      (size_t)(h * (cout / 8) + g) * 128 + r * 16 + col * 2;
-  out[byte / 2] = __float2bfloat16(W[idx]);
 }
 
 /* Weight gradient of one tap over one chunk of cells:
@@ -890,7 +707,7 @@ struct FlipUNet {
   float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
   uint2 *ffrag[NCONV] = {}, *bfrag[NCONV] = {};
   bf16 *tcw[NCONV] = {};  /* weights in the tcgen05 B-operand layout */
-  int tc = 0;             /* forward convolutions on tcgen05 where they fit */
+  int tc = 1;             /* forward convolutions on tcgen05 where they fit */
   int *tc_err = nullptr;
   int64_t adam_t = 0;
   bool frags_fresh = false;
@@ -942,7 +759,7 @@ int unet_init_device() {
       cudaFuncSetAttribute(k_conv3<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
       cudaFuncSetAttribute(k_conv3<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
       cudaFuncSetAttribute(k_conv3<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big) ||
-      cudaFuncSetAttribute(k_conv3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM_MAX))
+      conv_tc_init_device() != 0)
     return -1;
   done[dev] = true;
   return 0;
@@ -964,29 +781,12 @@ cudaError_t conv(FlipUNet *u, int n, int batch, int cin, int cout, const bf16 *X
   return cudaGetLastError();
 }
 
-bool tc_fits(int n, int cin, int cout) {
-  return n % TC_M == 0 && cin % 16 == 0 && cout % 16 == 0 && cout <= 64 &&
-         tc_smem(cin, cout) <= (size_t)TC_SMEM_MAX;
-}
-
-cudaError_t conv_tc(FlipUNet *u, int n, int batch, int cin, int cout, const bf16 *X,
-                    const bf16 *Wtc, const float *bias, bf16 *Y, int relu) {
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t items = (size_t)batch * n * n * (n / TC_M);
-  const unsigned grid = (unsigned)(items < (size_t)sms ? items : (size_t)sms);
-  k_conv3_tc<<<grid, TC_THREADS, tc_smem(cin, cout), u->stream>>>(
-      n, cin, cout, batch, X, reinterpret_cast<const uint4 *>(Wtc), bias, Y, relu, u->tc_err);
-  return cudaGetLastError();
-}
-
 /* forward convolution l: tcgen05 where it fits, mma.sync otherwise */
 cudaError_t conv_fwd(FlipUNet *u, int l, int n, int batch, const bf16 *X, bf16 *Y) {
   const int cin = kConv[l].cin, cout = kConv[l].cout;
   const float *bias = u->P + u->boff[l];
-  if (u->tc && tc_fits(n, cin, cout))
-    return conv_tc(u, n, batch, cin, cout, X, u->tcw[l], bias, Y, 1);
+  if (u->tc && conv_tc_supported(n, cin, cout))
+    return conv_tc_launch(u->stream, n, batch, cin, cout, X, u->tcw[l], bias, Y, 1, u->tc_err);
   return conv(u, n, batch, cin, cout, X, u->ffrag[l], bias, Y, 1);
 }
 
@@ -1057,9 +857,7 @@ int refresh_frags(FlipUNet *u) {
     const int nf = 27 * (cin / 16) * (cout / 8) * 32, nb = 27 * (cout / 16) * (cin / 8) * 32;
     k_pack<<<(nf + nb + EBLK - 1) / EBLK, EBLK, 0, u->stream>>>(cin, cout, u->P + u->woff[l],
                                                                u->ffrag[l], u->bfrag[l]);
-    if (u->tcw[l])
-      k_pack_tc<<<(27 * cin * cout + EBLK - 1) / EBLK, EBLK, 0, u->stream>>>(
-          cin, cout, u->P + u->woff[l], u->tcw[l]);
+    if (u->tc) UCK(conv_tc_pack(u->stream, cin, cout, u->P + u->woff[l], u->tcw[l]));
   }
   UCK(cudaGetLastError());
   u->frags_fresh = true;

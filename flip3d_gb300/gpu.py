@@ -444,7 +444,7 @@ class UNet:
         self._ck(self.lib.flipunet_set_stream(self.h, C.c_void_p(stream_handle)), "set_stream")
 
     def set_tensor_path(self, tcgen05: bool):
-        """Forward convolutions on tcgen05 where they fit (True) or mma.sync."""
+        """Forward convolutions on tcgen05 (True, the default) or mma.sync."""
         self._ck(self.lib.flipunet_set_tensor_path(self.h, 1 if tcgen05 else 0), "set_tensor_path")
 
     def params(self):

@@ -304,9 +304,9 @@ int flipunet_set_stream(FlipUNet *u, void *stream);
  * setting them resets the optimiser state. */
 int flipunet_get_params(FlipUNet *u, float *params);
 int flipunet_set_params(FlipUNet *u, const float *params);
-/* Forward convolutions on the tcgen05 tensor cores (TMEM accumulators) for
- * the levels whose k-lines are multiples of 128 cells (1), or everywhere on
- * the mma.sync path (0, the default). Training always uses mma.sync. */
+/* Forward 3x3x3 convolutions on the tcgen05 tensor cores (TMEM
+ * accumulators, 1, the default) or on the mma.sync path (0). Backward-data
+ * and weight-gradient convolutions always use mma.sync. */
 int flipunet_set_tensor_path(FlipUNet *u, int tcgen05);
 /* delta = the correction for systems (A, b, x0, r0), zero off the liquid. */
 int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,

@@ -50,13 +50,15 @@ def to_dev(torch, arrs, dtype):
     return torch.tensor(np.stack(arrs), dtype=dtype, device="cuda").contiguous()
 
 
-def test_unet_forward_and_gradients_match_cpu_oracle(gpu, torch):
+@pytest.mark.parametrize("tensor_path", ["mma.sync", "tcgen05"])
+def test_unet_forward_and_gradients_match_cpu_oracle(gpu, torch, tensor_path):
     from oracle import unet_oracle as U
     n, seeds = 16, [3, 4]
     sy = systems(gpu, n, seeds)
     A = to_dev(torch, [s[0] for s in sy], torch.uint8)
     b, x0, r0, x = (to_dev(torch, [s[k] for s in sy], torch.float32) for k in (2, 3, 4, 5))
     net = gpu.UNet(seed=5)
+    net.set_tensor_path(tensor_path == "tcgen05")
     p = net.params()
     rng = np.random.default_rng(1)
     woff, boff, hoff, total = U.layout()
@@ -160,14 +162,17 @@ def test_trained_warm_start_on_heldout_scenes(gpu, torch):
     assert res["learned_iters"] <= res["plain_iters"] + 1.0
 
 
-def test_tcgen05_forward_matches_mma_sync(gpu, torch):
-    """The tcgen05 (TMEM accumulator) convolutions of the 128-cell k-line
-    levels give the network output of the mma.sync path: the same BF16
-    products summed in FP32, in another order."""
-    n = 128
+@pytest.mark.parametrize("n,batch", [(128, 1), (32, 2)])
+def test_tcgen05_forward_matches_mma_sync(gpu, torch, n, batch):
+    """The tcgen05 convolutions (TMA-staged slabs, TMEM accumulators) give
+    the network output of the mma.sync path at every level size: 128-cell
+    segments (n=128) and runs across line ends (n <= 64, down to 4^3 at the
+    coarsest level of a 32^3 grid), one and two samples. The same BF16
+    products are summed in FP32 in another order."""
     rng = np.random.default_rng(5)
-    A = torch.tensor((rng.random(n ** 3) < 0.7).astype(np.uint8), device="cuda")
-    b, x0, r0 = (torch.tensor(rng.normal(0, 1, n ** 3).astype(np.float32), device="cuda")
+    m = batch * n ** 3
+    A = torch.tensor((rng.random(m) < 0.7).astype(np.uint8), device="cuda")
+    b, x0, r0 = (torch.tensor(rng.normal(0, 1, m).astype(np.float32), device="cuda")
                  for _ in range(3))
     net = gpu.UNet(seed=4)
     p = net.params()
@@ -180,9 +185,10 @@ def test_tcgen05_forward_matches_mma_sync(gpu, torch):
     outs = []
     for tc in (False, True):
         net.set_tensor_path(tc)
-        d = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+        d = torch.zeros(m, dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
-        net.predict(n, 1, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(), d.data_ptr())
+        net.predict(n, batch, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(),
+                    d.data_ptr())
         torch.cuda.synchronize()
         outs.append(d.cpu().numpy())
     rel = np.linalg.norm(outs[1] - outs[0]) / np.linalg.norm(outs[0])
