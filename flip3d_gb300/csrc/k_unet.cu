@@ -553,6 +553,83 @@ __global__ void k_delta_out(size_t n3, int batch, const uint8_t *__restrict__ A,
   delta[v] = A[v] == CELL_FLUID ? O[v] * scale[4 * (v / n3) + 3] : 0.0f;
 }
 
+/* Coarsened warm start: the network runs on the grid pooled c times
+ * (factor f = 2^c per axis). Training targets on that grid: per coarse
+ * cell, the liquid flag (any liquid child) and the averages of x and x0
+ * over its liquid children. */
+__global__ void k_pool_target(int nc_, int f, int batch, const uint8_t *__restrict__ A,
+                              const float *__restrict__ x, const float *__restrict__ x0,
+                              uint8_t *__restrict__ Ac, float *__restrict__ xc,
+                              float *__restrict__ x0c) {
+  const size_t nc3 = (size_t)nc_ * nc_ * nc_;
+  const size_t idx = (size_t)blockIdx.x * EBLK + threadIdx.x;
+  if (idx >= nc3 * batch) return;
+  const int n = nc_ * f;
+  const size_t s = idx / nc3, p = idx % nc3, n3 = (size_t)n * n * n;
+  const int I = (int)(p / ((size_t)nc_ * nc_)), J = (int)((p / nc_) % nc_), K = (int)(p % nc_);
+  int cnt = 0;
+  float sx = 0.0f, sx0 = 0.0f;
+  for (int a = 0; a < f; a++)
+    for (int b = 0; b < f; b++)
+      for (int c = 0; c < f; c++) {
+        const size_t v = s * n3 + ((size_t)(I * f + a) * n + (J * f + b)) * n + (K * f + c);
+        if (A[v] != CELL_FLUID) continue;
+        cnt++;
+        sx += x[v];
+        sx0 += x0[v];
+      }
+  Ac[idx] = cnt ? (uint8_t)CELL_FLUID : (uint8_t)0;
+  xc[idx] = cnt ? sx / (float)cnt : 0.0f;
+  x0c[idx] = cnt ? sx0 / (float)cnt : 0.0f;
+}
+
+/* count[s] = liquid cells of sample s (integer-valued, so the atomic
+ * double sums are exact and order-independent) */
+__global__ void k_count_fluid(size_t n3, const uint8_t *__restrict__ A, double *__restrict__ count) {
+  __shared__ int sh[EBLK];
+  const size_t s = blockIdx.y;
+  int c = 0;
+  for (size_t v = (size_t)blockIdx.x * EBLK + threadIdx.x; v < n3; v += (size_t)gridDim.x * EBLK)
+    c += A[s * n3 + v] == CELL_FLUID;
+  sh[threadIdx.x] = c;
+  __syncthreads();
+  for (int w = EBLK / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && sh[0]) atomicAdd(count + s, (double)sh[0]);
+}
+
+/* trilinear prolongation of a cell-centred field from nc^3 to (nc f)^3,
+ * clamped at the boundary */
+__global__ void k_prolong(int nc_, int f, int batch, const float *__restrict__ O,
+                          float *__restrict__ Of) {
+  const int n = nc_ * f;
+  const size_t n3 = (size_t)n * n * n, nc3 = (size_t)nc_ * nc_ * nc_;
+  const size_t idx = (size_t)blockIdx.x * EBLK + threadIdx.x;
+  if (idx >= n3 * batch) return;
+  const size_t s = idx / n3, v = idx % n3;
+  const int ii[3] = {(int)(v / ((size_t)n * n)), (int)((v / n) % n), (int)(v % n)};
+  int lo[3], hi[3];
+  float w[3];
+  for (int d = 0; d < 3; d++) {
+    const float xc = ((float)ii[d] + 0.5f) / (float)f - 0.5f;
+    const float fl = floorf(xc);
+    w[d] = xc - fl;
+    lo[d] = min(max((int)fl, 0), nc_ - 1);
+    hi[d] = min(max((int)fl + 1, 0), nc_ - 1);
+  }
+  const float *o = O + s * nc3;
+  float acc = 0.0f;
+  for (int q = 0; q < 8; q++) {
+    const int a = (q >> 2) & 1, b = (q >> 1) & 1, c = q & 1;
+    const float wt = (a ? w[0] : 1.0f - w[0]) * (b ? w[1] : 1.0f - w[1]) * (c ? w[2] : 1.0f - w[2]);
+    acc += wt * o[((size_t)(a ? hi[0] : lo[0]) * nc_ + (b ? hi[1] : lo[1])) * nc_ +
+                  (c ? hi[2] : lo[2])];
+  }
+  Of[idx] = acc;
+}
+
 /* BF16 fragments of W (fwd) and of the flipped, transposed W (bwd-data). */
 __global__ void k_pack(int cin, int cout, const float *__restrict__ W, uint2 *__restrict__ ffwd,
                        uint2 *__restrict__ fbwd) {
@@ -708,6 +785,7 @@ struct FlipUNet {
   uint2 *ffrag[NCONV] = {}, *bfrag[NCONV] = {};
   bf16 *tcw[NCONV] = {};  /* weights in the tcgen05 B-operand layout */
   int tc = 1;             /* forward convolutions on tcgen05 where they fit */
+  int coarse = 0;         /* the network runs on the grid pooled this many times */
   int *tc_err = nullptr;
   int64_t adam_t = 0;
   bool frags_fresh = false;
@@ -724,6 +802,11 @@ struct FlipUNet {
   size_t part_cap = 0, partb_cap = 0;
   double *hpart = nullptr;
   size_t hpart_cap = 0;
+  /* fine-grid buffers of the coarsened warm start */
+  int fw_n = 0, fw_b = 0;
+  bf16 *XF = nullptr, *XP = nullptr; /* fine features, one pooling step */
+  uint8_t *Ac = nullptr;
+  float *xc = nullptr, *x0c = nullptr, *Of = nullptr;
   char err[256] = {};
 };
 
@@ -865,18 +948,44 @@ int refresh_frags(FlipUNet *u) {
 }
 
 /* features and per-sample scales of a batch of systems */
-int prepare_inputs(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
-                   const float *x0, const float *r0) {
-  const size_t n3 = (size_t)n * n * n;
-  k_sample_sums<<<dim3(RB, batch), EBLK, 0, u->stream>>>(n3, A, b, r0, x0, u->red);
-  k_sample_scale<<<batch, RB, 0, u->stream>>>(batch, n, u->red, u->scale, u->count);
-  k_features<<<(unsigned)((n3 * batch + EBLK - 1) / EBLK), EBLK, 0, u->stream>>>(
-      n3, batch, A, b, r0, x0, u->scale, u->X0);
-  UCK(cudaGetLastError());
+unsigned eg(size_t count) { return (unsigned)((count + EBLK - 1) / EBLK); }
+
+/* fine-grid buffers of the coarsened warm start (grid n, network on n >> c) */
+int ensure_fine(FlipUNet *u, int n, int batch) {
+  if (!u->coarse || (u->fw_n == n && u->fw_b >= batch)) return FLIPGPU_OK;
+  const size_t B = (size_t)batch, V = (size_t)n * n * n, Vc = V >> (3 * u->coarse);
+  UCK(ualloc(u->XF, 16 * V * B));
+  UCK(ualloc(u->XP, 16 * (V / 8 + V / 64) * B));
+  UCK(ualloc(u->Ac, Vc * B));
+  UCK(ualloc(u->xc, Vc * B));
+  UCK(ualloc(u->x0c, Vc * B));
+  UCK(ualloc(u->Of, V * B));
+  u->fw_n = n;
+  u->fw_b = batch;
   return FLIPGPU_OK;
 }
 
-unsigned eg(size_t count) { return (unsigned)((count + EBLK - 1) / EBLK); }
+/* per-sample scales and the 16-channel input on the fine grid n; with
+ * coarsening c the features are average-pooled c times into X0 */
+int prepare_inputs(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
+                   const float *x0, const float *r0) {
+  const size_t n3 = (size_t)n * n * n;
+  const int c = u->coarse;
+  k_sample_sums<<<dim3(RB, batch), EBLK, 0, u->stream>>>(n3, A, b, r0, x0, u->red);
+  k_sample_scale<<<batch, RB, 0, u->stream>>>(batch, n, u->red, u->scale, u->count);
+  k_features<<<(unsigned)((n3 * batch + EBLK - 1) / EBLK), EBLK, 0, u->stream>>>(
+      n3, batch, A, b, r0, x0, u->scale, c ? u->XF : u->X0);
+  const bf16 *src = u->XF;
+  bf16 *tmp[2] = {u->XP, u->XP + 16 * (n3 / 8) * batch};
+  for (int k = 1; k <= c; k++) {
+    const int nk = n >> k;
+    bf16 *dst = k == c ? u->X0 : tmp[k - 1];
+    k_pool<<<eg((size_t)nk * nk * nk * batch * 8), EBLK, 0, u->stream>>>(nk, 16, batch, src, dst);
+    src = dst;
+  }
+  UCK(cudaGetLastError());
+  return FLIPGPU_OK;
+}
 
 int forward(FlipUNet *u, int n, int batch) {
   const int B = batch;
@@ -1047,7 +1156,7 @@ int flipunet_destroy(FlipUNet *u) {
                   u->P2, u->A2, u->E2, u->P3, u->A3, u->E3, u->U2, u->B2, u->D2, u->U1,
                   u->B1, u->D1, u->U0, u->B0, u->D0, u->G1, u->G2, u->G3, u->S0, u->S1,
                   u->S2, u->O,  u->scale, u->red, u->count, u->loss, u->part, u->part_b,
-                  u->hpart};
+                  u->hpart, u->XF, u->XP, u->Ac, u->xc, u->x0c, u->Of};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int l = 0; l < NCONV; l++) {
@@ -1131,8 +1240,10 @@ int flipunet_set_params(FlipUNet *u, const float *params) {
 }
 
 static int check_shape(FlipUNet *u, int n, int batch) {
-  if (n < 8 || n % 8 != 0 || batch < 1 || batch > 64) {
-    snprintf(u->err, sizeof u->err, "grid size must be a multiple of 8 and batch 1..64");
+  const int q = 8 << u->coarse;
+  if (n < q || n % q != 0 || batch < 1 || batch > 64) {
+    snprintf(u->err, sizeof u->err,
+             "grid size must be a multiple of %d (8 << coarsening) and batch 1..64", q);
     return FLIPGPU_EINVAL;
   }
   return FLIPGPU_OK;
@@ -1142,12 +1253,18 @@ int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const floa
                      const float *x0, const float *r0, float *delta) {
   if (!u || !A || !b || !x0 || !r0 || !delta) return FLIPGPU_EINVAL;
   int r;
-  if ((r = check_shape(u, n, batch)) || (r = ensure_workspace(u, n, batch)) ||
-      (r = refresh_frags(u)) || (r = prepare_inputs(u, n, batch, A, b, x0, r0)) ||
-      (r = forward(u, n, batch)))
+  const int nn = n >> u->coarse;
+  if ((r = check_shape(u, n, batch)) || (r = ensure_workspace(u, nn, batch)) ||
+      (r = ensure_fine(u, n, batch)) || (r = refresh_frags(u)) ||
+      (r = prepare_inputs(u, n, batch, A, b, x0, r0)) || (r = forward(u, nn, batch)))
     return r;
   const size_t n3 = (size_t)n * n * n;
-  k_delta_out<<<eg(n3 * batch), EBLK, 0, u->stream>>>(n3, batch, A, u->O, u->scale, delta);
+  const float *O = u->O;
+  if (u->coarse) {
+    k_prolong<<<eg(n3 * batch), EBLK, 0, u->stream>>>(nn, 1 << u->coarse, batch, u->O, u->Of);
+    O = u->Of;
+  }
+  k_delta_out<<<eg(n3 * batch), EBLK, 0, u->stream>>>(n3, batch, A, O, u->scale, delta);
   UCK(cudaGetLastError());
   if (u->tc) {
     int e = 0;
@@ -1161,6 +1278,15 @@ int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const floa
   return FLIPGPU_OK;
 }
 
+int flipunet_set_coarsening(FlipUNet *u, int levels) {
+  if (!u || levels < 0 || levels > 3) return FLIPGPU_EINVAL;
+  u->coarse = levels;
+  u->fw_n = 0; /* fine buffers are sized per coarsening */
+  return FLIPGPU_OK;
+}
+
+int flipunet_get_coarsening(const FlipUNet *u) { return u ? u->coarse : -1; }
+
 int flipunet_set_tensor_path(FlipUNet *u, int tcgen05) {
   if (!u) return FLIPGPU_EINVAL;
   u->tc = tcgen05 ? 1 : 0;
@@ -1171,10 +1297,24 @@ int flipunet_set_tensor_path(FlipUNet *u, int tcgen05) {
 static int grads(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
                  const float *x0, const float *r0, const float *x, double *loss) {
   int r;
-  if ((r = check_shape(u, n, batch)) || (r = ensure_workspace(u, n, batch)) ||
-      (r = refresh_frags(u)) || (r = prepare_inputs(u, n, batch, A, b, x0, r0)) ||
-      (r = forward(u, n, batch)) || (r = backward(u, n, batch, A, x, x0)))
+  const int nn = n >> u->coarse;
+  if ((r = check_shape(u, n, batch)) || (r = ensure_workspace(u, nn, batch)) ||
+      (r = ensure_fine(u, n, batch)) || (r = refresh_frags(u)) ||
+      (r = prepare_inputs(u, n, batch, A, b, x0, r0)) || (r = forward(u, nn, batch)))
     return r;
+  if (u->coarse) {
+    /* targets, liquid flags and liquid counts on the network's grid */
+    const size_t nc3 = (size_t)nn * nn * nn;
+    k_pool_target<<<eg(nc3 * batch), EBLK, 0, u->stream>>>(nn, 1 << u->coarse, batch, A, x, x0,
+                                                           u->Ac, u->xc, u->x0c);
+    UCK(cudaMemsetAsync(u->count, 0, sizeof(double) * batch, u->stream));
+    k_count_fluid<<<dim3(64, batch), EBLK, 0, u->stream>>>(nc3, u->Ac, u->count);
+    UCK(cudaGetLastError());
+    A = u->Ac;
+    x = u->xc;
+    x0 = u->x0c;
+  }
+  if ((r = backward(u, nn, batch, A, x, x0))) return r;
   if (loss) {
     UCK(cudaMemcpyAsync(loss, u->loss, sizeof(double), cudaMemcpyDeviceToHost, u->stream));
     UCK(cudaStreamSynchronize(u->stream));

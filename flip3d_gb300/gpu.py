@@ -6,6 +6,7 @@ without a GPU raises.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 
 import numpy as np
@@ -101,6 +102,8 @@ SIGNATURES = {
     "flipunet_last_error": (C.c_char_p, [C.c_void_p]),
     "flipunet_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipunet_set_tensor_path": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipunet_set_coarsening": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipunet_get_coarsening": (C.c_int, [C.c_void_p]),
     "flipunet_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipunet_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipunet_predict": (C.c_int, [C.c_void_p, C.c_int, C.c_int] + [C.c_void_p] * 5),
@@ -443,6 +446,15 @@ class UNet:
     def set_stream(self, stream_handle):
         self._ck(self.lib.flipunet_set_stream(self.h, C.c_void_p(stream_handle)), "set_stream")
 
+    def set_coarsening(self, levels: int):
+        """Run the network on the grid pooled `levels` times (0..3) and
+        prolong its output trilinearly to the solver's grid."""
+        self._ck(self.lib.flipunet_set_coarsening(self.h, int(levels)), "set_coarsening")
+
+    @property
+    def coarsening(self) -> int:
+        return int(self.lib.flipunet_get_coarsening(self.h))
+
     def set_tensor_path(self, tcgen05: bool):
         """Forward convolutions on tcgen05 (True, the default) or mma.sync."""
         self._ck(self.lib.flipunet_set_tensor_path(self.h, 1 if tcgen05 else 0), "set_tensor_path")
@@ -457,11 +469,18 @@ class UNet:
         assert p.shape[0] == self.nparam
         self._ck(self.lib.flipunet_set_params(self.h, _ptr(p)), "set_params")
 
-    def save(self, path):
+    def save(self, path, **meta):
+        """Parameters as raw float32; the coarsening (and any extra keys)
+        in a JSON file beside them."""
         self.params().tofile(path)
+        with open(path + ".json", "w") as f:
+            json.dump({"coarsening": self.coarsening, **meta}, f)
 
     def load(self, path):
         self.set_params(np.fromfile(path, np.float32))
+        if os.path.exists(path + ".json"):
+            with open(path + ".json") as f:
+                self.set_coarsening(int(json.load(f).get("coarsening", 0)))
 
     def predict(self, n, batch, A, b, x0, r0, delta):
         self._ck(self.lib.flipunet_predict(self.h, n, batch, *[C.c_void_p(a) for a in

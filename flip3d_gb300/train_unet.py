@@ -6,8 +6,8 @@ solved on seeded random scenes (1-4 liquid boxes/spheres, pool depth
 U(0, 0.4), velocities N(0, 1)), the correction from the previous step's
 pressure to the solution. Torch holds the device tensors; it is plumbing.
 
-    python -m flip3d_gb300.train_unet --n 64 --scenes 40 --steps 50 --every 5 \\
-        --epochs 4 --out flip3d_gb300/unet_weights.bin
+    python -m flip3d_gb300.train_unet --n 128 --coarsen 2 --scenes 40 --steps 50 \\
+        --every 5 --epochs 30 --out flip3d_gb300/unet_weights.bin
 """
 from __future__ import annotations
 
@@ -139,6 +139,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--coarsen", type=int, default=0,
+                    help="run the network on the grid pooled this many times")
     ap.add_argument("--init", default=None, help="start from these weights")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
@@ -152,12 +154,13 @@ def main(argv=None):
     net = gpu.UNet(seed=a.seed)
     if a.init:
         net.load(a.init)
+    net.set_coarsening(a.coarsen)
     before = evaluate(net, held, a.n)
     hist = train(net, data, a.n, a.epochs, a.batch, a.lr, a.seed, log=print)
     t2 = time.perf_counter()
     after = evaluate(net, held, a.n)
     if a.out:
-        net.save(a.out)
+        net.save(a.out, trained_n=a.n, train_systems=int(data["A"].shape[0]))
     print(json.dumps({"n": a.n, "train_systems": int(data["A"].shape[0]),
                       "heldout_systems": int(held["A"].shape[0]), "collect_s": t1 - t0,
                       "train_s": t2 - t1, "loss": hist, "untrained": before, "trained": after}))

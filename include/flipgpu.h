@@ -308,6 +308,14 @@ int flipunet_set_params(FlipUNet *u, const float *params);
  * accumulators, 1, the default) or on the mma.sync path (0). Backward-data
  * and weight-gradient convolutions always use mma.sync. */
 int flipunet_set_tensor_path(FlipUNet *u, int tcgen05);
+/* Coarsened warm start (levels 0..3, default 0): the 16 input features are
+ * computed on the solver's grid n, average-pooled `levels` times, the
+ * network runs on the (n >> levels)^3 grid and its output is prolonged
+ * trilinearly back to n before the A-norm-optimal step. Training targets
+ * are the liquid-cell averages of x and x0 over each coarse cell. n must be
+ * a multiple of 8 << levels. */
+int flipunet_set_coarsening(FlipUNet *u, int levels);
+int flipunet_get_coarsening(const FlipUNet *u);
 /* delta = the correction for systems (A, b, x0, r0), zero off the liquid. */
 int flipunet_predict(FlipUNet *u, int n, int batch, const uint8_t *A, const float *b,
                      const float *x0, const float *r0, float *delta);

@@ -120,6 +120,54 @@ def features(A, b, x0, r0):
     return X, st, fl
 
 
+def pool_features(X, levels, round_bf16=False):
+    """The 16-channel input average-pooled `levels` times (rounded to BF16
+    after every pooling, as k_pool stores it)."""
+    r = bf16 if round_bf16 else (lambda a: a)
+    X = r(X)
+    for _ in range(levels):
+        X = r(pool(X))
+    return X
+
+
+def pool_target(A, x, x0, levels):
+    """Coarse liquid flags and the liquid-cell averages of x and x0 over
+    each (2^levels)^3 block (flip3d_gb300/csrc/k_unet.cu k_pool_target)."""
+    f = 1 << levels
+    Bn, n = A.shape[0], A.shape[1]
+    m = n // f
+    fl = (A == 1).reshape(Bn, m, f, m, f, m, f)
+    cnt = fl.sum(axis=(2, 4, 6))
+
+    def avg(a):
+        a32 = np.float32(a).astype(np.float64).reshape(Bn, m, f, m, f, m, f)
+        s = np.where(fl, a32, 0.0).sum(axis=(2, 4, 6))
+        return np.where(cnt > 0, s / np.maximum(cnt, 1), 0.0)
+    Ac = np.where(cnt > 0, 1, 0).astype(np.uint8)
+    return Ac, avg(x), avg(x0)
+
+
+def prolong(O, levels):
+    """Trilinear prolongation of a cell-centred [B, m, m, m] field to
+    (m 2^levels)^3, clamped at the boundary (k_prolong)."""
+    f = 1 << levels
+    m = O.shape[1]
+    n = m * f
+    xc = (np.arange(n) + 0.5) / f - 0.5
+    lo = np.floor(xc).astype(int)
+    w = xc - lo
+    a = np.clip(lo, 0, m - 1)
+    b = np.clip(lo + 1, 0, m - 1)
+    out = O
+    for axis in (1, 2, 3):
+        shp = [1, 1, 1, 1]
+        shp[axis] = n
+        wa = (1.0 - w).reshape(shp)
+        wb = w.reshape(shp)
+        out = np.take(out, a, axis=axis) * wa + np.take(out, b, axis=axis) * wb
+    return out
+
+
 def forward(p, X, round_bf16=False):
     W, Bs, wh, bh = unpack(np.asarray(p, np.float64))
     r = bf16 if round_bf16 else (lambda a: a)
@@ -143,10 +191,16 @@ def forward(p, X, round_bf16=False):
     return t
 
 
-def loss_and_grads(p, A, b, x0, r0, x, round_bf16=False):
+def loss_and_grads(p, A, b, x0, r0, x, round_bf16=False, levels=0):
     """Loss (mean squared error over liquid cells of the batch) and its
-    gradient with respect to the flat parameter vector."""
+    gradient with respect to the flat parameter vector. With `levels` > 0
+    the network sees the pooled features and the loss compares it with the
+    pooled targets on the coarse grid."""
     X, sx, fl = features(A, b, x0, r0)
+    if levels:
+        X = pool_features(X, levels, round_bf16)
+        A, x, x0 = pool_target(A, x, x0, levels)
+        fl = A == 1
     t = forward(p, X, round_bf16)
     W, Bs, wh, bh = unpack(np.asarray(p, np.float64))
     r = bf16 if round_bf16 else (lambda a: a)

@@ -95,6 +95,50 @@ def test_unet_forward_and_gradients_match_cpu_oracle(gpu, torch, tensor_path):
     assert np.median([e for e, _, _ in errs]) < 2e-2
 
 
+def test_coarsened_warm_start_matches_cpu_oracle(gpu, torch):
+    """Coarsening 1 at 32^3: pooled features into the network on 16^3, its
+    output prolonged trilinearly, and the loss and gradients against the
+    pooled targets; all against the oracle's restatement."""
+    from oracle import unet_oracle as U
+    n, seeds, lv = 32, [3, 4], 1
+    sy = systems(gpu, n, seeds)
+    A = to_dev(torch, [s[0] for s in sy], torch.uint8)
+    b, x0, r0, x = (to_dev(torch, [s[k] for s in sy], torch.float32) for k in (2, 3, 4, 5))
+    net = gpu.UNet(seed=6)
+    net.set_coarsening(lv)
+    assert net.coarsening == lv
+    p = net.params()
+    rng = np.random.default_rng(2)
+    woff, boff, hoff, total = U.layout()
+    for l, (cin, cout, _) in enumerate(U.CONVS):
+        p[boff[l]:boff[l] + cout] = rng.normal(0.0, 0.05, cout)
+    p[hoff:hoff + 16] = rng.normal(0.0, 0.3, 16)
+    net.set_params(p)
+    delta = torch.zeros(len(seeds), n ** 3, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    net.predict(n, len(seeds), A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(),
+                delta.data_ptr())
+    torch.cuda.synchronize()
+    loss, g = net.gradients(n, len(seeds), A.data_ptr(), b.data_ptr(), x0.data_ptr(),
+                            r0.data_ptr(), x.data_ptr())
+    shp = (len(seeds), n, n, n)
+    An, bn, x0n, r0n, xn = (t.cpu().numpy().reshape(shp) for t in (A, b, x0, r0, x))
+    X, st, fl = U.features(An, bn, x0n, r0n)
+    t = U.forward(p.astype(np.float64), U.pool_features(X, lv, True), round_bf16=True)
+    want = np.where(fl, U.prolong(t["O"], lv) * st[:, None, None, None], 0.0)
+    got = delta.cpu().numpy().reshape(shp)
+    rel = np.linalg.norm(got - want) / np.linalg.norm(want)
+    assert rel < 3e-2, rel
+    oloss, og, _ = U.loss_and_grads(p.astype(np.float64), An, bn, x0n, r0n, xn,
+                                    round_bf16=True, levels=lv)
+    assert abs(loss - oloss) <= 1e-2 * abs(oloss), (loss, oloss)
+    errs = [np.linalg.norm(g[a:a + m] - og[a:a + m]) / max(np.linalg.norm(og[a:a + m]), 1e-30)
+            for l, (cin, cout, _) in enumerate(U.CONVS)
+            for a, m in ((woff[l], 27 * cin * cout), (boff[l], cout))]
+    print("coarsened gradient relative errors", np.round(errs, 4))
+    assert max(errs) < 6e-2 and np.median(errs) < 2e-2
+
+
 def test_unet_training_reduces_the_loss(gpu, torch):
     n = 16
     sy = systems(gpu, n, [7, 8, 9, 10])

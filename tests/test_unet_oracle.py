@@ -41,3 +41,25 @@ def test_bf16_rounding_is_round_to_nearest_even():
     r = U.bf16(x)
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.015625 and r[3] == -2.5
     assert abs(r[4] - 3.0e-5) <= 3.0e-5 * 2 ** -8
+
+
+def test_prolongation_and_pooled_targets():
+    """Trilinear prolongation keeps constants and reproduces linear fields
+    away from the clamped boundary; pooled targets average liquid cells
+    only."""
+    from oracle import unet_oracle as U
+    c = np.full((1, 4, 4, 4), 2.5)
+    assert np.allclose(U.prolong(c, 2), 2.5)
+    i = np.arange(4, dtype=float)
+    lin = (i[:, None, None] + 0 * i[None, :, None] + 0 * i[None, None, :])[None]
+    up = U.prolong(lin, 1)[0]
+    fine = (np.arange(8) + 0.5) / 2 - 0.5
+    assert np.allclose(up[1:-1, 3, 3], fine[1:-1])
+    A = np.zeros((1, 4, 4, 4), np.uint8)
+    A[0, 0, 0, 0] = 1
+    A[0, 1, 1, 1] = 1
+    x = np.zeros((1, 4, 4, 4), np.float32)
+    x[0, 0, 0, 0], x[0, 1, 1, 1], x[0, 0, 1, 0] = 2.0, 4.0, 100.0
+    Ac, xc, _ = U.pool_target(A, x, x, 1)
+    assert Ac[0, 0, 0, 0] == 1 and Ac.sum() == 1
+    assert xc[0, 0, 0, 0] == 3.0
