@@ -315,6 +315,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "mic", "ref"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "ref"],
+                    help="particle-gather arithmetic: native FP32 (fast) or the reference's "
+                         "float expressions bit for bit (ref)")
     ap.add_argument("--scene", default="dam_break", choices=["dam_break", "sphere_into_pool"],
                     help="dam_break (column x<0.4, y<0.8) or sphere_into_pool (pool 0.25, "
                          "sphere r 0.15 falling at 2 m/s)")
@@ -350,7 +353,8 @@ def main():
            "ref": gpu.PRECOND_REF}[args.precond]
     mode = gpu.SOLVE_REF if args.precond == "ref" else gpu.SOLVE_FAST
     prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1,
-                             mic_tau=0.97 if args.precond == "mic" else 0.0)
+                             mic_tau=0.97 if args.precond == "mic" else 0.0,
+                             arith=gpu.ARITH_FAST if args.arith == "fast" else gpu.ARITH_REF)
     sim = gpu.Simulation(prm)
     sim.set_scene(sc)
     sim.calibrate_max_density()
@@ -456,6 +460,8 @@ def main():
             "data": "synthetic",
             "config": {"workload": f"{args.scene} N={args.n}, 8 particles/cell, rel-res 1e-6",
                        "particles": P, "grid": args.n, "solver": f"FP32 PCG {args.precond}, FP64 dots",
+                       "arith": f"particle gathers {args.arith} "
+                                f"({'native FP32' if args.arith == 'fast' else 'reference bit-exact'})",
                        "l2": "inputs larger than L2 (state ~0.6 GB per step)",
                        "parallelism": f"replicas x{world}"},
             "solve": {"ms_per_solve": statistics.mean(solve_ms), "iters": statistics.mean(iters),

@@ -216,12 +216,14 @@ SimConst make_const(const FlipGpu *h) {
   float kh = (float)(4.0 * (double)p.density / n);
   c.kd_hh = kh * kh;
   c.kd_rcp = pow2_rcp(c.kd_hh);
+  c.kd_inv = 1.0f / c.kd_hh;
   c.max_dens = h->max_dens;
   const float RE = (float)1.4;
   c.re_p2g_hh = RE * RE;
   c.re_corr = (float)((double)p.density / n);
   c.re_corr_hh = c.re_corr * c.re_corr;
   c.corr_rcp = pow2_rcp(c.re_corr_hh);
+  c.corr_inv = 1.0f / c.re_corr_hh;
   c.re_repo = (float)(1.0 / n);
   c.re_repo_hh = c.re_repo * c.re_repo;
   c.r2_floor = smallest_float_ge(1.0e-5);
@@ -277,6 +279,7 @@ void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles) {
   p->eps_abs = -1.0;
   p->max_iters = 0;
   p->refine_steps = 0;
+  p->arith = FLIPGPU_ARITH_REF;
 }
 
 const char *flipgpu_last_error(const FlipGpu *h) { return h ? h->err : "null handle"; }

@@ -31,6 +31,7 @@ struct SimConst {
   float kd_hh;        /* density kernel radius^2: h*h of (float)(4*DENSITY/N) */
   float kd_rcp;       /* 1/kd_hh when kd_hh is a power of two, else 0 */
   float corr_rcp;     /* 1/re_corr_hh when it is a power of two, else 0 */
+  float kd_inv, corr_inv; /* 1/kd_hh, 1/re_corr_hh in float (FAST arithmetic) */
   float max_dens;
   float re_p2g_hh;    /* RE*RE for P2G (src/mapper.cpp:14) */
   float re_corr;      /* DENSITY/N (src/flip3D.cpp:1242) */

@@ -9,6 +9,11 @@
  * contiguous run of slots. Every float expression follows the reference's
  * evaluation order and promotions (nvcc -fmad=false; refmath.h for the
  * double-promoted ones), so the results are the reference's bit for bit.
+ *
+ * The gathers and the per-particle updates are templated on an arithmetic
+ * policy: RefArith reproduces those expressions (the default), FastArith
+ * evaluates the same formulas in native FP32 with fused multiply-adds and
+ * the fast division intrinsic (FLIPGPU_ARITH_FAST).
  */
 #include "devcommon.cuh"
 
@@ -17,6 +22,71 @@ using namespace refmath;
 namespace {
 
 constexpr int BLK = 256;
+
+/* The reference's expressions, bit for bit (refmath.h). */
+struct RefArith {
+  static __device__ __forceinline__ float hypot2(float a, float b, float c) {
+    return hypot2_ref(a, b, c);
+  }
+  static __device__ __forceinline__ float length(float a, float b, float c) {
+    return length_ref(a, b, c);
+  }
+  static __device__ __forceinline__ float sharp(float r2, float hh, float r2_floor, float small) {
+    return sharp_ref(r2, hh, r2_floor, small);
+  }
+  static __device__ __forceinline__ float smooth_density(const SimConst &c, float r2) {
+    return c.kd_rcp != 0.0f ? smooth_ref_pow2(r2, c.kd_rcp) : smooth_ref(r2, c.kd_hh);
+  }
+  static __device__ __forceinline__ float smooth_corr(const SimConst &c, float r2) {
+    return c.corr_rcp != 0.0f ? smooth_ref_pow2(r2, c.corr_rcp) : smooth_ref(r2, c.re_corr_hh);
+  }
+  static __device__ __forceinline__ float blend(const SimConst &c, float pic, float flip) {
+    return blend_ref(pic, flip, c.c1h, c.c1l, c.c2h, c.c2l, c.c1, c.c2);
+  }
+  static __device__ __forceinline__ float euler(const SimConst &c, float p, float v) {
+    return axpy_fd(p, v, c.dt_h, c.dt_l, c.dt);
+  }
+  /* the wall push p + (push_re - dist) n, in double as the reference has it */
+  static __device__ __forceinline__ float push(const SimConst &c, float p, float dist, float nq) {
+    return (float)((double)p + (c.push_re - (double)dist) * (double)nq);
+  }
+  /* w dx / dist re, left to right */
+  static __device__ __forceinline__ float spring_term(float w, float d, float dist, float re) {
+    return w * d / dist * re;
+  }
+};
+
+/* The same formulas in native FP32. */
+struct FastArith {
+  static __device__ __forceinline__ float hypot2(float a, float b, float c) {
+    return fmaf(a, a, fmaf(b, b, c * c));
+  }
+  static __device__ __forceinline__ float length(float a, float b, float c) {
+    return sqrtf(hypot2(a, b, c));
+  }
+  static __device__ __forceinline__ float sharp(float r2, float hh, float, float) {
+    return r2 < hh ? fmaxf(__fdividef(hh, fmaxf(r2, 1.0e-5f)) - 1.0f, 0.0f) : 0.0f;
+  }
+  static __device__ __forceinline__ float smooth_density(const SimConst &c, float r2) {
+    return fmaxf(fmaf(-r2, c.kd_inv, 1.0f), 0.0f);
+  }
+  static __device__ __forceinline__ float smooth_corr(const SimConst &c, float r2) {
+    return fmaxf(fmaf(-r2, c.corr_inv, 1.0f), 0.0f);
+  }
+  static __device__ __forceinline__ float blend(const SimConst &c, float pic, float flip) {
+    return fmaf((float)c.c2, flip, (float)c.c1 * pic);
+  }
+  static __device__ __forceinline__ float euler(const SimConst &c, float p, float v) {
+    return fmaf(v, (float)c.dt, p);
+  }
+  static __device__ __forceinline__ float push(const SimConst &c, float p, float dist, float nq) {
+    return fmaf((float)c.push_re - dist, nq, p);
+  }
+  static __device__ __forceinline__ float spring_term(float w, float d, float dist, float re) {
+    return __fdividef(w * re, dist) * d;
+  }
+};
+
 constexpr int REPO_GRID = 152 * 4; /* grid-stride launches over the stuck list */
 constexpr int REPO_ROUNDS = 16;    /* parallel resample rounds before the ordered tail */
 
@@ -75,6 +145,7 @@ __device__ __forceinline__ void fetch_velocity(int n, float fn, const float *__r
 
 /* ------------------------------------------------------ computeDensity */
 
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
           const float4 *__restrict__ spos, float *__restrict__ dens,
@@ -94,8 +165,8 @@ k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restric
   visit_cells(c.n, cs, ci - 1, ci + 1, cj - 1, cj + 1, ck - 1, ck + 1, [&](uint32_t b) {
     float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) == CELL_WALL) return;
-    float d2 = hypot2_ref(Q.x - P.x, Q.y - P.y, Q.z - P.z);
-    wsum += c.kd_rcp != 0.0f ? smooth_ref_pow2(d2, c.kd_rcp) : smooth_ref(d2, c.kd_hh);
+    float d2 = AR::hypot2(Q.x - P.x, Q.y - P.y, Q.z - P.z);
+    wsum += AR::smooth_density(c, d2);
   });
   float d = wsum / c.max_dens;
   dens[p] = d;
@@ -110,6 +181,7 @@ k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restric
  * kernel radius RE=1.4, so its weights are exactly 0 and it is skipped.
  * Writes the saved grid (save_grid) and the boundary-enforced grid
  * (enforce_boundary, src/flip3D.cpp:783-805) in one pass. */
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__restrict__ spg,
       const float4 *__restrict__ svel, const uint8_t *__restrict__ A, float *__restrict__ u0,
@@ -135,9 +207,9 @@ k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__
   visit_cells(n, cs, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], [&](uint32_t b) {
     float4 Q = __ldg(spg + b);
     if (unpack_type(Q.w) != CELL_FLUID) return;
-    float r2 = hypot2_ref(Q.x - fp[0], Q.y - fp[1], Q.z - fp[2]);
+    float r2 = AR::hypot2(Q.x - fp[0], Q.y - fp[1], Q.z - fp[2]);
     if (!(r2 < hh)) return; /* weight exactly 0 */
-    float w = sharp_ref(r2, hh, c.r2_floor, c.sharp_small_p2g);
+    float w = AR::sharp(r2, hh, c.r2_floor, c.sharp_small_p2g);
     float4 V = __ldg(svel + b);
     float vc = comp == 0 ? V.x : (comp == 1 ? V.y : V.z);
     sumx += w * vc;
@@ -186,6 +258,7 @@ k_g2p(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
 
 /* The FLIP block of solve_picflip (src/flip3D.cpp:1071-1097): sample the
  * grid change and the new grid, then u = (1-ALPHA)*pic + ALPHA*(u + du). */
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_flip_blend(SimConst c, const float *__restrict__ px, const float *__restrict__ py,
              const float *__restrict__ pz, const uint8_t *__restrict__ type,
@@ -203,7 +276,7 @@ k_flip_blend(SimConst c, const float *__restrict__ px, const float *__restrict__
 #pragma unroll
   for (int q = 0; q < 3; q++) {
     float flip = du[q] + v[q];
-    v[q] = blend_ref(pic[q], flip, c.c1h, c.c1l, c.c2h, c.c2l, c.c1, c.c2);
+    v[q] = AR::blend(c, pic[q], flip);
   }
   vx[p] = v[0];
   vy[p] = v[1];
@@ -217,6 +290,7 @@ k_flip_blend(SimConst c, const float *__restrict__ px, const float *__restrict__
  * closer than 1.5*DENSITY/N and drop the normal velocity, then flag it if it
  * is stuck. Each particle only reads itself and the (static) wall
  * particles, so the reference's serial loop is order-independent. */
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz,
          float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz,
@@ -236,7 +310,7 @@ k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__re
   float v[3];
   fetch_velocity(n, c.fn, u0, u1, u2, pp[0], pp[1], pp[2], v);
 #pragma unroll
-  for (int q = 0; q < 3; q++) pp[q] = axpy_fd(pp[q], v[q], c.dt_h, c.dt_l, c.dt);
+  for (int q = 0; q < 3; q++) pp[q] = AR::euler(c, pp[q], v[q]);
   /* p = fmax(r, fmin(1.0-r, p)) */
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -250,7 +324,7 @@ k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__re
       k = cell_clamp_minmax(pp[2], c.fn, n);
   visit_cells(n, wall_start, i - 1, i + 1, j - 1, j + 1, k - 1, k + 1, [&](uint32_t w) {
     float4 Q = __ldg(wall_pos + w);
-    float dist = length_ref(pp[0] - Q.x, pp[1] - Q.y, pp[2] - Q.z);
+    float dist = AR::length(pp[0] - Q.x, pp[1] - Q.y, pp[2] - Q.z);
     if (!(dist <= c.push_re_thr)) return; /* (double)dist < 1.5*DENSITY/N */
     float4 Nw = __ldg(wall_nrm + w);
     float nrm[3] = {Nw.x, Nw.y, Nw.z};
@@ -259,9 +333,8 @@ k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__re
       nrm[1] = (pp[1] - Q.y) / dist;
       nrm[2] = (pp[2] - Q.z) / dist;
     }
-    double push = c.push_re - (double)dist;
 #pragma unroll
-    for (int q = 0; q < 3; q++) pp[q] = (float)((double)pp[q] + push * (double)nrm[q]);
+    for (int q = 0; q < 3; q++) pp[q] = AR::push(c, pp[q], dist, nrm[q]);
     float dot = uu[0] * nrm[0] + uu[1] * nrm[1] + uu[2] * nrm[2];
 #pragma unroll
     for (int q = 0; q < 3; q++) uu[q] -= dot * nrm[q];
@@ -645,6 +718,7 @@ __device__ __noinline__ float wall_kick_add(float s, double k, float nrm) {
  * the exact arithmetic runs over the list in the same order. Writes the
  * moved position to the canonical arrays; neighbours come from the sorted
  * snapshot. */
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
          const float4 *__restrict__ spos, const float *__restrict__ nx,
@@ -670,13 +744,12 @@ k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict
       uint32_t b = near_list[t][threadIdx.x];
       float4 Q = __ldg(spos + b);
       float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
-      float dist = length_ref(dx, dy, dz);
-      float w = 50.0f * (c.corr_rcp != 0.0f ? smooth_ref_pow2(dist * dist, c.corr_rcp)
-                                            : smooth_ref(dist * dist, c.re_corr_hh));
+      float dist = AR::length(dx, dy, dz);
+      float w = 50.0f * AR::smooth_corr(c, dist * dist);
       if (dist > c.corr_near_thr) {
-        spring[0] += w * dx / dist * re;
-        spring[1] += w * dy / dist * re;
-        spring[2] += w * dz / dist * re;
+        spring[0] += AR::spring_term(w, dx, dist, re);
+        spring[1] += AR::spring_term(w, dy, dist, re);
+        spring[2] += AR::spring_term(w, dz, dist, re);
       } else if (unpack_type(Q.w) == CELL_FLUID) {
         uint32_t o = perm[b];
         for (int q = 0; q < 3; q++) {
@@ -695,7 +768,7 @@ k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict
   visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     if (b == (uint32_t)a) return;
     float4 Q = __ldg(spos + b);
-    if (hypot2_ref(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
+    if (AR::hypot2(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
     near_list[cnt][threadIdx.x] = b;
     if (++cnt == NEAR_CAP) flush();
   });
@@ -708,6 +781,7 @@ k_spring(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict
 /* Velocity resample at the moved position (src/corrector.cpp:91-114 with
  * resample at :15-47): the same reach restriction and near list, with the
  * sharp kernel's exact support test r2 < re^2. */
+template <class AR>
 __global__ void __launch_bounds__(BLK)
 k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
            const float4 *__restrict__ spos, const float4 *__restrict__ svel,
@@ -733,8 +807,8 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
     for (int t = 0; t < cnt; t++) {
       uint32_t b = near_list[t][threadIdx.x];
       float4 Q = __ldg(spos + b);
-      float d2 = hypot2_ref(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
-      float w = sharp_ref(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
+      float d2 = AR::hypot2(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
+      float w = AR::sharp(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
       float4 V = __ldg(svel + b);
       u[0] += w * V.x;
       u[1] += w * V.y;
@@ -746,7 +820,7 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
   visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) != CELL_FLUID) return;
-    float d2 = hypot2_ref(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
+    float d2 = AR::hypot2(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
     if (!(d2 < c.re_corr_hh)) return;
     near_list[cnt][threadIdx.x] = b;
     if (++cnt == NEAR_CAP) flush();
@@ -832,8 +906,13 @@ cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, floa
 cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
-  k_density<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
-                                                         h->dens, h->sdens);
+  const unsigned g = grid_for(h->np, BLK);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST)
+    k_density<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
+                                                   h->sdens);
+  else
+    k_density<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
+                                                  h->sdens);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -841,8 +920,14 @@ cudaError_t launch_density(FlipGpu *h) {
 cudaError_t launch_p2g(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
   dim3 grid(grid_for(h->nf, BLK), 3);
-  k_p2g<<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0],
-                                     h->u[1], h->u[2], h->us[0], h->us[1], h->us[2]);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST)
+    k_p2g<FastArith><<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel,
+                                                  h->A, h->u[0], h->u[1], h->u[2], h->us[0],
+                                                  h->us[1], h->us[2]);
+  else
+    k_p2g<RefArith><<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel,
+                                                 h->A, h->u[0], h->u[1], h->u[2], h->us[0],
+                                                 h->us[1], h->us[2]);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -859,9 +944,15 @@ cudaError_t launch_g2p(FlipGpu *h) {
 cudaError_t launch_flip_blend(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
-  k_flip_blend<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(
-      c, h->px, h->py, h->pz, h->type, h->u[0], h->u[1], h->u[2], h->us[0], h->us[1],
-      h->us[2], h->vx, h->vy, h->vz);
+  const unsigned g = grid_for(h->np, BLK);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST)
+    k_flip_blend<FastArith><<<g, BLK, 0, h->stream>>>(c, h->px, h->py, h->pz, h->type, h->u[0],
+                                                      h->u[1], h->u[2], h->us[0], h->us[1],
+                                                      h->us[2], h->vx, h->vy, h->vz);
+  else
+    k_flip_blend<RefArith><<<g, BLK, 0, h->stream>>>(c, h->px, h->py, h->pz, h->type, h->u[0],
+                                                     h->u[1], h->u[2], h->us[0], h->us[1],
+                                                     h->us[2], h->vx, h->vy, h->vz);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -869,9 +960,15 @@ cudaError_t launch_flip_blend(FlipGpu *h) {
 cudaError_t launch_advect(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
-  k_advect<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(
-      c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
-      h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
+  const unsigned g = grid_for(h->np, BLK);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST)
+    k_advect<FastArith><<<g, BLK, 0, h->stream>>>(
+        c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
+        h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
+  else
+    k_advect<RefArith><<<g, BLK, 0, h->stream>>>(
+        c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
+        h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -956,12 +1053,18 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
 cudaError_t launch_correct(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
-  k_spring<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
-                                                        h->nx, h->ny, h->nz, h->px, h->py,
-                                                        h->pz);
-  k_resample<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
-                                                          h->svel, h->px, h->py, h->pz, h->vx,
-                                                          h->vy, h->vz);
+  const unsigned g = grid_for(h->np, BLK);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST) {
+    k_spring<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,
+                                                  h->ny, h->nz, h->px, h->py, h->pz);
+    k_resample<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->svel,
+                                                    h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+  } else {
+    k_spring<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,
+                                                 h->ny, h->nz, h->px, h->py, h->pz);
+    k_resample<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->svel,
+                                                   h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+  }
   FG_LAUNCHED(h, 2);
   return cudaGetLastError();
 }

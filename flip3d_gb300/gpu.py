@@ -20,6 +20,7 @@ ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOCONV", -5: "ENAN", -6
           -7: "ETOOBIG"}
 PRECOND_NONE, PRECOND_REF, PRECOND_IC, PRECOND_JACOBI = 0, 1, 2, 3
 SOLVE_REF, SOLVE_FAST = 0, 1
+ARITH_REF, ARITH_FAST = 0, 1
 
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
@@ -31,7 +32,8 @@ class Params(C.Structure):
                 ("alpha", C.c_double), ("dt", C.c_double), ("gravity", C.c_double),
                 ("subcell", C.c_int), ("seed", C.c_uint64), ("solve_mode", C.c_int),
                 ("precond", C.c_int), ("mic_tau", C.c_double), ("rel_tol", C.c_double),
-                ("eps_abs", C.c_double), ("max_iters", C.c_int), ("refine_steps", C.c_int)]
+                ("eps_abs", C.c_double), ("max_iters", C.c_int), ("refine_steps", C.c_int),
+                ("arith", C.c_int)]
 
 
 class SolveStats(C.Structure):

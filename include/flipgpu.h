@@ -58,6 +58,15 @@ extern "C" {
 #define FLIPGPU_SOLVE_REF 0
 #define FLIPGPU_SOLVE_FAST 1
 
+/* Particle-gather arithmetic (density, P2G, FLIP blend, advection, the
+ * corrector's spring and resample). REF: the reference's float expressions
+ * and double promotions reproduced bit for bit (error-free transforms).
+ * FAST: native FP32 with fused multiply-adds and the fast division
+ * intrinsic; results agree with REF to FP32 rounding per step. The sort,
+ * the grid stages and the solver are unaffected. */
+#define FLIPGPU_ARITH_REF 0
+#define FLIPGPU_ARITH_FAST 1
+
 typedef struct FlipGpuParams {
   int n;              /* N: grid cells per axis (src/flip3D.cpp:25) */
   int max_particles;  /* capacity of the particle arrays */
@@ -82,6 +91,7 @@ typedef struct FlipGpuParams {
                          Default 0: with x in FP32 the true residual levels
                          off near the FP32 rounding of A x (about 1e-4 of
                          ||b|| at n=128), where restarts cannot help. */
+  int arith;          /* FLIPGPU_ARITH_*: particle-gather arithmetic */
 } FlipGpuParams;
 
 typedef struct FlipGpuSolveStats {

@@ -427,6 +427,40 @@ def test_mesh_on_stale_lists_matches_oracle(gpu, orc):
     assert np.array_equal(m["normals"].ravel(), om["normals"])
 
 
+def test_fast_arithmetic_tracks_the_reference_step(gpu, orc):
+    """FLIPGPU_ARITH_FAST (native FP32 gathers) against the reference's
+    steps on the oracle, 2 steps of the N=32 dam break with the FAST solver:
+    the same tolerances as the FAST-solver step test (positions 2e-5 of the
+    unit cube, velocities 2e-3 of the largest speed). FAST arithmetic is
+    deterministic run to run."""
+    sc = scenes.dam_break(32, seed=2)
+    n = sc.n
+    md = orc.max_density(n)
+    osim = orc.Sim(sc, orc.params(n, orc.PRECOND_REF, rel_tol=1e-6, seed=4), md)
+    sims = []
+    for _ in range(2):
+        g = make_sim(gpu, n, sc.count, rel_tol=1e-6, seed=4, solve_mode=gpu.SOLVE_FAST,
+                     precond=gpu.PRECOND_JACOBI, arith=gpu.ARITH_FAST)
+        g.set_scene(sc)
+        g.set_max_density(md)
+        sims.append(g)
+    for _ in range(2):
+        osim.step()
+        for g in sims:
+            assert g.step().status == 0
+    opos, ovel, odens, otyp = osim.get()
+    gpos, gvel, gdens, _ = sims[0].get_particles()
+    fl = otyp == 1
+    vscale = float(np.abs(ovel[fl]).max())
+    print("fast arithmetic vs ref: max dpos", np.abs(gpos - opos).max(), "max dvel",
+          np.abs(gvel[fl] - ovel[fl]).max(), "max ddens", np.abs(gdens - odens).max())
+    assert np.abs(gpos - opos).max() <= 2e-5
+    assert np.abs(gvel[fl] - ovel[fl]).max() <= 2e-3 * max(vscale, 1.0)
+    assert np.abs(gdens - odens).max() <= 1e-4
+    for x, y in zip(sims[0].get_particles(), sims[1].get_particles()):
+        assert np.array_equal(x, y)
+
+
 def _fast_sim(gpu, sc, seed=3):
     s = make_sim(gpu, sc.n, sc.count, rel_tol=1e-6, seed=seed, solve_mode=gpu.SOLVE_FAST,
                  precond=gpu.PRECOND_JACOBI)
