@@ -347,7 +347,9 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    t_build = time.perf_counter()
     sc = getattr(scenes, args.scene)(args.n, seed=rank)
+    t_build = time.perf_counter() - t_build
     P = sc.count
     pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "mic": gpu.PRECOND_IC,
            "ref": gpu.PRECOND_REF}[args.precond]
@@ -356,7 +358,16 @@ def main():
                              mic_tau=0.97 if args.precond == "mic" else 0.0,
                              arith=gpu.ARITH_FAST if args.arith == "fast" else gpu.ARITH_REF)
     sim = gpu.Simulation(prm)
+    t_up = time.perf_counter()
     sim.set_scene(sc)
+    t_up = time.perf_counter() - t_up
+    # the same particles seeded on the device (flipgpu_seed_scene)
+    t_seed = time.perf_counter()
+    sim.seed_scene(sc.objects, seed=rank)
+    t_seed = time.perf_counter() - t_seed
+    setup = {"host_build_s": round(t_build, 4), "host_upload_s": round(t_up, 4),
+             "device_seed_s": round(t_seed, 4),
+             "note": "scene setup, not part of value: numpy build + upload vs flipgpu_seed_scene"}
     sim.calibrate_max_density()
 
     def barrier():
@@ -468,6 +479,7 @@ def main():
                       "kind": f"plain PCG ({args.precond})",
                       "true_rel_residual_fp64": max(true_rel) if true_rel else None},
             "solver_comparison": solve_cmp,
+            "setup": setup,
             "stages_ms": {k: round(v[0] / max(v[1], 1), 4) for k, v in prof.items()},
             "mesh": {"ms": mesh_ms, "vertices": mesh_v, "faces": mesh_f,
                      "note": "mesher::generateMesh after the last step, host-timed, "

@@ -284,6 +284,8 @@ void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles) {
 
 const char *flipgpu_last_error(const FlipGpu *h) { return h ? h->err : "null handle"; }
 
+int flipgpu_particle_count(const FlipGpu *h) { return h ? h->np : -1; }
+
 int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   if (!p || !out) return FLIPGPU_EINVAL;
   *out = nullptr;

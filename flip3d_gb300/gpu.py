@@ -36,6 +36,11 @@ class Params(C.Structure):
                 ("arith", C.c_int)]
 
 
+class SceneObject(C.Structure):
+    _fields_ = [("shape", C.c_int), ("lo", C.c_float * 3), ("hi", C.c_float * 3),
+                ("c", C.c_float * 3), ("r", C.c_float), ("vel", C.c_float * 3)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
                 ("b2", C.c_double), ("ms", C.c_double), ("warm", C.c_int),
@@ -58,6 +63,9 @@ SIGNATURES = {
     "flipgpu_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "flipgpu_sync": (C.c_int, [C.c_void_p]),
     "flipgpu_set_step": (C.c_int, [C.c_void_p, C.c_int64]),
+    "flipgpu_seed_scene": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_double,
+                                     C.c_double]),
+    "flipgpu_particle_count": (C.c_int, [C.c_void_p]),
     "flipgpu_set_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_get_particles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -203,6 +211,21 @@ class Simulation:
 
     def set_scene(self, scene):
         self.set_particles(scene.pos, scene.type, scene.vel, scene.nrm)
+
+    def seed_scene(self, objects, seed=0, density=0.5, jitter=0.25):
+        """flipgpu_seed_scene: the particles scenes.build(n, objects, seed,
+        density, jitter) makes on the host, generated on the device."""
+        from . import scenes as _sc
+        arr = (SceneObject * max(len(objects), 1))()
+        for o, obj in zip(arr, objects):
+            if isinstance(obj, _sc.Box):
+                o.shape, o.lo[:], o.hi[:] = 0, obj.lo, obj.hi
+            else:
+                o.shape, o.c[:], o.r = 1, obj.c, obj.r
+            o.vel[:] = obj.vel
+        self._ck(self.lib.flipgpu_seed_scene(self.h, arr, len(objects), seed, density, jitter),
+                 "seed_scene")
+        self.np = int(self.lib.flipgpu_particle_count(self.h))
 
     def get_particles(self):
         pos = np.zeros((self.np, 3), np.float32)

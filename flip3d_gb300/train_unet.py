@@ -128,6 +128,32 @@ def evaluate(net, data, n):
             "pred_rel_err": prediction_error(net, data, n)}
 
 
+def time_predict(n, weights=None, reps=10, tcgen05=True):
+    """Device ms of one forward pass (flipunet_predict) on a seeded random
+    n^3 system with 70 % liquid, after two warm-up calls."""
+    import torch
+    rng = np.random.default_rng(5)
+    A = torch.tensor((rng.random(n ** 3) < 0.7).astype(np.uint8), device="cuda")
+    b, x0, r0 = (torch.tensor(rng.normal(0, 1, n ** 3).astype(np.float32), device="cuda")
+                 for _ in range(3))
+    net = gpu.UNet(seed=4)
+    if weights:
+        net.load(weights)
+    net.set_tensor_path(tcgen05)
+    d = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+    args = [t.data_ptr() for t in (A, b, x0, r0, d)]
+    for _ in range(2):
+        net.predict(n, 1, *args)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        net.predict(n, 1, *args)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--n", type=int, default=64)
@@ -142,9 +168,16 @@ def main(argv=None):
     ap.add_argument("--coarsen", type=int, default=0,
                     help="run the network on the grid pooled this many times")
     ap.add_argument("--init", default=None, help="start from these weights")
+    ap.add_argument("--time-predict", type=int, default=0, metavar="N",
+                    help="only time the forward pass on an N^3 system (both tensor paths)")
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
     gpu.load()
+    if a.time_predict:
+        out = {path: time_predict(a.time_predict, a.init, reps=2 if a.time_predict >= 256 else 10,
+                                  tcgen05=path == "tcgen05") for path in ("tcgen05", "mma.sync")}
+        print(json.dumps({"n": a.time_predict, "predict_ms": out}))
+        return
     t0 = time.perf_counter()
     train_seeds = range(1000 + a.seed, 1000 + a.seed + a.scenes)
     hold_seeds = range(5000 + a.seed, 5000 + a.seed + a.holdout)

@@ -129,6 +129,33 @@ int flipgpu_set_step(FlipGpu *h, int64_t step);
 
 /* Particle state. Pointers are host memory unless on_device != 0. Any
  * pointer may be NULL to skip that array (set: keeps zeros/old values). */
+/* A liquid object of a seeded scene: a lattice point belongs to the first
+ * object containing it (pushParticle, src/flip3D.cpp:580-647). Boxes are
+ * open intervals lo < p < hi; spheres |p - c| < r in float. */
+#define FLIPGPU_SHAPE_BOX 0
+#define FLIPGPU_SHAPE_SPHERE 1
+typedef struct FlipSceneObject {
+  int shape;          /* FLIPGPU_SHAPE_* */
+  float lo[3], hi[3]; /* box corners */
+  float c[3];         /* sphere centre */
+  float r;            /* sphere radius */
+  float vel[3];       /* initial velocity of the object's particles */
+} FlipSceneObject;
+
+/* flip3D::init's scene setup on the device (src/flip3D.cpp:649-777): a
+ * lattice of spacing density cells in the interior, each point kept if it
+ * lies in an object, jittered by +-jitter cell per axis with
+ * flip_rand31(seed, FLIP_RNG_SEED stream, lattice index) and dropped if the
+ * jitter moves it into a wall cell; then one wall particle per cell of the
+ * outer layer with its face normal (compute_wall_normal,
+ * src/flip3D.cpp:75-130) and the static wall lists. Replaces the particle
+ * state; the particle order is liquid in lattice order, then walls in cell
+ * order. At most 16 objects. */
+int flipgpu_seed_scene(FlipGpu *h, const FlipSceneObject *objs, int nobj, uint64_t seed,
+                       double density, double jitter);
+/* particles currently in the handle (liquid and wall) */
+int flipgpu_particle_count(const FlipGpu *h);
+
 int flipgpu_set_particles(FlipGpu *h, int count, const float *pos,
                           const float *vel, const uint8_t *type,
                           const float *nrm, const float *dens, int on_device);
