@@ -41,6 +41,14 @@ class SceneObject(C.Structure):
                 ("c", C.c_float * 3), ("r", C.c_float), ("vel", C.c_float * 3)]
 
 
+class Checkpoint(C.Structure):
+    _fields_ = [("n", C.c_int), ("count", C.c_int), ("max_dens", C.c_float),
+                ("pour_time", C.c_int), ("pour_pos", C.c_float * 2), ("pour_rad", C.c_float),
+                ("pos", C.c_void_p), ("vel", C.c_void_p), ("nrm", C.c_void_p),
+                ("type", C.c_void_p), ("visible", C.c_void_p), ("dens", C.c_void_p),
+                ("press", C.c_void_p), ("wall_normal", C.c_void_p)]
+
+
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
                 ("b2", C.c_double), ("ms", C.c_double), ("warm", C.c_int),
@@ -66,6 +74,12 @@ SIGNATURES = {
     "flipgpu_seed_scene": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_double,
                                      C.c_double]),
     "flipgpu_particle_count": (C.c_int, [C.c_void_p]),
+    "flipgpu_checkpoint_write": (C.c_int, [C.c_char_p, C.c_void_p]),
+    "flipgpu_checkpoint_count": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
+    "flipgpu_checkpoint_read": (C.c_int, [C.c_char_p, C.c_void_p]),
+    "flipgpu_save_state": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_void_p, C.c_float]),
+    "flipgpu_load_state": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_int), C.c_void_p,
+                                     C.POINTER(C.c_float)]),
     "flipgpu_set_particles": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_get_particles": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -170,6 +184,57 @@ def _c(a, dt):
     return None if a is None else np.ascontiguousarray(a, dtype=dt)
 
 
+CHECKPOINT_KEYS = ("pos", "vel", "nrm", "type", "visible", "dens", "press", "wall_normal")
+
+
+def checkpoint_write(path: str, n: int, state: dict):
+    """Write the reference's checkpoint layout (flipgpu_checkpoint_write)
+    from host arrays: pos/vel/nrm [P,3], type/visible u8 [P] (visible
+    optional), dens [P], press [n^3], wall_normal [n^3,4], and the header
+    values max_dens, pour_time, pour_pos, pour_rad."""
+    lib = load()
+    arr = {}
+    for k, dt in (("pos", np.float32), ("vel", np.float32), ("nrm", np.float32),
+                  ("type", np.uint8), ("visible", np.uint8), ("dens", np.float32),
+                  ("press", np.float32), ("wall_normal", np.float32)):
+        arr[k] = None if state.get(k) is None else np.ascontiguousarray(state[k], dtype=dt)
+    c = Checkpoint()
+    c.n, c.count = n, int(arr["type"].shape[0])
+    c.max_dens = float(state.get("max_dens", 0.0))
+    c.pour_time = int(state.get("pour_time", -1))
+    c.pour_pos[:] = [float(v) for v in state.get("pour_pos", (0.0, 0.0))]
+    c.pour_rad = float(state.get("pour_rad", 0.0))
+    for k in CHECKPOINT_KEYS:
+        setattr(c, k, None if arr[k] is None else arr[k].ctypes.data)
+    rc = lib.flipgpu_checkpoint_write(path.encode(), C.byref(c))
+    if rc != 0:
+        raise FlipGpuError(f"checkpoint_write failed: {ERRORS.get(rc, rc)}")
+
+
+def checkpoint_read(path: str, n: int) -> dict:
+    """The content of a reference-layout checkpoint for grid n."""
+    lib = load()
+    cnt = C.c_int(0)
+    rc = lib.flipgpu_checkpoint_count(path.encode(), n, C.byref(cnt))
+    if rc != 0:
+        raise FlipGpuError(f"not a checkpoint of an n={n} grid: {path}")
+    P = cnt.value
+    out = {"pos": np.zeros((P, 3), np.float32), "vel": np.zeros((P, 3), np.float32),
+           "nrm": np.zeros((P, 3), np.float32), "type": np.zeros(P, np.uint8),
+           "visible": np.zeros(P, np.uint8), "dens": np.zeros(P, np.float32),
+           "press": np.zeros(n ** 3, np.float32), "wall_normal": np.zeros((n ** 3, 4), np.float32)}
+    c = Checkpoint()
+    c.n, c.count = n, P
+    for k in CHECKPOINT_KEYS:
+        setattr(c, k, out[k].ctypes.data)
+    rc = lib.flipgpu_checkpoint_read(path.encode(), C.byref(c))
+    if rc != 0:
+        raise FlipGpuError(f"checkpoint_read failed: {ERRORS.get(rc, rc)}")
+    out.update(max_dens=c.max_dens, pour_time=c.pour_time, pour_pos=tuple(c.pour_pos),
+               pour_rad=c.pour_rad, count=P)
+    return out
+
+
 class Simulation:
     """One device-resident simulation (a FlipGpu handle)."""
 
@@ -211,6 +276,22 @@ class Simulation:
 
     def set_scene(self, scene):
         self.set_particles(scene.pos, scene.type, scene.vel, scene.nrm)
+
+    def save_state(self, path, pour_time=-1, pour_pos=(0.0, 0.0), pour_rad=0.12):
+        """The reference's checkpoint file of this state (flipgpu_save_state)."""
+        pp = (C.c_float * 2)(*pour_pos)
+        self._ck(self.lib.flipgpu_save_state(self.h, path.encode(), pour_time, pp, pour_rad),
+                 "save_state")
+
+    def load_state(self, path):
+        """Replace the state from a reference checkpoint; returns the pour
+        settings it carried."""
+        t, r = C.c_int(0), C.c_float(0)
+        pp = (C.c_float * 2)()
+        self._ck(self.lib.flipgpu_load_state(self.h, path.encode(), C.byref(t), pp, C.byref(r)),
+                 "load_state")
+        self.np = int(self.lib.flipgpu_particle_count(self.h))
+        return {"pour_time": t.value, "pour_pos": tuple(pp), "pour_rad": r.value}
 
     def seed_scene(self, objects, seed=0, density=0.5, jitter=0.25):
         """flipgpu_seed_scene: the particles scenes.build(n, objects, seed,

@@ -153,6 +153,46 @@ typedef struct FlipSceneObject {
  * order. At most 16 objects. */
 int flipgpu_seed_scene(FlipGpu *h, const FlipSceneObject *objs, int nobj, uint64_t seed,
                        double density, double jitter);
+/* The reference's checkpoint file (saveState/loadState,
+ * src/flip3D.cpp:453-578), float build, native byte order:
+ *   int nparticle; float max_dens; int pourTime; float pourPos[2];
+ *   float pourRad; nparticle x 72-byte particle records (src/common.h:34-45:
+ *   float p[3], u[3], n[3]; char type, visible, remove, thinparticle;
+ *   float tmp[2][3], m, dens); press, n^3 floats with k fastest;
+ *   wall_normal, n^3 x 4 floats (normal x, y, z and the perimeter flag).
+ * Host arrays; n is not in the file (the reference's N is compiled in) and
+ * fixes the grid sections' size. The writer stores remove = thinparticle = 0,
+ * tmp = 0 (scratch in the reference, partly never initialised), m = 1 and
+ * visible = (type == FLUID) when visible is null. */
+typedef struct FlipCheckpoint {
+  int n;
+  int count;
+  float max_dens;
+  int pour_time;
+  float pour_pos[2];
+  float pour_rad;
+  float *pos, *vel, *nrm; /* [count*3] */
+  uint8_t *type;          /* [count] */
+  uint8_t *visible;       /* [count], may be null */
+  float *dens;            /* [count] */
+  float *press;           /* [n^3] */
+  float *wall_normal;     /* [n^3*4] */
+} FlipCheckpoint;
+int flipgpu_checkpoint_write(const char *path, const FlipCheckpoint *c);
+/* particle count of a checkpoint for grid n (checks the file size) */
+int flipgpu_checkpoint_count(const char *path, int n, int *count);
+/* fills the caller's arrays (sized by flipgpu_checkpoint_count) */
+int flipgpu_checkpoint_read(const char *path, FlipCheckpoint *c);
+/* The handle's state as a checkpoint: particles, pressure, max_dens, and
+ * the wall-normal grid compute_wall_normal (src/flip3D.cpp:75-164) gives
+ * for the current walls, computed on the device. pour_* are carried
+ * through (the benchmark scenes do not pour). */
+int flipgpu_save_state(FlipGpu *h, const char *path, int pour_time, const float *pour_pos,
+                       float pour_rad);
+/* Replace the handle's particles, pressure and max_dens from a checkpoint
+ * (grid n of the handle); pour_* may be null. */
+int flipgpu_load_state(FlipGpu *h, const char *path, int *pour_time, float *pour_pos,
+                       float *pour_rad);
 /* particles currently in the handle (liquid and wall) */
 int flipgpu_particle_count(const FlipGpu *h);
 

@@ -435,3 +435,17 @@ extern "C" float fr_max_density(void) {
   particles.clear();
   return md;
 }
+
+/* flip3D::init's own scene setup (src/flip3D.cpp:649-777: the walls and
+ * damBreakTest objects at N=32, jittered with the keyed draws that replace
+ * rand() in this unit, wall-cell removal, compute_wall_normal) followed by
+ * its saveState (src/flip3D.cpp:453-516): writes render/save/0_scene.dat
+ * under the current directory. Returns the particle count. */
+extern "C" int fr_init_and_save(uint64_t seed) {
+  g_seed = seed;
+  g_rng_step = 0;
+  g_place_count = 0;
+  flip3D::init(0);
+  saveState();
+  return (int)particles.size();
+}

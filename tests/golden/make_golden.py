@@ -235,6 +235,58 @@ def task_mesh_driver(out: str, steps: int = 3):
                         faces_sub=f[sf])
 
 
+CKPT_RECORD = np.dtype([("p", "<f4", 3), ("u", "<f4", 3), ("n", "<f4", 3), ("type", "i1"),
+                        ("visible", "i1"), ("remove", "i1"), ("thin", "i1"),
+                        ("tmp", "<f4", 6), ("m", "<f4"), ("dens", "<f4")])
+
+
+def checkpoint_canonical(raw: bytes, n: int):
+    """Parse a reference checkpoint (src/flip3D.cpp:453-516) and zero the
+    bytes the reference leaves undefined: each record's tmp[2][3] (scratch,
+    partly never initialised) and remove (not set by pushParticle), and the
+    wall normals of cells that are neither wall nor perimeter cells
+    (allocated without initialisation when no particle visits them)."""
+    assert CKPT_RECORD.itemsize == 72
+    count = int(np.frombuffer(raw, "<i4", 1, 0)[0])
+    parts = np.frombuffer(raw, CKPT_RECORD, count, 24).copy()
+    off = 24 + 72 * count
+    press = np.frombuffer(raw, "<f4", n ** 3, off).copy()
+    wn = np.frombuffer(raw, "<f4", 4 * n ** 3, off + 4 * n ** 3).reshape(n ** 3, 4).copy()
+    assert len(raw) == off + 20 * n ** 3
+    wall = np.zeros(n ** 3, bool)
+    w = parts[parts["type"] == 2]["p"]
+    c = np.clip(w * np.float32(n), 0, n - 1).astype(np.int64)
+    wall[(c[:, 0] * n + c[:, 1]) * n + c[:, 2]] = True
+    other = ~wall & (wn[:, 3] != 1.0)
+    wn[other, :3] = 0.0
+    parts["tmp"] = 0.0
+    parts["remove"] = 0
+    canonical = raw[:24] + parts.tobytes() + press.tobytes() + wn.tobytes()
+    return parts, press, wn, canonical
+
+
+def task_checkpoint(out: str):
+    """The reference's own init + saveState at N=32 (its damBreakTest scene):
+    the parsed content and the digest of the canonical bytes."""
+    L = load_ref()
+    L.fr_init_and_save.restype = C.c_int
+    L.fr_init_and_save.argtypes = [C.c_uint64]
+    count = L.fr_init_and_save(SEED)
+    n = L.fr_grid_n()
+    with open(os.path.join("render", "save", "0_scene.dat"), "rb") as f:
+        raw = f.read()
+    parts, press, wn, canonical = checkpoint_canonical(raw, n)
+    assert parts.shape[0] == count
+    hdr = np.frombuffer(raw, "<f4", 6, 0)
+    np.savez_compressed(
+        out, n=n, count=count, max_dens=hdr[1], pour_time=np.frombuffer(raw, "<i4", 1, 8)[0],
+        pour_pos=hdr[3:5], pour_rad=hdr[5], pos=parts["p"], vel=parts["u"], nrm=parts["n"],
+        type=parts["type"].astype(np.uint8), visible=parts["visible"].astype(np.uint8),
+        thin=parts["thin"].astype(np.uint8), m=parts["m"], dens=parts["dens"], press=press,
+        wall_normal=wn, canonical_sha256=hashlib.sha256(canonical).hexdigest(),
+        file_bytes=len(raw))
+
+
 TASKS = {
     "components_n16": lambda out: task_components(out, 16),
     "components_n13": lambda out: task_components(out, 13),
@@ -245,6 +297,7 @@ TASKS = {
     "mesh_n16": lambda out: task_mesh(out, 16),
     "mesh_n13": lambda out: task_mesh(out, 13),
     "mesh_driver_n32": lambda out: task_mesh_driver(out, 3),
+    "checkpoint_n32": task_checkpoint,
 }
 
 
