@@ -392,6 +392,7 @@ int flipgpu_destroy(FlipGpu *h) {
   cudaStreamSynchronize(h->stream);
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->graph) cudaGraphDestroy(h->graph);
+  export_free(h);
   mesh_free(h);
   if (h->wdelta) {
     cudaFree(h->wdelta);

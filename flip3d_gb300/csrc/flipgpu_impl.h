@@ -136,6 +136,7 @@ struct FlipGpu {
 
   float *stage;       /* AoS staging for downloads */
   MeshBufs *mesh;     /* mesher buffers, allocated by the first mesh call */
+  struct ExportJob *exportjob; /* the mesh export in flight (export.cu) */
 
   /* learned warm start (k_unet.cu) */
   FlipUNet *warm;     /* network, or null for the previous-step guess */
@@ -203,6 +204,11 @@ cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, floa
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
 /* stats of the last solve read from the device (for steps run without a
  * host sync) */
+int mesh_download_async(FlipGpu *h, double *vertices, double *normals, int32_t *faces,
+                        int64_t *nv, int64_t *nf);
+/* the asynchronous mesh export of export.cu: join and free */
+int export_join(FlipGpu *h);
+void export_free(FlipGpu *h);
 int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
 int particles_init_device();

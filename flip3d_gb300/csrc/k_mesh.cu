@@ -701,6 +701,25 @@ int mesh_get(FlipGpu *h, double *vertices, double *normals, int32_t *faces, floa
   return e == cudaSuccess ? FLIPGPU_OK : FLIPGPU_ECUDA;
 }
 
+/* counts of the last mesh and, if the pointers are set, its copies into
+ * host memory enqueued on the handle's stream (no synchronisation) */
+int mesh_download_async(FlipGpu *h, double *vertices, double *normals, int32_t *faces,
+                        int64_t *nv, int64_t *nf) {
+  MeshBufs *m = h->mesh;
+  if (!m || !m->valid) return FLIPGPU_EINVAL;
+  *nv = m->nv;
+  *nf = m->nf;
+  cudaError_t e = cudaSuccess;
+  const size_t vb = 3 * (size_t)m->nv * sizeof(double);
+  if (vertices && vb) e = cudaMemcpyAsync(vertices, m->V, vb, cudaMemcpyDeviceToHost, h->stream);
+  if (normals && vb && e == cudaSuccess)
+    e = cudaMemcpyAsync(normals, m->N, vb, cudaMemcpyDeviceToHost, h->stream);
+  if (faces && m->nf && e == cudaSuccess)
+    e = cudaMemcpyAsync(faces, m->F, 3 * (size_t)m->nf * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                        h->stream);
+  return e == cudaSuccess ? FLIPGPU_OK : FLIPGPU_ECUDA;
+}
+
 cudaError_t launch_implicit_points(FlipGpu *h, int count, const float *pts, double *out) {
   if (count == 0) return cudaSuccess;
   FieldConst f;

@@ -74,6 +74,13 @@ SIGNATURES = {
     "flipgpu_seed_scene": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_double,
                                      C.c_double]),
     "flipgpu_particle_count": (C.c_int, [C.c_void_p]),
+    "flipgpu_write_obj": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_int64, C.c_float]),
+    "flipgpu_write_sunflow": (C.c_int, [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_int64, C.c_float]),
+    "flipgpu_export_mesh": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_float, C.c_int,
+                                      C.c_char_p]),
+    "flipgpu_export_wait": (C.c_int, [C.c_void_p]),
     "flipgpu_checkpoint_write": (C.c_int, [C.c_char_p, C.c_void_p]),
     "flipgpu_checkpoint_count": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
     "flipgpu_checkpoint_read": (C.c_int, [C.c_char_p, C.c_void_p]),
@@ -184,6 +191,23 @@ def _c(a, dt):
     return None if a is None else np.ascontiguousarray(a, dtype=dt)
 
 
+EXPORT_OBJ, EXPORT_SUNFLOW = 1, 2
+
+
+def write_mesh_files(obj_path, sunflow_path, vertices, normals, faces, wall_thick):
+    """exporter::write3D's OBJ and Sunflow scene files for a host mesh
+    (either path may be None)."""
+    lib = load()
+    v = np.ascontiguousarray(vertices, np.float64)
+    nv = np.ascontiguousarray(normals, np.float64)
+    f = np.ascontiguousarray(faces, np.int32)
+    args = (v.ctypes.data, nv.ctypes.data, v.size // 3, f.ctypes.data, f.size // 3,
+            float(wall_thick))
+    for path, fn in ((obj_path, lib.flipgpu_write_obj), (sunflow_path, lib.flipgpu_write_sunflow)):
+        if path is not None and fn(path.encode(), *args) != 0:
+            raise FlipGpuError(f"cannot write {path}")
+
+
 CHECKPOINT_KEYS = ("pos", "vel", "nrm", "type", "visible", "dens", "press", "wall_normal")
 
 
@@ -276,6 +300,19 @@ class Simulation:
 
     def set_scene(self, scene):
         self.set_particles(scene.pos, scene.type, scene.vel, scene.nrm)
+
+    def export_mesh(self, directory, frame, wall_thick, formats=3, sunflow_template=None,
+                    wait=True):
+        """Write the last mesh (after mesh()) as the reference's OBJ and/or
+        Sunflow files under directory; asynchronous unless wait."""
+        t = None if sunflow_template is None else sunflow_template.encode()
+        self._ck(self.lib.flipgpu_export_mesh(self.h, directory.encode(), frame, wall_thick,
+                                              formats, t), "export_mesh")
+        if wait:
+            self._ck(self.lib.flipgpu_export_wait(self.h), "export_wait")
+
+    def export_wait(self):
+        self._ck(self.lib.flipgpu_export_wait(self.h), "export_wait")
 
     def save_state(self, path, pour_time=-1, pour_pos=(0.0, 0.0), pour_rad=0.12):
         """The reference's checkpoint file of this state (flipgpu_save_state)."""

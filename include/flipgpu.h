@@ -193,6 +193,30 @@ int flipgpu_save_state(FlipGpu *h, const char *path, int pour_time, const float 
  * (grid n of the handle); pour_* may be null. */
 int flipgpu_load_state(FlipGpu *h, const char *path, int *pour_time, float *pour_pos,
                        float *pour_rad);
+/* The files exporter::write3D writes for a mesh (src/exporter.cpp:70-167),
+ * byte-identical text: write_obj's Wavefront OBJ (vertices
+ * s*(v - wall_thick) with s = 1/(1 - 2 wall_thick), y and z swapped;
+ * normals; faces 1-based as f a//a b//b c//c) and writeSunflow's scene file
+ * (include template.sc; the mesh object with each vertex clamped to
+ * [0.001, 0.999] after the wall offset and scaled by 100/(1 - 2 wall_thick);
+ * 0-based triangles). Host arrays as flipgpu_get_mesh returns them. */
+int flipgpu_write_obj(const char *path, const double *vertices, const double *normals,
+                      int64_t n_vertices, const int32_t *faces, int64_t n_faces,
+                      float wall_thick);
+int flipgpu_write_sunflow(const char *path, const double *vertices, const double *normals,
+                          int64_t n_vertices, const int32_t *faces, int64_t n_faces,
+                          float wall_thick);
+#define FLIPGPU_EXPORT_OBJ 1
+#define FLIPGPU_EXPORT_SUNFLOW 2
+/* Export the last flipgpu_mesh result as dir/obj/<frame>_scene.obj and/or
+ * dir/sunflow/<frame>_scene.sc (plus dir/sunflow/template.sc when
+ * sunflow_template is given). Returns once the download is enqueued; the
+ * formatting and writing run on a host thread. flipgpu_export_wait joins it
+ * and returns its status; the next export, or destroying the handle, joins
+ * it too. */
+int flipgpu_export_mesh(FlipGpu *h, const char *dir, int frame, float wall_thick, int formats,
+                        const char *sunflow_template);
+int flipgpu_export_wait(FlipGpu *h);
 /* particles currently in the handle (liquid and wall) */
 int flipgpu_particle_count(const FlipGpu *h);
 

@@ -449,3 +449,13 @@ extern "C" int fr_init_and_save(uint64_t seed) {
   saveState();
   return (int)particles.size();
 }
+
+/* exporter::write3D (src/exporter.cpp:160-167) on the last fr_mesh /
+ * fr_sim_mesh result: render/obj/<step>_scene.obj and
+ * render/sunflow/{template.sc,<step>_scene.sc} under the current directory. */
+extern "C" void fr_export(int step, float wall_thick) {
+  mkdir("render", 0755);
+  std::vector<Object> objs;
+  std::vector<particle *> parts;
+  exporter::write3D(step, g_mesh_v, g_mesh_n, g_mesh_f, objs, parts, wall_thick);
+}

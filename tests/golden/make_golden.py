@@ -212,6 +212,28 @@ def task_mesh(out: str, n: int):
                         normals=nr, faces=f)
 
 
+def task_export(out: str, n: int = 16, frame: int = 7):
+    """exporter::write3D on the mesh of the mesh_n16 task's scene: digests and
+    sizes of the OBJ and Sunflow scene files it writes."""
+    L = load_ref()
+    L.fr_export.argtypes = [C.c_int, C.c_float]
+    sc = component_scene(n)
+    counts = np.zeros(2, np.int64)
+    L.fr_mesh(n, sc.count, sc.pos, sc.type, np.float32(0.5), counts)
+    v, nr, f = _mesh_arrays(L, counts)
+    wt = np.float32(1.0 / n)
+    L.fr_export(frame, wt)
+    rec = {"n": n, "frame": frame, "wall_thick": wt, "counts": counts}
+    for tag, path in (("obj", f"render/obj/{frame}_scene.obj"),
+                      ("sunflow", f"render/sunflow/{frame}_scene.sc")):
+        raw = open(path, "rb").read()
+        rec[f"{tag}_sha256"] = hashlib.sha256(raw).hexdigest()
+        rec[f"{tag}_bytes"] = len(raw)
+        rec[f"{tag}_head"] = np.frombuffer(raw[:512], np.uint8)
+    rec["mesh_sha256"] = hashlib.sha256(v.tobytes() + nr.tobytes() + f.tobytes()).hexdigest()
+    np.savez_compressed(out, **rec)
+
+
 def task_mesh_driver(out: str, steps: int = 3):
     """The mesh write_mesh makes after `steps` driver steps at N=32: digests
     and subsets (the oracle rebuilds the state by running its own steps)."""
@@ -298,6 +320,7 @@ TASKS = {
     "mesh_n13": lambda out: task_mesh(out, 13),
     "mesh_driver_n32": lambda out: task_mesh_driver(out, 3),
     "checkpoint_n32": task_checkpoint,
+    "export_n16": task_export,
 }
 
 
