@@ -81,6 +81,8 @@ SIGNATURES = {
     "flipgpu_export_mesh": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_float, C.c_int,
                                       C.c_char_p]),
     "flipgpu_export_wait": (C.c_int, [C.c_void_p]),
+    "flipgpu_preview": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "flipgpu_write_bmp": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "flipgpu_checkpoint_write": (C.c_int, [C.c_char_p, C.c_void_p]),
     "flipgpu_checkpoint_count": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
     "flipgpu_checkpoint_read": (C.c_int, [C.c_char_p, C.c_void_p]),
@@ -310,6 +312,18 @@ class Simulation:
                                               formats, t), "export_mesh")
         if wait:
             self._ck(self.lib.flipgpu_export_wait(self.h), "export_wait")
+
+    def preview(self, width=1024, height=700):
+        """write_frame's point-splat image: uint8 [height, width, 4]."""
+        img = np.zeros((height, width, 4), np.uint8)
+        self._ck(self.lib.flipgpu_preview(self.h, img.ctypes.data, width, height, 0), "preview")
+        return img
+
+    def write_preview(self, path, width=1024, height=700):
+        img = self.preview(width, height)
+        if self.lib.flipgpu_write_bmp(path.encode(), img.ctypes.data, width, height) != 0:
+            raise FlipGpuError(f"cannot write {path}")
+        return img
 
     def export_wait(self):
         self._ck(self.lib.flipgpu_export_wait(self.h), "export_wait")

@@ -217,6 +217,15 @@ int flipgpu_write_sunflow(const char *path, const double *vertices, const double
 int flipgpu_export_mesh(FlipGpu *h, const char *dir, int frame, float wall_thick, int formats,
                         const char *sunflow_template);
 int flipgpu_export_wait(FlipGpu *h);
+/* The reference's point-splat preview (write_frame, src/flip3D.cpp:1133-1192)
+ * of the current particles as a width x height RGBA8 buffer (the reference
+ * draws 1024 x 700): liquid particles rotated and projected, each blending
+ * exp(-DENSITY*N/23) of (0.3, 0.5, 0.8) into 2x2 pixels; alpha 255.
+ * rgba is host or device memory (on_device). */
+int flipgpu_preview(FlipGpu *h, uint8_t *rgba, int width, int height, int on_device);
+/* write_bmp (src/write_bmp.cpp): a 24-bit BMP of an RGBA8 buffer, rows in
+ * buffer order. */
+int flipgpu_write_bmp(const char *path, const uint8_t *rgba, int width, int height);
 /* particles currently in the handle (liquid and wall) */
 int flipgpu_particle_count(const FlipGpu *h);
 

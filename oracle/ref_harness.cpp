@@ -459,3 +459,11 @@ extern "C" void fr_export(int step, float wall_thick) {
   std::vector<particle *> parts;
   exporter::write3D(step, g_mesh_v, g_mesh_n, g_mesh_f, objs, parts, wall_thick);
 }
+
+/* write_frame (src/flip3D.cpp:1133-1192) on the driver's particles:
+ * render/preview/frame_<step>.bmp under the current directory. */
+extern "C" void fr_write_frame(void) {
+  mkdir("render", 0755);
+  mkdir("render/preview", 0755);
+  write_frame();
+}

@@ -234,6 +234,24 @@ def task_export(out: str, n: int = 16, frame: int = 7):
     np.savez_compressed(out, **rec)
 
 
+def task_preview(out: str):
+    """write_frame's BMP (1024 x 700, step 0) for two N=32 scenes set up in the
+    driver: digests and sizes."""
+    L = load_ref()
+    n = L.fr_grid_n()
+    md = L.fr_max_density()
+    rec = {"n": n}
+    for tag, sc in (("pool_sphere", scenes.pool_sphere(n, seed=0)),
+                    ("random_s5", scenes.random_scene(n, 5))):
+        L.fr_sim_setup(sc.count, sc.pos, sc.vel, sc.type, sc.nrm, md, SEED, 1e-6)
+        L.fr_write_frame()
+        raw = open(os.path.join("render", "preview", "frame_0.bmp"), "rb").read()
+        rec[f"{tag}_sha256"] = hashlib.sha256(raw).hexdigest()
+        rec[f"{tag}_bytes"] = len(raw)
+        rec[f"{tag}_covered"] = int((np.frombuffer(raw[54:], np.uint8) > 0).sum())
+    np.savez_compressed(out, **rec)
+
+
 def task_mesh_driver(out: str, steps: int = 3):
     """The mesh write_mesh makes after `steps` driver steps at N=32: digests
     and subsets (the oracle rebuilds the state by running its own steps)."""
@@ -321,6 +339,7 @@ TASKS = {
     "mesh_driver_n32": lambda out: task_mesh_driver(out, 3),
     "checkpoint_n32": task_checkpoint,
     "export_n16": task_export,
+    "preview_n32": task_preview,
 }
 
 
