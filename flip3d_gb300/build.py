@@ -21,6 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SOURCES = ["api.cu", "k_sort.cu", "k_particles.cu", "k_grid.cu", "k_pcg.cu", "k_mesh.cu", "k_unet.cu",
            "k_conv_tc.cu", "k_scene.cu", "checkpoint.cu", "export.cu", "k_preview.cu",
+           "autotune.cu",
            "noalloc_sort.cu"]
 FLAGS = {name: ["-fmad=false"] for name in SOURCES}
 

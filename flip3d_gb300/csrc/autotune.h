@@ -1,0 +1,26 @@
+/*
+ * autotune.h — launch-configuration autotuner of libflipgpu.
+ *
+ * A kernel whose results do not depend on its tile shape or schedule (each
+ * output's arithmetic is fixed; only the grouping of work changes) offers a
+ * list of candidate configurations. The first launch for a key (the kernel
+ * and its problem sizes) times every candidate on the caller's stream with
+ * CUDA events (one warm-up launch, then the median of three) and keeps the
+ * fastest; later launches use it. Nothing is tuned while the stream is
+ * being captured into a graph (the default candidate, index 0, runs), and
+ * FLIPGPU_AUTOTUNE=0 or flipgpu_set_autotune(0) turns tuning off.
+ */
+#pragma once
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <string>
+#include <vector>
+
+namespace autotune {
+
+/* index of the configuration to run for key; run(i) launches candidate i */
+int choose(const std::string &key, const std::vector<std::string> &names, cudaStream_t st,
+           const std::function<cudaError_t(int)> &run);
+
+} // namespace autotune

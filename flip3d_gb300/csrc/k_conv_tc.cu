@@ -54,6 +54,12 @@
 #include <algorithm>
 #include <cstdint>
 
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "autotune.h"
 #include "conv_tc.h"
 
 typedef __nv_bfloat16 bf16;
@@ -402,7 +408,10 @@ __global__ void k_conv_tc_pack(int cin, int cout, const float *__restrict__ W,
   out[byte / 2] = __float2bfloat16(W[idx]);
 }
 
-bool tc_plan(int n, int cin, int cout, int batch, TcShape &sh, size_t &smem) {
+/* R_req / S_req > 0 ask for that many lines per unit / pipeline stages
+ * (false if they do not fit); 0 takes the default */
+bool tc_plan(int n, int cin, int cout, int batch, TcShape &sh, size_t &smem, int R_req = 0,
+             int S_req = 0) {
   if (n < 2 || batch < 1 || cin < 16 || cin % 16 || cout < 16 || cout % 16 || cout > 64)
     return false;
   sh = TcShape{};
@@ -415,21 +424,25 @@ bool tc_plan(int n, int cin, int cout, int batch, TcShape &sh, size_t &smem) {
   sh.segs = n / sh.lk;
   sh.P = sh.lk + 2;
   int R = 0, T = 0;
-  if (sh.lk == 128) {
+  auto tiles = [&](int r) { return sh.lk == 128 ? r : (r * sh.P - 2 + 127) / 128; };
+  auto fits = [&](int r) {
+    const int t = tiles(r);
+    return r >= 1 && r <= n && n % r == 0 && t <= 5 && 2 * t * cout <= 512;
+  };
+  if (R_req > 0) {
+    if (!fits(R_req)) return false;
+    R = R_req;
+  } else if (sh.lk == 128) {
     R = 4;
-    T = 4;
   } else {
-    for (int r = 16; r >= 1; r >>= 1) {
-      if (r > n || n % r) continue;
-      const int t = (r * sh.P - 2 + 127) / 128;
-      if (2 * t * cout <= 512 && t <= 5) {
+    for (int r = 16; r >= 1; r >>= 1)
+      if (fits(r)) {
         R = r;
-        T = t;
         break;
       }
-    }
   }
   if (!R) return false;
+  T = tiles(R);
   sh.R = R;
   sh.T = T;
   sh.nslab = (n + R - 1) / R;
@@ -439,8 +452,9 @@ bool tc_plan(int n, int cin, int cout, int batch, TcShape &sh, size_t &smem) {
   sh.w_bytes = 9u * (uint32_t)cout * 32u;
   sh.stage_bytes = 2u * sh.plane_stride + ((sh.w_bytes + 127u) & ~127u);
   const size_t fixed = TC_GUARD + sizeof(TcCtl) + 128;
-  int S = TC_STAGES;
-  while (S > 2 && (size_t)S * sh.stage_bytes + fixed > TC_SMEM_MAX) S--;
+  int S = S_req > 0 ? S_req : TC_STAGES;
+  if (S_req > 0 && (S_req < 2 || S_req > TC_STAGES)) return false;
+  while (S_req <= 0 && S > 2 && (size_t)S * sh.stage_bytes + fixed > TC_SMEM_MAX) S--;
   if ((size_t)S * sh.stage_bytes + fixed > TC_SMEM_MAX) return false;
   sh.stages = S;
   uint32_t nc = 32;
@@ -495,11 +509,33 @@ int conv_tc_init_device() {
   return 0;
 }
 
-cudaError_t conv_tc_launch(cudaStream_t st, int n, int batch, int cin, int cout, const bf16 *X,
-                           const bf16 *Wtc, const float *bias, bf16 *Y, int relu, int *err) {
+namespace {
+
+/* the plan's (lines per unit, stages) choices for the autotuner; the
+ * default first */
+std::vector<std::pair<int, int>> tc_candidates(int n, int cin, int cout, int batch) {
+  std::vector<std::pair<int, int>> out;
   TcShape sh;
   size_t smem;
-  if (!tc_plan(n, cin, cout, batch, sh, smem)) return cudaErrorInvalidValue;
+  if (!tc_plan(n, cin, cout, batch, sh, smem)) return out;
+  out.push_back({sh.R, sh.stages});
+  const int rs[] = {1, 2, 4, 8, 16};
+  const int ss[] = {3, 4, 6};
+  for (int r : rs)
+    for (int s : ss) {
+      if (r == sh.R && s == sh.stages) continue;
+      TcShape c;
+      if (tc_plan(n, cin, cout, batch, c, smem, r, s)) out.push_back({r, s});
+    }
+  return out;
+}
+
+cudaError_t tc_launch_one(cudaStream_t st, int n, int batch, int cin, int cout, const bf16 *X,
+                          const bf16 *Wtc, const float *bias, bf16 *Y, int relu, int *err,
+                          int R, int S) {
+  TcShape sh;
+  size_t smem;
+  if (!tc_plan(n, cin, cout, batch, sh, smem, R, S)) return cudaErrorInvalidValue;
   if (conv_tc_init_device() != 0) return cudaErrorInvalidDeviceFunction;
   PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
   if (!enc) return cudaErrorNotSupported;
@@ -528,4 +564,27 @@ cudaError_t conv_tc_launch(cudaStream_t st, int n, int batch, int cin, int cout,
   default: k_conv_tc<5><<<grid, TC_THREADS, smem, st>>>(map, sh, Wtc, bias, Y, relu, err); break;
   }
   return cudaGetLastError();
+}
+
+} // namespace
+
+/* lines per unit (the tile shape) and pipeline depth picked by the
+ * autotuner per (n, cin, cout, batch); the result does not depend on them */
+cudaError_t conv_tc_launch(cudaStream_t st, int n, int batch, int cin, int cout, const bf16 *X,
+                           const bf16 *Wtc, const float *bias, bf16 *Y, int relu, int *err) {
+  const auto cands = tc_candidates(n, cin, cout, batch);
+  if (cands.empty()) return cudaErrorInvalidValue;
+  std::vector<std::string> names;
+  char buf[64];
+  for (const auto &c : cands) {
+    snprintf(buf, sizeof buf, "R=%d S=%d", c.first, c.second);
+    names.push_back(buf);
+  }
+  snprintf(buf, sizeof buf, "conv_tc n=%d cin=%d cout=%d batch=%d", n, cin, cout, batch);
+  const int pick = autotune::choose(buf, names, st, [&](int i) {
+    return tc_launch_one(st, n, batch, cin, cout, X, Wtc, bias, Y, relu, err, cands[i].first,
+                         cands[i].second);
+  });
+  return tc_launch_one(st, n, batch, cin, cout, X, Wtc, bias, Y, relu, err, cands[pick].first,
+                       cands[pick].second);
 }

@@ -82,6 +82,8 @@ SIGNATURES = {
                                       C.c_char_p]),
     "flipgpu_export_wait": (C.c_int, [C.c_void_p]),
     "flipgpu_preview": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "flipgpu_set_autotune": (C.c_int, [C.c_int]),
+    "flipgpu_autotune_report": (C.c_int, [C.c_char_p, C.c_int]),
     "flipgpu_write_bmp": (C.c_int, [C.c_char_p, C.c_void_p, C.c_int, C.c_int]),
     "flipgpu_checkpoint_write": (C.c_int, [C.c_char_p, C.c_void_p]),
     "flipgpu_checkpoint_count": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
@@ -194,6 +196,19 @@ def _c(a, dt):
 
 
 EXPORT_OBJ, EXPORT_SUNFLOW = 1, 2
+
+
+def set_autotune(on: int):
+    """flipgpu_set_autotune: 0 off, 1 on, -1 on and forget decisions."""
+    load().flipgpu_set_autotune(int(on))
+
+
+def autotune_report() -> str:
+    lib = load()
+    size = lib.flipgpu_autotune_report(None, 0)
+    buf = C.create_string_buffer(size + 1)
+    lib.flipgpu_autotune_report(buf, size + 1)
+    return buf.value.decode()
 
 
 def write_mesh_files(obj_path, sunflow_path, vertices, normals, faces, wall_thick):

@@ -176,7 +176,8 @@ def main(argv=None):
     if a.time_predict:
         out = {path: time_predict(a.time_predict, a.init, reps=2 if a.time_predict >= 256 else 10,
                                   tcgen05=path == "tcgen05") for path in ("tcgen05", "mma.sync")}
-        print(json.dumps({"n": a.time_predict, "predict_ms": out}))
+        print(json.dumps({"n": a.time_predict, "predict_ms": out,
+                          "autotune": gpu.autotune_report().splitlines()}))
         return
     t0 = time.perf_counter()
     train_seeds = range(1000 + a.seed, 1000 + a.seed + a.scenes)

@@ -226,6 +226,15 @@ int flipgpu_preview(FlipGpu *h, uint8_t *rgba, int width, int height, int on_dev
 /* write_bmp (src/write_bmp.cpp): a 24-bit BMP of an RGBA8 buffer, rows in
  * buffer order. */
 int flipgpu_write_bmp(const char *path, const uint8_t *rgba, int width, int height);
+/* The launch-configuration autotuner: kernels whose results do not depend
+ * on their tile shape or schedule (the U-Net's tcgen05 convolutions: lines
+ * per unit and pipeline depth) time their candidates on first use per
+ * problem size and keep the fastest. on = 0 turns tuning off (defaults run),
+ * 1 on (the default; FLIPGPU_AUTOTUNE=0 in the environment starts it off),
+ * -1 on and forgets the decisions made so far. The report is one line per
+ * key: the choice and every candidate's median ms; returns its length. */
+int flipgpu_set_autotune(int on);
+int flipgpu_autotune_report(char *buf, int len);
 /* particles currently in the handle (liquid and wall) */
 int flipgpu_particle_count(const FlipGpu *h);
 

@@ -206,6 +206,31 @@ def test_trained_warm_start_on_heldout_scenes(gpu, torch):
     assert res["learned_iters"] <= res["plain_iters"] + 1.0
 
 
+def test_autotuned_convolutions_match_the_defaults(gpu, torch):
+    """The autotuner picks each tcgen05 convolution's lines per unit and
+    pipeline depth on first use; every choice computes the same output, so
+    the tuned network equals the default configuration's bit for bit."""
+    n = 64
+    rng = np.random.default_rng(3)
+    A = torch.tensor((rng.random(n ** 3) < 0.6).astype(np.uint8), device="cuda")
+    b, x0, r0 = (torch.tensor(rng.normal(0, 1, n ** 3).astype(np.float32), device="cuda")
+                 for _ in range(3))
+    net = gpu.UNet(seed=8)
+    outs = []
+    for mode in (-1, 0):
+        gpu.set_autotune(mode)
+        d = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        net.predict(n, 1, A.data_ptr(), b.data_ptr(), x0.data_ptr(), r0.data_ptr(), d.data_ptr())
+        torch.cuda.synchronize()
+        outs.append(d.cpu().numpy())
+    gpu.set_autotune(1)
+    rep = gpu.autotune_report()
+    print(rep)
+    assert "conv_tc n=64" in rep
+    assert np.array_equal(outs[0], outs[1])
+
+
 @pytest.mark.parametrize("n,batch", [(128, 1), (32, 2)])
 def test_tcgen05_forward_matches_mma_sync(gpu, torch, n, batch):
     """The tcgen05 convolutions (TMA-staged slabs, TMEM accumulators) give
