@@ -338,7 +338,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->repo_draw, cap) AL(h->repo_res, cap) AL(h->repo_old, cap)
   AL(h->repo_cnt, cap + 1) AL(h->repo_start, cap + 1) AL(h->repo_list, cap)
   AL(h->repo_state, cap)
-  h->nbx = (p->n + 7) / 8;
+  h->nbx = (p->n + 15) / 16; /* 16^3 wavefront bricks (k_pcg.cu BRK) */
   h->nbricks = h->nbx * h->nbx * h->nbx;
   AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
   AL(h->ticket, 1) AL(h->brick_part, h->nbricks) AL(h->dstep, 1)

@@ -1384,24 +1384,26 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
  * the cell flag instead of the value, plus the MIC(0) modification weighted
  * by tau; and its triangular solves (src/solver.cpp:141-180). A cell depends
  * on its -x/-y/-z neighbours (forward) or +x/+y/+z neighbours (backward), so
- * cells on one plane i+j+k are independent. The grid is cut into 8^3 bricks;
- * a brick depends on the three bricks before it along the axes. Bricks are
- * handed to warps by an atomic ticket in wavefront order; a warp waits (bounded)
- * for its three predecessors' epoch flags, loads the brick and its halo into
- * shared memory, runs the 22 intra-brick planes separated by __syncwarp, writes
- * back and publishes its flag. Tickets are taken in an order where every
- * dependency has a smaller ticket, so a waiting warp only waits for warps
- * that already run. */
-constexpr int BRK = 8;
+ * cells on one plane i+j+k are independent. The grid is cut into 16^3
+ * bricks; a brick depends on the three bricks before it along the axes.
+ * Bricks are handed to whole CTAs by an atomic ticket in wavefront order; a
+ * CTA waits (bounded) for its three predecessors' epoch flags, loads the
+ * brick and its halo into shared memory, runs the 46 intra-brick planes
+ * separated by __syncthreads (one cell per thread per plane), writes back and
+ * publishes its flag. Tickets are taken in an order where every dependency
+ * has a smaller ticket, so a waiting CTA only waits for CTAs that already
+ * run. A 16^3 brick gives 3(n/16)-2 brick levels per sweep (22 at n = 128)
+ * where 8^3 warp bricks gave 46; each value is computed from the same
+ * neighbours in the same order, so the brick size does not change it. */
+constexpr int BRK = 16;
 constexpr int BRK3 = BRK * BRK * BRK;
 constexpr int HB = BRK + 2;
 constexpr int HB3 = HB * HB * HB;
 constexpr int NPLANES = 3 * BRK - 2;
-constexpr int WARPS_PER_CTA = CG_BLOCK / 32;
 constexpr unsigned long long FLAG_SPIN_LIMIT = 1ull << 24;
 
 struct BrickPlanes {
-  unsigned short cell[BRK3];       /* (i<<6)|(j<<3)|k sorted by i+j+k */
+  unsigned short cell[BRK3];       /* (i<<8)|(j<<4)|k sorted by i+j+k */
   unsigned short start[NPLANES + 1];
 };
 __constant__ BrickPlanes c_planes;
@@ -1423,10 +1425,10 @@ __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-/* Lane 0 waits (bounded) until flag >= epoch with acquire loads; the warp
- * barrier and fence then order the other lanes' loads after it. */
+/* Thread 0 waits (bounded) until flag >= epoch with acquire loads; the block
+ * barrier and fence then order the other threads' loads after it. */
 __device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, int *iflags) {
-  if ((threadIdx.x & 31) == 0) {
+  if (threadIdx.x == 0) {
     unsigned long long spins = 0;
     while (ld_acquire(flag) < epoch) {
       if (++spins > FLAG_SPIN_LIMIT) {
@@ -1436,15 +1438,16 @@ __device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, 
       __nanosleep(64);
     }
   }
-  __syncwarp();
+  __syncthreads();
   __threadfence();
 }
 
-/* kind: 0 build the factor, 1 forward solve, 2 backward solve */
+/* kind: 0 build the factor, 1 forward solve, 2 backward solve; the whole
+ * CTA works on one brick */
 __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl_tab, int brick,
                            int kind, unsigned epoch_f, unsigned epoch_b, const float *r,
                            float *qz) {
-  const int lane = threadIdx.x & 31;
+  const int tid = threadIdx.x;
   const int n = a.s.n, nbx = a.nbx;
   const int BI = brick / (nbx * nbx), BJ = (brick / nbx) % nbx, BK = brick % nbx;
   const int i0 = BI * BRK, j0 = BJ * BRK, k0 = BK * BRK;
@@ -1456,11 +1459,12 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl
   /* All loads of a phase are issued unconditionally and together (the
    * fluid mask is applied afterwards), so a phase costs one L2 round trip
    * instead of one per cell. */
-  constexpr int OWN = BRK3 / 32;       /* own cells per lane */
-  constexpr int HALO = 3 * BRK * BRK / 32; /* halo cells per lane */
+  constexpr int OWN = BRK3 / CG_BLOCK;            /* own cells per thread */
+  constexpr int HALO = 3 * BRK * BRK / CG_BLOCK;  /* halo cells per thread */
+  static_assert(OWN * CG_BLOCK == BRK3 && HALO * CG_BLOCK == 3 * BRK * BRK, "brick tiling");
   auto own_cell = [&](int u, int &h, size_t &c, bool &in) {
-    int t = lane + 32 * u;
-    int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
+    int t = tid + CG_BLOCK * u;
+    int bi = t >> 8, bj = (t >> 4) & 15, bk = t & 15;
     h = hidx(bi, bj, bk);
     in = inside(i0 + bi, j0 + bj, k0 + bk);
     c = in ? cidx(i0 + bi, j0 + bj, k0 + bk) : 0;
@@ -1528,7 +1532,7 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl
     int ha[HALO];
 #pragma unroll
     for (int u = 0; u < HALO; u++) {
-      int t = lane + 32 * u;
+      int t = tid + CG_BLOCK * u;
       int face = t / (BRK * BRK), uu = (t / BRK) % BRK, w = t % BRK;
       /* face 0: (hf,uu,w), face 1: (uu,hf,w), face 2: (uu,w,hf) */
       int bi = face == 0 ? hf : uu, bj = face == 1 ? hf : (face == 0 ? uu : w),
@@ -1549,13 +1553,13 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl
       sm.v[ha[u]] = f ? va[u] : 0.0f;
     }
   }
-  __syncwarp();
+  __syncthreads();
   const float tau = a.mic_tau;
   for (int pl = 0; pl < NPLANES; pl++) {
     const int d = kind == 2 ? NPLANES - 1 - pl : pl;
-    for (int e = pl_tab.start[d] + lane; e < pl_tab.start[d + 1]; e += 32) {
+    for (int e = pl_tab.start[d] + tid; e < pl_tab.start[d + 1]; e += CG_BLOCK) {
       unsigned cc = pl_tab.cell[e];
-      int bi = cc >> 6, bj = (cc >> 3) & 7, bk = cc & 7;
+      int bi = cc >> 8, bj = (cc >> 4) & 15, bk = cc & 15;
       int h = hidx(bi, bj, bk);
       if (!sm.fl[h]) continue;
       const int hm[3] = {hidx(bi - 1, bj, bk), hidx(bi, bj - 1, bk), hidx(bi, bj, bk - 1)};
@@ -1593,12 +1597,12 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl
         sm.v[h] = (sm.v[h] + sm.p[h] * t) * sm.p[h];
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
   /* write back, per-brick z.r for the backward solve, publish */
   FF zr = ff_zero();
-  for (int t = lane; t < BRK3; t += 32) {
-    int bi = t >> 6, bj = (t >> 3) & 7, bk = t & 7;
+  for (int t = tid; t < BRK3; t += CG_BLOCK) {
+    int bi = t >> 8, bj = (t >> 4) & 15, bk = t & 15;
     int i = i0 + bi, j = j0 + bj, k = k0 + bk;
     int h = hidx(bi, bj, bk);
     if (!inside(i, j, k)) continue;
@@ -1611,32 +1615,35 @@ __device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl
     }
   }
   if (kind == 2) {
-    for (int o = 16; o > 0; o >>= 1) zr = ff_merge(zr, ff_shfl_down(zr, o));
-    if (lane == 0) a.brick_part[brick] = make_float2(zr.hi, zr.lo);
+    const FF tot = block_sum_ff<CG_BLOCK>(zr);
+    if (tid == 0) a.brick_part[brick] = make_float2(tot.hi, tot.lo);
   }
   __threadfence();
-  __syncwarp();
-  if (lane == 0) st_release((kind == 2 ? a.bflag : a.fflag) + brick, kind == 2 ? epoch_b : epoch_f);
+  __syncthreads();
+  if (tid == 0) st_release((kind == 2 ? a.bflag : a.fflag) + brick, kind == 2 ? epoch_b : epoch_f);
 }
 
 /* Run one factor build (tasks = nbricks) or one forward+backward apply
- * (tasks = 2*nbricks) over the ticket counter. */
-__device__ void wavefront(const CgArgs &a, BrickSmem *sm_all, const BrickPlanes &pl_tab,
-                          bool build, unsigned epoch_f, unsigned epoch_b, const float *r,
-                          float *qz) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  BrickSmem &sm = sm_all[warp];
+ * (tasks = 2*nbricks) over the ticket counter, one brick per CTA at a time. */
+__device__ void wavefront(const CgArgs &a, BrickSmem *sm, const BrickPlanes &pl_tab, bool build,
+                          unsigned epoch_f, unsigned epoch_b, const float *r, float *qz) {
+  __shared__ unsigned s_ticket;
+  __shared__ int s_stop;
   const unsigned tasks = build ? (unsigned)a.nbricks : 2u * (unsigned)a.nbricks;
   while (true) {
-    unsigned t = 0;
-    if (lane == 0) t = atomicAdd(a.ticket, 1u);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t >= tasks) break;
-    if (*(volatile int *)(a.iflags + IF_TIMEOUT)) break;
+    if (threadIdx.x == 0) {
+      s_ticket = atomicAdd(a.ticket, 1u);
+      s_stop = *(volatile int *)(a.iflags + IF_TIMEOUT);
+    }
+    __syncthreads();
+    const unsigned t = s_ticket;
+    const int stop = s_stop;
+    __syncthreads(); /* every thread has read the ticket before the next one overwrites it */
+    if (t >= tasks || stop) break;
     if (t < (unsigned)a.nbricks)
-      brick_task(a, sm, pl_tab, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
+      brick_task(a, *sm, pl_tab, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
     else
-      brick_task(a, sm, pl_tab, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r,
+      brick_task(a, *sm, pl_tab, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r,
                  qz);
   }
 }
@@ -2162,7 +2169,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   return FLIPGPU_OK;
 }
 
-size_t ic_smem_bytes() { return sizeof(BrickSmem) * WARPS_PER_CTA; }
+size_t ic_smem_bytes() { return sizeof(BrickSmem); }
 
 /* Intra-brick plane lists, uploaded once per device. */
 int ic_init_device() {
@@ -2177,7 +2184,7 @@ int ic_init_device() {
     for (int i = 0; i < BRK; i++)
       for (int j = 0; j < BRK; j++)
         for (int k = 0; k < BRK; k++)
-          if (i + j + k == d) bp.cell[e++] = (unsigned short)((i << 6) | (j << 3) | k);
+          if (i + j + k == d) bp.cell[e++] = (unsigned short)((i << 8) | (j << 4) | k);
   }
   bp.start[NPLANES] = (unsigned short)e;
   if (cudaMemcpyToSymbol(c_planes, &bp, sizeof bp) != cudaSuccess) return -1;

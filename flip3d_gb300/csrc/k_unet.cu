@@ -293,23 +293,24 @@ __global__ void k_wgrad_reduce(int nchunks, int wcount, int cout, const float *_
 /* ------------------------------------------------------------------ elementwise */
 
 /* per sample and block: sums over liquid cells of b^2, r0^2, x0^2 and the
- * liquid count */
+ * liquid count; each thread sums its cells in FP32 (FP64 arithmetic is a
+ * small fraction of FP32's on this GPU), the block tree is FP64 */
 __global__ void k_sample_sums(size_t n3, const uint8_t *__restrict__ A, const float *__restrict__ b,
                               const float *__restrict__ r0, const float *__restrict__ x0,
                               double *__restrict__ part) {
   __shared__ double sh[EBLK][4];
   const size_t s = blockIdx.y;
-  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  float a[4] = {0.0f, 0.0f, 0.0f, 0.0f};
   for (size_t v = (size_t)blockIdx.x * EBLK + threadIdx.x; v < n3; v += (size_t)RB * EBLK) {
     const size_t i = s * n3 + v;
     if (A[i] != CELL_FLUID) continue;
-    const double bb = b[i], rr = r0[i], xx = x0[i];
-    a[0] += bb * bb;
-    a[1] += rr * rr;
-    a[2] += xx * xx;
-    a[3] += 1.0;
+    const float bb = b[i], rr = r0[i], xx = x0[i];
+    a[0] = fmaf(bb, bb, a[0]);
+    a[1] = fmaf(rr, rr, a[1]);
+    a[2] = fmaf(xx, xx, a[2]);
+    a[3] += 1.0f;
   }
-  for (int q = 0; q < 4; q++) sh[threadIdx.x][q] = a[q];
+  for (int q = 0; q < 4; q++) sh[threadIdx.x][q] = (double)a[q];
   __syncthreads();
   for (int w = EBLK / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w)
@@ -408,25 +409,25 @@ __global__ void k_pool_bwd(int n, int C, int batch, const bf16 *__restrict__ dP,
   dX[idx] = __float2bfloat16(g);
 }
 
-/* U[v] = [coarse[parent(v)] (C1) | skip[v] (C2)] */
+/* U[v] = [coarse[parent(v)] (C1) | skip[v] (C2)]; one thread per 8 channels
+ * of a cell, 32-bit index arithmetic (n^3 * batch * C/8 < 2^32) */
 __global__ void k_up_cat(int n, int C1, int C2, int batch, const bf16 *__restrict__ coarse,
                          const bf16 *__restrict__ skip, bf16 *__restrict__ U) {
-  const int nc_ = n / 2, C = C1 + C2;
-  const size_t n3 = (size_t)n * n * n, nc3 = (size_t)nc_ * nc_ * nc_;
-  const size_t idx = (size_t)blockIdx.x * EBLK + threadIdx.x;
-  if (idx >= n3 * batch * (C / 8)) return;
-  const int q = (int)(idx % (C / 8));
-  const size_t vc = idx / (C / 8);
-  const size_t s = vc / n3, v = vc % n3;
+  const unsigned nc_ = (unsigned)n / 2, C = (unsigned)(C1 + C2), C8 = C / 8, un = (unsigned)n;
+  const unsigned n3 = un * un * un, nc3 = nc_ * nc_ * nc_;
+  const unsigned idx = blockIdx.x * EBLK + threadIdx.x;
+  if (idx >= n3 * (unsigned)batch * C8) return;
+  const unsigned q = idx % C8, vc = idx / C8;
+  const unsigned s = vc / n3, v = vc - s * n3;
   uint4 val;
-  if (q * 8 < C1) {
-    const int i = (int)(v / ((size_t)n * n)), j = (int)((v / n) % n), k = (int)(v % n);
-    const size_t p = ((size_t)(i / 2) * nc_ + j / 2) * nc_ + k / 2;
-    val = *reinterpret_cast<const uint4 *>(coarse + (s * nc3 + p) * C1 + q * 8);
+  if (q * 8 < (unsigned)C1) {
+    const unsigned k = v % un, t = v / un, j = t % un, i = t / un;
+    const unsigned p = ((i / 2) * nc_ + j / 2) * nc_ + k / 2;
+    val = *reinterpret_cast<const uint4 *>(coarse + ((size_t)s * nc3 + p) * C1 + q * 8);
   } else {
-    val = *reinterpret_cast<const uint4 *>(skip + (s * n3 + v) * C2 + (q * 8 - C1));
+    val = *reinterpret_cast<const uint4 *>(skip + ((size_t)s * n3 + v) * C2 + (q * 8 - C1));
   }
-  *reinterpret_cast<uint4 *>(U + (s * n3 + v) * C + q * 8) = val;
+  *reinterpret_cast<uint4 *>(U + ((size_t)s * n3 + v) * C + q * 8) = val;
 }
 
 /* dCoarse[p][c] = sum over the eight children of dU[child][c], c < C1 */
