@@ -209,7 +209,7 @@ int flipgpu_save_state(FlipGpu *h, const char *path, int pour_time, const float 
                             h->stream) == cudaSuccess;
   float *cx[3] = {h->nx, h->ny, h->nz};
   std::vector<float> comp(np);
-  for (int d = 0; ok && d < 3; d++) {
+  for (int d = 0; ok && np > 0 && d < 3; d++) {
     ok = cudaMemcpyAsync(comp.data(), cx[d], np * sizeof(float), cudaMemcpyDeviceToHost,
                          h->stream) == cudaSuccess &&
          cudaStreamSynchronize(h->stream) == cudaSuccess;

@@ -596,7 +596,7 @@ cudaError_t mesh_run_impl(FlipGpu *h, int64_t *nverts, int64_t *nfaces) {
   uint32_t nv = 0, nt = 0;
   MCK(read_u32(h, m->vbase + nn, &nv));
   MCK(read_u32(h, m->tbase + ncell, &nt));
-  if (nv > m->vcap) {
+  if (nv >= m->vcap) { /* also the first time: ccnt[nv] is written even when nv = 0 */
     size_t cap = nv + nv / 4 + 1024;
     MCK(dalloc_n(m->vf, 3 * cap));
     MCK(dalloc_n(m->V, 3 * cap));
@@ -607,7 +607,7 @@ cudaError_t mesh_run_impl(FlipGpu *h, int64_t *nverts, int64_t *nfaces) {
     MCK(dalloc_n(m->cbase, cap + 1));
     m->vcap = cap;
   }
-  if (nt > m->tcap) {
+  if (nt >= m->tcap) {
     size_t cap = nt + nt / 4 + 1024;
     MCK(dalloc_n(m->T, 3 * cap));
     MCK(dalloc_n(m->TN, 3 * cap));
@@ -637,7 +637,7 @@ cudaError_t mesh_run_impl(FlipGpu *h, int64_t *nverts, int64_t *nfaces) {
   MCK(scan_exclusive_tmp(h, m->keep, m->fbase, (size_t)nt + 1, m->tmp, m->tmp_blocks));
   uint32_t nf = 0;
   MCK(read_u32(h, m->fbase + nt, &nf));
-  if (nf > m->fcap) {
+  if (nf >= m->fcap) {
     size_t cap = nf + nf / 4 + 1024;
     MCK(dalloc_n(m->conn, 6 * cap));
     MCK(dalloc_n(m->F, 3 * cap));

@@ -129,7 +129,7 @@ int flipgpu_preview(FlipGpu *h, uint8_t *rgba, int width, int height, int on_dev
     k_preview_resolve<<<(unsigned)((npix + PBLK - 1) / PBLK), PBLK, 0, h->stream>>>(c, cnt, out);
     e = cudaGetLastError();
   }
-  FG_LAUNCHED(h, 2);
+  FG_LAUNCHED(h, h->np > 0 ? 2 : 1);
   if (e == cudaSuccess && !on_device)
     e = cudaMemcpyAsync(rgba, dbuf, 4 * npix, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
