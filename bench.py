@@ -72,18 +72,20 @@ def run_batch(args):
     # together
     b = gpu.Batch(sims)
     b.capture()
+    clocks = ClockSampler(0)
+    clocks.start()
+    clocks.wait_first()
     for _ in range(args.warmup):
         b.step()
     b.sync()
-    clocks = ClockSampler(0)
-    clocks.start()
     launches0 = sum(s.launches for s in sims)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         b.step()
     b.sync()
-    t_bat = time.perf_counter() - t0
-    clk = clocks.stop()
+    t1 = time.perf_counter()
+    t_bat = t1 - t0
+    clk = clocks.stop((t0, t1))
     launches = sum(s.launches for s in sims) - launches0
     value = P * args.steps / t_bat
     sizes = {}
@@ -175,11 +177,28 @@ def hbm_peak():
         return FALLBACK_HBM, "fallback"
 
 
-def stage_bytes(stage, P, n, iters):
+def liquid_chunk_cells(A):
+    """Cells of the 128-cell chunks (32 quads of the x-major order) that hold
+    liquid: the cells the single-reduction PCG sweeps every iteration."""
+    import numpy as np
+
+    f = np.asarray(A).reshape(-1) == 1
+    pad = (-f.size) % 128
+    if pad:
+        f = np.concatenate([f, np.zeros(pad, dtype=bool)])
+    return int(f.reshape(-1, 128).any(axis=1).sum()) * 128
+
+
+def stage_bytes(stage, P, n, iters, sweep_cells=None):
     """Algorithmic bytes of one call of a stage: every input read once and
-    every output written once, nothing else."""
+    every output written once, nothing else. The PCG solve is one setup pass
+    over the grid (A, x, b, M^-1 read, 13 B; r and x written, 8 B) and per
+    iteration 49 B per cell of the liquid chunks (sweep_cells; the whole
+    grid when not given): A 1 + diagonal 4 + M^-1 4 + U, Wt, St, p, x
+    4 each read, U, Wt, St, p, x 4 each written."""
     C = n ** 3
     F = 3 * (n + 1) * n * n
+    cells = C if sweep_cells is None else sweep_cells
     table = {
         # count: pos 12 r, key 4 w, rank 4 w; scatter: key+rank 8 r, perm 4 w;
         # cell counts/starts 3*4*C; payload: perm 4 + pos 12 + vel 12 + type 1 + dens 4 r,
@@ -189,7 +208,7 @@ def stage_bytes(stage, P, n, iters):
         "mark_water": P * 8 + 4 * C + 5 * C,
         "p2g": P * 32 + 4 * C + C + 2 * 4 * F,
         "divergence": C + 4 * F + 4 * C,
-        "solve": max(iters, 1) * 41 * C,
+        "solve": 21 * C + max(iters, 1) * 49 * cells,
         "gradient": 4 * F * 2 + 9 * C,
         "extrapolate": 4 * F * 3 + C,
         "g2p_flip": P * (12 + 1 + 12 + 12) + 2 * 4 * F,
@@ -201,7 +220,11 @@ def stage_bytes(stage, P, n, iters):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms. Started
+    before the warm-up (its first sample is awaited, so the tool's start-up
+    stays out of the timed region); stop(window) keeps the samples that
+    arrived during the timed window, or the two nearest to it when the
+    window is shorter than the sampling period."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -225,18 +248,30 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
-    def stop(self):
+    def wait_first(self, timeout=5.0):
+        t0 = time.perf_counter()
+        while self.proc and not self.rows and time.perf_counter() - t0 < timeout:
+            time.sleep(0.01)
+
+    def stop(self, window=None):
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
+        rows = self.rows
+        if window is not None and rows:
+            a, b = window
+            inside = [r for r in rows if a <= r[0] <= b + 0.25]
+            rows = inside if inside else sorted(
+                rows, key=lambda r: min(abs(r[0] - a), abs(r[0] - b)))[:2]
+        rows = [r[1] for r in rows]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        for r in rows:
             try:
                 sm.append(float(r[1]))
                 mx.append(float(r[2]))
@@ -379,15 +414,17 @@ def main():
     stream = torch.cuda.Stream()
     sim.set_stream(stream.cuda_stream)
     solve_ms, iters, true_rel = [], [], []
+    clocks = ClockSampler(local)
+    clocks.start()
+    clocks.wait_first()
     for _ in range(args.warmup):
         sim.step()
     barrier()
-    clocks = ClockSampler(local)
-    clocks.start()
     launches0 = sim.launches
     start_ev = torch.cuda.Event(enable_timing=True)
     end_ev = torch.cuda.Event(enable_timing=True)
     stream.synchronize()
+    t_clk0 = time.perf_counter()
     start_ev.record(stream)
     for _ in range(args.steps):
         st = sim.step()
@@ -397,8 +434,9 @@ def main():
             true_rel.append((st.r2_true / st.b2) ** 0.5)
     end_ev.record(stream)
     stream.synchronize()
+    t_clk1 = time.perf_counter()
     barrier()
-    clk = clocks.stop()
+    clk = clocks.stop((t_clk0, t_clk1))
     launches = sim.launches - launches0
     ms = start_ev.elapsed_time(end_ev)
     if world > 1:
@@ -417,7 +455,8 @@ def main():
     dom = max(prof, key=lambda s: prof[s][0])
     dom_ms = prof[dom][0] / max(prof[dom][1], 1)
     it_prof = int(st.iterations)
-    nbytes = stage_bytes(dom, P, args.n, it_prof)
+    sweep_cells = liquid_chunk_cells(sim.get_grid()[1])
+    nbytes = stage_bytes(dom, P, args.n, it_prof, sweep_cells)
     peak, peak_kind = hbm_peak()
     achieved = nbytes / (dom_ms / 1e3) / 1e9
     traffic = measured_traffic(dom, args.n)
@@ -487,7 +526,11 @@ def main():
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind, "algorithmic_bytes": nbytes,
-                         "ms_per_launch": dom_ms},
+                         "ms_per_launch": dom_ms,
+                         "bytes_model": "stage_bytes(): every input read once, every output "
+                                        "written once; the solve counts its per-iteration "
+                                        "sweep over the liquid chunks only",
+                         "sweep_cells": sweep_cells},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": P * 24,
                     "d2h_bytes_per_step": P * 24},

@@ -167,7 +167,7 @@ void free_all(FlipGpu *h) {
                   h->nz, h->key, h->rank, h->perm, h->cell_start, h->cell_count, h->spos,
                   h->spg, h->svel, h->sdens, h->wall_start, h->wall_pos, h->wall_nrm, h->u[0],
                   h->u[1], h->u[2], h->us[0], h->us[1], h->us[2], h->A, h->L, h->press,
-                  h->div, h->r, h->z, h->s, h->s1, h->w, h->w1, h->pdir, h->bar, h->P, h->Pf, h->diag,
+                  h->div, h->r, h->z, h->s, h->s1, h->w, h->w1, h->pdir, h->chunk_off, h->chunk_list, h->bar, h->P, h->Pf, h->diag,
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
@@ -330,7 +330,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
     AL(h->u[c], nf) AL(h->us[c], nf)
   }
   AL(h->A, nc) AL(h->L, nc) AL(h->press, nc) AL(h->div, nc) AL(h->r, nc) AL(h->z, nc)
-  AL(h->s, nc) AL(h->s1, nc) AL(h->w, nc) AL(h->w1, nc) AL(h->pdir, nc) AL(h->P, 2 * nc) AL(h->Pf, nc) AL(h->diag, nc)
+  AL(h->s, nc) AL(h->s1, nc) AL(h->w, nc) AL(h->w1, nc) AL(h->pdir, nc) AL(h->chunk_off, nc / 128 + 2) AL(h->chunk_list, nc / 128 + 1) AL(h->P, 2 * nc) AL(h->Pf, nc) AL(h->diag, nc)
   AL(h->partial, 8192) AL(h->bar, 2)
   AL(h->scal, SC_COUNT) AL(h->iflags, IF_COUNT) AL(h->flag, cap) AL(h->scan_a, scan_n)
   AL(h->scan_b, scan_n) AL(h->scan_tmp, h->scan_cap) AL(h->stuck_idx, cap)
@@ -376,7 +376,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
     return FLIPGPU_ECUDA;
   }
   if (cg_grid_size(h->cg_grid) != 0)
-    h->cg_grid[0] = h->cg_grid[1] = h->cg_grid[2] = h->cg_grid[3] = 0;
+    for (int v = 0; v < CG_VARIANTS; v++) h->cg_grid[v] = 0;
   if (particles_init_device() != 0) {
     free_all(h);
     cudaStreamDestroy(h->own_stream);

@@ -64,6 +64,8 @@ struct SimConst {
   const int64_t *dstep; /* the step counter in device memory (graph replays advance it) */
 };
 
+constexpr int CG_VARIANTS = 5; /* persistent CG kernels (k_pcg.cu cg_grid_size) */
+
 struct FlipGpu {
   FlipGpuParams prm;
   int n;
@@ -111,6 +113,8 @@ struct FlipGpu {
   /* solver */
   float *r, *z, *s, *s1, *w;
   float *w1, *pdir;   /* single-reduction CG: second w buffer, directions */
+  unsigned *chunk_off;  /* single-reduction CG: liquid flags of the 32-quad chunks, scanned */
+  unsigned *chunk_list; /* ... and the indices of the chunks that hold liquid */
   double *P;          /* REF preconditioner diagonal (double, as the reference) */
   float *Pf;          /* FP32 preconditioner diagonal / IC factor */
   float *diag;        /* FP32 matvec diagonal (FAST mode) */
@@ -118,7 +122,8 @@ struct FlipGpu {
   double *scal;       /* device scalars of the CG recurrence */
   int *iflags;        /* device flags/counters */
   unsigned *bar;      /* grid barrier of the persistent CG: count, generation */
-  int cg_grid[4];     /* cooperative CG grids: REF, FAST, FAST quads, FAST IC (0 = none) */
+  int cg_grid[CG_VARIANTS]; /* cooperative CG grids (0 = none): REF, FAST, FAST single-
+                               reduction (small blocks), FAST IC, single-reduction (large) */
   int nbx, nbricks;   /* 8^3 bricks of the IC wavefront */
   unsigned *brick_order, *fflag, *bflag, *ticket;
   float2 *brick_part;

@@ -22,6 +22,7 @@
  * r.r <= rel_tol^2 * b.b.
  */
 #include <cstdio>
+#include <type_traits>
 #include <vector>
 
 #include "devcommon.cuh"
@@ -439,6 +440,10 @@ k_scalar(int what, int mode, int nparts, const double *__restrict__ partial,
  * not depend on timing. Each thread owns the same cells in every phase; the
  * only cross-thread reads (neighbours, partials) bypass L1 (ld.cg). */
 constexpr int CG_BLOCK = 256;
+/* the single-reduction CG runs one block per SM: 384 threads keep a chunk's
+ * loads in registers (latency-bound small grids), 512 threads keep more
+ * chunks in flight (bandwidth-bound large grids, n >= CG1_LARGE_N) */
+constexpr int CG1_BLOCK_SMALL = 384, CG1_BLOCK_LARGE = 512, CG1_LARGE_N = 192;
 constexpr unsigned long long BAR_SPIN_LIMIT = 1ull << 26; /* ~seconds, then ETIMEOUT */
 
 struct CgArgs {
@@ -449,6 +454,8 @@ struct CgArgs {
   const float *b;
   float *x, *r, *z, *s0, *s1, *w;
   float *w1, *p;               /* single-reduction CG: second w buffer, directions */
+  const unsigned *chunk_list;  /* single-reduction CG: the 32-quad chunks holding liquid */
+  const unsigned *chunk_count; /* ... and their number */
   const double *P;
   const float *diag;
   const float *Pf;
@@ -499,6 +506,50 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags,
   }
   __syncthreads();
   /* one value per block, so a block always leaves the loop as a whole */
+  return ok != 0;
+}
+
+/* A counting grid barrier: bar[0] counts the arrivals of the whole launch
+ * (zeroed before it), so the epoch-th barrier is complete when it reaches
+ * epoch x gridDim.x. Thread 0 arrives with a release add after the block's
+ * __syncthreads and polls with acquire loads: two L2 round trips, no reset
+ * and no generation word. The wait gives up after 2 s of %globaltimer,
+ * flags FLIPGPU_ETIMEOUT and returns false in that block (the others give up
+ * at their next barrier). */
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool count_barrier(unsigned *bar, unsigned &epoch, int *iflags) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    epoch++;
+    const unsigned target = epoch * gridDim.x;
+    unsigned v;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(v) : "l"(bar) : "memory");
+    v += 1;
+    bool good = true;
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
+    while ((int)(v - target) < 0) {
+      if ((++spins & 1023u) == 0) {
+        const unsigned long long t = global_ns();
+        if (t0 == 0) {
+          t0 = t;
+        } else if (t - t0 > 2000000000ull) {
+          atomicExch(iflags + IF_TIMEOUT, 1);
+          good = false;
+          break;
+        }
+      }
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+    }
+    ok = good;
+  }
+  __syncthreads();
   return ok != 0;
 }
 
@@ -729,11 +780,11 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
   }
 }
 
-/* FAST-mode CG on quads of 4 consecutive k-cells (n % 4 == 0): 16-byte
- * loads, every neighbour load of a quad issued together, k-neighbours passed
- * between lanes by shuffles (a warp's lanes hold consecutive quads of a
- * k-row), quads without fluid skipped after phase 0 (their vectors stay 0).
- * Warps walk tiles of 32 quads so that shuffles always see a full warp. */
+/* Matvec on quads of 4 consecutive k-cells (n % 4 == 0) for the first
+ * residual of the single-reduction CG: 16-byte loads, every neighbour load of
+ * a quad issued together, k-neighbours passed between lanes by shuffles (a
+ * warp's lanes hold consecutive quads of a k-row; warps walk tiles of 32
+ * quads so that shuffles always see a full warp). */
 struct QuadNb {
   float4 sn;      /* s_new at the neighbour quad (0 where not FLUID) */
 };
@@ -841,169 +892,12 @@ __device__ __forceinline__ void quad_matvec(const CgArgs &a, size_t q, bool vali
                    fv[2] ? acc[2] * s : 0.0f, fv[3] ? acc[3] * s : 0.0f);
 }
 
-__global__ void __launch_bounds__(CG_BLOCK) k_cg_quad(CgArgs a) {
-  const unsigned nb = gridDim.x;
-  const int n = a.s.n;
-  const int qrow = n / 4;
-  const size_t qplane = (size_t)qrow * n;
-  const size_t nq = a.nc / 4;
-  const size_t warps = (size_t)nb * (CG_BLOCK / 32);
-  const size_t wid = (size_t)blockIdx.x * (CG_BLOCK / 32) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  float4 *x4 = reinterpret_cast<float4 *>(a.x);
-  float4 *r4 = reinterpret_cast<float4 *>(a.r);
-  float4 *z4 = reinterpret_cast<float4 *>(a.z);
-  float4 *w4p = reinterpret_cast<float4 *>(a.w);
-  const float4 *b4 = reinterpret_cast<const float4 *>(a.b);
-  const float4 *pf4 = reinterpret_cast<const float4 *>(a.Pf);
-  auto decode_q = [&](size_t q, int &i, int &j, int &kq) {
-    kq = (int)(q % qrow);
-    j = (int)((q / qrow) % n);
-    i = (int)(q / qplane);
-  };
-  auto acc4 = [](FF &f, float4 u, float4 v) {
-    ff_add_prod(f, u.x, v.x);
-    ff_add_prod(f, u.y, v.y);
-    ff_add_prod(f, u.z, v.z);
-    ff_add_prod(f, u.w, v.w);
-  };
-
-  /* phase 0: r = b - A x, z = M^-1 r (zeros outside FLUID); b.b, r.r, z.r */
-  FF pbb = ff_zero(), prr = ff_zero(), pzr = ff_zero();
-  for (size_t base = wid * 32; base < nq; base += warps * 32) {
-    size_t q = base + lane;
-    bool valid = q < nq;
-    int i = 0, j = 0, kq = 0;
-    if (valid) decode_q(q, i, j, kq);
-    float4 xs, ax;
-    uchar4 A4;
-    quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.x, a.x, 0.0f, true, xs, ax, A4);
-    if (!valid) continue;
-    float4 bv = b4[q];
-    const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
-    float bb[4] = {bv.x, bv.y, bv.z, bv.w}, av[4] = {ax.x, ax.y, ax.z, ax.w};
-    float rv[4], zv[4], xv[4];
-    float4 pf = (fv[0] || fv[1] || fv[2] || fv[3]) ? pf4[q] : make_float4(0, 0, 0, 0);
-    float pfv[4] = {pf.x, pf.y, pf.z, pf.w};
-    float4 xo = x4[q];
-    float xov[4] = {xo.x, xo.y, xo.z, xo.w};
-#pragma unroll
-    for (int t = 0; t < 4; t++) {
-      if (fv[t]) {
-        ff_add_prod(pbb, bb[t], bb[t]);
-        rv[t] = bb[t] - av[t];
-        zv[t] = rv[t] * pfv[t];
-        ff_add_prod(prr, rv[t], rv[t]);
-        ff_add_prod(pzr, zv[t], rv[t]);
-        xv[t] = xov[t];
-      } else {
-        rv[t] = zv[t] = xv[t] = 0.0f;
-      }
-    }
-    r4[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
-    z4[q] = make_float4(zv[0], zv[1], zv[2], zv[3]);
-    x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
-  }
-  store_partial(a.part, 0, nb, pbb);
-  store_partial(a.part, 1, nb, prr);
-  store_partial(a.part, 2, nb, pzr);
-  if (!grid_barrier(a.bar, a.iflags)) return;
-  double b2, rr, azr, unused;
-  sum_partials(a.part, 0, 1, nb, b2, rr);
-  sum_partials(a.part, 2, -1, nb, azr, unused);
-  const double eps = a.rel_tol * a.rel_tol * b2;
-  int done = rr <= eps ? 1 : 0, iters = 0;
-  double e2 = rr;
-  float *so = a.s0, *sn = a.s1;
-  float beta_f = 0.0f;
-  bool first = true;
-  while (!done) {
-    /* phase A: s_new = z + beta*s_old, w = A s_new; w.s_new */
-    FF pws = ff_zero();
-    for (size_t base = wid * 32; base < nq; base += warps * 32) {
-      size_t q = base + lane;
-      bool valid = q < nq;
-      int i = 0, j = 0, kq = 0;
-      if (valid) decode_q(q, i, j, kq);
-      float4 sn4, wv;
-      uchar4 A4;
-      quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.z, so, beta_f, first,
-                  sn4, wv, A4);
-      if (!valid || !(fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w))) continue;
-      reinterpret_cast<float4 *>(sn)[q] = sn4;
-      w4p[q] = wv;
-      acc4(pws, wv, sn4);
-    }
-    store_partial(a.part, 3, nb, pws);
-    if (!grid_barrier(a.bar, a.iflags)) return;
-    double ws;
-    sum_partials(a.part, 3, -1, nb, ws, unused);
-    const double alpha = azr / ws;
-    const float alpha_f = (float)alpha;
-    /* phase B: x += alpha s, r -= alpha w, z = M^-1 r; r.r, z.r */
-    prr = ff_zero();
-    pzr = ff_zero();
-    for (size_t base = wid * 32; base < nq; base += warps * 32) {
-      size_t q = base + lane;
-      if (q >= nq) continue;
-      uchar4 A4 = reinterpret_cast<const uchar4 *>(a.A)[q];
-      const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
-      if (!(fv[0] || fv[1] || fv[2] || fv[3])) continue;
-      float4 xv = x4[q], sv = reinterpret_cast<const float4 *>(sn)[q], rv = r4[q], wv = w4p[q],
-             pf = pf4[q];
-      float X[4] = {xv.x, xv.y, xv.z, xv.w}, S[4] = {sv.x, sv.y, sv.z, sv.w};
-      float R[4] = {rv.x, rv.y, rv.z, rv.w}, W[4] = {wv.x, wv.y, wv.z, wv.w};
-      float PF[4] = {pf.x, pf.y, pf.z, pf.w}, Z[4];
-#pragma unroll
-      for (int t = 0; t < 4; t++) {
-        if (fv[t]) {
-          X[t] = fmaf(alpha_f, S[t], X[t]);
-          R[t] = fmaf(-alpha_f, W[t], R[t]);
-          Z[t] = R[t] * PF[t];
-          ff_add_prod(prr, R[t], R[t]);
-          ff_add_prod(pzr, Z[t], R[t]);
-        } else {
-          Z[t] = 0.0f;
-        }
-      }
-      x4[q] = make_float4(X[0], X[1], X[2], X[3]);
-      r4[q] = make_float4(R[0], R[1], R[2], R[3]);
-      z4[q] = make_float4(Z[0], Z[1], Z[2], Z[3]);
-    }
-    store_partial(a.part, 4, nb, prr);
-    store_partial(a.part, 5, nb, pzr);
-    if (!grid_barrier(a.bar, a.iflags)) return;
-    double zr;
-    sum_partials(a.part, 4, 5, nb, rr, zr);
-    iters++;
-    e2 = rr;
-    if (e2 <= eps) done = 1;
-    else if (!(e2 == e2)) done = 2;
-    else if (iters >= a.max_iters) done = 3;
-    beta_f = (float)(zr / azr);
-    azr = zr;
-    first = false;
-    float *t = so;
-    so = sn;
-    sn = t;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    a.iflags[IF_DONE] = done;
-    a.iflags[IF_ITERS] = iters;
-    a.iflags[IF_NAN] = done == 2;
-    a.scal[SC_ERR2] = e2;
-    a.scal[SC_B2] = b2;
-    a.scal[SC_EPS] = eps;
-  }
-}
-
-
 /* K per-thread partial sums reduced over the block into
  * part[(k0+q)*nb + blockIdx.x] with one __syncthreads (warp shuffle trees,
  * then thread q merges the warps' value q in a fixed order). */
-template <int K>
+template <int K, int BLOCK = CG_BLOCK>
 __device__ __forceinline__ void store_partials(float2 *part, int k0, unsigned nb, FF (&v)[K]) {
-  __shared__ FF wp[K][CG_BLOCK / 32];
+  __shared__ FF wp[K][BLOCK / 32];
 #pragma unroll
   for (int q = 0; q < K; q++)
     for (int o = 16; o > 0; o >>= 1) v[q] = ff_merge(v[q], ff_shfl_down(v[q], o));
@@ -1014,27 +908,38 @@ __device__ __forceinline__ void store_partials(float2 *part, int k0, unsigned nb
   __syncthreads();
   if (threadIdx.x < K) {
     FF t = wp[threadIdx.x][0];
-    for (int i = 1; i < CG_BLOCK / 32; i++) t = ff_merge(t, wp[threadIdx.x][i]);
+    for (int i = 1; i < BLOCK / 32; i++) t = ff_merge(t, wp[threadIdx.x][i]);
     part[(size_t)(k0 + threadIdx.x) * nb + blockIdx.x] = make_float2(t.hi, t.lo);
   }
 }
 
 /* Sums over the nb block partials of slots k0..k0+K-1, by warp 0 (lane-
  * strided merges, then a shuffle tree: the same order in every block);
- * valid in thread 0. */
+ * valid in thread 0. Each lane issues its loads for up to 32 x PL blocks
+ * before the first merge: one L2 round trip instead of one per 32 blocks. */
 template <int K>
 __device__ __forceinline__ void warp_sum_partials(const float2 *part, int k0, unsigned nb,
                                                   double (&out)[K]) {
+  constexpr int PL = 10;
   const int lane = threadIdx.x & 31;
   FF v[K];
 #pragma unroll
   for (int q = 0; q < K; q++) v[q] = ff_zero();
-  for (unsigned i = lane; i < nb; i += 32)
+  for (unsigned base = 0; base < nb; base += 32 * PL) {
+    float2 buf[K][PL];
 #pragma unroll
-    for (int q = 0; q < K; q++) {
-      const float2 a = __ldcg(part + (size_t)(k0 + q) * nb + i);
-      v[q] = ff_merge(v[q], FF{a.x, a.y});
+    for (int t = 0; t < PL; t++) {
+      const unsigned i = base + lane + 32 * t;
+#pragma unroll
+      for (int q = 0; q < K; q++)
+        buf[q][t] = i < nb ? __ldcg(part + (size_t)(k0 + q) * nb + i) : make_float2(0.0f, 0.0f);
     }
+#pragma unroll
+    for (int t = 0; t < PL; t++)
+      if (base + lane + 32 * t < nb)
+#pragma unroll
+        for (int q = 0; q < K; q++) v[q] = ff_merge(v[q], FF{buf[q][t].x, buf[q][t].y});
+  }
 #pragma unroll
   for (int q = 0; q < K; q++) {
     for (int o = 16; o > 0; o >>= 1) v[q] = ff_merge(v[q], ff_shfl_down(v[q], o));
@@ -1046,47 +951,54 @@ __device__ __forceinline__ void warp_sum_partials(const float2 *part, int k0, un
  * (Chronopoulos-Gear): with u = M^-1 r and w = A u,
  *   p = u + beta p,  s = w + beta s  (s = A p),  x += alpha p,  r -= alpha s,
  *   gamma = r.u, delta = w.u,  beta' = gamma'/gamma,
- *   alpha' = gamma' / (delta' - beta' gamma' / alpha),
- * and the new w = A u' needs u' = M^-1 (r - alpha (w + beta s_old)) at the
- * neighbours, which every thread recomputes from the previous iteration's
- * r, w, s (kept in ping-pong buffers), so one sweep and one barrier make an
- * iteration. Quads of 4 k-cells per thread as in k_cg_quad; partial sums
- * alternate between two slot sets so that a slow reader of one iteration's
- * sums never sees the next iteration's. */
-struct Cg1Nb {
+ *   alpha' = gamma' / (delta' - beta' gamma' / alpha).
+ * The vectors are kept scaled by the Jacobi preconditioner M^-1 = 1/diag:
+ * U = M^-1 r (= u), Wt = M^-1 w, St = M^-1 s. The new w = A u' needs
+ * u' = U - alpha (Wt + beta St) at the neighbours, which every thread
+ * recomputes from the previous iteration's U, Wt, St (ping-pong buffers), so
+ * one sweep and one barrier make an iteration and a neighbour quad costs
+ * three float4 loads and its flags. The residual of the dot products is
+ * r = diag U. Quads of 4 k-cells per thread; partial sums alternate between
+ * two slot sets so that a slow reader of one iteration's sums never sees
+ * the next iteration's. */
+struct Cg1Q {
   uchar4 A;
-  float4 pf, r, w, s;
+  float4 u, w, s;
 };
 
-__device__ __forceinline__ float4 cg1_unext(uchar4 A4, float4 pf, float4 r, float4 w, float4 s,
-                                            float alpha, float beta, bool first) {
-  auto one = [&](unsigned char a, float pfv, float rv, float wv, float sv) {
-    if (!fl(a)) return 0.0f;
-    const float sn = first ? wv : wv + beta * sv;
-    return pfv * (rv - alpha * sn);
-  };
-  return make_float4(one(A4.x, pf.x, r.x, w.x, s.x), one(A4.y, pf.y, r.y, w.y, s.y),
-                     one(A4.z, pf.z, r.z, w.z, s.z), one(A4.w, pf.w, r.w, w.w, s.w));
+/* The 32-quad chunks of the single-reduction CG that hold liquid, in
+ * increasing order (flags by one warp per chunk, an exclusive scan, a
+ * scatter): the CG sweeps visit only these. */
+__global__ void __launch_bounds__(BLK) k_cg1_chunk_flags(size_t nq, const uchar4 *__restrict__ A4,
+                                                        unsigned *__restrict__ flag) {
+  const size_t chunk = ((size_t)blockIdx.x * BLK + threadIdx.x) >> 5;
+  const size_t nch = (nq + 31) / 32;
+  if (chunk > nch) return; /* whole warps */
+  const int lane = threadIdx.x & 31;
+  const size_t q = chunk * 32 + lane;
+  bool f = false;
+  if (chunk < nch && q < nq) {
+    const uchar4 v = A4[q];
+    f = fl(v.x) || fl(v.y) || fl(v.z) || fl(v.w);
+  }
+  const unsigned any = __ballot_sync(0xffffffffu, f);
+  if (lane == 0) flag[chunk] = (chunk < nch && any) ? 1u : 0u; /* flag[nch] = 0 */
 }
 
-__device__ __forceinline__ float cg1_unext1(const CgArgs &a, size_t c, const float *R,
-                                            const float *W, const float *S, float alpha,
-                                            float beta, bool first, int &isfl) {
-  isfl = fl(a.A[c]);
-  if (!isfl) return 0.0f;
-  const float wv = __ldcg(W + c);
-  const float sn = first ? wv : wv + beta * __ldcg(S + c);
-  return a.Pf[c] * (__ldcg(R + c) - alpha * sn);
+__global__ void __launch_bounds__(BLK) k_cg1_chunk_scatter(size_t nch, const unsigned *__restrict__ off,
+                                                          unsigned *__restrict__ list) {
+  const size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (c < nch && off[c + 1] != off[c]) list[off[c]] = (unsigned)c;
 }
 
-__global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
+template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_cg1(CgArgs a) {
   const unsigned nb = gridDim.x;
   const int n = a.s.n;
   const int qrow = n / 4;
   const size_t qplane = (size_t)qrow * n;
   const size_t nq = a.nc / 4;
-  const size_t warps = (size_t)nb * (CG_BLOCK / 32);
-  const size_t wid = (size_t)blockIdx.x * (CG_BLOCK / 32) + (threadIdx.x >> 5);
+  const size_t warps = (size_t)nb * (BLOCK / 32);
+  const size_t wid = (size_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   const unsigned FULL = 0xffffffffu;
   float4 *x4 = reinterpret_cast<float4 *>(a.x);
@@ -1096,15 +1008,18 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
   const float4 *d4p = reinterpret_cast<const float4 *>(a.diag);
   const uchar4 *A4p = reinterpret_cast<const uchar4 *>(a.A);
   float *R[2] = {a.r, a.z}, *W[2] = {a.w, a.w1}, *S[2] = {a.s0, a.s1};
+  /* quad index -> (i, j, k/4) in 32-bit arithmetic (nq < 2^31 on this path) */
   auto decode_q = [&](size_t q, int &i, int &j, int &kq) {
-    kq = (int)(q % qrow);
-    j = (int)((q / qrow) % n);
-    i = (int)(q / qplane);
+    const unsigned q32 = (unsigned)q, row = q32 / (unsigned)qrow;
+    kq = (int)(q32 - row * (unsigned)qrow);
+    i = (int)(row / (unsigned)n);
+    j = (int)(row - (unsigned)i * (unsigned)n);
   };
   const float hs = a.s.inv_h2_f;
+  unsigned epoch = 0; /* barriers passed (count_barrier) */
 
-  /* phase 0a: r = b - A x on the liquid; b.b, r.r */
-  FF pbb = ff_zero(), prr = ff_zero();
+  /* phase 0a: r = b - A x on the liquid, U = M^-1 r; b.b, r.r, gamma = r.U */
+  FF pbb = ff_zero(), prr = ff_zero(), pg0 = ff_zero();
   for (size_t base = wid * 32; base < nq; base += warps * 32) {
     size_t q = base + lane;
     bool valid = q < nq;
@@ -1114,43 +1029,47 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
     uchar4 A4;
     quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.x, a.x, 0.0f, true, xs, ax, A4);
     if (!valid) continue;
-    const float4 bv = b4[q];
+    const float4 bv = b4[q], pf = pf4[q];
     const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
     const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, av[4] = {ax.x, ax.y, ax.z, ax.w};
+    const float pfv[4] = {pf.x, pf.y, pf.z, pf.w};
     const float4 xo = x4[q];
     const float xov[4] = {xo.x, xo.y, xo.z, xo.w};
-    float rv[4], xv[4];
+    float uv[4], xv[4];
 #pragma unroll
     for (int t = 0; t < 4; t++) {
       if (fv[t]) {
         ff_add_prod(pbb, bb[t], bb[t]);
-        rv[t] = bb[t] - av[t];
-        ff_add_prod(prr, rv[t], rv[t]);
+        const float rv = bb[t] - av[t];
+        ff_add_prod(prr, rv, rv);
+        uv[t] = pfv[t] * rv;
+        ff_add_prod(pg0, rv, uv[t]);
         xv[t] = xov[t];
       } else {
-        rv[t] = xv[t] = 0.0f;
+        uv[t] = xv[t] = 0.0f;
       }
     }
-    reinterpret_cast<float4 *>(R[0])[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    reinterpret_cast<float4 *>(R[0])[q] = make_float4(uv[0], uv[1], uv[2], uv[3]);
     x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
   }
   __shared__ float s_alpha, s_beta;
   __shared__ int s_done;
   {
-    FF v[2] = {pbb, prr};
-    store_partials<2>(a.part, 0, nb, v);
+    FF v[3] = {pbb, prr, pg0};
+    store_partials<3, BLOCK>(a.part, 0, nb, v);
   }
-  if (!grid_barrier(a.bar, a.iflags)) return;
+  if (!count_barrier(a.bar, epoch, a.iflags)) return;
   /* the FP64 scalar work runs on thread 0 of each block (the sums are the
    * same in every block) and reaches the others through shared memory */
-  double b2 = 0.0, eps = 0.0, e2 = 0.0;
+  double b2 = 0.0, eps = 0.0, e2 = 0.0, gamma = 0.0;
   int done = 0, iters = 0;
   if (threadIdx.x < 32) {
-    double t[2];
-    warp_sum_partials<2>(a.part, 0, nb, t);
+    double t[3];
+    warp_sum_partials<3>(a.part, 0, nb, t);
     if (threadIdx.x == 0) {
       b2 = t[0];
       e2 = t[1];
+      gamma = t[2];
       eps = a.rel_tol * a.rel_tol * b2;
       s_done = e2 <= eps ? 1 : 0;
     }
@@ -1158,99 +1077,109 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
   __syncthreads();
   done = s_done;
 
-  /* the sweep: for the quads of this warp, from R[cur], W[cur], S[cur]
-   * (and the directions) at step (alpha, beta, first) to R/W/S[cur^1];
-   * init: only w = A M^-1 r (alpha = 0, no s, no updates) */
-  auto sweep = [&](int cur, float alpha, float beta, bool first, bool init, FF &pg, FF &pd,
+  /* the sweep: for the liquid chunks of this warp (32 quads each, from the
+   * chunk list), from U/Wt/St[cur] (and the directions) at step
+   * (alpha, beta, first) to U/Wt/St[cur^1]; init: only Wt = M^-1 A U
+   * (alpha = 0, no s, no updates). Every load of a chunk (its own quad, the
+   * four i/j neighbour quads, the k neighbour cell of the edge lanes) is
+   * issued before the first use, so a chunk costs one L2 round trip; no load
+   * waits on a cell flag (air values are loaded and then ignored). */
+  const unsigned nact = __ldcg(a.chunk_count);
+  auto sweep = [&](int cur, float alpha, float beta, auto first_c, auto init_c, FF &pg, FF &pd,
                    FF &pr) {
-    const float *Ro = R[cur], *Wo = W[cur], *So = S[cur];
-    float *Rn = R[cur ^ 1], *Wn = W[cur ^ 1], *Sn = S[cur ^ 1];
-    for (size_t base = wid * 32; base < nq; base += warps * 32) {
-      const size_t q = base + lane;
+    constexpr bool first = decltype(first_c)::value, init = decltype(init_c)::value;
+    const float *Uo = R[cur], *Wo = W[cur], *So = S[cur];
+    float *Un = R[cur ^ 1], *Wn = W[cur ^ 1], *Sn = S[cur ^ 1];
+    const float4 zero = make_float4(0, 0, 0, 0);
+    auto load_q = [&](Cg1Q &v, size_t qq) {
+      v.A = A4p[qq];
+      v.u = __ldcg(reinterpret_cast<const float4 *>(Uo) + qq);
+      v.w = init ? zero : __ldcg(reinterpret_cast<const float4 *>(Wo) + qq);
+      v.s = (init || first) ? zero : __ldcg(reinterpret_cast<const float4 *>(So) + qq);
+    };
+    /* u' = U - alpha (Wt + beta St) on the liquid, 0 elsewhere */
+    auto u1 = [&](unsigned char f, float u, float w, float s) {
+      if (!fl(f)) return 0.0f;
+      if (init) return u;
+      return u - alpha * (first ? w : w + beta * s);
+    };
+    auto u_of = [&](const Cg1Q &v) {
+      return make_float4(u1(v.A.x, v.u.x, v.w.x, v.s.x), u1(v.A.y, v.u.y, v.w.y, v.s.y),
+                         u1(v.A.z, v.u.z, v.w.z, v.s.z), u1(v.A.w, v.u.w, v.w.w, v.s.w));
+    };
+    unsigned cnext = wid < nact ? __ldg(a.chunk_list + wid) : 0u;
+    for (size_t t = wid; t < nact; t += warps) {
+      const size_t q = (size_t)cnext * 32 + lane;
+      if (t + warps < nact) cnext = __ldg(a.chunk_list + t + warps); /* next chunk, early */
       const bool valid = q < nq;
-      int i = 0, j = 0, kq = 0;
-      if (valid) decode_q(q, i, j, kq);
       const size_t qs = valid ? q : 0;
-      const uchar4 A4 = valid ? A4p[qs] : make_uchar4(0, 0, 0, 0);
-      const bool any = fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w);
-      float4 pf = make_float4(0, 0, 0, 0), r = pf, w = pf, so = pf, un = pf, sn = pf, rn = pf;
-      if (any) {
-        pf = pf4[qs];
-        r = __ldcg(reinterpret_cast<const float4 *>(Ro) + qs);
-        if (!init) {
-          w = __ldcg(reinterpret_cast<const float4 *>(Wo) + qs);
-          if (!first) so = __ldcg(reinterpret_cast<const float4 *>(So) + qs);
-        }
-        if (init) {
-          un = make_float4(fl(A4.x) ? pf.x * r.x : 0.0f, fl(A4.y) ? pf.y * r.y : 0.0f,
-                           fl(A4.z) ? pf.z * r.z : 0.0f, fl(A4.w) ? pf.w * r.w : 0.0f);
+      int i = 0, j = 0, kq = 0;
+      decode_q(qs, i, j, kq);
+      const size_t c0 = 4 * qs;
+      const int k0 = 4 * kq;
+      /* own quad */
+      Cg1Q own;
+      load_q(own, qs);
+      const float4 dg = __ldg(d4p + qs), pf = __ldg(pf4 + qs);
+      const float4 po = (init || first) ? zero : p4[qs];
+      const float4 xo = init ? zero : __ldcg(x4 + qs); /* phase 0a wrote x by another map */
+      /* i/j neighbour quads */
+      const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
+      const long off[4] = {(long)qplane, -(long)qplane, (long)qrow, -(long)qrow};
+      Cg1Q nbq[4];
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        if (has[d]) {
+          load_q(nbq[d], (size_t)((long)qs + off[d]));
         } else {
-          un = cg1_unext(A4, pf, r, w, so, alpha, beta, first);
+          nbq[d].A = make_uchar4(0, 0, 0, 0);
+          nbq[d].u = nbq[d].w = nbq[d].s = zero;
         }
       }
+      /* the k neighbour across the chunk's ends: cell c0-1 for lane 0, c0+4
+       * for lane 31 (inside the chunk the shuffles below carry it) */
+      const bool edge = (lane == 0 && k0 > 0) || (lane == 31 && k0 + 4 < n);
+      const size_t ce = lane == 0 ? c0 - 1 : c0 + 4;
+      unsigned char eA = 0;
+      float eu0 = 0.0f, ew = 0.0f, es = 0.0f;
+      if (edge) {
+        eA = a.A[ce];
+        eu0 = __ldcg(Uo + ce);
+        if (!init) {
+          ew = __ldcg(Wo + ce);
+          if (!first) es = __ldcg(So + ce);
+        }
+      }
+      const uchar4 A4 = own.A;
+      const float4 un = u_of(own);
+      const bool any = fl(A4.x) || fl(A4.y) || fl(A4.z) || fl(A4.w);
       /* k neighbours across quads */
       float left = __shfl_up_sync(FULL, un.w, 1);
       int left_fl = __shfl_up_sync(FULL, (int)fl(A4.w), 1);
       float right = __shfl_down_sync(FULL, un.x, 1);
       int right_fl = __shfl_down_sync(FULL, (int)fl(A4.x), 1);
       if (!valid || !any) continue;
-      const size_t c0 = 4 * q;
-      const int k0 = 4 * kq;
+      const float eu = edge ? u1(eA, eu0, ew, es) : 0.0f;
       if (k0 == 0) {
         left_fl = 0;
       } else if (lane == 0) {
-        left = init ? (fl(a.A[c0 - 1]) ? a.Pf[c0 - 1] * __ldcg(Ro + c0 - 1) : 0.0f)
-                    : cg1_unext1(a, c0 - 1, Ro, Wo, So, alpha, beta, first, left_fl);
-        left_fl = fl(a.A[c0 - 1]);
+        left = eu;
+        left_fl = fl(eA);
       }
       if (k0 + 4 >= n) {
         right_fl = 0;
       } else if (lane == 31) {
-        right = init ? (fl(a.A[c0 + 4]) ? a.Pf[c0 + 4] * __ldcg(Ro + c0 + 4) : 0.0f)
-                     : cg1_unext1(a, c0 + 4, Ro, Wo, So, alpha, beta, first, right_fl);
-        right_fl = fl(a.A[c0 + 4]);
+        right = eu;
+        right_fl = fl(eA);
       }
-      /* i/j neighbour quads, two at a time (loads of a pair issued together) */
-      const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
-      const long off[4] = {(long)qplane, -(long)qplane, (long)qrow, -(long)qrow};
-      const float4 dg = __ldg(d4p + q);
       float acc[4] = {dg.x * un.x, dg.y * un.y, dg.z * un.z, dg.w * un.w};
 #pragma unroll
-      for (int h2 = 0; h2 < 4; h2 += 2) {
-        Cg1Nb nbq[2];
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-          const int d = h2 + e;
-          const float4 zero = make_float4(0, 0, 0, 0);
-          nbq[e].A = make_uchar4(0, 0, 0, 0);
-          nbq[e].pf = nbq[e].r = nbq[e].w = nbq[e].s = zero;
-          if (has[d]) {
-            const size_t qq = (size_t)((long)q + off[d]);
-            nbq[e].A = A4p[qq];
-            nbq[e].pf = pf4[qq];
-            nbq[e].r = __ldcg(reinterpret_cast<const float4 *>(Ro) + qq);
-            if (!init) {
-              nbq[e].w = __ldcg(reinterpret_cast<const float4 *>(Wo) + qq);
-              if (!first) nbq[e].s = __ldcg(reinterpret_cast<const float4 *>(So) + qq);
-            }
-          }
-        }
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-          float4 v;
-          if (init) {
-            v = make_float4(fl(nbq[e].A.x) ? nbq[e].pf.x * nbq[e].r.x : 0.0f,
-                            fl(nbq[e].A.y) ? nbq[e].pf.y * nbq[e].r.y : 0.0f,
-                            fl(nbq[e].A.z) ? nbq[e].pf.z * nbq[e].r.z : 0.0f,
-                            fl(nbq[e].A.w) ? nbq[e].pf.w * nbq[e].r.w : 0.0f);
-          } else {
-            v = cg1_unext(nbq[e].A, nbq[e].pf, nbq[e].r, nbq[e].w, nbq[e].s, alpha, beta, first);
-          }
-          acc[0] -= v.x;
-          acc[1] -= v.y;
-          acc[2] -= v.z;
-          acc[3] -= v.w;
-        }
+      for (int d = 0; d < 4; d++) {
+        const float4 v = u_of(nbq[d]);
+        acc[0] -= v.x;
+        acc[1] -= v.y;
+        acc[2] -= v.z;
+        acc[3] -= v.w;
       }
       const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
       const float uv[4] = {un.x, un.y, un.z, un.w};
@@ -1258,70 +1187,64 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
       acc[1] -= (fv[0] ? uv[0] : 0.0f) + (fv[2] ? uv[2] : 0.0f);
       acc[2] -= (fv[1] ? uv[1] : 0.0f) + (fv[3] ? uv[3] : 0.0f);
       acc[3] -= (fv[2] ? uv[2] : 0.0f) + (right_fl ? right : 0.0f);
-      float wn[4];
+      const float PF[4] = {pf.x, pf.y, pf.z, pf.w}, DG[4] = {dg.x, dg.y, dg.z, dg.w};
+      float wn[4], wt[4];
 #pragma unroll
-      for (int t = 0; t < 4; t++) wn[t] = fv[t] ? acc[t] * hs : 0.0f;
-      reinterpret_cast<float4 *>(Wn)[q] = make_float4(wn[0], wn[1], wn[2], wn[3]);
+      for (int t2 = 0; t2 < 4; t2++) {
+        wn[t2] = fv[t2] ? acc[t2] * hs : 0.0f;
+        wt[t2] = PF[t2] * wn[t2];
+      }
+      reinterpret_cast<float4 *>(Wn)[q] = make_float4(wt[0], wt[1], wt[2], wt[3]);
       if (init) {
 #pragma unroll
-        for (int t = 0; t < 4; t++)
-          if (fv[t]) {
-            const float rt = t == 0 ? r.x : t == 1 ? r.y : t == 2 ? r.z : r.w;
-            ff_add_prod(pg, rt, uv[t]);
-            ff_add_prod(pd, wn[t], uv[t]);
-          }
-        /* R[cur^1] mirrors R[cur] so the first sweep reads the same r */
-        reinterpret_cast<float4 *>(Rn)[q] = r;
+        for (int t2 = 0; t2 < 4; t2++)
+          if (fv[t2]) ff_add_prod(pd, wn[t2], uv[t2]);
+        /* U[cur^1] mirrors U[cur] so the first sweep reads the same U */
+        reinterpret_cast<float4 *>(Un)[q] = own.u;
         continue;
       }
-      /* own updates: p, s, x, r */
-      const float4 w4 = w, s4 = so;
-      const float4 po = first ? make_float4(0, 0, 0, 0) : p4[q];
-      const float4 xo = x4[q];
-      const float Wv[4] = {w4.x, w4.y, w4.z, w4.w}, Sv[4] = {s4.x, s4.y, s4.z, s4.w};
+      /* own updates: p, St, x, U (= u') */
+      const float Uv[4] = {own.u.x, own.u.y, own.u.z, own.u.w};
+      const float Wv[4] = {own.w.x, own.w.y, own.w.z, own.w.w};
+      const float Sv[4] = {own.s.x, own.s.y, own.s.z, own.s.w};
       const float Pv[4] = {po.x, po.y, po.z, po.w}, Xv[4] = {xo.x, xo.y, xo.z, xo.w};
-      const float Rv[4] = {r.x, r.y, r.z, r.w}, PF[4] = {pf.x, pf.y, pf.z, pf.w};
-      float pn[4], snn[4], xn[4], rnn[4];
+      float pn[4], stn[4], xn[4];
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
-        if (fv[t]) {
-          const float u = PF[t] * Rv[t];
-          pn[t] = first ? u : u + beta * Pv[t];
-          snn[t] = first ? Wv[t] : Wv[t] + beta * Sv[t];
-          xn[t] = Xv[t] + alpha * pn[t];
-          rnn[t] = Rv[t] - alpha * snn[t];
-          ff_add_prod(pg, rnn[t], uv[t]);
-          ff_add_prod(pd, wn[t], uv[t]);
-          ff_add_prod(pr, rnn[t], rnn[t]);
+      for (int t2 = 0; t2 < 4; t2++) {
+        if (fv[t2]) {
+          pn[t2] = first ? Uv[t2] : Uv[t2] + beta * Pv[t2];
+          stn[t2] = first ? Wv[t2] : Wv[t2] + beta * Sv[t2];
+          xn[t2] = Xv[t2] + alpha * pn[t2];
+          const float rn = DG[t2] * uv[t2]; /* r' = diag u' */
+          ff_add_prod(pg, rn, uv[t2]);
+          ff_add_prod(pd, wn[t2], uv[t2]);
+          ff_add_prod(pr, rn, rn);
         } else {
-          pn[t] = snn[t] = xn[t] = rnn[t] = 0.0f;
+          pn[t2] = stn[t2] = xn[t2] = 0.0f;
         }
       }
       p4[q] = make_float4(pn[0], pn[1], pn[2], pn[3]);
       x4[q] = make_float4(xn[0], xn[1], xn[2], xn[3]);
-      reinterpret_cast<float4 *>(Sn)[q] = make_float4(snn[0], snn[1], snn[2], snn[3]);
-      reinterpret_cast<float4 *>(Rn)[q] = make_float4(rnn[0], rnn[1], rnn[2], rnn[3]);
-      (void)sn;
-      (void)rn;
+      reinterpret_cast<float4 *>(Sn)[q] = make_float4(stn[0], stn[1], stn[2], stn[3]);
+      reinterpret_cast<float4 *>(Un)[q] = un;
     }
   };
 
-  /* phase 0b: w0 = A M^-1 r0 (into W[1]); gamma0 = r.u, delta0 = w.u */
-  FF pg = ff_zero(), pd = ff_zero(), pr = ff_zero();
-  sweep(0, 0.0f, 0.0f, true, true, pg, pd, pr);
+  /* phase 0b: Wt0 = M^-1 A U0 (into W[1]); delta0 = w.u */
   {
-    FF v[2] = {pg, pd};
-    store_partials<2>(a.part, 2, nb, v);
+    FF pg = ff_zero(), pd = ff_zero(), pr = ff_zero();
+    sweep(0, 0.0f, 0.0f, std::true_type{}, std::true_type{}, pg, pd, pr);
+    FF v[1] = {pd};
+    store_partials<1, BLOCK>(a.part, 3, nb, v);
   }
-  if (!grid_barrier(a.bar, a.iflags)) return;
-  double gamma = 0.0, alpha = 0.0, beta = 0.0;
+  if (!count_barrier(a.bar, epoch, a.iflags)) return;
+  double alpha = 0.0, beta = 0.0;
   if (threadIdx.x < 32) {
-    double t[2];
-    warp_sum_partials<2>(a.part, 2, nb, t);
+    double t[1];
+    warp_sum_partials<1>(a.part, 3, nb, t);
     if (threadIdx.x == 0) {
-      gamma = t[0];
-      alpha = gamma / t[1];
-      if (!(alpha == alpha) || !(t[1] > 0.0)) done = done ? done : 2;
+      alpha = gamma / t[0];
+      if (!(alpha == alpha) || !(t[0] > 0.0)) done = done ? done : 2;
       s_alpha = (float)alpha;
       s_done = done;
     }
@@ -1329,15 +1252,18 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_cg1(CgArgs a) {
   __syncthreads();
   float alpha_f = s_alpha, beta_f = 0.0f;
   done = s_done;
-  int cur = 1; /* R[1] = r0, W[1] = w0 */
+  int cur = 1; /* U[1] = U0, W[1] = Wt0 */
   bool first = true;
   int set = 0;
   while (!done) {
     FF v[3] = {ff_zero(), ff_zero(), ff_zero()};
-    sweep(cur, alpha_f, beta_f, first, false, v[0], v[1], v[2]);
+    if (first)
+      sweep(cur, alpha_f, beta_f, std::true_type{}, std::false_type{}, v[0], v[1], v[2]);
+    else
+      sweep(cur, alpha_f, beta_f, std::false_type{}, std::false_type{}, v[0], v[1], v[2]);
     const int k0 = set ? 3 : 0;
-    store_partials<3>(a.part, k0, nb, v);
-    if (!grid_barrier(a.bar, a.iflags)) return;
+    store_partials<3, BLOCK>(a.part, k0, nb, v);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
     set ^= 1;
     cur ^= 1;
     first = false;
@@ -1884,6 +1810,13 @@ static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   return FLIPGPU_OK;
 }
 
+/* threads per block of a persistent CG kernel */
+static int cg_block_of(const void *kern) {
+  if (kern == (const void *)k_cg_cg1<CG1_BLOCK_SMALL>) return CG1_BLOCK_SMALL;
+  if (kern == (const void *)k_cg_cg1<CG1_BLOCK_LARGE>) return CG1_BLOCK_LARGE;
+  return CG_BLOCK;
+}
+
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   const int n = h->n;
   const size_t nc = h->nc;
@@ -1995,15 +1928,36 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
                                                  : (const void *)k_cg<FLIPGPU_SOLVE_FAST>;
     int grid = h->cg_grid[mode == FLIPGPU_SOLVE_REF ? 0 : 1];
     size_t smem = 0;
-    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0) {
-      kern = (const void *)k_cg_cg1;
-      grid = h->cg_grid[2];
+    a.chunk_list = nullptr;
+    a.chunk_count = nullptr;
+    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0 &&
+        nc / 4 < (size_t)1 << 31) {
+      const bool large = n >= CG1_LARGE_N;
+      kern = large ? (const void *)k_cg_cg1<CG1_BLOCK_LARGE> : (const void *)k_cg_cg1<CG1_BLOCK_SMALL>;
+      grid = h->cg_grid[large ? 4 : 2];
+      /* the chunks holding liquid (A is fixed during the solve) */
+      const size_t nq = nc / 4, nch = (nq + 31) / 32;
+      k_cg1_chunk_flags<<<grid_for((nch + 1) * 32, BLK), BLK, 0, S>>>(
+          nq, reinterpret_cast<const uchar4 *>(h->A), h->chunk_off);
+      FG_LAUNCHED(h, 1);
+      cudaError_t e = scan_exclusive(h, h->chunk_off, h->chunk_off, nch + 1);
+      if (e == cudaSuccess) {
+        k_cg1_chunk_scatter<<<grid_for(nch, BLK), BLK, 0, S>>>(nch, h->chunk_off, h->chunk_list);
+        FG_LAUNCHED(h, 1);
+        e = cudaGetLastError();
+      }
+      if (e != cudaSuccess) {
+        snprintf(h->err, sizeof h->err, "solve: chunk list: %s", cudaGetErrorString(e));
+        return FLIPGPU_ECUDA;
+      }
+      a.chunk_list = h->chunk_list;
+      a.chunk_count = h->chunk_off + nch;
     }
     /* no more blocks than the grid has work for (about two quads or eight
      * cells per thread): small grids keep short barriers and leave the rest
      * of the GPU to other simulations */
     if (precond != FLIPGPU_PRECOND_IC) {
-      const size_t per_block = (size_t)CG_BLOCK * 8;
+      const size_t per_block = (size_t)cg_block_of(kern) * 8;
       const size_t want = (nc + per_block - 1) / per_block;
       if (want < (size_t)grid) grid = want > 0 ? (int)want : 1;
     }
@@ -2030,7 +1984,8 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
           cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
         }
       }
-      cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(CG_BLOCK), kargs, smem, S);
+      const int block = cg_block_of(kern);
+      cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
       FG_LAUNCHED(h, 1);
       if (e != cudaSuccess) {
         snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
@@ -2195,20 +2150,24 @@ int ic_init_device() {
   return 0;
 }
 
-/* Cooperative grid of each CG variant: SMs x resident blocks (at most 4). */
+/* Cooperative grid of each CG variant (REF, FAST, single-reduction with
+ * small blocks, IC, single-reduction with large blocks): SMs x resident
+ * blocks (at most 4). */
 int cg_grid_size(int *out) {
   int dev = 0, sms = 0, coop = 0;
-  out[0] = out[1] = out[2] = out[3] = 0;
+  for (int v = 0; v < CG_VARIANTS; v++) out[v] = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return -1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   if (!coop) return 0;
   if (ic_init_device() != 0) return -1;
-  const void *k[4] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>, (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
-                      (const void *)k_cg_cg1, (const void *)k_cg_ic};
-  for (int v = 0; v < 4; v++) {
+  const void *k[CG_VARIANTS] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>,
+                                (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
+                                (const void *)k_cg_cg1<CG1_BLOCK_SMALL>, (const void *)k_cg_ic,
+                                (const void *)k_cg_cg1<CG1_BLOCK_LARGE>};
+  for (int v = 0; v < CG_VARIANTS; v++) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], CG_BLOCK,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], cg_block_of(k[v]),
                                                   v == 3 ? ic_smem_bytes() : 0);
     if (per_sm > 4) per_sm = 4;
     out[v] = sms * per_sm;
