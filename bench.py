@@ -109,8 +109,9 @@ def run_batch(args):
 def solver_comparison(gpu, sim, prm, n, systems=3):
     """ms per solve and CG iterations to rel-res 1e-6 on pressure systems
     captured from the next steps of the run, each solved from the same
-    previous-step guess by: plain Jacobi PCG, plain MIC(0) PCG, and both with
-    the learned warm start (trained weights in flip3d_gb300/)."""
+    previous-step guess by: plain Jacobi PCG, plain MIC(0) PCG, plain
+    multigrid PCG, and each with the learned warm start (trained weights in
+    flip3d_gb300/)."""
     sim.set_capture(True)
     caught = []
     for _ in range(systems):
@@ -123,9 +124,13 @@ def solver_comparison(gpu, sim, prm, n, systems=3):
         net.load(WEIGHTS)
     variants = [("plain_jacobi", gpu.PRECOND_JACOBI, 0.0, None),
                 ("plain_mic", gpu.PRECOND_IC, 0.97, None)]
+    if n % 4 == 0:
+        variants.append(("plain_mg", gpu.PRECOND_MG, 0.0, None))
     if net is not None:
         variants += [("learned_jacobi", gpu.PRECOND_JACOBI, 0.0, net),
                      ("learned_mic", gpu.PRECOND_IC, 0.97, net)]
+        if n % 4 == 0:
+            variants.append(("learned_mg", gpu.PRECOND_MG, 0.0, net))
     out = {}
     for name, pre, tau, w in variants:
         p = gpu.Params.from_buffer_copy(prm)
@@ -150,6 +155,12 @@ def solver_comparison(gpu, sim, prm, n, systems=3):
             out["plain_mic"]["ms_per_solve"]
         out["learned_vs_plain_jacobi"] = out["learned_jacobi"]["ms_per_solve"] / \
             out["plain_jacobi"]["ms_per_solve"]
+    if "plain_mg" in out:
+        out["plain_mg_vs_plain_mic"] = out["plain_mg"]["ms_per_solve"] / \
+            out["plain_mic"]["ms_per_solve"]
+    if "learned_mg" in out:
+        out["learned_mg_vs_plain_mic"] = out["learned_mg"]["ms_per_solve"] / \
+            out["plain_mic"]["ms_per_solve"]
     out["systems"] = systems
     return out
 
@@ -189,16 +200,34 @@ def liquid_chunk_cells(A):
     return int(f.reshape(-1, 128).any(axis=1).sum()) * 128
 
 
-def stage_bytes(stage, P, n, iters, sweep_cells=None):
+def mg_coarse_cells(n):
+    """Cells of the multigrid levels below the solver's grid (ceil(m/2) per
+    axis down to at most 4)."""
+    tot, m = 0, n
+    while m > 4:
+        m = (m + 1) // 2
+        tot += m ** 3
+    return tot
+
+
+def stage_bytes(stage, P, n, iters, sweep_cells=None, precond="jacobi"):
     """Algorithmic bytes of one call of a stage: every input read once and
     every output written once, nothing else. The PCG solve is one setup pass
     over the grid (A, x, b, M^-1 read, 13 B; r and x written, 8 B) and per
-    iteration 49 B per cell of the liquid chunks (sweep_cells; the whole
-    grid when not given): A 1 + diagonal 4 + M^-1 4 + U, Wt, St, p, x
-    4 each read, U, Wt, St, p, x 4 each written."""
+    iteration, over the cells of the liquid chunks (sweep_cells; the whole
+    grid when not given):
+      Jacobi (single reduction): 49 B: A 1 + diagonal 4 + M^-1 4 + U, Wt, St,
+        p, x 4 each read, U, Wt, St, p, x 4 each written;
+      multigrid: 136 B on the solver's grid (seven passes, each reading A and
+        the diagonal, 5 B, and its vectors: p' = z + beta p and A p' 16 B,
+        the x/r update and first half sweep 28 B, two black and one red half
+        sweep 12 B each, the residual 12 B, the prolongation 8.5 B) plus 90 B
+        per cell of every coarser level (three half sweeps, a residual, the
+        restriction's writes and the prolongation, about 15 B each)."""
     C = n ** 3
     F = 3 * (n + 1) * n * n
     cells = C if sweep_cells is None else sweep_cells
+    solve_iter = 49 * cells if precond != "mg" else 136 * cells + 90 * mg_coarse_cells(n)
     table = {
         # count: pos 12 r, key 4 w, rank 4 w; scatter: key+rank 8 r, perm 4 w;
         # cell counts/starts 3*4*C; payload: perm 4 + pos 12 + vel 12 + type 1 + dens 4 r,
@@ -208,7 +237,7 @@ def stage_bytes(stage, P, n, iters, sweep_cells=None):
         "mark_water": P * 8 + 4 * C + 5 * C,
         "p2g": P * 32 + 4 * C + C + 2 * 4 * F,
         "divergence": C + 4 * F + 4 * C,
-        "solve": 21 * C + max(iters, 1) * 49 * cells,
+        "solve": 21 * C + max(iters, 1) * solve_iter,
         "gradient": 4 * F * 2 + 9 * C,
         "extrapolate": 4 * F * 3 + C,
         "g2p_flip": P * (12 + 1 + 12 + 12) + 2 * 4 * F,
@@ -349,7 +378,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=128)
-    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "ic", "mic", "ref"])
+    ap.add_argument("--precond", default="mg", choices=["jacobi", "ic", "mic", "mg", "ref"],
+                    help="preconditioner of the FAST-mode PCG (mg: multigrid V-cycle)")
     ap.add_argument("--arith", default="fast", choices=["fast", "ref"],
                     help="particle-gather arithmetic: native FP32 (fast) or the reference's "
                          "float expressions bit for bit (ref)")
@@ -365,6 +395,8 @@ def main():
                          "CUDA graphs on per-scene streams) and one at a time")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.precond == "mg" and (args.n % 4 != 0 or args.n < 8):
+        args.precond = "jacobi"  # the multigrid solver works on quads of cells
     if args.batch_scenes > 0:
         run_batch(args)
         return
@@ -387,7 +419,7 @@ def main():
     t_build = time.perf_counter() - t_build
     P = sc.count
     pre = {"jacobi": gpu.PRECOND_JACOBI, "ic": gpu.PRECOND_IC, "mic": gpu.PRECOND_IC,
-           "ref": gpu.PRECOND_REF}[args.precond]
+           "mg": gpu.PRECOND_MG, "ref": gpu.PRECOND_REF}[args.precond]
     mode = gpu.SOLVE_REF if args.precond == "ref" else gpu.SOLVE_FAST
     prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1,
                              mic_tau=0.97 if args.precond == "mic" else 0.0,
@@ -456,7 +488,7 @@ def main():
     dom_ms = prof[dom][0] / max(prof[dom][1], 1)
     it_prof = int(st.iterations)
     sweep_cells = liquid_chunk_cells(sim.get_grid()[1])
-    nbytes = stage_bytes(dom, P, args.n, it_prof, sweep_cells)
+    nbytes = stage_bytes(dom, P, args.n, it_prof, sweep_cells, args.precond)
     peak, peak_kind = hbm_peak()
     achieved = nbytes / (dom_ms / 1e3) / 1e9
     traffic = measured_traffic(dom, args.n)
@@ -528,8 +560,8 @@ def main():
                          "peak_source": peak_kind, "algorithmic_bytes": nbytes,
                          "ms_per_launch": dom_ms,
                          "bytes_model": "stage_bytes(): every input read once, every output "
-                                        "written once; the solve counts its per-iteration "
-                                        "sweep over the liquid chunks only",
+                                        "written once; the solve counts its solver-grid "
+                                        "passes over the liquid chunks only",
                          "sweep_cells": sweep_cells},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": P * 24,

@@ -394,6 +394,7 @@ int flipgpu_destroy(FlipGpu *h) {
   if (h->graph) cudaGraphDestroy(h->graph);
   export_free(h);
   mesh_free(h);
+  mg_free(h);
   if (h->wdelta) {
     cudaFree(h->wdelta);
     cudaFree(h->wpart);

@@ -64,7 +64,7 @@ struct SimConst {
   const int64_t *dstep; /* the step counter in device memory (graph replays advance it) */
 };
 
-constexpr int CG_VARIANTS = 5; /* persistent CG kernels (k_pcg.cu cg_grid_size) */
+constexpr int CG_VARIANTS = 6; /* persistent CG kernels (k_pcg.cu cg_grid_size) */
 
 struct FlipGpu {
   FlipGpuParams prm;
@@ -113,6 +113,11 @@ struct FlipGpu {
   /* solver */
   float *r, *z, *s, *s1, *w;
   float *w1, *pdir;   /* single-reduction CG: second w buffer, directions */
+  /* MG preconditioner (k_pcg.cu mg_alloc): levels 1.. and level-0 scratch */
+  int mg_nlev, mg_lb, mg_m[10];
+  uint8_t *mg_flags[10];
+  float *mg_diag[10], *mg_x[10], *mg_b[10], *mg_res[10];
+  float *mg_p2, *mg_q;
   unsigned *chunk_off;  /* single-reduction CG: liquid flags of the 32-quad chunks, scanned */
   unsigned *chunk_list; /* ... and the indices of the chunks that hold liquid */
   double *P;          /* REF preconditioner diagonal (double, as the reference) */
@@ -123,7 +128,8 @@ struct FlipGpu {
   int *iflags;        /* device flags/counters */
   unsigned *bar;      /* grid barrier of the persistent CG: count, generation */
   int cg_grid[CG_VARIANTS]; /* cooperative CG grids (0 = none): REF, FAST, FAST single-
-                               reduction (small blocks), FAST IC, single-reduction (large) */
+                               reduction (small blocks), FAST IC, single-reduction (large),
+                               FAST MG */
   int nbx, nbricks;   /* 8^3 bricks of the IC wavefront */
   unsigned *brick_order, *fflag, *bflag, *ticket;
   float2 *brick_part;
@@ -216,6 +222,8 @@ int export_join(FlipGpu *h);
 void export_free(FlipGpu *h);
 int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
+int mg_alloc(FlipGpu *h);  /* MG preconditioner buffers (idempotent) */
+void mg_free(FlipGpu *h);
 int particles_init_device();
 
 /* device-wide exclusive scan of n uint32 (in may equal out) */

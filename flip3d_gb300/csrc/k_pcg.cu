@@ -22,6 +22,7 @@
  * r.r <= rel_tol^2 * b.b.
  */
 #include <cstdio>
+#include <cstring>
 #include <type_traits>
 #include <vector>
 
@@ -446,6 +447,24 @@ constexpr int CG_BLOCK = 256;
 constexpr int CG1_BLOCK_SMALL = 384, CG1_BLOCK_LARGE = 512, CG1_LARGE_N = 192;
 constexpr unsigned long long BAR_SPIN_LIMIT = 1ull << 26; /* ~seconds, then ETIMEOUT */
 
+/* Geometric multigrid levels of the MG preconditioner (level 0 is the
+ * solver's grid; level l has ceil(n / 2^l) cells per axis). */
+constexpr int MG_MAX_LEVELS = 10;
+struct MgLevel {
+  int m;                 /* cells per axis */
+  const uint8_t *flags;  /* CELL_FLUID / CELL_AIR / CELL_WALL */
+  const float *diag;     /* level 0: the operator's diagonal; coarser: non-wall neighbours */
+  float *x, *b, *res;    /* correction, right-hand side, residual */
+  float hs, ihs;         /* 1 / h^2 of the level and its inverse */
+  int lgm;               /* log2(m) when m is a power of two, else -1 */
+};
+struct MgArgs {
+  MgLevel lv[MG_MAX_LEVELS];
+  int nlev;              /* number of levels */
+  int lb;                /* levels lb.. are solved by block 0 alone */
+  int coarse_sweeps;     /* symmetric Gauss-Seidel sweeps on the coarsest level */
+};
+
 struct CgArgs {
   SolveArgs s;
   size_t nc;
@@ -474,6 +493,9 @@ struct CgArgs {
   unsigned *fflag, *bflag;     /* epoch of the last forward / backward sweep done */
   unsigned *ticket;
   float2 *brick_part;          /* per-brick z.r partials */
+  /* MG-preconditioned CG */
+  float *p2, *q;               /* second direction buffer, A p */
+  MgArgs mg;
 };
 
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags,
@@ -1303,6 +1325,762 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_cg1(CgArgs
   }
 }
 
+/* ------------------------------------------ multigrid-preconditioned CG */
+
+/* MG-PCG (FAST mode, n % 4 == 0): PCG whose preconditioner is one symmetric
+ * V-cycle of geometric multigrid, the structure of McAdams, Sifakis and
+ * Teran ("A parallel multigrid Poisson solver for fluids simulation on large
+ * grids", SCA 2010):
+ *   - smoothing: red-black Gauss-Seidel, one red then black half sweep
+ *     before the coarse correction and black then red after it (red: i+j+k
+ *     even), starting from a zero correction;
+ *   - restriction: the average of the 8 children's residuals; prolongation:
+ *     the coarse correction added to its 8 children;
+ *   - coarser operators: the 7-point Laplacian rediscretised on the
+ *     coarsened flags (a coarse cell is liquid if a child is, else air if a
+ *     child is, else wall; air is a zero Dirichlet value, wall a zero flux);
+ *   - the coarsest level (at most 4^3 cells): coarse_sweeps red-black
+ *     sweeps, then as many black-red ones.
+ * Every count is fixed and the post-smoothing mirrors the pre-smoothing, so
+ * the V-cycle is a fixed symmetric operator, as PCG needs. One persistent
+ * cooperative launch per solve: level 0 runs on quads over the liquid
+ * chunks, the middle levels on cells grid-wide, and the levels of at most
+ * 16^3 cells inside block 0's shared memory; counting barriers separate the
+ * phases. x is 0 off the liquid on every level, so neighbour sums need no
+ * flags. */
+constexpr int MGU = 4;            /* cells per thread and round, loads first */
+constexpr unsigned MG_BLOCK_CELLS = 4096; /* levels this small run in block 0 */
+
+template <bool GLOBAL> __device__ __forceinline__ float mg_ld(const float *p) {
+  if (GLOBAL) return __ldcg(p);
+  return *p;
+}
+
+__device__ __forceinline__ void mg_decode(unsigned c, unsigned m, int &i, int &j, int &k) {
+  const unsigned row = c / m;
+  k = (int)(c - row * m);
+  i = (int)(row / m);
+  j = (int)(row - (unsigned)i * m);
+}
+
+/* the same with shifts when m = 2^lg (lg >= 0) */
+__device__ __forceinline__ void mg_decode(unsigned c, unsigned m, int lg, int &i, int &j,
+                                          int &k) {
+  if (lg >= 0) {
+    k = (int)(c & (m - 1));
+    j = (int)((c >> lg) & (m - 1));
+    i = (int)(c >> (2 * lg));
+  } else {
+    mg_decode(c, m, i, j, k);
+  }
+}
+
+template <bool GLOBAL>
+__device__ __forceinline__ float mg_nbsum(const float *x, int m, int i, int j, int k, unsigned c) {
+  const unsigned mm = (unsigned)m * m;
+  float s = 0.0f;
+  if (i > 0) s += mg_ld<GLOBAL>(x + c - mm);
+  if (i + 1 < m) s += mg_ld<GLOBAL>(x + c + mm);
+  if (j > 0) s += mg_ld<GLOBAL>(x + c - m);
+  if (j + 1 < m) s += mg_ld<GLOBAL>(x + c + m);
+  if (k > 0) s += mg_ld<GLOBAL>(x + c - 1);
+  if (k + 1 < m) s += mg_ld<GLOBAL>(x + c + 1);
+  return s;
+}
+
+/* red-black half sweep: liquid cells of `color` take
+ * x = (b / hs + sum of the neighbours' x) / diag */
+template <bool GLOBAL>
+__device__ void mg_gs(const MgLevel &L, int color, unsigned start, unsigned stride) {
+  const unsigned m = (unsigned)L.m, tot = m * m * m;
+  if (L.lgm >= 1) {
+    /* m = 2^lg: enumerate the cells of the colour only (k = 2 kk + parity) */
+    const int lg = L.lgm;
+    const unsigned half = tot >> 1, hm = m >> 1;
+    for (unsigned h0 = start; h0 < half; h0 += stride * MGU) {
+      float nbs[MGU], bv[MGU], dv[MGU];
+      unsigned cc[MGU];
+      bool upd[MGU];
+#pragma unroll
+      for (int u = 0; u < MGU; u++) {
+        const unsigned h = h0 + (unsigned)u * stride;
+        upd[u] = false;
+        nbs[u] = bv[u] = 0.0f;
+        dv[u] = 1.0f;
+        cc[u] = 0;
+        if (h < half) {
+          const unsigned row = h >> (lg - 1);
+          const int j = (int)(row & (m - 1)), i = (int)(row >> lg);
+          const int k = 2 * (int)(h & (hm - 1)) + ((i + j + color) & 1);
+          const unsigned c = (row << lg) + (unsigned)k;
+          cc[u] = c;
+          upd[u] = L.flags[c] == CELL_FLUID;
+          bv[u] = mg_ld<GLOBAL>(L.b + c);
+          dv[u] = L.diag[c];
+          nbs[u] = mg_nbsum<GLOBAL>(L.x, (int)m, i, j, k, c);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < MGU; u++)
+        if (upd[u]) L.x[cc[u]] = __fdividef(bv[u] * L.ihs + nbs[u], dv[u]);
+    }
+    return;
+  }
+  for (unsigned c0 = start; c0 < tot; c0 += stride * MGU) {
+    float nbs[MGU], bv[MGU], dv[MGU];
+    bool upd[MGU];
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      upd[u] = false;
+      nbs[u] = bv[u] = 0.0f;
+      dv[u] = 1.0f;
+      if (c < tot) {
+        int i, j, k;
+        mg_decode(c, m, L.lgm, i, j, k);
+        if (((i + j + k) & 1) == color) {
+          upd[u] = L.flags[c] == CELL_FLUID;
+          bv[u] = mg_ld<GLOBAL>(L.b + c);
+          dv[u] = L.diag[c];
+          nbs[u] = mg_nbsum<GLOBAL>(L.x, (int)m, i, j, k, c);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MGU; u++)
+      if (upd[u]) L.x[c0 + (unsigned)u * stride] = __fdividef(bv[u] * L.ihs + nbs[u], dv[u]);
+  }
+}
+
+/* res = b - A x on the liquid, 0 elsewhere */
+template <bool GLOBAL>
+__device__ void mg_residual(const MgLevel &L, unsigned start, unsigned stride) {
+  const unsigned m = (unsigned)L.m, tot = m * m * m;
+  for (unsigned c0 = start; c0 < tot; c0 += stride * MGU) {
+    float nbs[MGU], bv[MGU], dv[MGU], xv[MGU];
+    bool fl_[MGU];
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      fl_[u] = false;
+      nbs[u] = bv[u] = dv[u] = xv[u] = 0.0f;
+      if (c < tot) {
+        int i, j, k;
+        mg_decode(c, m, L.lgm, i, j, k);
+        fl_[u] = L.flags[c] == CELL_FLUID;
+        bv[u] = mg_ld<GLOBAL>(L.b + c);
+        dv[u] = L.diag[c];
+        xv[u] = mg_ld<GLOBAL>(L.x + c);
+        nbs[u] = mg_nbsum<GLOBAL>(L.x, (int)m, i, j, k, c);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      if (c < tot) L.res[c] = fl_[u] ? bv[u] - L.hs * (dv[u] * xv[u] - nbs[u]) : 0.0f;
+    }
+  }
+}
+
+/* coarse b = mean of the 8 children's residuals; coarse x = its first red
+ * half sweep from zero (b / (hs diag) on red liquid cells, 0 elsewhere) */
+template <bool GF, bool GC>
+__device__ void mg_restrict(const MgLevel &F, const MgLevel &Cl, unsigned start, unsigned stride) {
+  const unsigned mc = (unsigned)Cl.m, totc = mc * mc * mc, mf = (unsigned)F.m;
+  for (unsigned c0 = start; c0 < totc; c0 += stride * MGU) {
+    float sum[MGU];
+    bool red[MGU], fl_[MGU];
+    float dv[MGU];
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      sum[u] = 0.0f;
+      red[u] = fl_[u] = false;
+      dv[u] = 1.0f;
+      if (c < totc) {
+        int I, J, K;
+        mg_decode(c, mc, Cl.lgm, I, J, K);
+        red[u] = ((I + J + K) & 1) == 0;
+        fl_[u] = Cl.flags[c] == CELL_FLUID;
+        dv[u] = Cl.diag[c];
+        if ((mf & 1u) == 0) { /* the k pair as one aligned float2 */
+#pragma unroll
+          for (int a = 0; a < 2; a++)
+#pragma unroll
+            for (int b = 0; b < 2; b++) {
+              const unsigned i = 2u * I + a, j = 2u * J + b;
+              const float2 *pp =
+                  reinterpret_cast<const float2 *>(F.res + (i * mf + j) * mf + 2u * K);
+              const float2 v = GF ? __ldcg(pp) : *pp;
+              sum[u] += v.x;
+              sum[u] += v.y;
+            }
+        } else {
+#pragma unroll
+          for (int a = 0; a < 2; a++)
+#pragma unroll
+            for (int b = 0; b < 2; b++)
+#pragma unroll
+              for (int d = 0; d < 2; d++) {
+                const unsigned i = 2u * I + a, j = 2u * J + b, k = 2u * K + d;
+                if (i < mf && j < mf && k < mf)
+                  sum[u] += mg_ld<GF>(F.res + (i * mf + j) * mf + k);
+              }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      if (c >= totc) continue;
+      const float bc = sum[u] * 0.125f;
+      Cl.b[c] = bc;
+      Cl.x[c] = (red[u] && fl_[u]) ? __fdividef(bc * Cl.ihs, dv[u]) : 0.0f;
+    }
+  }
+}
+
+/* x += the parent's correction on the liquid */
+template <bool GF, bool GC>
+__device__ void mg_prolong(const MgLevel &F, const MgLevel &Cl, unsigned start, unsigned stride) {
+  const unsigned mf = (unsigned)F.m, tot = mf * mf * mf, mc = (unsigned)Cl.m;
+  for (unsigned c0 = start; c0 < tot; c0 += stride * MGU) {
+    float xv[MGU], ev[MGU];
+    bool fl_[MGU];
+#pragma unroll
+    for (int u = 0; u < MGU; u++) {
+      const unsigned c = c0 + (unsigned)u * stride;
+      fl_[u] = false;
+      xv[u] = ev[u] = 0.0f;
+      if (c < tot) {
+        int i, j, k;
+        mg_decode(c, mf, F.lgm, i, j, k);
+        const unsigned pc =
+            (((unsigned)i >> 1) * mc + ((unsigned)j >> 1)) * mc + ((unsigned)k >> 1);
+        fl_[u] = F.flags[c] == CELL_FLUID;
+        xv[u] = mg_ld<GF>(F.x + c);
+        ev[u] = mg_ld<GC>(Cl.x + pc);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < MGU; u++)
+      if (fl_[u]) F.x[c0 + (unsigned)u * stride] = xv[u] + ev[u];
+  }
+}
+
+/* The levels lb.. in block 0's shared memory: V-cycle from level lb's b and
+ * first half sweep (in global memory, from the restriction) to level lb's
+ * corrected x (written back to global memory). */
+__device__ void mg_block_levels(const MgArgs &mg, MgLevel *sl) {
+  const unsigned t = threadIdx.x, S = blockDim.x;
+  const int lb = mg.lb, last = mg.nlev - 1;
+  const MgLevel &G = mg.lv[lb];
+  const unsigned m0 = (unsigned)G.m, tot0 = m0 * m0 * m0;
+  for (unsigned c0 = t; c0 < tot0; c0 += S * 8) {
+    float bv[8], xv[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const unsigned c = c0 + (unsigned)u * S;
+      bv[u] = c < tot0 ? __ldcg(G.b + c) : 0.0f;
+      xv[u] = c < tot0 ? __ldcg(G.x + c) : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const unsigned c = c0 + (unsigned)u * S;
+      if (c < tot0) {
+        sl[lb].b[c] = bv[u];
+        sl[lb].x[c] = xv[u];
+      }
+    }
+  }
+  __syncthreads();
+  for (int l = lb; l < last; l++) {
+    mg_gs<false>(sl[l], 1, t, S);
+    __syncthreads();
+    mg_residual<false>(sl[l], t, S);
+    __syncthreads();
+    mg_restrict<false, false>(sl[l], sl[l + 1], t, S);
+    __syncthreads();
+  }
+  /* coarsest: the restriction did the first red half sweep */
+  mg_gs<false>(sl[last], 1, t, S);
+  __syncthreads();
+  for (int it = 1; it < mg.coarse_sweeps; it++) {
+    mg_gs<false>(sl[last], 0, t, S);
+    __syncthreads();
+    mg_gs<false>(sl[last], 1, t, S);
+    __syncthreads();
+  }
+  for (int it = 0; it < mg.coarse_sweeps; it++) {
+    mg_gs<false>(sl[last], 1, t, S);
+    __syncthreads();
+    mg_gs<false>(sl[last], 0, t, S);
+    __syncthreads();
+  }
+  for (int l = last - 1; l >= lb; l--) {
+    mg_prolong<false, false>(sl[l], sl[l + 1], t, S);
+    __syncthreads();
+    mg_gs<false>(sl[l], 1, t, S);
+    __syncthreads();
+    mg_gs<false>(sl[l], 0, t, S);
+    __syncthreads();
+  }
+  for (unsigned c = t; c < tot0; c += S) G.x[c] = sl[lb].x[c];
+}
+
+/* Shared-memory bytes of block 0's levels (flags, diag, x, b, res). */
+__host__ __device__ inline size_t mg_block_bytes(const int *m, int lb, int nlev) {
+  size_t b = 0;
+  for (int l = lb; l < nlev; l++) {
+    const size_t c = (size_t)m[l] * m[l] * m[l];
+    b += (c + 15) / 16 * 16 + 4 * 4 * c;
+  }
+  return b;
+}
+
+/* Level-0 phases on quads of the liquid chunks. */
+enum MgPhase { MG_MATVEC, MG_UPDATE, MG_BLACK, MG_RES, MG_PROLONG, MG_RED_DOT };
+
+template <int PH, int BLOCK>
+__device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float beta, const float *pold,
+                                         float *pnew, FF &acc0) {
+  const int n = a.s.n, qrow = n / 4;
+  const size_t qplane = (size_t)qrow * n, nq = a.nc / 4;
+  const size_t warps = (size_t)gridDim.x * (BLOCK / 32);
+  const size_t wid = (size_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const unsigned FULL = 0xffffffffu;
+  const MgLevel &L0 = a.mg.lv[0];
+  const float hs = L0.hs, ihs = L0.ihs;
+  const uchar4 *A4p = reinterpret_cast<const uchar4 *>(a.A);
+  const float4 *d4p = reinterpret_cast<const float4 *>(a.diag);
+  float *zf = L0.x, *rf = a.r;
+  const float4 zero = make_float4(0, 0, 0, 0);
+  const unsigned nact = __ldcg(a.chunk_count);
+  unsigned cnext = wid < nact ? __ldg(a.chunk_list + wid) : 0u;
+  for (size_t t = wid; t < nact; t += warps) {
+    const size_t q = (size_t)cnext * 32 + lane;
+    if (t + warps < nact) cnext = __ldg(a.chunk_list + t + warps);
+    const bool valid = q < nq;
+    const size_t qs = valid ? q : 0;
+    const unsigned q32 = (unsigned)qs, row = q32 / (unsigned)qrow;
+    const int kq = (int)(q32 - row * (unsigned)qrow);
+    const int i = (int)(row / (unsigned)n), j = (int)(row - (unsigned)i * (unsigned)n);
+    const int k0 = 4 * kq;
+    const size_t c0 = 4 * qs;
+    const uchar4 A4 = A4p[qs];
+    const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+    const int par0 = (i + j + k0) & 1; /* colour of the quad's first cell */
+    constexpr bool NB = PH == MG_MATVEC || PH == MG_BLACK || PH == MG_RES || PH == MG_RED_DOT;
+    /* the field whose neighbours are summed: p' = z + beta p (MATVEC) or z */
+    float4 own = zero;
+    float4 nbq[4] = {zero, zero, zero, zero};
+    float edge = 0.0f;
+    const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
+    const long off[4] = {(long)qplane, -(long)qplane, (long)qrow, -(long)qrow};
+    const bool ed = (lane == 0 && k0 > 0) || (lane == 31 && k0 + 4 < n);
+    const size_t ce = lane == 0 ? c0 - 1 : c0 + 4;
+    if (PH == MG_MATVEC) {
+      const float4 z4 = __ldcg(reinterpret_cast<const float4 *>(zf) + qs);
+      const float4 p4 = __ldcg(reinterpret_cast<const float4 *>(pold) + qs);
+      own = make_float4(z4.x + beta * p4.x, z4.y + beta * p4.y, z4.z + beta * p4.z,
+                        z4.w + beta * p4.w);
+#pragma unroll
+      for (int d = 0; d < 4; d++)
+        if (has[d]) {
+          const size_t qq = (size_t)((long)qs + off[d]);
+          const float4 zn = __ldcg(reinterpret_cast<const float4 *>(zf) + qq);
+          const float4 pn = __ldcg(reinterpret_cast<const float4 *>(pold) + qq);
+          nbq[d] = make_float4(zn.x + beta * pn.x, zn.y + beta * pn.y, zn.z + beta * pn.z,
+                               zn.w + beta * pn.w);
+        }
+      if (ed) edge = __ldcg(zf + ce) + beta * __ldcg(pold + ce);
+    } else if (NB || PH == MG_PROLONG || PH == MG_UPDATE) {
+      if (PH != MG_UPDATE) own = __ldcg(reinterpret_cast<const float4 *>(zf) + qs);
+      if (NB) {
+#pragma unroll
+        for (int d = 0; d < 4; d++)
+          if (has[d])
+            nbq[d] = __ldcg(reinterpret_cast<const float4 *>(zf) + (size_t)((long)qs + off[d]));
+        if (ed) edge = __ldcg(zf + ce);
+      }
+    }
+    /* k neighbours across quads */
+    float left = __shfl_up_sync(FULL, own.w, 1);
+    float right = __shfl_down_sync(FULL, own.x, 1);
+    if (k0 == 0) left = 0.0f;
+    else if (lane == 0) left = edge;
+    if (k0 + 4 >= n) right = 0.0f;
+    else if (lane == 31) right = edge;
+    if (!valid || !(fv[0] || fv[1] || fv[2] || fv[3])) continue;
+    const float ov[4] = {own.x, own.y, own.z, own.w};
+    float nbs[4];
+    if (NB) {
+      const float kl[4] = {left, ov[0], ov[1], ov[2]}, kr[4] = {ov[1], ov[2], ov[3], right};
+      const float n0[4] = {nbq[0].x, nbq[0].y, nbq[0].z, nbq[0].w};
+      const float n1[4] = {nbq[1].x, nbq[1].y, nbq[1].z, nbq[1].w};
+      const float n2[4] = {nbq[2].x, nbq[2].y, nbq[2].z, nbq[2].w};
+      const float n3[4] = {nbq[3].x, nbq[3].y, nbq[3].z, nbq[3].w};
+#pragma unroll
+      for (int u = 0; u < 4; u++) nbs[u] = ((((n0[u] + n1[u]) + n2[u]) + n3[u]) + kl[u]) + kr[u];
+    }
+    if (PH == MG_MATVEC) {
+      const float4 dg = __ldg(d4p + qs);
+      const float dv[4] = {dg.x, dg.y, dg.z, dg.w};
+      float qv[4], pv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        pv[u] = fv[u] ? ov[u] : 0.0f;
+        qv[u] = fv[u] ? hs * (dv[u] * ov[u] - nbs[u]) : 0.0f;
+        if (fv[u]) ff_add_prod(acc0, pv[u], qv[u]);
+      }
+      reinterpret_cast<float4 *>(pnew)[q] = make_float4(pv[0], pv[1], pv[2], pv[3]);
+      reinterpret_cast<float4 *>(a.q)[q] = make_float4(qv[0], qv[1], qv[2], qv[3]);
+    } else if (PH == MG_UPDATE) {
+      /* x += alpha p', r -= alpha q; r.r; z: first red half sweep from 0 */
+      const float4 x4 = __ldcg(reinterpret_cast<const float4 *>(a.x) + q);
+      const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
+      const float4 p4 = __ldcg(reinterpret_cast<const float4 *>(pnew) + q);
+      const float4 q4 = __ldcg(reinterpret_cast<const float4 *>(a.q) + q);
+      const float4 dg = __ldg(d4p + qs);
+      const float xv[4] = {x4.x, x4.y, x4.z, x4.w}, rv[4] = {r4.x, r4.y, r4.z, r4.w};
+      const float pv[4] = {p4.x, p4.y, p4.z, p4.w}, qv[4] = {q4.x, q4.y, q4.z, q4.w};
+      const float dv[4] = {dg.x, dg.y, dg.z, dg.w};
+      float xn[4], rn[4], zn[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        if (fv[u]) {
+          xn[u] = xv[u] + alpha * pv[u];
+          rn[u] = rv[u] - alpha * qv[u];
+          ff_add_prod(acc0, rn[u], rn[u]);
+          zn[u] = ((par0 + u) & 1) == 0 ? __fdividef(rn[u] * ihs, dv[u]) : 0.0f;
+        } else {
+          xn[u] = xv[u];
+          rn[u] = zn[u] = 0.0f;
+        }
+      }
+      reinterpret_cast<float4 *>(a.x)[q] = make_float4(xn[0], xn[1], xn[2], xn[3]);
+      reinterpret_cast<float4 *>(rf)[q] = make_float4(rn[0], rn[1], rn[2], rn[3]);
+      reinterpret_cast<float4 *>(zf)[q] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+    } else if (PH == MG_PROLONG) {
+      const MgLevel &L1 = a.mg.lv[1];
+      const unsigned m1 = (unsigned)L1.m;
+      const unsigned pidx = (((unsigned)i >> 1) * m1 + ((unsigned)j >> 1)) * m1 + (unsigned)(k0 >> 1);
+      const float2 e = __ldcg(reinterpret_cast<const float2 *>(L1.x + pidx));
+      const float ev[4] = {e.x, e.x, e.y, e.y};
+      float zn[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) zn[u] = fv[u] ? ov[u] + ev[u] : 0.0f;
+      reinterpret_cast<float4 *>(zf)[q] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+    } else if (PH == MG_RES) {
+      const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
+      const float4 dg = __ldg(d4p + qs);
+      const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, dv[4] = {dg.x, dg.y, dg.z, dg.w};
+      float res[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) res[u] = fv[u] ? rv[u] - hs * (dv[u] * ov[u] - nbs[u]) : 0.0f;
+      reinterpret_cast<float4 *>(L0.res)[q] = make_float4(res[0], res[1], res[2], res[3]);
+    } else { /* MG_BLACK, MG_RED_DOT: half sweep of one colour */
+      const int color = PH == MG_BLACK ? 1 : 0;
+      const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
+      const float4 dg = __ldg(d4p + qs);
+      const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, dv[4] = {dg.x, dg.y, dg.z, dg.w};
+      float zn[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        zn[u] = ov[u];
+        if (fv[u] && ((par0 + u) & 1) == color) zn[u] = __fdividef(rv[u] * ihs + nbs[u], dv[u]);
+        if (PH == MG_RED_DOT && fv[u]) ff_add_prod(acc0, rv[u], zn[u]);
+      }
+      reinterpret_cast<float4 *>(zf)[q] = make_float4(zn[0], zn[1], zn[2], zn[3]);
+    }
+  }
+}
+
+template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs a) {
+  const unsigned nb = gridDim.x;
+  const int n = a.s.n;
+  const int qrow = n / 4;
+  const size_t qplane = (size_t)qrow * n;
+  const size_t nq = a.nc / 4;
+  const size_t warps = (size_t)nb * (BLOCK / 32);
+  const size_t wid = (size_t)blockIdx.x * (BLOCK / 32) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  float4 *x4 = reinterpret_cast<float4 *>(a.x);
+  const float4 *b4 = reinterpret_cast<const float4 *>(a.b);
+  const MgArgs &mg = a.mg;
+  const unsigned gt = blockIdx.x * BLOCK + threadIdx.x, gs = nb * BLOCK;
+  unsigned epoch = 0;
+  __shared__ float s_alpha, s_beta;
+  __shared__ int s_done;
+  extern __shared__ __align__(16) unsigned char mg_smem[];
+
+  /* block 0: its levels' flags and diagonals into shared memory (fixed
+   * during the solve) */
+  MgLevel sl[MG_MAX_LEVELS];
+  if (blockIdx.x == 0) {
+    unsigned char *pp = mg_smem;
+    for (int l = mg.lb; l < mg.nlev; l++) {
+      const unsigned m = (unsigned)mg.lv[l].m, c = m * m * m;
+      sl[l] = mg.lv[l];
+      uint8_t *fl8 = pp;
+      pp += (c + 15) / 16 * 16;
+      float *dg = reinterpret_cast<float *>(pp);
+      sl[l].x = dg + c;
+      sl[l].b = dg + 2 * c;
+      sl[l].res = dg + 3 * c;
+      pp += 4 * 4 * (size_t)c;
+      for (unsigned e = threadIdx.x; e < c; e += BLOCK) {
+        fl8[e] = mg.lv[l].flags[e];
+        dg[e] = mg.lv[l].diag[e];
+      }
+      sl[l].flags = fl8;
+      sl[l].diag = dg;
+    }
+  }
+
+  /* phase 0: r = b - A x on the liquid (x zeroed elsewhere); b.b, r.r */
+  FF pbb = ff_zero(), prr = ff_zero();
+  for (size_t base = wid * 32; base < nq; base += warps * 32) {
+    size_t q = base + lane;
+    bool valid = q < nq;
+    int i = 0, j = 0, kq = 0;
+    if (valid) {
+      const unsigned q32 = (unsigned)q, row = q32 / (unsigned)qrow;
+      kq = (int)(q32 - row * (unsigned)qrow);
+      i = (int)(row / (unsigned)n);
+      j = (int)(row - (unsigned)i * (unsigned)n);
+    }
+    float4 xs, ax;
+    uchar4 A4;
+    quad_matvec(a, valid ? q : 0, valid, qrow, qplane, i, j, kq, a.x, a.x, 0.0f, true, xs, ax, A4);
+    if (!valid) continue;
+    const float4 bv = b4[q];
+    const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
+    const float bb[4] = {bv.x, bv.y, bv.z, bv.w}, av[4] = {ax.x, ax.y, ax.z, ax.w};
+    const float4 xo = x4[q];
+    const float xov[4] = {xo.x, xo.y, xo.z, xo.w};
+    float rv[4], xv[4];
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+      if (fv[t]) {
+        ff_add_prod(pbb, bb[t], bb[t]);
+        rv[t] = bb[t] - av[t];
+        ff_add_prod(prr, rv[t], rv[t]);
+        xv[t] = xov[t];
+      } else {
+        rv[t] = xv[t] = 0.0f;
+      }
+    }
+    reinterpret_cast<float4 *>(a.r)[q] = make_float4(rv[0], rv[1], rv[2], rv[3]);
+    x4[q] = make_float4(xv[0], xv[1], xv[2], xv[3]);
+  }
+  {
+    FF v[2] = {pbb, prr};
+    store_partials<2, BLOCK>(a.part, 0, nb, v);
+  }
+  if (!count_barrier(a.bar, epoch, a.iflags)) return;
+  double b2 = 0.0, eps = 0.0, e2 = 0.0, rz = 0.0, alpha = 0.0, beta = 0.0;
+  int done = 0, iters = 0;
+  if (threadIdx.x < 32) {
+    double t[2];
+    warp_sum_partials<2>(a.part, 0, nb, t);
+    if (threadIdx.x == 0) {
+      b2 = t[0];
+      e2 = t[1];
+      eps = a.rel_tol * a.rel_tol * b2;
+      s_done = e2 <= eps ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  done = s_done;
+
+  /* z = V-cycle(r) after the level-0 first red half sweep (MG_UPDATE);
+   * the final red half sweep accumulates r.z */
+  auto vcycle_rest = [&](FF &prz) -> bool {
+    FF none = ff_zero();
+    mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    mg_quads<MG_RES, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    mg_restrict<true, true>(mg.lv[0], mg.lv[1], gt, gs);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    for (int l = 1; l < mg.lb; l++) {
+      mg_gs<true>(mg.lv[l], 1, gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_residual<true>(mg.lv[l], gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_restrict<true, true>(mg.lv[l], mg.lv[l + 1], gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    }
+    if (blockIdx.x == 0) mg_block_levels(mg, sl);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    for (int l = mg.lb - 1; l >= 1; l--) {
+      mg_prolong<true, true>(mg.lv[l], mg.lv[l + 1], gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_gs<true>(mg.lv[l], 1, gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_gs<true>(mg.lv[l], 0, gt, gs);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    }
+    mg_quads<MG_PROLONG, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    mg_quads<MG_RED_DOT, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, prz);
+    return true;
+  };
+
+  float *P[2] = {a.p, a.p2};
+  int pc = 0; /* P[pc]: the previous direction (zero before the first) */
+  if (!done) {
+    FF none = ff_zero(), prz = ff_zero();
+    /* with alpha = 0 the update pass only starts the V-cycle (P and q are
+     * zero on entry) */
+    mg_quads<MG_UPDATE, BLOCK>(a, 0.0f, 0.0f, P[0], P[1], none);
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
+    if (!vcycle_rest(prz)) return;
+    {
+      FF v[1] = {prz};
+      store_partials<1, BLOCK>(a.part, 2, nb, v);
+    }
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
+    if (threadIdx.x < 32) {
+      double t[1];
+      warp_sum_partials<1>(a.part, 2, nb, t);
+      if (threadIdx.x == 0) {
+        rz = t[0];
+        if (!(rz == rz) || !(rz > 0.0)) done = 2;
+        s_done = done;
+      }
+    }
+    __syncthreads();
+    done = s_done;
+  }
+  float beta_f = 0.0f;
+  while (!done) {
+    /* p' = z + beta p, q = A p', p'.q */
+    FF ppq = ff_zero();
+    mg_quads<MG_MATVEC, BLOCK>(a, 0.0f, beta_f, P[pc], P[pc ^ 1], ppq);
+    {
+      FF v[1] = {ppq};
+      store_partials<1, BLOCK>(a.part, 3, nb, v);
+    }
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
+    if (threadIdx.x < 32) {
+      double t[1];
+      warp_sum_partials<1>(a.part, 3, nb, t);
+      if (threadIdx.x == 0) {
+        alpha = rz / t[0];
+        if (!(alpha == alpha) || !(t[0] > 0.0)) done = 2;
+        s_alpha = (float)alpha;
+        s_done = done;
+      }
+    }
+    __syncthreads();
+    done = s_done;
+    if (done) break;
+    /* x += alpha p', r -= alpha q, r.r; the V-cycle's first half sweep */
+    FF prr2 = ff_zero();
+    mg_quads<MG_UPDATE, BLOCK>(a, s_alpha, 0.0f, P[pc], P[pc ^ 1], prr2);
+    {
+      FF v[1] = {prr2};
+      store_partials<1, BLOCK>(a.part, 4, nb, v);
+    }
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
+    iters++;
+    if (threadIdx.x < 32) {
+      double t[1];
+      warp_sum_partials<1>(a.part, 4, nb, t);
+      if (threadIdx.x == 0) {
+        e2 = t[0];
+        if (e2 <= eps) done = 1;
+        else if (!(e2 == e2)) done = 2;
+        else if (iters >= a.max_iters) done = 3;
+        s_done = done;
+      }
+    }
+    __syncthreads();
+    done = s_done;
+    if (done) break;
+    FF prz = ff_zero();
+    if (!vcycle_rest(prz)) return;
+    {
+      FF v[1] = {prz};
+      store_partials<1, BLOCK>(a.part, 5, nb, v);
+    }
+    if (!count_barrier(a.bar, epoch, a.iflags)) return;
+    if (threadIdx.x < 32) {
+      double t[1];
+      warp_sum_partials<1>(a.part, 5, nb, t);
+      if (threadIdx.x == 0) {
+        const double rzn = t[0];
+        beta = rzn / rz;
+        rz = rzn;
+        if (!(beta == beta)) done = 2;
+        s_beta = (float)beta;
+        s_done = done;
+      }
+    }
+    __syncthreads();
+    beta_f = s_beta;
+    done = s_done;
+    pc ^= 1;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.iflags[IF_DONE] = done;
+    a.iflags[IF_ITERS] = iters;
+    a.iflags[IF_NAN] = done == 2;
+    a.scal[SC_ERR2] = e2;
+    a.scal[SC_B2] = b2;
+    a.scal[SC_EPS] = eps;
+  }
+}
+
+/* coarse flags: liquid if a child is, else air if a child is, else wall */
+__global__ void __launch_bounds__(BLK) k_mg_coarsen(const uint8_t *__restrict__ ff, int mf,
+                                                    uint8_t *__restrict__ cf, int mc) {
+  const unsigned c = blockIdx.x * BLK + threadIdx.x, tot = (unsigned)mc * mc * mc;
+  if (c >= tot) return;
+  int I, J, K;
+  mg_decode(c, (unsigned)mc, I, J, K);
+  bool anyf = false, anya = false;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int d = 0; d < 2; d++) {
+        const int i = 2 * I + a, j = 2 * J + b, k = 2 * K + d;
+        if (i < mf && j < mf && k < mf) {
+          const uint8_t f = ff[((size_t)i * mf + j) * mf + k];
+          anyf |= f == CELL_FLUID;
+          anya |= f == CELL_AIR;
+        }
+      }
+  cf[c] = anyf ? CELL_FLUID : (anya ? CELL_AIR : CELL_WALL);
+}
+
+/* coarse diagonal: the liquid cell's neighbours that are not wall (cells
+ * outside the grid are wall; at least 1) */
+__global__ void __launch_bounds__(BLK) k_mg_diag(const uint8_t *__restrict__ cf, int m,
+                                                 float *__restrict__ diag) {
+  const unsigned c = blockIdx.x * BLK + threadIdx.x, tot = (unsigned)m * m * m;
+  if (c >= tot) return;
+  if (cf[c] != CELL_FLUID) {
+    diag[c] = 0.0f;
+    return;
+  }
+  int i, j, k;
+  mg_decode(c, (unsigned)m, i, j, k);
+  const unsigned mm = (unsigned)m * m;
+  int d = 0;
+  d += i > 0 && cf[c - mm] != CELL_WALL;
+  d += i + 1 < m && cf[c + mm] != CELL_WALL;
+  d += j > 0 && cf[c - m] != CELL_WALL;
+  d += j + 1 < m && cf[c + m] != CELL_WALL;
+  d += k > 0 && cf[c - 1] != CELL_WALL;
+  d += k + 1 < m && cf[c + 1] != CELL_WALL;
+  diag[c] = (float)(d > 0 ? d : 1); /* a liquid cell walled in on all sides */
+}
+
 /* ------------------------------------------- IC(0)/MIC(0) as wavefronts */
 
 /* The lexicographic incomplete-Cholesky factor of the reference's
@@ -1810,11 +2588,70 @@ static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   return FLIPGPU_OK;
 }
 
+constexpr int MG_COARSE_SWEEPS = 2; /* the iteration count does not depend on it */
+constexpr int CG_MG_BLOCK = 512;
+constexpr size_t MG_SMEM_MAX = 96 * 1024; /* block 0's levels: <= 16^3 + 8^3 + 4^3 cells */
+
 /* threads per block of a persistent CG kernel */
 static int cg_block_of(const void *kern) {
   if (kern == (const void *)k_cg_cg1<CG1_BLOCK_SMALL>) return CG1_BLOCK_SMALL;
   if (kern == (const void *)k_cg_cg1<CG1_BLOCK_LARGE>) return CG1_BLOCK_LARGE;
+  if (kern == (const void *)k_cg_mg<CG_MG_BLOCK>) return CG_MG_BLOCK;
   return CG_BLOCK;
+}
+
+/* The level sizes (n, ceil(n/2), ... down to at most 4 per axis), the first
+ * level solved in block 0 (at most 16^3 cells) and the buffers of levels
+ * 1.. plus the level-0 scratch (residual, second direction, A p). */
+int mg_alloc(FlipGpu *h) {
+  if (h->mg_nlev > 0) return FLIPGPU_OK;
+  int m = h->n, nlev = 0;
+  int lv[MG_MAX_LEVELS];
+  lv[nlev++] = m;
+  while (m > 4 && nlev < MG_MAX_LEVELS) {
+    m = (m + 1) / 2;
+    lv[nlev++] = m;
+  }
+  if (nlev < 2 || lv[nlev - 1] > 4) return FLIPGPU_EINVAL;
+  int lb = 1;
+  while (lb < nlev - 1 && (size_t)lv[lb] * lv[lb] * lv[lb] > MG_BLOCK_CELLS) lb++;
+  if (mg_block_bytes(lv, lb, nlev) > MG_SMEM_MAX) return FLIPGPU_EINVAL;
+  const size_t nc = h->nc;
+  bool ok = cudaMalloc(&h->mg_res[0], nc * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&h->mg_p2, nc * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&h->mg_q, nc * sizeof(float)) == cudaSuccess;
+  for (int l = 1; ok && l < nlev; l++) {
+    const size_t c = (size_t)lv[l] * lv[l] * lv[l];
+    ok = cudaMalloc(&h->mg_flags[l], c) == cudaSuccess &&
+         cudaMalloc(&h->mg_diag[l], c * sizeof(float)) == cudaSuccess &&
+         cudaMalloc(&h->mg_x[l], c * sizeof(float)) == cudaSuccess &&
+         cudaMalloc(&h->mg_b[l], c * sizeof(float)) == cudaSuccess &&
+         cudaMalloc(&h->mg_res[l], c * sizeof(float)) == cudaSuccess;
+  }
+  if (!ok) {
+    mg_free(h);
+    return FLIPGPU_ENOMEM;
+  }
+  for (int l = 0; l < nlev; l++) h->mg_m[l] = lv[l];
+  h->mg_lb = lb;
+  h->mg_nlev = nlev;
+  return FLIPGPU_OK;
+}
+
+void mg_free(FlipGpu *h) {
+  for (int l = 0; l < MG_MAX_LEVELS; l++) {
+    if (h->mg_flags[l]) cudaFree(h->mg_flags[l]);
+    if (h->mg_diag[l]) cudaFree(h->mg_diag[l]);
+    if (h->mg_x[l]) cudaFree(h->mg_x[l]);
+    if (h->mg_b[l]) cudaFree(h->mg_b[l]);
+    if (h->mg_res[l]) cudaFree(h->mg_res[l]);
+    h->mg_flags[l] = nullptr;
+    h->mg_diag[l] = h->mg_x[l] = h->mg_b[l] = h->mg_res[l] = nullptr;
+  }
+  if (h->mg_p2) cudaFree(h->mg_p2);
+  if (h->mg_q) cudaFree(h->mg_q);
+  h->mg_p2 = h->mg_q = nullptr;
+  h->mg_nlev = 0;
 }
 
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
@@ -1876,6 +2713,19 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   /* persistent single-launch CG unless the REF preconditioner has an entry
    * equal to 1.0 (then its neighbour terms act and it runs sequentially) */
   bool persistent = precond != FLIPGPU_PRECOND_NONE && h->cg_grid[0] > 0;
+  if (precond == FLIPGPU_PRECOND_MG) {
+    if (mode != FLIPGPU_SOLVE_FAST || n % 4 != 0 || n < 8 || h->cg_grid[5] <= 0 ||
+        nc / 4 >= (size_t)1 << 31) {
+      snprintf(h->err, sizeof h->err, "solve: the MG preconditioner needs FAST mode, n %% 4 == 0, "
+                                      "n >= 8 and a cooperative launch");
+      return FLIPGPU_EINVAL;
+    }
+    const int r = mg_alloc(h);
+    if (r != FLIPGPU_OK) {
+      snprintf(h->err, sizeof h->err, "solve: multigrid buffers (%d)", r);
+      return r;
+    }
+  }
   if (precond == FLIPGPU_PRECOND_IC && (mode != FLIPGPU_SOLVE_FAST || h->cg_grid[3] <= 0)) {
     snprintf(h->err, sizeof h->err, "solve: the IC preconditioner needs FAST mode and a "
                                     "cooperative launch");
@@ -1930,12 +2780,10 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     size_t smem = 0;
     a.chunk_list = nullptr;
     a.chunk_count = nullptr;
-    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0 &&
-        nc / 4 < (size_t)1 << 31) {
-      const bool large = n >= CG1_LARGE_N;
-      kern = large ? (const void *)k_cg_cg1<CG1_BLOCK_LARGE> : (const void *)k_cg_cg1<CG1_BLOCK_SMALL>;
-      grid = h->cg_grid[large ? 4 : 2];
-      /* the chunks holding liquid (A is fixed during the solve) */
+    a.p2 = a.q = nullptr;
+    std::memset(&a.mg, 0, sizeof a.mg);
+    /* the 32-quad chunks holding liquid (A is fixed during the solve) */
+    auto chunk_list = [&]() -> cudaError_t {
       const size_t nq = nc / 4, nch = (nq + 31) / 32;
       k_cg1_chunk_flags<<<grid_for((nch + 1) * 32, BLK), BLK, 0, S>>>(
           nq, reinterpret_cast<const uchar4 *>(h->A), h->chunk_off);
@@ -1946,12 +2794,65 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
         FG_LAUNCHED(h, 1);
         e = cudaGetLastError();
       }
+      a.chunk_list = h->chunk_list;
+      a.chunk_count = h->chunk_off + nch;
+      return e;
+    };
+    if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_JACOBI && n % 4 == 0 &&
+        nc / 4 < (size_t)1 << 31) {
+      const bool large = n >= CG1_LARGE_N;
+      kern = large ? (const void *)k_cg_cg1<CG1_BLOCK_LARGE> : (const void *)k_cg_cg1<CG1_BLOCK_SMALL>;
+      grid = h->cg_grid[large ? 4 : 2];
+      cudaError_t e = chunk_list();
       if (e != cudaSuccess) {
         snprintf(h->err, sizeof h->err, "solve: chunk list: %s", cudaGetErrorString(e));
         return FLIPGPU_ECUDA;
       }
-      a.chunk_list = h->chunk_list;
-      a.chunk_count = h->chunk_off + nch;
+    }
+    if (precond == FLIPGPU_PRECOND_MG) {
+      kern = (const void *)k_cg_mg<CG_MG_BLOCK>;
+      grid = h->cg_grid[5];
+      smem = mg_block_bytes(h->mg_m, h->mg_lb, h->mg_nlev);
+      cudaError_t e = chunk_list();
+      /* levels: 0 = the solver's grid (z the correction, r its right-hand
+       * side); coarser ones from the coarsened flags */
+      MgArgs &mg = a.mg;
+      mg.nlev = h->mg_nlev;
+      mg.lb = h->mg_lb;
+      mg.coarse_sweeps = MG_COARSE_SWEEPS;
+      float hs = sa.inv_h2_f;
+      for (int l = 0; l < mg.nlev; l++) {
+        MgLevel &L = mg.lv[l];
+        L.m = h->mg_m[l];
+        L.flags = l == 0 ? h->A : h->mg_flags[l];
+        L.diag = l == 0 ? h->diag : h->mg_diag[l];
+        L.x = l == 0 ? h->z : h->mg_x[l];
+        L.b = l == 0 ? h->r : h->mg_b[l];
+        L.res = h->mg_res[l];
+        L.hs = hs;
+        L.ihs = 1.0f / hs;
+        L.lgm = (L.m & (L.m - 1)) == 0 ? __builtin_ctz((unsigned)L.m) : -1;
+        hs *= 0.25f;
+      }
+      for (int l = 1; e == cudaSuccess && l < mg.nlev; l++) {
+        const size_t c = (size_t)h->mg_m[l] * h->mg_m[l] * h->mg_m[l];
+        k_mg_coarsen<<<grid_for(c, BLK), BLK, 0, S>>>(mg.lv[l - 1].flags, h->mg_m[l - 1],
+                                                      h->mg_flags[l], h->mg_m[l]);
+        k_mg_diag<<<grid_for(c, BLK), BLK, 0, S>>>(h->mg_flags[l], h->mg_m[l], h->mg_diag[l]);
+        FG_LAUNCHED(h, 2);
+        e = cudaGetLastError();
+      }
+      a.p2 = h->mg_p2;
+      a.q = h->mg_q;
+      /* zero off the liquid chunks (the sweeps only write inside them) and
+       * finite direction buffers for the first iteration */
+      float *zero_bufs[5] = {h->z, h->mg_res[0], h->pdir, h->mg_p2, h->mg_q};
+      for (float *zb : zero_bufs)
+        if (e == cudaSuccess) e = cudaMemsetAsync(zb, 0, nc * sizeof(float), S);
+      if (e != cudaSuccess) {
+        snprintf(h->err, sizeof h->err, "solve: multigrid setup: %s", cudaGetErrorString(e));
+        return FLIPGPU_ECUDA;
+      }
     }
     /* no more blocks than the grid has work for (about two quads or eight
      * cells per thread): small grids keep short barriers and leave the rest
@@ -2146,12 +3047,15 @@ int ic_init_device() {
   if (cudaFuncSetAttribute(k_cg_ic, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)ic_smem_bytes()) != cudaSuccess)
     return -1;
+  if (cudaFuncSetAttribute(k_cg_mg<CG_MG_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)MG_SMEM_MAX) != cudaSuccess)
+    return -1;
   done[dev] = true;
   return 0;
 }
 
 /* Cooperative grid of each CG variant (REF, FAST, single-reduction with
- * small blocks, IC, single-reduction with large blocks): SMs x resident
+ * small blocks, IC, single-reduction with large blocks, MG): SMs x resident
  * blocks (at most 4). */
 int cg_grid_size(int *out) {
   int dev = 0, sms = 0, coop = 0;
@@ -2164,11 +3068,12 @@ int cg_grid_size(int *out) {
   const void *k[CG_VARIANTS] = {(const void *)k_cg<FLIPGPU_SOLVE_REF>,
                                 (const void *)k_cg<FLIPGPU_SOLVE_FAST>,
                                 (const void *)k_cg_cg1<CG1_BLOCK_SMALL>, (const void *)k_cg_ic,
-                                (const void *)k_cg_cg1<CG1_BLOCK_LARGE>};
+                                (const void *)k_cg_cg1<CG1_BLOCK_LARGE>,
+                                (const void *)k_cg_mg<CG_MG_BLOCK>};
   for (int v = 0; v < CG_VARIANTS; v++) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k[v], cg_block_of(k[v]),
-                                                  v == 3 ? ic_smem_bytes() : 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, k[v], cg_block_of(k[v]), v == 3 ? ic_smem_bytes() : v == 5 ? MG_SMEM_MAX : 0);
     if (per_sm > 4) per_sm = 4;
     out[v] = sms * per_sm;
     if (out[v] * 6 > 8192) out[v] = 8192 / 6;

@@ -18,7 +18,7 @@ LIB_PATH = _build.LIB
 OK = 0
 ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ENOCONV", -5: "ENAN", -6: "ETIMEOUT",
           -7: "ETOOBIG"}
-PRECOND_NONE, PRECOND_REF, PRECOND_IC, PRECOND_JACOBI = 0, 1, 2, 3
+PRECOND_NONE, PRECOND_REF, PRECOND_IC, PRECOND_JACOBI, PRECOND_MG = 0, 1, 2, 3, 4
 SOLVE_REF, SOLVE_FAST = 0, 1
 ARITH_REF, ARITH_FAST = 0, 1
 

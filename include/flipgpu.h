@@ -45,11 +45,15 @@ extern "C" {
  * terms only act on values equal to 1.0, so in practice it scales by the
  * diagonal. IC is the same lexicographic incomplete-Cholesky factor with the
  * neighbour test on the cell flag (mic_tau 0 = IC(0), 0.97 = MIC(0)),
- * applied as wavefronts. JACOBI is plain diagonal scaling in FP32. */
+ * applied as wavefronts. JACOBI is plain diagonal scaling in FP32. MG is
+ * one symmetric geometric-multigrid V-cycle per iteration (red-black
+ * Gauss-Seidel smoothing, coarse operators rediscretised on coarsened cell
+ * flags); FAST mode with n % 4 == 0 and n >= 8 only. */
 #define FLIPGPU_PRECOND_NONE 0
 #define FLIPGPU_PRECOND_REF 1
 #define FLIPGPU_PRECOND_IC 2
 #define FLIPGPU_PRECOND_JACOBI 3
+#define FLIPGPU_PRECOND_MG 4
 
 /* Solver arithmetic. REF: the reference's promotions (double matvec sums,
  * float(r.r) stop test, power-of-4 relative tolerance, see rel_tol). FAST:
