@@ -1639,7 +1639,12 @@ __host__ __device__ inline size_t mg_block_bytes(const int *m, int lb, int nlev)
 }
 
 /* Level-0 phases on quads of the liquid chunks. */
-enum MgPhase { MG_MATVEC, MG_UPDATE, MG_BLACK, MG_RES, MG_PROLONG, MG_RED_DOT };
+/* MG_BLACK_PROLONG: the black half sweep after the coarse correction, with
+ * the prolongation folded in: every value is read as z plus the parent's
+ * correction, and only the black cells are written (the red cells keep
+ * their uncorrected z, which the neighbours of this phase read and correct
+ * themselves; the red half sweep that follows overwrites every red cell). */
+enum MgPhase { MG_MATVEC, MG_UPDATE, MG_BLACK, MG_RES, MG_RED_DOT, MG_BLACK_PROLONG };
 
 template <int PH, int BLOCK>
 __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float beta, const float *pold,
@@ -1671,9 +1676,10 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
     const uchar4 A4 = A4p[qs];
     const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
     const int par0 = (i + j + k0) & 1; /* colour of the quad's first cell */
-    constexpr bool NB = PH == MG_MATVEC || PH == MG_BLACK || PH == MG_RES || PH == MG_RED_DOT;
+    constexpr bool NB = PH == MG_MATVEC || PH == MG_BLACK || PH == MG_RES || PH == MG_RED_DOT ||
+                        PH == MG_BLACK_PROLONG;
     /* the field whose neighbours are summed: p' = z + beta p (MATVEC) or z */
-    float4 own = zero;
+    float4 own = zero, own0 = zero; /* own0: as loaded, before any correction */
     float4 nbq[4] = {zero, zero, zero, zero};
     float edge = 0.0f;
     const bool has[4] = {i + 1 < n, i > 0, j + 1 < n, j > 0};
@@ -1695,14 +1701,42 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
                                zn.w + beta * pn.w);
         }
       if (ed) edge = __ldcg(zf + ce) + beta * __ldcg(pold + ce);
-    } else if (NB || PH == MG_PROLONG || PH == MG_UPDATE) {
-      if (PH != MG_UPDATE) own = __ldcg(reinterpret_cast<const float4 *>(zf) + qs);
+    } else {
+      if (NB) own = __ldcg(reinterpret_cast<const float4 *>(zf) + qs);
+      own0 = own;
       if (NB) {
 #pragma unroll
         for (int d = 0; d < 4; d++)
           if (has[d])
             nbq[d] = __ldcg(reinterpret_cast<const float4 *>(zf) + (size_t)((long)qs + off[d]));
         if (ed) edge = __ldcg(zf + ce);
+      }
+      if (PH == MG_BLACK_PROLONG) {
+        /* add the parents' corrections on the liquid (level 1 holds them) */
+        const MgLevel &L1 = a.mg.lv[1];
+        const unsigned m1 = (unsigned)L1.m;
+        auto par2 = [&](int ii, int jj) {
+          const unsigned idx = (((unsigned)ii >> 1) * m1 + ((unsigned)jj >> 1)) * m1 +
+                               (unsigned)(k0 >> 1);
+          return __ldcg(reinterpret_cast<const float2 *>(L1.x + idx));
+        };
+        auto add = [](float4 &v, uchar4 f, float2 e) {
+          v.x += fl(f.x) ? e.x : 0.0f;
+          v.y += fl(f.y) ? e.x : 0.0f;
+          v.z += fl(f.z) ? e.y : 0.0f;
+          v.w += fl(f.w) ? e.y : 0.0f;
+        };
+        const int di[4] = {1, -1, 0, 0}, dj[4] = {0, 0, 1, -1};
+        add(own, A4, par2(i, j));
+#pragma unroll
+        for (int d = 0; d < 4; d++)
+          if (has[d]) add(nbq[d], A4p[(size_t)((long)qs + off[d])], par2(i + di[d], j + dj[d]));
+        if (ed) {
+          const int ke = lane == 0 ? k0 - 1 : k0 + 4;
+          const unsigned idx =
+              (((unsigned)i >> 1) * m1 + ((unsigned)j >> 1)) * m1 + (unsigned)(ke >> 1);
+          if (fl(a.A[ce])) edge += __ldcg(L1.x + idx);
+        }
       }
     }
     /* k neighbours across quads */
@@ -1762,16 +1796,6 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
       reinterpret_cast<float4 *>(a.x)[q] = make_float4(xn[0], xn[1], xn[2], xn[3]);
       reinterpret_cast<float4 *>(rf)[q] = make_float4(rn[0], rn[1], rn[2], rn[3]);
       reinterpret_cast<float4 *>(zf)[q] = make_float4(zn[0], zn[1], zn[2], zn[3]);
-    } else if (PH == MG_PROLONG) {
-      const MgLevel &L1 = a.mg.lv[1];
-      const unsigned m1 = (unsigned)L1.m;
-      const unsigned pidx = (((unsigned)i >> 1) * m1 + ((unsigned)j >> 1)) * m1 + (unsigned)(k0 >> 1);
-      const float2 e = __ldcg(reinterpret_cast<const float2 *>(L1.x + pidx));
-      const float ev[4] = {e.x, e.x, e.y, e.y};
-      float zn[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++) zn[u] = fv[u] ? ov[u] + ev[u] : 0.0f;
-      reinterpret_cast<float4 *>(zf)[q] = make_float4(zn[0], zn[1], zn[2], zn[3]);
     } else if (PH == MG_RES) {
       const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
       const float4 dg = __ldg(d4p + qs);
@@ -1780,15 +1804,16 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
 #pragma unroll
       for (int u = 0; u < 4; u++) res[u] = fv[u] ? rv[u] - hs * (dv[u] * ov[u] - nbs[u]) : 0.0f;
       reinterpret_cast<float4 *>(L0.res)[q] = make_float4(res[0], res[1], res[2], res[3]);
-    } else { /* MG_BLACK, MG_RED_DOT: half sweep of one colour */
-      const int color = PH == MG_BLACK ? 1 : 0;
+    } else { /* MG_BLACK, MG_BLACK_PROLONG, MG_RED_DOT: half sweep of one colour */
+      const int color = PH == MG_RED_DOT ? 0 : 1;
       const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
       const float4 dg = __ldg(d4p + qs);
       const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, dv[4] = {dg.x, dg.y, dg.z, dg.w};
+      const float o0[4] = {own0.x, own0.y, own0.z, own0.w};
       float zn[4];
 #pragma unroll
       for (int u = 0; u < 4; u++) {
-        zn[u] = ov[u];
+        zn[u] = o0[u];
         if (fv[u] && ((par0 + u) & 1) == color) zn[u] = __fdividef(rv[u] * ihs + nbs[u], dv[u]);
         if (PH == MG_RED_DOT && fv[u]) ff_add_prod(acc0, rv[u], zn[u]);
       }
@@ -1923,9 +1948,7 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs 
       mg_gs<true>(mg.lv[l], 0, gt, gs);
       if (!count_barrier(a.bar, epoch, a.iflags)) return false;
     }
-    mg_quads<MG_PROLONG, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
-    if (!count_barrier(a.bar, epoch, a.iflags)) return false;
-    mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+    mg_quads<MG_BLACK_PROLONG, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
     if (!count_barrier(a.bar, epoch, a.iflags)) return false;
     mg_quads<MG_RED_DOT, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, prz);
     return true;
@@ -2670,7 +2693,9 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   sa.inv_h2 = 1.0 / (double)h2f;
   sa.inv_h2_f = (float)sa.inv_h2;
   const double ref_eps = 1.0e-2 * ((double)n * n * n);
-  const long cap = h->prm.max_iters > 0 ? h->prm.max_iters : (long)nc;
+  long cap = h->prm.max_iters > 0 ? h->prm.max_iters : (long)nc;
+  /* a multigrid solve that needs more than this has failed: stop early */
+  if (h->prm.max_iters <= 0 && h->prm.precond == FLIPGPU_PRECOND_MG && cap > 1000) cap = 1000;
   const int max_iters = cap > 0x7fffffff ? 0x7fffffff : (int)cap;
   cudaStream_t S = h->stream;
   const unsigned G = grid_for(nc, BLK);

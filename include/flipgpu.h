@@ -87,7 +87,8 @@ typedef struct FlipGpuParams {
                          reference's absolute 1e-2*n^3 by 4^k until it is at
                          most rel_tol^2*b.b; 0 keeps the reference's own */
   double eps_abs;     /* REF mode: explicit absolute r.r bound if >= 0 */
-  int max_iters;      /* CG iteration cap; <=0: n^3 like the reference */
+  int max_iters;      /* CG iteration cap; <=0: n^3 like the reference
+                         (1000 with the MG preconditioner) */
   int refine_steps;   /* FAST mode: after CG stops, the true residual b - A x
                          is recomputed in FP64 (stats r2_true); while it
                          misses rel_tol and the last restart cut it at least

@@ -59,6 +59,29 @@ def test_mg_pcg_solves_the_system(gpu, orc, n, scene):
     assert err < 1e-3, err
 
 
+def test_mg_pcg_at_full_size(gpu, orc):
+    """The N=128 dam break (every SM in the grid, four grid-wide levels):
+    iteration count, the residual of the FP32 answer on the host, and two
+    solves bit-identical (a race between the phases would break that)."""
+    n = 128
+    A, L, b = system(orc, n)
+    sols = []
+    for _ in range(2):
+        sim = gpu.Simulation(gpu.default_params(n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                                                precond=gpu.PRECOND_MG, max_iters=200))
+        sim.set_grid(A=A, L=L, press=np.zeros(n ** 3, np.float32), div=b)
+        st = sim.solve()
+        assert st.status == 0 and st.iterations <= 40, (st.status, st.iterations)
+        sols.append(sim.get_grid()[3])
+    diff = int(np.sum(sols[0] != sols[1]))
+    assert diff == 0, f"{diff} values differ between two solves"
+    # the solver answers A x = -b (the reference negates b, src/solver.cpp:231)
+    r = -b.astype(np.float64) - orc.matvec(n, A, L, sols[0]).astype(np.float64)
+    fl = A == 1
+    rel = np.linalg.norm(r[fl]) / np.linalg.norm(b[fl].astype(np.float64))
+    assert rel <= 1e-3, rel
+
+
 def test_mg_pcg_is_deterministic(gpu, orc):
     A, L, b = system(orc, 32)
     st1, p1 = fast_solve(gpu, 32, A, L, b, gpu.PRECOND_MG)
