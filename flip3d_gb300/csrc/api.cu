@@ -204,6 +204,24 @@ struct StageClock {
 
 } // namespace
 
+/* After the corrector's spring: the positions are final, so the transfer
+ * stream interleaves them into the sorted grid-position buffer (unused by
+ * the resample) and copies them to the host while the resample runs. */
+cudaError_t xfer_positions_out(FlipGpu *h) {
+  cudaError_t e = cudaEventRecord(h->xev[2], h->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(h->xstream, h->xev[2], 0);
+  if (e != cudaSuccess) return e;
+  float *stage = reinterpret_cast<float *>(h->spg);
+  k_interleave<<<grid_for(h->np, BLK), BLK, 0, h->xstream>>>(h->np, h->px, h->py, h->pz, stage);
+  FG_LAUNCHED(h, 1);
+  e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h->xfer_pos_out, stage, (size_t)h->np * 3 * sizeof(float),
+                        cudaMemcpyDeviceToHost, h->xstream);
+  return e;
+}
+
+
 SimConst make_const(const FlipGpu *h) {
   SimConst c;
   const FlipGpuParams &p = h->prm;
@@ -395,6 +413,11 @@ int flipgpu_destroy(FlipGpu *h) {
   export_free(h);
   mesh_free(h);
   mg_free(h);
+  if (h->xstream) {
+    cudaStreamSynchronize(h->xstream);
+    for (int e = 0; e < 3; e++) cudaEventDestroy(h->xev[e]);
+    cudaStreamDestroy(h->xstream);
+  }
   if (h->wdelta) {
     cudaFree(h->wdelta);
     cudaFree(h->wpart);
@@ -813,6 +836,12 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
   CK(h, launch_sort(h, 1));
   clk.mark(FLIPGPU_STAGE_DENSITY);
   CK(h, launch_density(h));
+  if (h->defer_vel) {
+    /* flipgpu_step_host: the velocities have arrived on the transfer stream */
+    CK(h, cudaStreamWaitEvent(h->stream, h->xev[1], 0));
+    h->defer_vel = 0;
+    CK(h, launch_payload_vel(h));
+  }
   int r = picflip(h, st, &clk);
   if (r != FLIPGPU_OK) return r;
   /* advect_particle with reposition; its closing sort serves the corrector,
@@ -833,6 +862,54 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
 int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
   if (!h) return FLIPGPU_EINVAL;
   return step_body(h, st);
+}
+
+/* the transfer stream and its events, on first use */
+static int xfer_init(FlipGpu *h) {
+  if (h->xstream) return FLIPGPU_OK;
+  CK(h, cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking));
+  for (int e = 0; e < 3; e++) CK(h, cudaEventCreateWithFlags(&h->xev[e], cudaEventDisableTiming));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_step_host(FlipGpu *h, const float *pos_in, const float *vel_in, float *pos_out,
+                      float *vel_out, FlipGpuSolveStats *st) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r = xfer_init(h);
+  if (r != FLIPGPU_OK) return r;
+  /* positions in on the step's stream (staged through the sorted-position
+   * buffer, as flipgpu_put_state does) */
+  if ((r = put3(h, pos_in, 0, h->px, h->py, h->pz)) != FLIPGPU_OK) return r;
+  /* velocities in on the transfer stream, staged through the sorted-velocity
+   * buffer, which the step does not touch before the deferred payload */
+  if (vel_in && h->np > 0) {
+    CK(h, cudaEventRecord(h->xev[0], h->stream));
+    CK(h, cudaStreamWaitEvent(h->xstream, h->xev[0], 0));
+    float *stage = reinterpret_cast<float *>(h->svel);
+    CK(h, cudaMemcpyAsync(stage, vel_in, (size_t)h->np * 3 * sizeof(float),
+                          cudaMemcpyHostToDevice, h->xstream));
+    k_deinterleave<<<grid_for(h->np, BLK), BLK, 0, h->xstream>>>(h->np, stage, h->vx, h->vy,
+                                                                 h->vz);
+    FG_LAUNCHED(h, 1);
+    CK(h, cudaGetLastError());
+    CK(h, cudaEventRecord(h->xev[1], h->xstream));
+    h->defer_vel = 1;
+  }
+  h->cells_valid = false;
+  h->xfer_pos_out = h->np > 0 ? pos_out : nullptr;
+  r = step_body(h, st);
+  h->xfer_pos_out = nullptr;
+  if (h->defer_vel) { /* the step stopped before the payload */
+    cudaStreamWaitEvent(h->stream, h->xev[1], 0);
+    h->defer_vel = 0;
+  }
+  if (r == FLIPGPU_OK && vel_out)
+    r = get3(h, vel_out, 0, h->vx, h->vy, h->vz, reinterpret_cast<float *>(h->spos));
+  /* join the transfer stream before returning */
+  CK(h, cudaEventRecord(h->xev[2], h->xstream));
+  CK(h, cudaStreamWaitEvent(h->stream, h->xev[2], 0));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return r;
 }
 
 static int async_ok(FlipGpu *h) {

@@ -113,6 +113,11 @@ struct FlipGpu {
   /* solver */
   float *r, *z, *s, *s1, *w;
   float *w1, *pdir;   /* single-reduction CG: second w buffer, directions */
+  /* flipgpu_step_host: transfers overlapped with the step on a second stream */
+  cudaStream_t xstream;
+  cudaEvent_t xev[3];
+  int defer_vel, defer_gravity;   /* payload velocities after the upload */
+  float *xfer_pos_out;            /* host destination of the positions, or null */
   /* MG preconditioner (k_pcg.cu mg_alloc): levels 1.. and level-0 scratch */
   int mg_nlev, mg_lb, mg_m[10];
   uint8_t *mg_flags[10];
@@ -197,6 +202,11 @@ SimConst make_const(const FlipGpu *h);
 /* launchers (one per reference stage or sub-stage); return cudaError_t */
 cudaError_t launch_sort(FlipGpu *h, int apply_gravity);
 cudaError_t launch_payload(FlipGpu *h, int apply_gravity);
+/* the velocity half of a deferred payload (FlipGpu::defer_vel) */
+cudaError_t launch_payload_vel(FlipGpu *h);
+/* flipgpu_step_host: download the corrected positions on the transfer
+ * stream while the velocity resample runs (called between the two) */
+cudaError_t xfer_positions_out(FlipGpu *h);
 cudaError_t launch_density(FlipGpu *h);
 cudaError_t launch_mark_water(FlipGpu *h);
 cudaError_t launch_add_force(FlipGpu *h);

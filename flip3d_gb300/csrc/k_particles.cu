@@ -1054,18 +1054,25 @@ cudaError_t launch_correct(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
   const unsigned g = grid_for(h->np, BLK);
-  if (h->prm.arith == FLIPGPU_ARITH_FAST) {
+  const bool fast = h->prm.arith == FLIPGPU_ARITH_FAST;
+  if (fast)
     k_spring<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,
                                                   h->ny, h->nz, h->px, h->py, h->pz);
-    k_resample<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->svel,
-                                                    h->px, h->py, h->pz, h->vx, h->vy, h->vz);
-  } else {
+  else
     k_spring<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,
                                                  h->ny, h->nz, h->px, h->py, h->pz);
+  FG_LAUNCHED(h, 1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  /* the positions are final: their download can run beside the resample */
+  if (h->xfer_pos_out && (e = xfer_positions_out(h)) != cudaSuccess) return e;
+  if (fast)
+    k_resample<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->svel,
+                                                    h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+  else
     k_resample<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->svel,
                                                    h->px, h->py, h->pz, h->vx, h->vy, h->vz);
-  }
-  FG_LAUNCHED(h, 2);
+  FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
 

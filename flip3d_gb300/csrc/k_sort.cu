@@ -185,6 +185,40 @@ __global__ void k_payload(SimConst c, int apply_gravity, const uint32_t *__restr
   sdens[a] = dens[p];
 }
 
+/* The payload in two parts, for steps whose velocities arrive while the
+ * sort runs: positions, grid positions and densities first, the velocities
+ * (with add_ExtForce) once they are on the device. Same values as k_payload. */
+__global__ void k_payload_pos(SimConst c, const uint32_t *__restrict__ perm,
+                              const float *__restrict__ px, const float *__restrict__ py,
+                              const float *__restrict__ pz, const uint8_t *__restrict__ type,
+                              const float *__restrict__ dens, float4 *__restrict__ spos,
+                              float4 *__restrict__ spg, float *__restrict__ sdens) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= c.np) return;
+  uint32_t p = perm[a];
+  float x = px[p], y = py[p], z = pz[p];
+  float tw = pack_type(type[p]);
+  spos[a] = make_float4(x, y, z, tw);
+  spg[a] = make_float4(fmaxf(0.0f, fminf(c.fn, c.fn * x)), fmaxf(0.0f, fminf(c.fn, c.fn * y)),
+                       fmaxf(0.0f, fminf(c.fn, c.fn * z)), tw);
+  sdens[a] = dens[p];
+}
+
+__global__ void k_payload_vel(SimConst c, int apply_gravity, const uint32_t *__restrict__ perm,
+                              float *__restrict__ vx, float *__restrict__ vy,
+                              float *__restrict__ vz, const uint8_t *__restrict__ type,
+                              float4 *__restrict__ svel) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= c.np) return;
+  uint32_t p = perm[a];
+  float ux = vx[p], uy = vy[p], uz = vz[p];
+  if (apply_gravity && type[p] == CELL_FLUID) {
+    uy = refmath::add_fd(uy, c.grav_h, c.grav_l, c.grav);
+    vy[p] = uy;
+  }
+  svel[a] = make_float4(ux, uy, uz, 0.0f);
+}
+
 } // namespace
 
 cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
@@ -208,9 +242,26 @@ size_t scan_tmp_blocks(size_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 cudaError_t launch_payload(FlipGpu *h, int apply_gravity) {
   SimConst c = make_const(h);
   if (h->np == 0) return cudaSuccess;
+  if (h->defer_vel) {
+    /* the velocities are still being uploaded (flipgpu_step_host) */
+    k_payload_pos<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
+        c, h->perm, h->px, h->py, h->pz, h->type, h->dens, h->spos, h->spg, h->sdens);
+    FG_LAUNCHED(h, 1);
+    h->defer_gravity = apply_gravity;
+    return cudaGetLastError();
+  }
   k_payload<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
       c, apply_gravity, h->perm, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens,
       h->spos, h->spg, h->svel, h->sdens);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_payload_vel(FlipGpu *h) {
+  SimConst c = make_const(h);
+  if (h->np == 0) return cudaSuccess;
+  k_payload_vel<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
+      c, h->defer_gravity, h->perm, h->vx, h->vy, h->vz, h->type, h->svel);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }

@@ -113,6 +113,8 @@ SIGNATURES = {
     "flipgpu_advect": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "flipgpu_correct": (C.c_int, [C.c_void_p]),
     "flipgpu_step": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_step_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.POINTER(SolveStats)]),
     "flipgpu_launch_count": (C.c_int64, [C.c_void_p]),
     "flipgpu_put_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
@@ -589,6 +591,25 @@ class Simulation:
 
     def step(self):
         return self._stats_call(self.lib.flipgpu_step, "step")
+
+    def step_host(self, pos_in=None, vel_in=None, pos_out=None, vel_out=None):
+        """One step on host AoS float[np][3] buffers (numpy arrays, ideally
+        views of pinned memory; in and out may be the same arrays): upload,
+        step and download with the transfers overlapped with the step."""
+        def addr(a, writable):
+            if a is None:
+                return None
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and
+                    a.flags["C_CONTIGUOUS"] and a.size == 3 * self.np):
+                raise ValueError("step_host wants contiguous float32 arrays of np x 3")
+            if writable and not a.flags["WRITEABLE"]:
+                raise ValueError("step_host output arrays must be writable")
+            return C.c_void_p(a.ctypes.data)
+        st = SolveStats()
+        self._ck(self.lib.flipgpu_step_host(self.h, addr(pos_in, False), addr(vel_in, False),
+                                            addr(pos_out, True), addr(vel_out, True),
+                                            C.byref(st)), "step_host")
+        return st
 
 
 class UNet:

@@ -328,6 +328,15 @@ int flipgpu_advect(FlipGpu *h, int *stuck);
 int flipgpu_correct(FlipGpu *h);
 /* simulateStep (src/flip3D.cpp:1194-1264) without preview and mesh I/O. */
 int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *stats);
+/* One step on host data: the same results as flipgpu_put_state(pos_in,
+ * vel_in) + flipgpu_step + flipgpu_get_particles(pos_out, vel_out), with
+ * the transfers overlapped with the step on a second stream (the velocities
+ * upload while the sort and density run; the positions download while the
+ * corrector's velocity resample runs). Any pointer may be NULL (skipped);
+ * in and out may be the same buffers. Host AoS float[np][3]; pinned memory
+ * gives the full transfer rate. Returns after everything is done. */
+int flipgpu_step_host(FlipGpu *h, const float *pos_in, const float *vel_in, float *pos_out,
+                      float *vel_out, FlipGpuSolveStats *stats);
 
 /* Replace positions and velocities of the current particle set (same count
  * and types as the last flipgpu_set_particles), host or device AoS. This is
