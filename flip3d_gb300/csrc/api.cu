@@ -840,7 +840,7 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
     /* flipgpu_step_host: the velocities have arrived on the transfer stream */
     CK(h, cudaStreamWaitEvent(h->stream, h->xev[1], 0));
     h->defer_vel = 0;
-    CK(h, launch_payload_vel(h));
+    CK(h, launch_payload_vel(h, h->defer_gravity));
   }
   int r = picflip(h, st, &clk);
   if (r != FLIPGPU_OK) return r;

@@ -202,8 +202,9 @@ SimConst make_const(const FlipGpu *h);
 /* launchers (one per reference stage or sub-stage); return cudaError_t */
 cudaError_t launch_sort(FlipGpu *h, int apply_gravity);
 cudaError_t launch_payload(FlipGpu *h, int apply_gravity);
-/* the velocity half of a deferred payload (FlipGpu::defer_vel) */
-cudaError_t launch_payload_vel(FlipGpu *h);
+/* the velocity half of the payload: the deferred one (FlipGpu::defer_vel)
+ * or a refresh of the sorted velocities */
+cudaError_t launch_payload_vel(FlipGpu *h, int apply_gravity);
 /* flipgpu_step_host: download the corrected positions on the transfer
  * stream while the velocity resample runs (called between the two) */
 cudaError_t xfer_positions_out(FlipGpu *h);

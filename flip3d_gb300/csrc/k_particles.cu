@@ -1038,8 +1038,9 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
                                           h->vx, h->vy, h->vz, h->repo_old, h->repo_state, left);
   FG_LAUNCHED(h, 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  /* refresh the sorted velocities of the resampled particles */
-  if ((e = launch_payload(h, 0)) != cudaSuccess) return e;
+  /* refresh the sorted velocities of the resampled particles (positions,
+   * grid positions and densities are those of the sort above) */
+  if ((e = launch_payload_vel(h, 0)) != cudaSuccess) return e;
   if (stuck_host) {
     int v = 0;
     e = cudaMemcpyAsync(&v, h->iflags + IF_NSTUCK, sizeof(int), cudaMemcpyDeviceToHost,

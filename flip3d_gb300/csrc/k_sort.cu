@@ -257,11 +257,11 @@ cudaError_t launch_payload(FlipGpu *h, int apply_gravity) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_payload_vel(FlipGpu *h) {
+cudaError_t launch_payload_vel(FlipGpu *h, int apply_gravity) {
   SimConst c = make_const(h);
   if (h->np == 0) return cudaSuccess;
   k_payload_vel<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
-      c, h->defer_gravity, h->perm, h->vx, h->vy, h->vz, h->type, h->svel);
+      c, apply_gravity, h->perm, h->vx, h->vy, h->vz, h->type, h->svel);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
