@@ -13,6 +13,7 @@
 
     python tests/long_runs.py pool --steps 200
     python tests/long_runs.py dam_break --steps 500
+    python tests/long_runs.py dam_break --steps 300 --precond mg --arith fast
 
 Prints one JSON object. Test infrastructure: the oracle is the checker.
 """
@@ -69,13 +70,15 @@ def pool(steps=200, every=20, rel_tol=1e-6, seed=3):
             "rel_tol": rel_tol, "seconds": time.perf_counter() - t0, "records": rec}
 
 
-def dam_break(steps=500, every=100, rel_tol=1e-6, n=128):
+def dam_break(steps=500, every=100, rel_tol=1e-6, n=128, precond="jacobi", arith="ref"):
     sc = scenes.dam_break(n, seed=0)
     sims = {}
-    for name, mode, pre in (("fast", gpu.SOLVE_FAST, gpu.PRECOND_JACOBI),
-                            ("ref", gpu.SOLVE_REF, gpu.PRECOND_REF)):
+    fast_pre = gpu.PRECOND_MG if precond == "mg" else gpu.PRECOND_JACOBI
+    fast_arith = gpu.ARITH_FAST if arith == "fast" else gpu.ARITH_REF
+    for name, mode, pre, ar in (("fast", gpu.SOLVE_FAST, fast_pre, fast_arith),
+                                ("ref", gpu.SOLVE_REF, gpu.PRECOND_REF, gpu.ARITH_REF)):
         s = gpu.Simulation(gpu.default_params(n, sc.count, rel_tol=rel_tol, seed=1,
-                                              solve_mode=mode, precond=pre))
+                                              solve_mode=mode, precond=pre, arith=ar))
         s.set_scene(sc)
         s.calibrate_max_density()
         sims[name] = s
@@ -102,7 +105,8 @@ def dam_break(steps=500, every=100, rel_tol=1e-6, n=128):
                         "centre_shift": float(np.linalg.norm(np.subtract(fs["centre"],
                                                                          rs["centre"]))),
                         "kinetic_rel": abs(fs["kinetic"] - rs["kinetic"]) / max(rs["kinetic"], 1e-30)})
-    return {"workload": f"dam_break N={n}, FAST (FP32 + FP64 dots) vs REF solver arithmetic",
+    return {"workload": f"dam_break N={n}, FAST solver (FP32 + FP64 dots, {precond} "
+                        f"preconditioner, {arith} gathers) vs the REF step",
             "steps": steps, "rel_tol": rel_tol, "seconds": time.perf_counter() - t0,
             "records": rec}
 
@@ -112,12 +116,16 @@ def main(argv=None):
     ap.add_argument("which", choices=["pool", "dam_break"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--every", type=int, default=None)
+    ap.add_argument("--precond", choices=["jacobi", "mg"], default="jacobi",
+                    help="dam_break: preconditioner of the FAST solver")
+    ap.add_argument("--arith", choices=["ref", "fast"], default="ref",
+                    help="dam_break: particle-gather arithmetic of the FAST run")
     a = ap.parse_args(argv)
     gpu.load()
     if a.which == "pool":
         out = pool(a.steps or 200, a.every or 20)
     else:
-        out = dam_break(a.steps or 500, a.every or 100)
+        out = dam_break(a.steps or 500, a.every or 100, precond=a.precond, arith=a.arith)
     print(json.dumps(out))
 
 
