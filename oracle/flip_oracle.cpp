@@ -14,7 +14,7 @@
  * default). Cross-cell sums run in the reference's loop order, so results do
  * not depend on the OpenMP thread count.
  *
- * Deliberate differences from the reference, all documented in the design doc:
+ * Deliberate differences from the reference (the only two):
  *   - rand()/random_shuffle are replaced by the counter-based generator of
  *     include/flip_rng.h (the reference harness applies the same patch);
  *   - the trilinear fetch of the v grid clamps k+1 to the row where the
