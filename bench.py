@@ -200,6 +200,9 @@ def liquid_chunk_cells(A):
     return int(f.reshape(-1, 128).any(axis=1).sum()) * 128
 
 
+MG_SWEEPS = 2  # red-black sweeps per level and side of the V-cycle (the library default)
+
+
 def mg_coarse_cells(n):
     """Cells of the multigrid levels below the solver's grid (ceil(m/2) per
     axis down to at most 4)."""
@@ -218,16 +221,22 @@ def stage_bytes(stage, P, n, iters, sweep_cells=None, precond="jacobi"):
     grid when not given):
       Jacobi (single reduction): 49 B: A 1 + diagonal 4 + M^-1 4 + U, Wt, St,
         p, x 4 each read, U, Wt, St, p, x 4 each written;
-      multigrid: 136 B on the solver's grid (seven passes, each reading A and
-        the diagonal, 5 B, and its vectors: p' = z + beta p and A p' 16 B,
-        the x/r update and first half sweep 28 B, two black and one red half
-        sweep 12 B each, the residual 12 B, the prolongation 8.5 B) plus 90 B
-        per cell of every coarser level (three half sweeps, a residual, the
-        restriction's writes and the prolongation, about 15 B each)."""
+      multigrid with nu smoothing sweeps: on the solver's grid p' = z + beta p
+        and A p' 16 B, the x/r update with the first half sweep 28 B, the
+        residual 12 B, 4 nu - 1 more half sweeps 12 B each (the one after the
+        coarse correction also reads the parents, 0.5 B), and every one of
+        those 4 nu + 2 passes reads A and the diagonal, 5 B (nu = 2: 190.5 B);
+        plus 15 B per pass on every coarser level, 4 nu + 2 passes (half
+        sweeps, residual, the restriction's writes, prolongation)."""
     C = n ** 3
     F = 3 * (n + 1) * n * n
     cells = C if sweep_cells is None else sweep_cells
-    solve_iter = 49 * cells if precond != "mg" else 136 * cells + 90 * mg_coarse_cells(n)
+    if precond == "mg":
+        hs = 4 * MG_SWEEPS - 1
+        per_cell = 16 + 28 + 12 + 12 * hs + 0.5 + 5 * (hs + 3)
+        solve_iter = per_cell * cells + 15 * (4 * MG_SWEEPS + 2) * mg_coarse_cells(n)
+    else:
+        solve_iter = 49 * cells
     table = {
         # count: pos 12 r, key 4 w, rank 4 w; scatter: key+rank 8 r, perm 4 w;
         # cell counts/starts 3*4*C; payload: perm 4 + pos 12 + vel 12 + type 1 + dens 4 r,
@@ -237,7 +246,7 @@ def stage_bytes(stage, P, n, iters, sweep_cells=None, precond="jacobi"):
         "mark_water": P * 8 + 4 * C + 5 * C,
         "p2g": P * 32 + 4 * C + C + 2 * 4 * F,
         "divergence": C + 4 * F + 4 * C,
-        "solve": 21 * C + max(iters, 1) * solve_iter,
+        "solve": int(21 * C + max(iters, 1) * solve_iter),
         "gradient": 4 * F * 2 + 9 * C,
         "extrapolate": 4 * F * 3 + C,
         "g2p_flip": P * (12 + 1 + 12 + 12) + 2 * 4 * F,
@@ -422,7 +431,7 @@ def main():
            "mg": gpu.PRECOND_MG, "ref": gpu.PRECOND_REF}[args.precond]
     mode = gpu.SOLVE_REF if args.precond == "ref" else gpu.SOLVE_FAST
     prm = gpu.default_params(args.n, P, rel_tol=1e-6, solve_mode=mode, precond=pre, seed=1,
-                             mic_tau=0.97 if args.precond == "mic" else 0.0,
+                             mic_tau=0.97 if args.precond == "mic" else 0.0, mg_sweeps=MG_SWEEPS,
                              arith=gpu.ARITH_FAST if args.arith == "fast" else gpu.ARITH_REF)
     sim = gpu.Simulation(prm)
     t_up = time.perf_counter()
@@ -540,7 +549,10 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {"workload": f"{args.scene} N={args.n}, 8 particles/cell, rel-res 1e-6",
-                       "particles": P, "grid": args.n, "solver": f"FP32 PCG {args.precond}, FP64 dots",
+                       "particles": P, "grid": args.n,
+                       "solver": f"FP32 PCG {args.precond}, FP64 dots" +
+                                 (f", {MG_SWEEPS} red-black sweeps per level" if args.precond == "mg"
+                                  else ""),
                        "arith": f"particle gathers {args.arith} "
                                 f"({'native FP32' if args.arith == 'fast' else 'reference bit-exact'})",
                        "l2": "inputs larger than L2 (state ~0.6 GB per step)",

@@ -298,6 +298,7 @@ void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles) {
   p->max_iters = 0;
   p->refine_steps = 0;
   p->arith = FLIPGPU_ARITH_REF;
+  p->mg_sweeps = 0;
 }
 
 const char *flipgpu_last_error(const FlipGpu *h) { return h ? h->err : "null handle"; }

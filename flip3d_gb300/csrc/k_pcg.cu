@@ -463,6 +463,7 @@ struct MgArgs {
   int nlev;              /* number of levels */
   int lb;                /* levels lb.. are solved by block 0 alone */
   int coarse_sweeps;     /* symmetric Gauss-Seidel sweeps on the coarsest level */
+  int nu;                /* red-black sweeps before (and black-red after) the correction */
 };
 
 struct CgArgs {
@@ -1331,9 +1332,9 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_cg1(CgArgs
  * V-cycle of geometric multigrid, the structure of McAdams, Sifakis and
  * Teran ("A parallel multigrid Poisson solver for fluids simulation on large
  * grids", SCA 2010):
- *   - smoothing: red-black Gauss-Seidel, one red then black half sweep
- *     before the coarse correction and black then red after it (red: i+j+k
- *     even), starting from a zero correction;
+ *   - smoothing: red-black Gauss-Seidel, nu red-then-black sweeps before
+ *     the coarse correction and as many black-then-red sweeps after it
+ *     (red: i+j+k even), starting from a zero correction;
  *   - restriction: the average of the 8 children's residuals; prolongation:
  *     the coarse correction added to its 8 children;
  *   - coarser operators: the 7-point Laplacian rediscretised on the
@@ -1597,6 +1598,12 @@ __device__ void mg_block_levels(const MgArgs &mg, MgLevel *sl) {
   for (int l = lb; l < last; l++) {
     mg_gs<false>(sl[l], 1, t, S);
     __syncthreads();
+    for (int sw = 1; sw < mg.nu; sw++) {
+      mg_gs<false>(sl[l], 0, t, S);
+      __syncthreads();
+      mg_gs<false>(sl[l], 1, t, S);
+      __syncthreads();
+    }
     mg_residual<false>(sl[l], t, S);
     __syncthreads();
     mg_restrict<false, false>(sl[l], sl[l + 1], t, S);
@@ -1620,10 +1627,12 @@ __device__ void mg_block_levels(const MgArgs &mg, MgLevel *sl) {
   for (int l = last - 1; l >= lb; l--) {
     mg_prolong<false, false>(sl[l], sl[l + 1], t, S);
     __syncthreads();
-    mg_gs<false>(sl[l], 1, t, S);
-    __syncthreads();
-    mg_gs<false>(sl[l], 0, t, S);
-    __syncthreads();
+    for (int sw = 0; sw < mg.nu; sw++) {
+      mg_gs<false>(sl[l], 1, t, S);
+      __syncthreads();
+      mg_gs<false>(sl[l], 0, t, S);
+      __syncthreads();
+    }
   }
   for (unsigned c = t; c < tot0; c += S) G.x[c] = sl[lb].x[c];
 }
@@ -1644,7 +1653,7 @@ __host__ __device__ inline size_t mg_block_bytes(const int *m, int lb, int nlev)
  * correction, and only the black cells are written (the red cells keep
  * their uncorrected z, which the neighbours of this phase read and correct
  * themselves; the red half sweep that follows overwrites every red cell). */
-enum MgPhase { MG_MATVEC, MG_UPDATE, MG_BLACK, MG_RES, MG_RED_DOT, MG_BLACK_PROLONG };
+enum MgPhase { MG_MATVEC, MG_UPDATE, MG_BLACK, MG_RES, MG_RED_DOT, MG_BLACK_PROLONG, MG_RED };
 
 template <int PH, int BLOCK>
 __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float beta, const float *pold,
@@ -1677,7 +1686,7 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
     const bool fv[4] = {fl(A4.x), fl(A4.y), fl(A4.z), fl(A4.w)};
     const int par0 = (i + j + k0) & 1; /* colour of the quad's first cell */
     constexpr bool NB = PH == MG_MATVEC || PH == MG_BLACK || PH == MG_RES || PH == MG_RED_DOT ||
-                        PH == MG_BLACK_PROLONG;
+                        PH == MG_BLACK_PROLONG || PH == MG_RED;
     /* the field whose neighbours are summed: p' = z + beta p (MATVEC) or z */
     float4 own = zero, own0 = zero; /* own0: as loaded, before any correction */
     float4 nbq[4] = {zero, zero, zero, zero};
@@ -1804,8 +1813,8 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
 #pragma unroll
       for (int u = 0; u < 4; u++) res[u] = fv[u] ? rv[u] - hs * (dv[u] * ov[u] - nbs[u]) : 0.0f;
       reinterpret_cast<float4 *>(L0.res)[q] = make_float4(res[0], res[1], res[2], res[3]);
-    } else { /* MG_BLACK, MG_BLACK_PROLONG, MG_RED_DOT: half sweep of one colour */
-      const int color = PH == MG_RED_DOT ? 0 : 1;
+    } else { /* MG_BLACK, MG_BLACK_PROLONG, MG_RED, MG_RED_DOT: half sweep of one colour */
+      const int color = (PH == MG_RED_DOT || PH == MG_RED) ? 0 : 1;
       const float4 r4 = __ldcg(reinterpret_cast<const float4 *>(rf) + q);
       const float4 dg = __ldg(d4p + qs);
       const float rv[4] = {r4.x, r4.y, r4.z, r4.w}, dv[4] = {dg.x, dg.y, dg.z, dg.w};
@@ -1926,6 +1935,12 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs 
     FF none = ff_zero();
     mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
     if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    for (int sw = 1; sw < mg.nu; sw++) {
+      mg_quads<MG_RED, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    }
     mg_quads<MG_RES, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
     if (!count_barrier(a.bar, epoch, a.iflags)) return false;
     mg_restrict<true, true>(mg.lv[0], mg.lv[1], gt, gs);
@@ -1933,6 +1948,12 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs 
     for (int l = 1; l < mg.lb; l++) {
       mg_gs<true>(mg.lv[l], 1, gt, gs);
       if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      for (int sw = 1; sw < mg.nu; sw++) {
+        mg_gs<true>(mg.lv[l], 0, gt, gs);
+        if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+        mg_gs<true>(mg.lv[l], 1, gt, gs);
+        if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      }
       mg_residual<true>(mg.lv[l], gt, gs);
       if (!count_barrier(a.bar, epoch, a.iflags)) return false;
       mg_restrict<true, true>(mg.lv[l], mg.lv[l + 1], gt, gs);
@@ -1947,9 +1968,21 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs 
       if (!count_barrier(a.bar, epoch, a.iflags)) return false;
       mg_gs<true>(mg.lv[l], 0, gt, gs);
       if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      for (int sw = 1; sw < mg.nu; sw++) {
+        mg_gs<true>(mg.lv[l], 1, gt, gs);
+        if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+        mg_gs<true>(mg.lv[l], 0, gt, gs);
+        if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      }
     }
     mg_quads<MG_BLACK_PROLONG, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
     if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    for (int sw = 1; sw < mg.nu; sw++) {
+      mg_quads<MG_RED, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+      mg_quads<MG_BLACK, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, none);
+      if (!count_barrier(a.bar, epoch, a.iflags)) return false;
+    }
     mg_quads<MG_RED_DOT, BLOCK>(a, 0.0f, 0.0f, nullptr, nullptr, prz);
     return true;
   };
@@ -2612,6 +2645,8 @@ static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
 }
 
 constexpr int MG_COARSE_SWEEPS = 2; /* the iteration count does not depend on it */
+constexpr int MG_SWEEPS_DEFAULT = 2; /* measured: 1 -> 2 sweeps cut the solve 11 % at
+                                          n=128 and 35 % at n=256; 3 gain nothing */
 constexpr int CG_MG_BLOCK = 512;
 constexpr size_t MG_SMEM_MAX = 96 * 1024; /* block 0's levels: <= 16^3 + 8^3 + 4^3 cells */
 
@@ -2845,6 +2880,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       mg.nlev = h->mg_nlev;
       mg.lb = h->mg_lb;
       mg.coarse_sweeps = MG_COARSE_SWEEPS;
+      mg.nu = h->prm.mg_sweeps > 0 ? h->prm.mg_sweeps : MG_SWEEPS_DEFAULT;
       float hs = sa.inv_h2_f;
       for (int l = 0; l < mg.nlev; l++) {
         MgLevel &L = mg.lv[l];

@@ -33,7 +33,7 @@ class Params(C.Structure):
                 ("subcell", C.c_int), ("seed", C.c_uint64), ("solve_mode", C.c_int),
                 ("precond", C.c_int), ("mic_tau", C.c_double), ("rel_tol", C.c_double),
                 ("eps_abs", C.c_double), ("max_iters", C.c_int), ("refine_steps", C.c_int),
-                ("arith", C.c_int)]
+                ("arith", C.c_int), ("mg_sweeps", C.c_int)]
 
 
 class SceneObject(C.Structure):

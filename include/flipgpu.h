@@ -97,6 +97,9 @@ typedef struct FlipGpuParams {
                          off near the FP32 rounding of A x (about 1e-4 of
                          ||b|| at n=128), where restarts cannot help. */
   int arith;          /* FLIPGPU_ARITH_*: particle-gather arithmetic */
+  int mg_sweeps;      /* MG preconditioner: red-black Gauss-Seidel sweeps before
+                         the coarse correction (mirrored after it) on every
+                         level; <= 0: the library's default */
 } FlipGpuParams;
 
 typedef struct FlipGpuSolveStats {
