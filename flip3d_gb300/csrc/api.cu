@@ -865,10 +865,15 @@ int flipgpu_step(FlipGpu *h, FlipGpuSolveStats *st) {
   return step_body(h, st);
 }
 
-/* the transfer stream and its events, on first use */
+/* the transfer stream and its events, on first use. The stream has the
+ * device's highest priority: its (de)interleave kernels are dispatched
+ * ahead of the blocks the step's kernels still have queued, so the copies
+ * start at once instead of after the concurrent kernel drains. */
 static int xfer_init(FlipGpu *h) {
   if (h->xstream) return FLIPGPU_OK;
-  CK(h, cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking));
+  int least = 0, greatest = 0;
+  CK(h, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  CK(h, cudaStreamCreateWithPriority(&h->xstream, cudaStreamNonBlocking, greatest));
   for (int e = 0; e < 3; e++) CK(h, cudaEventCreateWithFlags(&h->xev[e], cudaEventDisableTiming));
   return FLIPGPU_OK;
 }
