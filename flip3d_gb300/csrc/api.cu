@@ -396,6 +396,16 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   }
   if (cg_grid_size(h->cg_grid) != 0)
     for (int v = 0; v < CG_VARIANTS; v++) h->cg_grid[v] = 0;
+  /* the multigrid buffers now, so that a captured step never allocates */
+  if (p->precond == FLIPGPU_PRECOND_MG && p->n % 4 == 0 && p->n >= 8) {
+    int r = mg_alloc(h);
+    if (r != FLIPGPU_OK) {
+      free_all(h);
+      cudaStreamDestroy(h->own_stream);
+      delete h;
+      return r;
+    }
+  }
   if (particles_init_device() != 0) {
     free_all(h);
     cudaStreamDestroy(h->own_stream);
@@ -443,6 +453,10 @@ int flipgpu_set_params(FlipGpu *h, const FlipGpuParams *p) {
   if (!h || !p) return FLIPGPU_EINVAL;
   if (p->n != h->prm.n || p->max_particles != h->prm.max_particles)
     return fail(h, FLIPGPU_EINVAL, "set_params: n and max_particles are fixed per handle");
+  if (p->precond == FLIPGPU_PRECOND_MG && p->n % 4 == 0 && p->n >= 8) {
+    int r = mg_alloc(h);
+    if (r != FLIPGPU_OK) return fail(h, r, "set_params: multigrid buffers");
+  }
   h->prm = *p;
   return FLIPGPU_OK;
 }

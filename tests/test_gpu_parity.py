@@ -461,19 +461,24 @@ def test_fast_arithmetic_tracks_the_reference_step(gpu, orc):
         assert np.array_equal(x, y)
 
 
-def _fast_sim(gpu, sc, seed=3):
+def _fast_sim(gpu, sc, seed=3, precond=None):
     s = make_sim(gpu, sc.n, sc.count, rel_tol=1e-6, seed=seed, solve_mode=gpu.SOLVE_FAST,
-                 precond=gpu.PRECOND_JACOBI)
+                 precond=gpu.PRECOND_JACOBI if precond is None else precond)
     s.set_scene(sc)
     s.calibrate_max_density()
     return s
 
 
-def test_async_and_graph_steps_match_plain_steps(gpu):
+@pytest.mark.parametrize("mg", [False, True])
+def test_async_and_graph_steps_match_plain_steps(gpu, mg):
     """flipgpu_step_async and a captured CUDA graph replay compute exactly
-    what flipgpu_step computes (the device step counter keys the draws)."""
+    what flipgpu_step computes (the device step counter keys the draws),
+    with the Jacobi and the multigrid persistent solves (the graph is
+    captured before any solve ran, so nothing may allocate inside it)."""
     sc = scenes.dam_break(32, seed=4)
-    ref, asy, gra = _fast_sim(gpu, sc), _fast_sim(gpu, sc), _fast_sim(gpu, sc)
+    pre = gpu.PRECOND_MG if mg else gpu.PRECOND_JACOBI
+    ref, asy, gra = (_fast_sim(gpu, sc, precond=pre), _fast_sim(gpu, sc, precond=pre),
+                     _fast_sim(gpu, sc, precond=pre))
     gra.capture_step()
     for _ in range(4):
         st = ref.step()
