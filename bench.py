@@ -51,9 +51,11 @@ def run_batch(args):
     scs = [scenes.batch_scene(1000 + i) for i in range(args.batch_scenes)]
     sims = []
     for i, sc in enumerate(scs):
+        mg = args.precond == "mg" and sc.n % 4 == 0 and sc.n >= 8
         s = gpu.Simulation(gpu.default_params(sc.n, sc.count, rel_tol=1e-6, seed=i,
                                               solve_mode=gpu.SOLVE_FAST,
-                                              precond=gpu.PRECOND_JACOBI))
+                                              precond=gpu.PRECOND_MG if mg else gpu.PRECOND_JACOBI,
+                                              mg_sweeps=MG_SWEEPS))
         s.set_scene(sc)
         s.calibrate_max_density()
         sims.append(s)
@@ -98,7 +100,7 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{len(scs)} scenes, N uniform from {{24,32,48,64,96}} "
                                f"({sizes}), pool U(0.1,0.4) + sphere r U(0.08,0.2), "
-                               f"{P} particles in all", "solver": "FP32 PCG jacobi, FP64 dots",
+                               f"{P} particles in all", "solver": f"FP32 PCG {args.precond}, FP64 dots",
                    "timing": "host wall clock around device-synchronised steps",
                    "l2": "inputs larger than L2"},
         "one_at_a_time": {"value": P * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},
