@@ -188,8 +188,11 @@ k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__
       float *__restrict__ u1, float *__restrict__ u2, float *__restrict__ us0,
       float *__restrict__ us1, float *__restrict__ us2) {
   const int n = c.n;
-  const int comp = blockIdx.y;
-  size_t f = (size_t)blockIdx.x * BLK + threadIdx.x;
+  /* consecutive blocks take the three components of the same face range,
+   * so the particles of a region are read from DRAM once and reused from L2
+   * by all three (one component after another re-read them per component) */
+  const int comp = (int)(blockIdx.x % 3u);
+  size_t f = (size_t)(blockIdx.x / 3u) * BLK + threadIdx.x;
   const size_t nf = (size_t)(n + 1) * n * n;
   if (f >= nf) return;
   int ex[3] = {n, n, n};
@@ -919,7 +922,7 @@ cudaError_t launch_density(FlipGpu *h) {
 
 cudaError_t launch_p2g(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
-  dim3 grid(grid_for(h->nf, BLK), 3);
+  const unsigned grid = 3u * grid_for(h->nf, BLK);
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
     k_p2g<FastArith><<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel,
                                                   h->A, h->u[0], h->u[1], h->u[2], h->us[0],
