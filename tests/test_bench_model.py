@@ -1,0 +1,36 @@
+"""The byte model behind bench.py's roofline line (host logic only)."""
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import bench  # noqa: E402
+
+
+def test_liquid_chunk_cells_counts_128_cell_chunks_with_liquid():
+    n = 16  # 4096 cells = 32 chunks of 128
+    A = np.zeros(n ** 3, np.uint8)
+    assert bench.liquid_chunk_cells(A) == 0
+    A[5] = 1          # chunk 0
+    A[127] = 1        # chunk 0 again
+    A[128 * 7] = 1    # chunk 7
+    A[128 * 9] = 2    # a wall cell does not count
+    assert bench.liquid_chunk_cells(A) == 2 * 128
+
+
+def test_mg_coarse_cells():
+    assert bench.mg_coarse_cells(128) == 64 ** 3 + 32 ** 3 + 16 ** 3 + 8 ** 3 + 4 ** 3
+    assert bench.mg_coarse_cells(48) == 24 ** 3 + 12 ** 3 + 6 ** 3 + 3 ** 3
+
+
+def test_solve_bytes_per_preconditioner():
+    n, iters, cells = 128, 10, 657280
+    C = n ** 3
+    jac = bench.stage_bytes("solve", 0, n, iters, cells, "jacobi")
+    assert jac == 21 * C + iters * 49 * cells
+    mg = bench.stage_bytes("solve", 0, n, iters, cells, "mg")
+    per_cell = 16 + 28 + 12 + 12 * (4 * bench.MG_SWEEPS - 1) + 0.5 + 5 * (4 * bench.MG_SWEEPS + 2)
+    assert bench.MG_SWEEPS != 2 or per_cell == 190.5
+    assert mg == int(21 * C + iters * (per_cell * cells +
+                                       15 * (4 * bench.MG_SWEEPS + 2) * bench.mg_coarse_cells(n)))
