@@ -182,6 +182,18 @@ def measured_traffic(stage, n):
     return None
 
 
+def roofline_note(traffic, nbytes):
+    """Reading of the roofline fraction when ncu measured the kernel's DRAM
+    traffic for this workload."""
+    if traffic is None or not nbytes:
+        return None
+    if traffic < 0.2 * nbytes:
+        return (f"ncu DRAM traffic {traffic} B per launch against {nbytes} algorithmic B: "
+                "the working set stays in L2, so HBM bandwidth does not bound this kernel "
+                "(its grid barriers and L2 latency do)")
+    return f"ncu DRAM traffic {traffic} B per launch against {nbytes} algorithmic B"
+
+
 def hbm_peak():
     try:
         with open(PEAKS) as f:
@@ -575,7 +587,8 @@ def main():
                          "bytes_model": "stage_bytes(): every input read once, every output "
                                         "written once; the solve counts its solver-grid "
                                         "passes over the liquid chunks only",
-                         "sweep_cells": sweep_cells},
+                         "sweep_cells": sweep_cells,
+                         "note": roofline_note(traffic, nbytes)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": P * 24,
                     "d2h_bytes_per_step": P * 24},

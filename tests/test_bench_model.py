@@ -34,3 +34,9 @@ def test_solve_bytes_per_preconditioner():
     assert bench.MG_SWEEPS != 2 or per_cell == 190.5
     assert mg == int(21 * C + iters * (per_cell * cells +
                                        15 * (4 * bench.MG_SWEEPS + 2) * bench.mg_coarse_cells(n)))
+
+
+def test_roofline_note():
+    assert bench.roofline_note(None, 10) is None
+    assert "stays in L2" in bench.roofline_note(39_000_000, 2_000_000_000)
+    assert "stays in L2" not in bench.roofline_note(1_900_000_000, 2_000_000_000)
