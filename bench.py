@@ -355,6 +355,24 @@ def cpu_step_rate(scene, seconds_cap=60.0):
     return scene.count * steps / dt, cores, steps, dt
 
 
+def max_over_ranks(value, world, device):
+    """The largest value over the ranks of the current process group (the
+    slowest replica's time); the value itself with one rank."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(particles_per_rank, world, steps, seconds):
+    """Whole-job particle-steps/s of `world` replicas that each advanced
+    `particles_per_rank` particles `steps` times in at most `seconds`."""
+    return particles_per_rank * world * steps / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -494,12 +512,8 @@ def main():
     clk = clocks.stop((t_clk0, t_clk1))
     launches = sim.launches - launches0
     ms = start_ev.elapsed_time(end_ev)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    total_particles = P * world
-    value = total_particles * args.steps / (ms / 1e3)
+    ms = max_over_ranks(ms, world, "cuda")
+    value = replica_throughput(P, world, args.steps, ms / 1e3)
 
     # per-stage profile (separate pass; events between stages)
     sim.set_profiling(True)
@@ -533,11 +547,8 @@ def main():
         sim.step_host(hp, hv, hp, hv)
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = total_particles * args.steps / e2e_s
+    e2e_s = max_over_ranks(e2e_s, world, "cuda")
+    e2e = replica_throughput(P, world, args.steps, e2e_s)
 
     # the metric's solver comparison on systems of this run (not in `value`)
     solve_cmp = None if args.no_solver_comparison else solver_comparison(gpu, sim, prm, args.n)
