@@ -167,7 +167,7 @@ void free_all(FlipGpu *h) {
                   h->nz, h->key, h->rank, h->perm, h->cell_start, h->cell_count, h->spos,
                   h->spg, h->svel, h->sdens, h->wall_start, h->wall_pos, h->wall_nrm, h->u[0],
                   h->u[1], h->u[2], h->us[0], h->us[1], h->us[2], h->A, h->L, h->press,
-                  h->div, h->r, h->z, h->s, h->s1, h->w, h->w1, h->pdir, h->chunk_off, h->chunk_list, h->bar, h->P, h->Pf, h->diag,
+                  h->div, h->press_lo, h->ir_b, h->ir_e, h->r, h->z, h->s, h->s1, h->w, h->w1, h->pdir, h->chunk_off, h->chunk_list, h->bar, h->P, h->Pf, h->diag,
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
@@ -296,7 +296,7 @@ void flipgpu_default_params(FlipGpuParams *p, int n, int max_particles) {
   p->rel_tol = 0.0;
   p->eps_abs = -1.0;
   p->max_iters = 0;
-  p->refine_steps = 0;
+  p->refine_steps = 4;
   p->arith = FLIPGPU_ARITH_REF;
   p->mg_sweeps = 0;
 }
@@ -349,6 +349,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
     AL(h->u[c], nf) AL(h->us[c], nf)
   }
   AL(h->A, nc) AL(h->L, nc) AL(h->press, nc) AL(h->div, nc) AL(h->r, nc) AL(h->z, nc)
+  AL(h->press_lo, nc) AL(h->ir_b, nc) AL(h->ir_e, nc)
   AL(h->s, nc) AL(h->s1, nc) AL(h->w, nc) AL(h->w1, nc) AL(h->pdir, nc) AL(h->chunk_off, nc / 128 + 2) AL(h->chunk_list, nc / 128 + 1) AL(h->P, 2 * nc) AL(h->Pf, nc) AL(h->diag, nc)
   AL(h->partial, 8192) AL(h->bar, 2)
   AL(h->scal, SC_COUNT) AL(h->iflags, IF_COUNT) AL(h->flag, cap) AL(h->scan_a, scan_n)
@@ -382,6 +383,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   cudaMemsetAsync(h->A, 0, nc, h->stream);
   cudaMemsetAsync(h->L, 0, nc * sizeof(float), h->stream);
   cudaMemsetAsync(h->press, 0, nc * sizeof(float), h->stream);
+  cudaMemsetAsync(h->press_lo, 0, nc * sizeof(float), h->stream);
   cudaMemsetAsync(h->div, 0, nc * sizeof(float), h->stream);
   cudaMemsetAsync(h->wall_start, 0, (nc + 1) * sizeof(uint32_t), h->stream);
   cudaMemsetAsync(h->iflags, 0, IF_COUNT * sizeof(int), h->stream);
@@ -539,7 +541,10 @@ int flipgpu_set_grid(FlipGpu *h, const float *u0, const float *u1, const float *
     if (us[c]) CK(h, cudaMemcpyAsync(h->u[c], us[c], h->nf * sizeof(float), kind, h->stream));
   if (A) CK(h, cudaMemcpyAsync(h->A, A, h->nc, kind, h->stream));
   if (L) CK(h, cudaMemcpyAsync(h->L, L, h->nc * sizeof(float), kind, h->stream));
-  if (press) CK(h, cudaMemcpyAsync(h->press, press, h->nc * sizeof(float), kind, h->stream));
+  if (press) {
+    CK(h, cudaMemcpyAsync(h->press, press, h->nc * sizeof(float), kind, h->stream));
+    h->press_lo_valid = 0;
+  }
   if (div) CK(h, cudaMemcpyAsync(h->div, div, h->nc * sizeof(float), kind, h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   return FLIPGPU_OK;
@@ -699,6 +704,21 @@ int flipgpu_fetch_velocity(FlipGpu *h, int count, const float *pts, float *out, 
 int flipgpu_resample(FlipGpu *h, int count, const float *pts, float *vel, float re,
                      int on_device) {
   return point_query(h, count, pts, vel, on_device, 1, re);
+}
+
+int flipgpu_get_pressure(FlipGpu *h, double *press, int on_device) {
+  if (!h || !press) return FLIPGPU_EINVAL;
+  double *dst = press;
+  if (!on_device) CK(h, cudaMalloc(&dst, h->nc * sizeof(double)));
+  launch_pressure_double(h, dst);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !on_device) {
+    e = cudaMemcpyAsync(press, dst, h->nc * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  }
+  if (!on_device) cudaFree(dst);
+  if (e != cudaSuccess) return fail(h, FLIPGPU_ECUDA, "get_pressure: %s", cudaGetErrorString(e));
+  return FLIPGPU_OK;
 }
 
 int flipgpu_solve(FlipGpu *h, FlipGpuSolveStats *st) {

@@ -149,7 +149,10 @@ int flipgpu_checkpoint_read(const char *path, FlipCheckpoint *c) {
   if (!path || !c || c->n < 1) return FLIPGPU_EINVAL;
   int np = 0;
   if (flipgpu_checkpoint_count(path, c->n, &np) != FLIPGPU_OK) return FLIPGPU_EINVAL;
-  if (np > c->count && c->count >= 0 && (c->pos || c->vel)) return FLIPGPU_ETOOBIG;
+  /* c->count is the capacity of every per-particle array given */
+  const bool per_particle = c->pos || c->vel || c->nrm || c->type || c->visible || c->dens;
+  if (c->count < 0) return FLIPGPU_EINVAL;
+  if (np > c->count && per_particle) return FLIPGPU_ETOOBIG;
   FILE *fp = fopen(path, "rb");
   if (!fp) return FLIPGPU_EINVAL;
   bool ok = fread(&np, sizeof(int), 1, fp) == 1 &&

@@ -112,6 +112,11 @@ struct FlipGpu {
 
   /* solver */
   float *r, *z, *s, *s1, *w;
+  /* mixed-precision refinement (FAST mode): the iterate is press + press_lo
+   * (a double-float pair), ir_b the right-hand side and ir_e the correction
+   * of the current inner FP32 solve */
+  float *press_lo, *ir_b, *ir_e;
+  int press_lo_valid; /* press_lo belongs to the current press (last solve refined) */
   float *w1, *pdir;   /* single-reduction CG: second w buffer, directions */
   /* flipgpu_step_host: transfers overlapped with the step on a second stream */
   cudaStream_t xstream;
@@ -182,6 +187,9 @@ enum {
   SC_DOT,        /* scratch result of the last dot */
   SC_ERR2_0,
   SC_TRUE2,      /* FP64 r.r of b - A x after a FAST solve */
+  SC_IR_B2,      /* refinement: b.b of the outer system */
+  SC_IR_TOL,     /* refinement: relative tolerance of the next inner solve */
+  SC_IR_PREV,    /* refinement: true r.r before the last inner solve */
   SC_COUNT
 };
 /* Device int slots (FlipGpu::iflags). */
@@ -194,6 +202,10 @@ enum {
   IF_NAN,
   IF_TIMEOUT,
   IF_REPO_LEFT,
+  IF_IR_DONE,    /* refinement: 0 running, 1 converged, 2 non-finite, 3 no
+                    convergence, 4 zero right-hand side (x = 0) */
+  IF_IR_ITERS,   /* refinement: inner CG iterations of all passes */
+  IF_IR_PASS,    /* refinement: inner solves run */
   IF_COUNT
 };
 
@@ -224,6 +236,8 @@ cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *
 cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, float *vel,
                                    float re);
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st);
+/* out[c] = press + press_lo (the refined iterate) as double, device memory */
+void launch_pressure_double(FlipGpu *h, double *out);
 /* stats of the last solve read from the device (for steps run without a
  * host sync) */
 int mesh_download_async(FlipGpu *h, double *vertices, double *normals, int32_t *faces,

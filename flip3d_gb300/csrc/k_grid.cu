@@ -65,7 +65,8 @@ k_divergence(SimConst c, const uint8_t *__restrict__ A, const float *__restrict_
 __global__ void __launch_bounds__(BLK)
 k_gradient_enforce(SimConst c, int subcell, int enforce, const uint8_t *__restrict__ A,
                    const float *__restrict__ L, const float *__restrict__ press,
-                   float *__restrict__ u0, float *__restrict__ u1, float *__restrict__ u2) {
+                   const float *__restrict__ press_lo, float *__restrict__ u0,
+                   float *__restrict__ u1, float *__restrict__ u2) {
   const int n = c.n;
   const int comp = blockIdx.y;
   size_t f = (size_t)blockIdx.x * BLK + threadIdx.x;
@@ -85,15 +86,23 @@ k_gradient_enforce(SimConst c, int subcell, int enforce, const uint8_t *__restri
   size_t cf = cell_id(n, i, j, k);
   size_t cb = comp == 0 ? cell_id(n, i - 1, j, k)
                         : (comp == 1 ? cell_id(n, i, j - 1, k) : cell_id(n, i, j, k - 1));
+  /* with a refined solve the pressure is the pair press + press_lo */
   float pf = press[cf], pb = press[cb];
+  const float lof = press_lo ? press_lo[cf] : 0.0f, lob = press_lo ? press_lo[cb] : 0.0f;
+  float lf = lof, lb = lob;
   float Lf = L[cf], Lb = L[cb];
   if (subcell && Lf * Lb < 0.0f) {
-    pf = Lf < 0.0f ? press[cf]
-                   : (float)((double)Lf / fmin(1.0e-3, (double)Lb) * (double)press[cb]);
-    pb = Lb < 0.0f ? press[cb]
-                   : (float)((double)Lb / fmin(1.0e-6, (double)Lf) * (double)press[cf]);
+    if (Lf >= 0.0f) {
+      pf = (float)((double)Lf / fmin(1.0e-3, (double)Lb) * ((double)press[cb] + (double)lob));
+      lf = 0.0f;
+    }
+    if (Lb >= 0.0f) {
+      pb = (float)((double)Lb / fmin(1.0e-6, (double)Lf) * ((double)press[cf] + (double)lof));
+      lb = 0.0f;
+    }
   }
-  float val = u[f] - (pf - pb) / c.h;
+  const float dp = press_lo ? (pf - pb) + (lf - lb) : pf - pb;
+  float val = u[f] - dp / c.h;
   if (enforce && (A[cf] == CELL_WALL) != (A[cb] == CELL_WALL)) val = 0.0f;
   u[f] = val;
 }
@@ -181,8 +190,9 @@ cudaError_t launch_divergence(FlipGpu *h) {
 cudaError_t launch_gradient_enforce(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
   dim3 grid(grid_for(h->nf, BLK), 3);
-  k_gradient_enforce<<<grid, BLK, 0, h->stream>>>(c, h->prm.subcell, enforce, h->A, h->L, h->press,
-                                                  h->u[0], h->u[1], h->u[2]);
+  k_gradient_enforce<<<grid, BLK, 0, h->stream>>>(
+      c, h->prm.subcell, enforce, h->A, h->L, h->press, h->press_lo_valid ? h->press_lo : nullptr,
+      h->u[0], h->u[1], h->u[2]);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }

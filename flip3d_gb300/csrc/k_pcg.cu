@@ -21,6 +21,7 @@
  * Jacobi or IC preconditioner in FP32, FP64 dots, stop when
  * r.r <= rel_tol^2 * b.b.
  */
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -497,7 +498,22 @@ struct CgArgs {
   /* MG-preconditioned CG */
   float *p2, *q;               /* second direction buffer, A p */
   MgArgs mg;
+  /* inner solve of the mixed-precision refinement (FAST mode): the launch
+   * returns at once when *ir_skip is set (the outer loop has finished), and
+   * the relative tolerance is *ir_tol (set by the outer loop) instead of
+   * rel_tol. Both null outside refinement. */
+  const int *ir_skip;
+  const double *ir_tol;
 };
+
+/* the launch is an inner solve the refinement no longer needs */
+__device__ __forceinline__ bool ir_skipped(const CgArgs &a) {
+  return a.ir_skip != nullptr && *(volatile const int *)a.ir_skip != 0;
+}
+
+__device__ __forceinline__ double cg_rel_tol(const CgArgs &a) {
+  return a.ir_tol != nullptr ? *(volatile const double *)a.ir_tol : a.rel_tol;
+}
 
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *iflags,
                                              unsigned *reset_ticket = nullptr) {
@@ -682,6 +698,7 @@ __device__ __forceinline__ float cg_precond(const CgArgs &a, size_t c, int i, in
 
 template <int MODE>
 __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
+  if (MODE != FLIPGPU_SOLVE_REF && ir_skipped(a)) return;
   const unsigned nb = gridDim.x;
   const size_t stride = (size_t)nb * CG_BLOCK;
   const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
@@ -725,7 +742,8 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg(CgArgs a) {
       while (eps > target && eps > 0.0) eps *= 0.25;
     }
   } else {
-    eps = a.rel_tol * a.rel_tol * b2;
+    const double rt = cg_rel_tol(a);
+    eps = rt * rt * b2;
   }
   int done = 0, iters = 0;
   double e2 = rr;
@@ -1015,6 +1033,7 @@ __global__ void __launch_bounds__(BLK) k_cg1_chunk_scatter(size_t nch, const uns
 }
 
 template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_cg1(CgArgs a) {
+  if (ir_skipped(a)) return;
   const unsigned nb = gridDim.x;
   const int n = a.s.n;
   const int qrow = n / 4;
@@ -1093,7 +1112,8 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_cg1(CgArgs
       b2 = t[0];
       e2 = t[1];
       gamma = t[2];
-      eps = a.rel_tol * a.rel_tol * b2;
+      const double rt = cg_rel_tol(a);
+      eps = rt * rt * b2;
       s_done = e2 <= eps ? 1 : 0;
     }
   }
@@ -1832,6 +1852,7 @@ __device__ __forceinline__ void mg_quads(const CgArgs &a, float alpha, float bet
 }
 
 template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs a) {
+  if (ir_skipped(a)) return;
   const unsigned nb = gridDim.x;
   const int n = a.s.n;
   const int qrow = n / 4;
@@ -1922,7 +1943,8 @@ template <int BLOCK> __global__ void __launch_bounds__(BLOCK, 1) k_cg_mg(CgArgs 
     if (threadIdx.x == 0) {
       b2 = t[0];
       e2 = t[1];
-      eps = a.rel_tol * a.rel_tol * b2;
+      const double rt = cg_rel_tol(a);
+      eps = rt * rt * b2;
       s_done = e2 <= eps ? 1 : 0;
     }
   }
@@ -2420,6 +2442,7 @@ __device__ __forceinline__ double sum_brick_parts(const CgArgs &a) {
 
 /* FAST-mode PCG with the wavefront IC(0)/MIC(0) preconditioner. */
 __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
+  if (ir_skipped(a)) return;
   extern __shared__ unsigned char dyn[];
   BrickSmem *sm = reinterpret_cast<BrickSmem *>(dyn);
   /* the intra-brick plane table, read with lane-varying indices */
@@ -2460,7 +2483,8 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   if (!grid_barrier(a.bar, a.iflags)) return;
   double b2, rr, unused;
   sum_partials(a.part, 0, 1, nb, b2, rr);
-  const double eps = a.rel_tol * a.rel_tol * b2;
+  const double rt = cg_rel_tol(a);
+  const double eps = rt * rt * b2;
   int done = rr <= eps ? 1 : 0, iters = 0;
   double e2 = rr, azr = 0.0;
   if (!done) {
@@ -2587,21 +2611,223 @@ __global__ void k_true_r2_sum(const double *__restrict__ part, double *__restric
   if (threadIdx.x == 0) scal[SC_TRUE2] = sh[0];
 }
 
+/* ------------------------------------------ mixed-precision refinement */
+
+/* The FAST solve refines: the iterate x = xhi + xlo is a double-float pair
+ * (about 48 significant bits), its residual r = b - A x is evaluated with
+ * error-free FP32 transforms, and each pass solves A e = r with the FP32
+ * PCG (any preconditioner) to a loose relative tolerance, then adds e to the
+ * pair. Stopping is on the residual of the pair, ||r|| <= rel_tol ||b||. With
+ * x stored in FP32 alone, b - A x levels off near the FP32 rounding of A x
+ * (about 1e-4 of ||b|| at n = 128), which no restart can move. GB300's FP64
+ * rate is about 1/64 of its FP32 rate, so the FP64-class arithmetic runs on
+ * the FP32 pipe; only per-block partials and scalars are doubles. */
+
+/* x + y for a double-float x and a float y (TwoSum, then renormalise) */
+__device__ __forceinline__ FF df_add_f(FF x, float y) {
+  float s, e;
+  refmath::two_sum(x.hi, y, s, e);
+  e += x.lo;
+  const float hi = s + e;
+  return FF{hi, e - (hi - s)};
+}
+
+/* x * y for a double-float x and a float y (exact product of the high
+ * word by FMA) */
+__device__ __forceinline__ FF df_mul_f(FF x, float y) {
+  const float p = x.hi * y;
+  float pe = fmaf(x.hi, y, -p);
+  pe = fmaf(x.lo, y, pe);
+  const float hi = p + pe;
+  return FF{hi, pe - (hi - p)};
+}
+
+constexpr double IR_INNER_FLOOR = 1e-3; /* tightest inner tolerance asked for:
+                                           the FP32 inner solve's true residual
+                                           follows its recursive one to about
+                                           there */
+
+/* r = b - A (xhi + xlo) on the liquid, rb = float(r), e = 0, and the block
+ * partials of r.r (and, on the first pass, b.b). The first pass starts from
+ * xlo = 0 and zeroes x off the liquid, as every FAST solve leaves it. */
+template <bool FIRST>
+__global__ void __launch_bounds__(BLK)
+k_ir_residual(SolveArgs s, const uint8_t *__restrict__ A, const float *__restrict__ diag,
+              const float *__restrict__ b, float *__restrict__ xhi, float *__restrict__ xlo,
+              float *__restrict__ rb, float *__restrict__ e, const int *__restrict__ iflags,
+              double *__restrict__ part) {
+  if (!FIRST && *(volatile const int *)(iflags + IF_IR_DONE)) return;
+  const int n = s.n;
+  const size_t nc = (size_t)n * n * n;
+  const size_t sj = n, si = (size_t)n * n;
+  FF rr = ff_zero(), bb = ff_zero();
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK) {
+    if (A[c] != CELL_FLUID) {
+      rb[c] = 0.0f;
+      e[c] = 0.0f;
+      if (FIRST) {
+        xhi[c] = 0.0f;
+        xlo[c] = 0.0f;
+      }
+      continue;
+    }
+    int i, j, k;
+    decode(c, n, i, j, k);
+    const float d = diag[c], hc = xhi[c];
+    const float p = d * hc;
+    FF S{p, fmaf(d, hc, -p)}; /* diag * xhi exactly */
+    float T = FIRST ? 0.0f : d * xlo[c];
+    auto nb = [&](size_t q) {
+      S = df_add_f(S, -xhi[q]);
+      if (!FIRST) T -= xlo[q];
+    };
+    if (i + 1 < n && A[c + si] == CELL_FLUID) nb(c + si);
+    if (i > 0 && A[c - si] == CELL_FLUID) nb(c - si);
+    if (j + 1 < n && A[c + sj] == CELL_FLUID) nb(c + sj);
+    if (j > 0 && A[c - sj] == CELL_FLUID) nb(c - sj);
+    if (k + 1 < n && A[c + 1] == CELL_FLUID) nb(c + 1);
+    if (k > 0 && A[c - 1] == CELL_FLUID) nb(c - 1);
+    S = df_add_f(S, T);
+    const FF ax = df_mul_f(S, s.inv_h2_f);
+    const float bc = b[c];
+    const FF r = df_add_f(FF{-ax.hi, -ax.lo}, bc);
+    const float r32 = r.hi + r.lo;
+    rb[c] = r32;
+    e[c] = 0.0f;
+    if (FIRST) {
+      xlo[c] = 0.0f;
+      ff_add_prod(bb, bc, bc);
+    }
+    ff_add_prod(rr, r32, r32);
+  }
+  const FF t = block_sum_ff<BLK>(rr);
+  if (threadIdx.x == 0) part[blockIdx.x] = ff_to_double(t);
+  if (FIRST) {
+    const FF t2 = block_sum_ff<BLK>(bb);
+    if (threadIdx.x == 0) part[RED_BLOCKS + blockIdx.x] = ff_to_double(t2);
+  }
+}
+
+/* One block of RED_BLOCKS threads: the true r.r (and b.b) in a fixed tree,
+ * then the outer loop's decision: converged, failed, or the next inner
+ * solve's relative tolerance, aimed at half the remaining reduction and no
+ * tighter than IR_INNER_FLOOR. */
+__global__ void __launch_bounds__(RED_BLOCKS)
+k_ir_check(int first, double rel_tol, int max_passes, const double *__restrict__ part,
+           double *__restrict__ scal, int *__restrict__ iflags) {
+  __shared__ double sh[RED_BLOCKS], sb[RED_BLOCKS];
+  if (!first && iflags[IF_IR_DONE]) return;
+  sh[threadIdx.x] = part[threadIdx.x];
+  sb[threadIdx.x] = first ? part[RED_BLOCKS + threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int w = RED_BLOCKS / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      sh[threadIdx.x] += sh[threadIdx.x + w];
+      sb[threadIdx.x] += sb[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double rr = sh[0];
+  if (first) scal[SC_IR_B2] = sb[0];
+  const double b2 = scal[SC_IR_B2];
+  scal[SC_TRUE2] = rr;
+  const int pass = iflags[IF_IR_PASS];
+  int done = 0;
+  if (!(rr == rr) || !(b2 == b2)) done = 2;
+  else if (b2 == 0.0) done = 4;
+  else if (rr <= rel_tol * rel_tol * b2) done = 1;
+  else if (pass >= max_passes) done = 3;
+  else if (pass > 0 && rr > 0.81 * scal[SC_IR_PREV]) done = 3; /* < 10 % per pass: stalled */
+  if (done) {
+    iflags[IF_IR_DONE] = done;
+    return;
+  }
+  double t = 0.5 * rel_tol * sqrt(b2 / rr);
+  t = t < IR_INNER_FLOOR ? IR_INNER_FLOOR : (t > 0.5 ? 0.5 : t);
+  scal[SC_IR_TOL] = t;
+  scal[SC_IR_PREV] = rr;
+}
+
+/* x += e after an inner solve (double-float add), unless the inner solve
+ * failed; a zero right-hand side sets x = 0. Block 0 books the pass. */
+__global__ void __launch_bounds__(BLK)
+k_ir_update(size_t nc, const uint8_t *__restrict__ A, const float *__restrict__ e,
+            float *__restrict__ xhi, float *__restrict__ xlo, int *__restrict__ iflags) {
+  const int ir = *(volatile const int *)(iflags + IF_IR_DONE);
+  if (ir != 0 && ir != 4) return;
+  const int inner = iflags[IF_DONE];
+  const bool failed = iflags[IF_TIMEOUT] != 0 || inner == 2;
+  if (ir == 0 && failed) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) iflags[IF_IR_DONE] = 2;
+    return;
+  }
+  for (size_t c = (size_t)blockIdx.x * BLK + threadIdx.x; c < nc; c += (size_t)gridDim.x * BLK) {
+    if (A[c] != CELL_FLUID) continue;
+    if (ir == 4) {
+      xhi[c] = 0.0f;
+      xlo[c] = 0.0f;
+      continue;
+    }
+    float s, err;
+    refmath::two_sum(xhi[c], e[c], s, err);
+    err += xlo[c];
+    const float hi = s + err;
+    xhi[c] = hi;
+    xlo[c] = err - (hi - s);
+  }
+  if (ir == 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+    iflags[IF_IR_ITERS] += iflags[IF_ITERS];
+    iflags[IF_IR_PASS] += 1;
+    /* an inner solve that hit its iteration cap still improved x; the next
+     * check decides whether the outer loop goes on */
+  }
+}
+
+/* xhi + xlo as double (flipgpu_get_pressure) */
+__global__ void __launch_bounds__(BLK)
+k_pressure_double(size_t nc, const float *__restrict__ xhi, const float *__restrict__ xlo,
+                  double *__restrict__ out) {
+  const size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (c < nc) out[c] = (double)xhi[c] + (xlo ? (double)xlo[c] : 0.0);
+}
+
+/* Statistics and status of the last solve from the device slots. A refined
+ * solve (IF_IR_PASS > 0 or a decision in IF_IR_DONE) reports its passes,
+ * the inner iterations of all of them and the true residual of the
+ * double-float iterate as r2; its status is that of the outer loop. */
+static void stats_from(const double *sc, const int *fl, FlipGpuSolveStats *st) {
+  *st = FlipGpuSolveStats();
+  const bool refined = fl[IF_IR_DONE] != 0 || fl[IF_IR_PASS] > 0;
+  st->b2 = sc[SC_B2];
+  st->r2 = sc[SC_ERR2];
+  st->r2_true = sc[SC_TRUE2];
+  if (refined) {
+    st->iterations = fl[IF_IR_ITERS];
+    st->refine_passes = fl[IF_IR_PASS];
+    st->b2 = sc[SC_IR_B2];
+    st->r2 = sc[SC_TRUE2];
+    const int ir = fl[IF_IR_DONE];
+    st->status = fl[IF_TIMEOUT] ? FLIPGPU_ETIMEOUT
+                 : ir == 2      ? FLIPGPU_ENAN
+                 : (ir == 1 || ir == 4) ? FLIPGPU_OK
+                                        : FLIPGPU_ENOCONV;
+  } else {
+    st->iterations = fl[IF_ITERS];
+    st->status = fl[IF_TIMEOUT] ? FLIPGPU_ETIMEOUT
+                 : fl[IF_NAN]   ? FLIPGPU_ENAN
+                 : fl[IF_DONE] == 3 ? FLIPGPU_ENOCONV
+                                    : FLIPGPU_OK;
+  }
+}
+
 int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st) {
   double sc[SC_COUNT];
   int fl[IF_COUNT];
   cudaMemcpyAsync(sc, h->scal, sizeof(sc), cudaMemcpyDeviceToHost, h->stream);
   cudaMemcpyAsync(fl, h->iflags, sizeof(fl), cudaMemcpyDeviceToHost, h->stream);
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return FLIPGPU_ECUDA;
-  *st = FlipGpuSolveStats();
-  st->iterations = fl[IF_ITERS];
-  st->status = fl[IF_TIMEOUT] ? FLIPGPU_ETIMEOUT
-               : fl[IF_NAN]   ? FLIPGPU_ENAN
-               : fl[IF_DONE] == 3 ? FLIPGPU_ENOCONV
-                                  : FLIPGPU_OK;
-  st->r2 = sc[SC_ERR2];
-  st->b2 = sc[SC_B2];
-  st->r2_true = sc[SC_TRUE2];
+  stats_from(sc, fl, st);
   return FLIPGPU_OK;
 }
 
@@ -2615,19 +2841,13 @@ static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
     snprintf(h->err, sizeof h->err, "solve: %s", cudaGetErrorString(e));
     return FLIPGPU_ECUDA;
   }
-  int status = FLIPGPU_OK;
-  if (host_flags[IF_TIMEOUT]) status = FLIPGPU_ETIMEOUT;
-  else if (host_flags[IF_NAN]) status = FLIPGPU_ENAN;
-  else if (host_flags[IF_DONE] == 3) status = FLIPGPU_ENOCONV;
-  if (st) {
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-    st->iterations = host_flags[IF_ITERS];
-    st->status = status;
-    st->r2 = sc[SC_ERR2];
-    st->b2 = sc[SC_B2];
-    st->ms = ms;
-  }
+  FlipGpuSolveStats one;
+  stats_from(sc, host_flags, &one);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  one.ms = ms;
+  if (st) *st = one;
+  const int status = one.status;
   if (status == FLIPGPU_ETIMEOUT) {
     snprintf(h->err, sizeof h->err, "solve: a grid barrier wait expired");
     return status;
@@ -2638,7 +2858,12 @@ static int finish_stats(FlipGpu *h, FlipGpuSolveStats *st, int mode) {
   }
   /* the reference stops silently at its cap */
   if (status == FLIPGPU_ENOCONV && mode != FLIPGPU_SOLVE_REF) {
-    snprintf(h->err, sizeof h->err, "solve: no convergence in %d iterations", host_flags[IF_ITERS]);
+    if (one.refine_passes > 0)
+      snprintf(h->err, sizeof h->err,
+               "solve: true residual %.3g of ||b|| after %d refinement passes (%d iterations)",
+               one.b2 > 0.0 ? sqrt(one.r2 / one.b2) : 0.0, one.refine_passes, one.iterations);
+    else
+      snprintf(h->err, sizeof h->err, "solve: no convergence in %d iterations", one.iterations);
     return status;
   }
   return FLIPGPU_OK;
@@ -2931,53 +3156,77 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
       cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
     }
-    /* FAST mode: after CG meets the tolerance on its recursive residual,
-     * the true residual is recomputed in FP64; while it misses the
-     * tolerance CG restarts from x (at most refine_steps times) */
-    const int passes = mode == FLIPGPU_SOLVE_FAST ? 1 + (h->prm.refine_steps > 0 ? h->prm.refine_steps : 0) : 1;
-    int total_iters = 0, rc = FLIPGPU_OK;
-    double last_true2 = 0.0;
-    for (int pass = 0; pass < passes; pass++) {
-      if (pass > 0) {
-        cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
-        if (precond == FLIPGPU_PRECOND_IC) {
-          cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
-          cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
-          cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
+    a.ir_skip = nullptr;
+    a.ir_tol = nullptr;
+    const int block = cg_block_of(kern);
+    auto reset_flags = [&]() {
+      cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
+      if (precond == FLIPGPU_PRECOND_IC) {
+        cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
+        cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
+        cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
+      }
+    };
+    if (mode == FLIPGPU_SOLVE_FAST && h->prm.refine_steps > 0) {
+      /* mixed-precision iterative refinement: the iterate is the
+       * double-float pair (press, press_lo); each pass solves A e = b - A x
+       * in FP32 from e = 0 to the tolerance the outer loop sets and adds e.
+       * The passes are launched up front and the kernels of passes that are
+       * no longer needed return at once, so nothing waits for the host. */
+      const int passes = h->prm.refine_steps;
+      a.b = h->ir_b;
+      a.x = h->ir_e;
+      a.ir_skip = h->iflags + IF_IR_DONE;
+      a.ir_tol = h->scal + SC_IR_TOL;
+      const unsigned ug = grid_for(nc, BLK) < 4096 ? grid_for(nc, BLK) : 4096;
+      k_ir_residual<true><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
+                                                      h->press_lo, h->ir_b, h->ir_e, h->iflags,
+                                                      h->partial);
+      k_ir_check<<<1, RED_BLOCKS, 0, S>>>(1, h->prm.rel_tol, passes, h->partial, h->scal,
+                                          h->iflags);
+      FG_LAUNCHED(h, 2);
+      for (int pass = 0; pass < passes; pass++) {
+        if (pass > 0) reset_flags();
+        cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
+        FG_LAUNCHED(h, 1);
+        if (e != cudaSuccess) {
+          snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
+          return FLIPGPU_ECUDA;
         }
+        k_ir_update<<<ug, BLK, 0, S>>>(nc, h->A, h->ir_e, h->press, h->press_lo, h->iflags);
+        k_ir_residual<false><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
+                                                         h->press_lo, h->ir_b, h->ir_e,
+                                                         h->iflags, h->partial);
+        k_ir_check<<<1, RED_BLOCKS, 0, S>>>(0, h->prm.rel_tol, passes, h->partial, h->scal,
+                                            h->iflags);
+        FG_LAUNCHED(h, 3);
       }
-      const int block = cg_block_of(kern);
-      cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
-      FG_LAUNCHED(h, 1);
-      if (e != cudaSuccess) {
-        snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
-        return FLIPGPU_ECUDA;
-      }
-      if (mode == FLIPGPU_SOLVE_FAST) {
-        k_true_r2<<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press, h->partial);
-        k_true_r2_sum<<<1, RED_BLOCKS, 0, S>>>(h->partial, h->scal);
-        FG_LAUNCHED(h, 2);
-      }
-      if (h->async_mode) break; /* stats stay on the device (read_solve_stats) */
+      h->press_lo_valid = 1;
+      if (h->async_mode) return FLIPGPU_OK; /* stats stay on the device (read_solve_stats) */
       cudaEventRecord(h->ev1, S);
       FlipGpuSolveStats one;
-      rc = finish_stats(h, &one, mode);
-      total_iters += one.iterations;
-      if (st) {
-        *st = one;
-        st->iterations = total_iters;
-      }
-      if (rc != FLIPGPU_OK || mode != FLIPGPU_SOLVE_FAST) break;
-      double true2 = 0.0;
-      cudaMemcpy(&true2, h->scal + SC_TRUE2, sizeof(double), cudaMemcpyDeviceToHost);
-      if (st) st->r2_true = true2;
-      /* stop when the true residual meets the tolerance, or when a restart
-       * no longer helps: with x stored in FP32 the true residual levels off
-       * near the FP32 rounding of A x */
-      if (true2 <= h->prm.rel_tol * h->prm.rel_tol * one.b2) break;
-      if (pass > 0 && true2 > 0.25 * last_true2) break;
-      last_true2 = true2;
+      const int rc = finish_stats(h, &one, mode);
+      if (st) *st = one;
+      warm_stats(st);
+      return rc;
     }
+    /* FAST mode without refinement: CG stops on its recursive residual with
+     * x in FP32, and the true residual b - A x is evaluated in FP64 after */
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
+    FG_LAUNCHED(h, 1);
+    if (e != cudaSuccess) {
+      snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
+      return FLIPGPU_ECUDA;
+    }
+    if (mode == FLIPGPU_SOLVE_FAST) {
+      k_true_r2<<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press, h->partial);
+      k_true_r2_sum<<<1, RED_BLOCKS, 0, S>>>(h->partial, h->scal);
+      FG_LAUNCHED(h, 2);
+      h->press_lo_valid = 0;
+    }
+    if (h->async_mode) return FLIPGPU_OK;
+    cudaEventRecord(h->ev1, S);
+    const int rc = finish_stats(h, st, mode);
     warm_stats(st);
     return rc;
   }
@@ -3087,6 +3336,12 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
 }
 
 size_t ic_smem_bytes() { return sizeof(BrickSmem); }
+
+void launch_pressure_double(FlipGpu *h, double *out) {
+  k_pressure_double<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(
+      h->nc, h->press, h->press_lo_valid ? h->press_lo : nullptr, out);
+  FG_LAUNCHED(h, 1);
+}
 
 /* Intra-brick plane lists, uploaded once per device. */
 int ic_init_device() {

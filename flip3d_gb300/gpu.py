@@ -53,7 +53,7 @@ class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("r2", C.c_double),
                 ("b2", C.c_double), ("ms", C.c_double), ("warm", C.c_int),
                 ("r2_prev", C.c_double), ("r2_guess", C.c_double), ("gamma", C.c_double),
-                ("warm_ms", C.c_double), ("r2_true", C.c_double)]
+                ("warm_ms", C.c_double), ("r2_true", C.c_double), ("refine_passes", C.c_int)]
 
 
 class FlipGpuError(RuntimeError):
@@ -108,6 +108,7 @@ SIGNATURES = {
     "flipgpu_p2g": (C.c_int, [C.c_void_p]),
     "flipgpu_g2p": (C.c_int, [C.c_void_p]),
     "flipgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
+    "flipgpu_get_pressure": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_project": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
     "flipgpu_picflip": (C.c_int, [C.c_void_p, C.POINTER(SolveStats)]),
     "flipgpu_advect": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -574,6 +575,13 @@ class Simulation:
 
     def solve(self):
         return self._stats_call(self.lib.flipgpu_solve, "solve")
+
+    def get_pressure(self):
+        """The last solve's pressure as float64 [n^3]: the double-float
+        iterate of a refined FAST solve, else the FP32 pressure grid."""
+        out = np.zeros(self.n ** 3, np.float64)
+        self._ck(self.lib.flipgpu_get_pressure(self.h, _ptr(out), 0), "get_pressure")
+        return out
 
     def project(self):
         return self._stats_call(self.lib.flipgpu_project, "project")

@@ -57,8 +57,10 @@ extern "C" {
 
 /* Solver arithmetic. REF: the reference's promotions (double matvec sums,
  * float(r.r) stop test, power-of-4 relative tolerance, see rel_tol). FAST:
- * FP32 matvec and preconditioner, FP64 dot products, stop on
- * ||r|| <= rel_tol*||b|| exactly, optional FP64 iterative refinement. */
+ * FP32 matvec and preconditioner, dot products with exact products summed
+ * as double-float pairs (about 48 significant bits, fixed reduction order),
+ * and mixed-precision iterative refinement on the true residual (see
+ * refine_steps): stop on ||b - A x|| <= rel_tol*||b||. */
 #define FLIPGPU_SOLVE_REF 0
 #define FLIPGPU_SOLVE_FAST 1
 
@@ -89,13 +91,20 @@ typedef struct FlipGpuParams {
   double eps_abs;     /* REF mode: explicit absolute r.r bound if >= 0 */
   int max_iters;      /* CG iteration cap; <=0: n^3 like the reference
                          (1000 with the MG preconditioner) */
-  int refine_steps;   /* FAST mode: after CG stops, the true residual b - A x
-                         is recomputed in FP64 (stats r2_true); while it
-                         misses rel_tol and the last restart cut it at least
-                         4x, CG restarts from x, at most refine_steps times.
-                         Default 0: with x in FP32 the true residual levels
+  int refine_steps;   /* FAST mode: mixed-precision iterative refinement with
+                         at most refine_steps passes (default 4). The iterate
+                         is a double-float pair (press holds its FP32
+                         rounding; flipgpu_get_pressure returns the pair as
+                         double); each pass evaluates the true residual
+                         b - A x with error-free FP32 transforms (about 48
+                         significant bits) and solves A e = r with the FP32
+                         PCG to a loose tolerance; the solve stops when
+                         ||b - A x|| <= rel_tol ||b|| and returns
+                         FLIPGPU_ENOCONV if the passes run out or stall.
+                         0: one FP32 PCG that stops on its recursive
+                         residual; its true residual (stats r2_true) levels
                          off near the FP32 rounding of A x (about 1e-4 of
-                         ||b|| at n=128), where restarts cannot help. */
+                         ||b|| at n=128). */
   int arith;          /* FLIPGPU_ARITH_*: particle-gather arithmetic */
   int mg_sweeps;      /* MG preconditioner: red-black Gauss-Seidel sweeps before
                          the coarse correction (mirrored after it) on every
@@ -113,8 +122,12 @@ typedef struct FlipGpuSolveStats {
   double r2_guess;    /* warm start: r.r of the guess CG started from */
   double gamma;       /* warm start: step taken along the network's correction */
   double warm_ms;     /* warm start: device time of network + step */
-  double r2_true;     /* FAST mode: FP64 r.r of b - A x at the end (the
-                         recursive r2 is what CG's stop test saw) */
+  double r2_true;     /* FAST mode: r.r of the true residual b - A x at the
+                         end (the iterate of the refinement, or x in FP32
+                         without it, whose recursive r2 is what CG's stop
+                         test saw) */
+  int refine_passes;  /* FAST mode with refinement: inner solves run; r2 is
+                         then r2_true and iterations counts all passes */
 } FlipGpuSolveStats;
 
 typedef struct FlipUNet FlipUNet;
@@ -189,7 +202,11 @@ typedef struct FlipCheckpoint {
 int flipgpu_checkpoint_write(const char *path, const FlipCheckpoint *c);
 /* particle count of a checkpoint for grid n (checks the file size) */
 int flipgpu_checkpoint_count(const char *path, int n, int *count);
-/* fills the caller's arrays (sized by flipgpu_checkpoint_count) */
+/* fills the caller's arrays (sized by flipgpu_checkpoint_count): c->count is
+ * the capacity of every per-particle array given (FLIPGPU_EINVAL if
+ * negative; FLIPGPU_ETOOBIG, with nothing read, if the file holds more
+ * particles and any per-particle pointer is set); on return it holds the
+ * file's particle count */
 int flipgpu_checkpoint_read(const char *path, FlipCheckpoint *c);
 /* The handle's state as a checkpoint: particles, pressure, max_dens, and
  * the wall-normal grid compute_wall_normal (src/flip3D.cpp:75-164) gives
@@ -316,6 +333,11 @@ int flipgpu_mesh(FlipGpu *h, int64_t *n_vertices, int64_t *n_faces);
  * may be NULL. */
 int flipgpu_get_mesh(FlipGpu *h, double *vertices, double *normals,
                      int32_t *faces, float *field);
+/* The pressure of the last solve as double[n^3]: with FAST-mode refinement
+ * the double-float iterate the solver's tolerance was met on (the pressure
+ * grid holds its FP32 rounding), otherwise the pressure grid itself. press is
+ * host or device memory (on_device). */
+int flipgpu_get_pressure(FlipGpu *h, double *press, int on_device);
 /* solver::solve (src/solver.cpp:224-241) on the handle's A, L, pressure
  * (initial guess, overwritten) and divergence (negated, as the reference
  * does). */

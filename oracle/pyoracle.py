@@ -288,3 +288,49 @@ class Sim:
 
 def set_threads(n):
     lib().orc_sim_set_threads(n)
+
+
+def fast_diag(n, A, L, subcell=1):
+    """Diagonal of the FAST-mode pressure operator: A_diag of
+    src/solver.cpp:103-117 in float with the reference's double promotions,
+    neighbours in the order i-1, i+1, j-1, j+1, k-1, k+1 (a wall or the
+    domain's edge subtracts 1, an air cell L_q / min(1e-6, L_c))."""
+    A3 = np.asarray(A, np.uint8).reshape(n, n, n)
+    L3 = np.asarray(L, np.float32).reshape(n, n, n).astype(np.float64)
+    Lc = np.fmin(1.0e-6, L3)
+    diag = np.full((n, n, n), 6.0, np.float32)
+    Ap = np.pad(A3, 1, constant_values=2)  # outside the grid counts as wall
+    Lp = np.pad(L3, 1)
+    for axis in range(3):
+        for step in (-1, 1):
+            sl = [slice(1, n + 1)] * 3
+            sl[axis] = slice(1 + step, n + 1 + step)
+            an, ln = Ap[tuple(sl)], Lp[tuple(sl)]
+            wall = an == 2
+            air = (an == 0) & bool(subcell)
+            d = diag.astype(np.float64)
+            diag = np.where(wall, (d - 1.0).astype(np.float32),
+                            np.where(air, (d - ln / Lc).astype(np.float32), diag))
+    return diag.reshape(-1)
+
+
+def fast_residual_fp64(n, A, L, b, x, subcell=1):
+    """b - M x in FP64 for the FAST-mode operator M = (diag*x - sum of the
+    fluid neighbours' x) * inv_h2 (its FP32 coefficients taken exactly), on
+    the fluid cells; zero elsewhere. x may be float64 (a refined iterate)."""
+    A3 = np.asarray(A, np.uint8).reshape(n, n, n)
+    fl = A3 == 1
+    x3 = np.where(fl, np.asarray(x, np.float64).reshape(n, n, n), 0.0)
+    diag = fast_diag(n, A, L, subcell).reshape(n, n, n).astype(np.float64)
+    h2f = np.float32(1.0 / (float(n) * n))
+    inv_h2_f = float(np.float32(1.0 / float(h2f)))
+    xp = np.pad(x3, 1)
+    nb = np.zeros_like(x3)
+    for axis in range(3):
+        for step in (-1, 1):
+            sl = [slice(1, n + 1)] * 3
+            sl[axis] = slice(1 + step, n + 1 + step)
+            nb += xp[tuple(sl)]
+    ax = (diag * x3 - nb) * inv_h2_f
+    r = np.where(fl, np.asarray(b, np.float32).reshape(n, n, n).astype(np.float64) - ax, 0.0)
+    return r.reshape(-1)

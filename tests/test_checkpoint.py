@@ -62,3 +62,34 @@ def test_reader_rejects_a_wrong_grid_size(gpu, golden, tmp_path):
     gpu.checkpoint_write(path, int(golden["n"]), _state(golden))
     with pytest.raises(gpu.FlipGpuError):
         gpu.checkpoint_read(path, 16)
+
+
+def test_reader_checks_the_capacity_of_every_particle_array(gpu, golden, tmp_path):
+    """c->count is the capacity of each per-particle array given: a file with
+    more particles is rejected whichever of them is set (ETOOBIG, nothing
+    written), and a negative count is an invalid argument."""
+    import ctypes as C
+    path = str(tmp_path / "ours.dat")
+    n = int(golden["n"])
+    gpu.checkpoint_write(path, n, _state(golden))
+    lib = gpu.load()
+    small = int(golden["count"]) - 1
+    for key, dt, width in (("type", np.uint8, 1), ("dens", np.float32, 1),
+                           ("nrm", np.float32, 3), ("visible", np.uint8, 1)):
+        buf = np.full(small * width, 7, dt)
+        c = gpu.Checkpoint()
+        c.n, c.count = n, small
+        setattr(c, key, buf.ctypes.data)
+        assert lib.flipgpu_checkpoint_read(path.encode(), C.byref(c)) == -7, key
+        assert (buf == 7).all(), key
+    c = gpu.Checkpoint()
+    c.n, c.count = n, -1
+    assert lib.flipgpu_checkpoint_read(path.encode(), C.byref(c)) == -1
+    # grid sections only: no per-particle array, any capacity
+    press = np.zeros(n ** 3, np.float32)
+    c = gpu.Checkpoint()
+    c.n, c.count = n, 0
+    c.press = press.ctypes.data
+    assert lib.flipgpu_checkpoint_read(path.encode(), C.byref(c)) == 0
+    assert c.count == int(golden["count"])
+    assert np.array_equal(press, golden["press"])

@@ -269,8 +269,9 @@ def test_solve_ic_wavefront_matches_fp64_factor(gpu, orc, name, tau):
     sweep order shows up as a different count or no convergence)."""
     g = np.load(f"{GOLD}/{name}.npz")
     n = int(g["n"])
+    # one PCG (no refinement passes), so that iteration counts compare
     sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
-                   precond=gpu.PRECOND_IC, mic_tau=tau)
+                   precond=gpu.PRECOND_IC, mic_tau=tau, refine_steps=0)
     sim.set_grid(A=g["A"], L=g["L"], press=np.zeros(n ** 3, np.float32), div=g["b"])
     st = sim.solve()
     assert st.status == 0
@@ -298,7 +299,7 @@ def test_solve_mic_on_a_dam_break(gpu, orc):
     prm = orc.params(n, orc.PRECOND_IC, rel_tol=1e-6, mic_tau=0.97)
     x6, _, it6, _, _ = orc.solve(prm, A, L, np.zeros(n ** 3, np.float32), b)
     sim = make_sim(gpu, n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
-                   precond=gpu.PRECOND_IC, mic_tau=0.97)
+                   precond=gpu.PRECOND_IC, mic_tau=0.97, refine_steps=0)
     sim.set_grid(A=A, L=L, press=np.zeros(n ** 3, np.float32), div=b)
     st = sim.solve()
     assert st.status == 0

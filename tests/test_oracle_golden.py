@@ -148,3 +148,20 @@ def test_mesh_after_driver_steps():
     assert sha(m["vertices"]) == str(g["vertices_sha"])
     assert sha(m["normals"]) == str(g["normals_sha"])
     assert sha(m["faces"]) == str(g["faces_sha"])
+
+
+def test_fast_operator_restatement_matches_the_oracle_matvec():
+    """The FP64 restatement of the FAST-mode operator (fast_residual_fp64,
+    used to check refined solves on the host) against the oracle's
+    compute_Ax (src/solver.cpp:29-41) on a reference system: the two differ
+    only in where float rounding happens."""
+    g = np.load(GOLD + "/solver_n16.npz")
+    n = int(g["n"])
+    A, L = g["A"], g["L"]
+    x = np.random.default_rng(3).normal(0, 1, n ** 3).astype(np.float32)
+    ax_ref = orc.matvec(n, A, L, x).astype(np.float64)
+    ax = -orc.fast_residual_fp64(n, A, L, np.zeros(n ** 3, np.float32), x)
+    fl = A == 1
+    scale = np.abs(ax_ref[fl]).max()
+    assert np.abs(ax[fl] - ax_ref[fl]).max() <= 1e-5 * scale
+    assert not ax[~fl].any()
