@@ -283,8 +283,10 @@ def stage_bytes(stage, P, n, iters, sweep_cells=None, precond="jacobi"):
         "solve": int(21 * C + max(iters, 1) * solve_iter),
         "gradient": 4 * F * 2 + 9 * C,
         "extrapolate": 4 * F * 3 + C,
-        "g2p_flip": P * (12 + 1 + 12 + 12) + 2 * 4 * F,
-        "advect": P * (12 + 12 + 1 + 4 + 12 + 12 + 1) + 4 * F + C,
+        # FLIP blend fused with advect_particle: pos, vel, type, dens read;
+        # pos, vel, stuck flag written; the new grid and its change read once
+        "g2p_flip": P * (12 + 12 + 1 + 4 + 12 + 12 + 1) + 2 * 4 * F + C,
+        "advect": 0,
         "reposition": P * 1 + C,
         "correct": P * (16 + 16 + 12 + 12 + 4) + 4 * C,
     }

@@ -811,7 +811,9 @@ int flipgpu_project(FlipGpu *h, FlipGpuSolveStats *st) {
   return FLIPGPU_OK;
 }
 
-static int picflip(FlipGpu *h, FlipGpuSolveStats *st, StageClock *clk) {
+/* solve_picflip; with blend false the FLIP blend is left to the caller
+ * (step_body fuses it with the advection) */
+static int picflip(FlipGpu *h, FlipGpuSolveStats *st, StageClock *clk, bool blend = true) {
   StageClock none(h);
   if (!clk) clk = &none;
   clk->mark(FLIPGPU_STAGE_MARK);
@@ -827,8 +829,10 @@ static int picflip(FlipGpu *h, FlipGpuSolveStats *st, StageClock *clk) {
   CK(h, launch_gradient_enforce(h, 1));
   clk->mark(FLIPGPU_STAGE_EXTRAP);
   CK(h, launch_extrapolate_delta(h));
-  clk->mark(FLIPGPU_STAGE_FLIP);
-  CK(h, launch_flip_blend(h));
+  if (blend) {
+    clk->mark(FLIPGPU_STAGE_FLIP);
+    CK(h, launch_flip_blend(h));
+  }
   return FLIPGPU_OK;
 }
 
@@ -877,13 +881,15 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
     h->defer_vel = 0;
     CK(h, launch_payload_vel(h, h->defer_gravity));
   }
-  int r = picflip(h, st, &clk);
+  int r = picflip(h, st, &clk, false);
   if (r != FLIPGPU_OK) return r;
-  /* advect_particle with reposition; its closing sort serves the corrector,
-   * whose own sort would see the same positions */
-  clk.mark(FLIPGPU_STAGE_ADVECT);
+  /* the FLIP blend and advect_particle in one kernel (both sample the new
+   * grid at the old positions), then reposition, whose closing sort serves
+   * the corrector (its own sort would see the same positions) */
+  clk.mark(FLIPGPU_STAGE_FLIP);
   CK(h, cudaMemsetAsync(h->iflags + IF_NSTUCK, 0, 2 * sizeof(int), h->stream));
-  CK(h, launch_advect(h));
+  CK(h, launch_flip_advect(h));
+  clk.mark(FLIPGPU_STAGE_ADVECT);
   clk.mark(FLIPGPU_STAGE_REPOSITION);
   CK(h, launch_reposition(h, nullptr));
   clk.mark(FLIPGPU_STAGE_CORRECT);

@@ -230,6 +230,8 @@ cudaError_t launch_gradient_enforce(FlipGpu *h, int enforce);
 cudaError_t launch_extrapolate_delta(FlipGpu *h);
 cudaError_t launch_flip_blend(FlipGpu *h);
 cudaError_t launch_advect(FlipGpu *h);
+/* launch_flip_blend + launch_advect in one kernel (one grid sample) */
+cudaError_t launch_flip_advect(FlipGpu *h);
 cudaError_t launch_reposition(FlipGpu *h, int *stuck_host);
 cudaError_t launch_correct(FlipGpu *h);
 cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *out);

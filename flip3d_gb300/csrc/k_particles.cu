@@ -15,6 +15,9 @@
  * evaluates the same formulas in native FP32 with fused multiply-adds and
  * the fast division intrinsic (FLIPGPU_ARITH_FAST).
  */
+#include <cstdlib>
+#include <cstring>
+
 #include "devcommon.cuh"
 
 using namespace refmath;
@@ -173,6 +176,53 @@ k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restric
   sdens[a] = d;
 }
 
+/* computeDensity in FAST arithmetic: k_density<FastArith> with each
+ * contiguous run unrolled four particles at a time (their loads issued
+ * together); a wall neighbour adds an exact zero, so the sums are those of
+ * k_density<FastArith> bit for bit. */
+__global__ void __launch_bounds__(BLK)
+k_density_fast(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+               const float4 *__restrict__ spos, float *__restrict__ dens,
+               float *__restrict__ sdens) {
+  int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  const float4 P = spos[a];
+  const uint32_t p = perm[a];
+  if (unpack_type(P.w) == CELL_WALL) {
+    dens[p] = 1.0f;
+    sdens[a] = 1.0f;
+    return;
+  }
+  const int n = c.n;
+  const int ci = cell_clamp(P.x, c.fn, n), cj = cell_clamp(P.y, c.fn, n),
+            ck = cell_clamp(P.z, c.fn, n);
+  const int i0 = max(ci - 1, 0), i1 = min(ci + 1, n - 1), j0 = max(cj - 1, 0),
+            j1 = min(cj + 1, n - 1), k0 = max(ck - 1, 0), k1 = min(ck + 1, n - 1);
+  auto term = [&](const float4 &Q) {
+    const float w = FastArith::smooth_density(c, FastArith::hypot2(Q.x - P.x, Q.y - P.y, Q.z - P.z));
+    return unpack_type(Q.w) == CELL_WALL ? 0.0f : w;
+  };
+  float wsum = 0.0f;
+  for (int si = i0; si <= i1; si++)
+    for (int sj = j0; sj <= j1; sj++) {
+      const size_t base = ((size_t)si * n + sj) * n;
+      uint32_t x = __ldg(cs + base + k0);
+      const uint32_t e = __ldg(cs + base + k1 + 1);
+      for (; x + 4 <= e; x += 4) {
+        const float4 Q0 = __ldg(spos + x), Q1 = __ldg(spos + x + 1), Q2 = __ldg(spos + x + 2),
+                     Q3 = __ldg(spos + x + 3);
+        wsum += term(Q0);
+        wsum += term(Q1);
+        wsum += term(Q2);
+        wsum += term(Q3);
+      }
+      for (; x < e; x++) wsum += term(__ldg(spos + x));
+    }
+  const float d = wsum / c.max_dens;
+  dens[p] = d;
+  sdens[a] = d;
+}
+
 /* ------------------------------------------------------------ mapP2G */
 
 /* One MAC face per thread (src/mapper.cpp:17-88). The reference gathers
@@ -289,31 +339,25 @@ k_flip_blend(SimConst c, const float *__restrict__ px, const float *__restrict__
 /* ----------------------------------------------------- advect_particle */
 
 /* advect_particle (src/flip3D.cpp:877-969) for one fluid particle: Euler
- * step through the grid, clamp inside the walls, push out of wall particles
- * closer than 1.5*DENSITY/N and drop the normal velocity, then flag it if it
- * is stuck. Each particle only reads itself and the (static) wall
- * particles, so the reference's serial loop is order-independent. */
+ * step through the grid velocity vg sampled at pp, clamp inside the walls,
+ * push out of wall particles closer than 1.5*DENSITY/N and drop the normal
+ * component of the particle velocity uu, then flag it if it is stuck. Each
+ * particle only reads itself and the (static) wall particles, so the
+ * reference's serial loop is order-independent. */
 template <class AR>
-__global__ void __launch_bounds__(BLK)
-k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz,
-         float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz,
-         const uint8_t *__restrict__ type, const float *__restrict__ dens,
-         const float *__restrict__ u0, const float *__restrict__ u1,
-         const float *__restrict__ u2, const uint8_t *__restrict__ A,
-         const uint32_t *__restrict__ wall_start, const float4 *__restrict__ wall_pos,
-         const float4 *__restrict__ wall_nrm, uint8_t *__restrict__ stuck) {
-  int p = blockIdx.x * BLK + threadIdx.x;
-  if (p >= c.np) return;
-  if (type[p] != CELL_FLUID) {
-    stuck[p] = 0;
-    return;
-  }
+__device__ __forceinline__ void advect_one(const SimConst &c, int p, float pp[3], const float vg[3],
+                                           float uu[3], float *__restrict__ px,
+                                           float *__restrict__ py, float *__restrict__ pz,
+                                           float *__restrict__ vx, float *__restrict__ vy,
+                                           float *__restrict__ vz, const float *__restrict__ dens,
+                                           const uint8_t *__restrict__ A,
+                                           const uint32_t *__restrict__ wall_start,
+                                           const float4 *__restrict__ wall_pos,
+                                           const float4 *__restrict__ wall_nrm,
+                                           uint8_t *__restrict__ stuck) {
   const int n = c.n;
-  float pp[3] = {px[p], py[p], pz[p]};
-  float v[3];
-  fetch_velocity(n, c.fn, u0, u1, u2, pp[0], pp[1], pp[2], v);
 #pragma unroll
-  for (int q = 0; q < 3; q++) pp[q] = AR::euler(c, pp[q], v[q]);
+  for (int q = 0; q < 3; q++) pp[q] = AR::euler(c, pp[q], vg[q]);
   /* p = fmax(r, fmin(1.0-r, p)) */
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -322,7 +366,6 @@ k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__re
     if (t < c.wall_r) t = c.wall_r;
     pp[q] = t;
   }
-  float uu[3] = {vx[p], vy[p], vz[p]};
   int i = cell_clamp_minmax(pp[0], c.fn, n), j = cell_clamp_minmax(pp[1], c.fn, n),
       k = cell_clamp_minmax(pp[2], c.fn, n);
   visit_cells(n, wall_start, i - 1, i + 1, j - 1, j + 1, k - 1, k + 1, [&](uint32_t w) {
@@ -360,6 +403,62 @@ k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__re
                                  A[cell_id(n, si, min(n - 1, sj + 1), sk)] == CELL_WALL))
     s = 1;
   stuck[p] = s;
+}
+
+template <class AR>
+__global__ void __launch_bounds__(BLK)
+k_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz,
+         float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz,
+         const uint8_t *__restrict__ type, const float *__restrict__ dens,
+         const float *__restrict__ u0, const float *__restrict__ u1,
+         const float *__restrict__ u2, const uint8_t *__restrict__ A,
+         const uint32_t *__restrict__ wall_start, const float4 *__restrict__ wall_pos,
+         const float4 *__restrict__ wall_nrm, uint8_t *__restrict__ stuck) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np) return;
+  if (type[p] != CELL_FLUID) {
+    stuck[p] = 0;
+    return;
+  }
+  float pp[3] = {px[p], py[p], pz[p]};
+  float v[3];
+  fetch_velocity(c.n, c.fn, u0, u1, u2, pp[0], pp[1], pp[2], v);
+  float uu[3] = {vx[p], vy[p], vz[p]};
+  advect_one<AR>(c, p, pp, v, uu, px, py, pz, vx, vy, vz, dens, A, wall_start, wall_pos,
+                 wall_nrm, stuck);
+}
+
+/* The FLIP blend of solve_picflip (src/flip3D.cpp:1071-1097) fused with
+ * advect_particle (src/flip3D.cpp:877-969): both sample the new grid at the
+ * particle's position before it moves, so one sample serves the PIC term of
+ * the blend and the Euler step. The results equal k_flip_blend followed by
+ * k_advect. */
+template <class AR>
+__global__ void __launch_bounds__(BLK)
+k_flip_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz,
+              float *__restrict__ vx, float *__restrict__ vy, float *__restrict__ vz,
+              const uint8_t *__restrict__ type, const float *__restrict__ dens,
+              const float *__restrict__ u0, const float *__restrict__ u1,
+              const float *__restrict__ u2, const float *__restrict__ d0,
+              const float *__restrict__ d1, const float *__restrict__ d2,
+              const uint8_t *__restrict__ A, const uint32_t *__restrict__ wall_start,
+              const float4 *__restrict__ wall_pos, const float4 *__restrict__ wall_nrm,
+              uint8_t *__restrict__ stuck) {
+  int p = blockIdx.x * BLK + threadIdx.x;
+  if (p >= c.np) return;
+  if (type[p] != CELL_FLUID) {
+    stuck[p] = 0;
+    return;
+  }
+  float pp[3] = {px[p], py[p], pz[p]};
+  float du[3], pic[3];
+  fetch_velocity(c.n, c.fn, d0, d1, d2, pp[0], pp[1], pp[2], du);
+  fetch_velocity(c.n, c.fn, u0, u1, u2, pp[0], pp[1], pp[2], pic);
+  float uu[3] = {vx[p], vy[p], vz[p]};
+#pragma unroll
+  for (int q = 0; q < 3; q++) uu[q] = AR::blend(c, pic[q], du[q] + uu[q]);
+  advect_one<AR>(c, p, pp, pic, uu, px, py, pz, vx, vy, vz, dens, A, wall_start, wall_pos,
+                 wall_nrm, stuck);
 }
 
 /* ------------------------------------------------------------ reposition */
@@ -836,6 +935,220 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
   }
 }
 
+/* ------------------------------------------- cell-per-thread gathers */
+
+__device__ __forceinline__ void cell_decode(size_t c, int n, int &i, int &j, int &k) {
+  const unsigned row = (unsigned)(c / (unsigned)n);
+  k = (int)(c - (size_t)row * n);
+  i = (int)(row / (unsigned)n);
+  j = (int)(row - (unsigned)i * n);
+}
+
+/* mapP2G (k_p2g's arithmetic and order): one thread per face cell (i, j, k)
+ * of the (n+1)^3 lattice computes the three faces there (u0 at (i, j, k)
+ * when j, k < n; u1 when i, k < n; u2 when i, j < n). Their neighbourhoods
+ * lie in cells [i-1, i+1] x [j-1, j+1] x [k-1, k+1]: each particle there is
+ * loaded once and tested against each face whose own cells hold it, which
+ * keeps every face's sums in k_p2g's order. */
+template <class AR>
+__global__ void __launch_bounds__(BLK)
+k_p2g_cells(SimConst c, int enforce, const uint32_t *__restrict__ cs,
+            const float4 *__restrict__ spg, const float4 *__restrict__ svel,
+            const uint8_t *__restrict__ A, float *__restrict__ u0, float *__restrict__ u1,
+            float *__restrict__ u2, float *__restrict__ us0, float *__restrict__ us1,
+            float *__restrict__ us2) {
+  const int n = c.n, m1 = n + 1;
+  const size_t t = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (t >= (size_t)m1 * m1 * m1) return;
+  int i, j, k;
+  cell_decode(t, m1, i, j, k);
+  const bool v0 = j < n && k < n, v1 = i < n && k < n, v2 = i < n && j < n;
+  const float hh = c.re_p2g_hh;
+  const float fi = (float)i, fj = (float)j, fk = (float)k;
+  const float hi = fi + 0.5f, hj = fj + 0.5f, hk = fk + 0.5f;
+  float sx[3] = {0.0f, 0.0f, 0.0f}, sw[3] = {0.0f, 0.0f, 0.0f};
+  const int i0 = max(i - 1, 0), i1 = min(i + 1, n - 1), j0 = max(j - 1, 0),
+            j1 = min(j + 1, n - 1), k0 = max(k - 1, 0), k1 = min(k + 1, n - 1);
+  if (k0 <= k1) {
+    for (int si = i0; si <= i1; si++)
+      for (int sj = j0; sj <= j1; sj++) {
+        const bool in0 = v0 && si <= i, in1 = v1 && sj <= j, in2 = v2;
+        if (!(in0 || in1 || in2)) continue;
+        const size_t base = ((size_t)si * n + sj) * n;
+        const uint32_t a = __ldg(cs + base + k0), b = __ldg(cs + base + k1 + 1);
+        /* u2's cells stop at k: the particles of cell k+1 are not its */
+        const uint32_t split = k + 1 <= k1 ? __ldg(cs + base + k + 1) : b;
+        for (uint32_t x = a; x < b; x++) {
+          const float4 Q = __ldg(spg + x);
+          if (unpack_type(Q.w) != CELL_FLUID) continue;
+          float w[3] = {0.0f, 0.0f, 0.0f};
+          bool acc[3] = {false, false, false};
+          if (in0) {
+            const float r2 = AR::hypot2(Q.x - fi, Q.y - hj, Q.z - hk);
+            if (r2 < hh) {
+              acc[0] = true;
+              w[0] = AR::sharp(r2, hh, c.r2_floor, c.sharp_small_p2g);
+            }
+          }
+          if (in1) {
+            const float r2 = AR::hypot2(Q.x - hi, Q.y - fj, Q.z - hk);
+            if (r2 < hh) {
+              acc[1] = true;
+              w[1] = AR::sharp(r2, hh, c.r2_floor, c.sharp_small_p2g);
+            }
+          }
+          if (in2 && x < split) {
+            const float r2 = AR::hypot2(Q.x - hi, Q.y - hj, Q.z - fk);
+            if (r2 < hh) {
+              acc[2] = true;
+              w[2] = AR::sharp(r2, hh, c.r2_floor, c.sharp_small_p2g);
+            }
+          }
+          if (!(acc[0] || acc[1] || acc[2])) continue;
+          const float4 V = __ldg(svel + x);
+          if (acc[0]) {
+            sx[0] += w[0] * V.x;
+            sw[0] += w[0];
+          }
+          if (acc[1]) {
+            sx[1] += w[1] * V.y;
+            sw[1] += w[1];
+          }
+          if (acc[2]) {
+            sx[2] += w[2] * V.z;
+            sw[2] += w[2];
+          }
+        }
+      }
+  }
+  const bool valid[3] = {v0, v1, v2};
+#pragma unroll
+  for (int comp = 0; comp < 3; comp++) {
+    if (!valid[comp]) continue;
+    const float val = (sw[comp] != 0.0f) ? sx[comp] / sw[comp] : 0.0f;
+    const int a = comp == 0 ? i : (comp == 1 ? j : k);
+    float out = val;
+    if (!enforce) {
+    } else if (a == 0 || a == n) {
+      out = 0.0f;
+    } else {
+      const size_t cc1 = cell_id(n, i, j, k);
+      const size_t cc0 = comp == 0 ? cell_id(n, i - 1, j, k)
+                                   : (comp == 1 ? cell_id(n, i, j - 1, k) : cell_id(n, i, j, k - 1));
+      if ((__ldg(A + cc1) == CELL_WALL) != (__ldg(A + cc0) == CELL_WALL)) out = 0.0f;
+    }
+    size_t f;
+    float *u, *us;
+    if (comp == 0) {
+      f = ((size_t)i * n + j) * n + k;
+      u = u0;
+      us = us0;
+    } else if (comp == 1) {
+      f = ((size_t)i * m1 + j) * n + k;
+      u = u1;
+      us = us1;
+    } else {
+      f = ((size_t)i * n + j) * m1 + k;
+      u = u2;
+      us = us2;
+    }
+    us[f] = val;
+    u[f] = out;
+  }
+}
+
+/* The corrector's spring and resample with the near-pair work inline
+ * instead of through k_spring's and k_resample's per-thread near lists
+ * (which hold 24 KB of shared memory per block); the same pairs in the same
+ * order, so the same results. */
+template <class AR>
+__global__ void __launch_bounds__(BLK)
+k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                const float4 *__restrict__ spos, const float *__restrict__ nx,
+                const float *__restrict__ ny, const float *__restrict__ nz,
+                float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz) {
+  const int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  const float4 P = __ldg(spos + a);
+  if (unpack_type(P.w) != CELL_FLUID) return;
+  const uint32_t pid = __ldg(perm + a);
+  const float re = c.re_corr;
+  const int x = cell_clamp_macro(P.x, c.fn), y = cell_clamp_macro(P.y, c.fn),
+            z = cell_clamp_macro(P.z, c.fn);
+  int i0, i1, j0, j1, k0, k1;
+  reach_range(P.x, c.corr_reach, c.fn, c.n, x, i0, i1);
+  reach_range(P.y, c.corr_reach, c.fn, c.n, y, j0, j1);
+  reach_range(P.z, c.corr_reach, c.fn, c.n, z, k0, k1);
+  float spring[3] = {0.0f, 0.0f, 0.0f};
+  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+    if (b == (uint32_t)a) return;
+    const float4 Q = __ldg(spos + b);
+    if (AR::hypot2(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
+    const float dx = P.x - Q.x, dy = P.y - Q.y, dz = P.z - Q.z;
+    const float dist = AR::length(dx, dy, dz);
+    const float w = 50.0f * AR::smooth_corr(c, dist * dist);
+    if (dist > c.corr_near_thr) {
+      spring[0] += AR::spring_term(w, dx, dist, re);
+      spring[1] += AR::spring_term(w, dy, dist, re);
+      spring[2] += AR::spring_term(w, dz, dist, re);
+    } else {
+      const uint32_t o = __ldg(perm + b);
+      if (unpack_type(Q.w) == CELL_FLUID) {
+        for (int d = 0; d < 3; d++) {
+          const uint32_t r = flip_rand31(c.seed, flip_stream(FLIP_RNG_KICK, (uint64_t)*c.dstep, d),
+                                         (uint64_t)pid, (uint64_t)o);
+          spring[d] = kick_add(spring[d], c.kick_fluid, (int)(r % 101));
+        }
+      } else {
+        const float nn[3] = {nx[o], ny[o], nz[o]};
+        for (int d = 0; d < 3; d++) spring[d] = wall_kick_add(spring[d], c.kick_wall, nn[d]);
+      }
+    }
+  });
+  px[pid] = P.x + c.dt_f * spring[0];
+  py[pid] = P.y + c.dt_f * spring[1];
+  pz[pid] = P.z + c.dt_f * spring[2];
+}
+
+template <class AR>
+__global__ void __launch_bounds__(BLK)
+k_resample_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+                  const float4 *__restrict__ spos, const float4 *__restrict__ svel,
+                  const float *__restrict__ px, const float *__restrict__ py,
+                  const float *__restrict__ pz, float *__restrict__ vx, float *__restrict__ vy,
+                  float *__restrict__ vz) {
+  const int a = blockIdx.x * BLK + threadIdx.x;
+  if (a >= c.np) return;
+  if (unpack_type(__ldg(spos + a).w) != CELL_FLUID) return;
+  const uint32_t p = __ldg(perm + a);
+  const float T[3] = {px[p], py[p], pz[p]};
+  const int ci = cell_clamp(T[0], c.fn, c.n), cj = cell_clamp(T[1], c.fn, c.n),
+            ck = cell_clamp(T[2], c.fn, c.n);
+  int i0, i1, j0, j1, k0, k1;
+  reach_range(T[0], c.corr_reach, c.fn, c.n, ci, i0, i1);
+  reach_range(T[1], c.corr_reach, c.fn, c.n, cj, j0, j1);
+  reach_range(T[2], c.corr_reach, c.fn, c.n, ck, k0, k1);
+  float u[3] = {0.0f, 0.0f, 0.0f};
+  float wsum = 0.0f;
+  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+    const float4 Q = __ldg(spos + b);
+    if (unpack_type(Q.w) != CELL_FLUID) return;
+    const float d2 = AR::hypot2(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
+    if (!(d2 < c.re_corr_hh)) return;
+    const float w = AR::sharp(d2, c.re_corr_hh, c.r2_floor, c.sharp_small_corr);
+    const float4 V = __ldg(svel + b);
+    u[0] += w * V.x;
+    u[1] += w * V.y;
+    u[2] += w * V.z;
+    wsum += w;
+  });
+  if (wsum != 0.0f) {
+    vx[p] = u[0] / wsum;
+    vy[p] = u[1] / wsum;
+    vz[p] = u[2] / wsum;
+  }
+}
+
 /* mapper::fetchVelocity at arbitrary points (AoS in and out). */
 __global__ void k_fetch_points(SimConst c, int count, const float *__restrict__ pts,
                                const float *__restrict__ u0, const float *__restrict__ u1,
@@ -906,10 +1219,27 @@ cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, floa
   return cudaGetLastError();
 }
 
+/* FAST arithmetic runs the gathers restructured for speed (P2G with one
+ * thread per face cell, density unrolled, the corrector without near
+ * lists); FLIPGPU_GATHER=particle in the environment selects the original
+ * per-particle kernels instead (read at each launch, so one process can
+ * compare the two: the results are identical) */
+static bool cell_gathers(const FlipGpu *h) {
+  if (h->prm.arith != FLIPGPU_ARITH_FAST) return false;
+  const char *e = getenv("FLIPGPU_GATHER");
+  return !(e && strcmp(e, "particle") == 0);
+}
+
 cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
   const unsigned g = grid_for(h->np, BLK);
+  if (cell_gathers(h)) {
+    k_density_fast<<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
+                                             h->sdens);
+    FG_LAUNCHED(h, 1);
+    return cudaGetLastError();
+  }
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
     k_density<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
                                                    h->sdens);
@@ -922,6 +1252,14 @@ cudaError_t launch_density(FlipGpu *h) {
 
 cudaError_t launch_p2g(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
+  if (cell_gathers(h)) {
+    const size_t m1 = (size_t)h->n + 1;
+    k_p2g_cells<FastArith><<<grid_for(m1 * m1 * m1, BLK), BLK, 0, h->stream>>>(
+        c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0], h->u[1], h->u[2], h->us[0],
+        h->us[1], h->us[2]);
+    FG_LAUNCHED(h, 1);
+    return cudaGetLastError();
+  }
   const unsigned grid = 3u * grid_for(h->nf, BLK);
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
     k_p2g<FastArith><<<grid, BLK, 0, h->stream>>>(c, enforce, h->cell_start, h->spg, h->svel,
@@ -956,6 +1294,22 @@ cudaError_t launch_flip_blend(FlipGpu *h) {
     k_flip_blend<RefArith><<<g, BLK, 0, h->stream>>>(c, h->px, h->py, h->pz, h->type, h->u[0],
                                                      h->u[1], h->u[2], h->us[0], h->us[1],
                                                      h->us[2], h->vx, h->vy, h->vz);
+  FG_LAUNCHED(h, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flip_advect(FlipGpu *h) {
+  if (h->np == 0) return cudaSuccess;
+  SimConst c = make_const(h);
+  const unsigned g = grid_for(h->np, BLK);
+  if (h->prm.arith == FLIPGPU_ARITH_FAST)
+    k_flip_advect<FastArith><<<g, BLK, 0, h->stream>>>(
+        c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
+        h->us[0], h->us[1], h->us[2], h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
+  else
+    k_flip_advect<RefArith><<<g, BLK, 0, h->stream>>>(
+        c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
+        h->us[0], h->us[1], h->us[2], h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -1059,6 +1413,20 @@ cudaError_t launch_correct(FlipGpu *h) {
   SimConst c = make_const(h);
   const unsigned g = grid_for(h->np, BLK);
   const bool fast = h->prm.arith == FLIPGPU_ARITH_FAST;
+  if (cell_gathers(h)) {
+    k_spring_inline<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
+                                                         h->nx, h->ny, h->nz, h->px, h->py,
+                                                         h->pz);
+    FG_LAUNCHED(h, 1);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (h->xfer_pos_out && (e = xfer_positions_out(h)) != cudaSuccess) return e;
+    k_resample_inline<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
+                                                           h->svel, h->px, h->py, h->pz, h->vx,
+                                                           h->vy, h->vz);
+    FG_LAUNCHED(h, 1);
+    return cudaGetLastError();
+  }
   if (fast)
     k_spring<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,
                                                   h->ny, h->nz, h->px, h->py, h->pz);

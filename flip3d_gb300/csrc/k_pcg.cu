@@ -23,6 +23,7 @@
  */
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -2645,7 +2646,7 @@ __device__ __forceinline__ FF df_mul_f(FF x, float y) {
 constexpr double IR_INNER_FLOOR = 1e-3; /* tightest inner tolerance asked for:
                                            the FP32 inner solve's true residual
                                            follows its recursive one to about
-                                           there */
+                                           there (FLIPGPU_IR_FLOOR overrides) */
 
 /* r = b - A (xhi + xlo) on the liquid, rb = float(r), e = 0, and the block
  * partials of r.r (and, on the first pass, b.b). The first pass starts from
@@ -2713,8 +2714,8 @@ k_ir_residual(SolveArgs s, const uint8_t *__restrict__ A, const float *__restric
  * solve's relative tolerance, aimed at half the remaining reduction and no
  * tighter than IR_INNER_FLOOR. */
 __global__ void __launch_bounds__(RED_BLOCKS)
-k_ir_check(int first, double rel_tol, int max_passes, const double *__restrict__ part,
-           double *__restrict__ scal, int *__restrict__ iflags) {
+k_ir_check(int first, double rel_tol, int max_passes, double floor_tol,
+           const double *__restrict__ part, double *__restrict__ scal, int *__restrict__ iflags) {
   __shared__ double sh[RED_BLOCKS], sb[RED_BLOCKS];
   if (!first && iflags[IF_IR_DONE]) return;
   sh[threadIdx.x] = part[threadIdx.x];
@@ -2744,7 +2745,7 @@ k_ir_check(int first, double rel_tol, int max_passes, const double *__restrict__
     return;
   }
   double t = 0.5 * rel_tol * sqrt(b2 / rr);
-  t = t < IR_INNER_FLOOR ? IR_INNER_FLOOR : (t > 0.5 ? 0.5 : t);
+  t = t < floor_tol ? floor_tol : (t > 0.5 ? 0.5 : t);
   scal[SC_IR_TOL] = t;
   scal[SC_IR_PREV] = rr;
 }
@@ -3179,11 +3180,16 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       a.ir_skip = h->iflags + IF_IR_DONE;
       a.ir_tol = h->scal + SC_IR_TOL;
       const unsigned ug = grid_for(nc, BLK) < 4096 ? grid_for(nc, BLK) : 4096;
+      double floor_tol = IR_INNER_FLOOR;
+      if (const char *ev = getenv("FLIPGPU_IR_FLOOR")) {
+        const double v = atof(ev);
+        if (v > 0.0 && v < 1.0) floor_tol = v;
+      }
       k_ir_residual<true><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
                                                       h->press_lo, h->ir_b, h->ir_e, h->iflags,
                                                       h->partial);
-      k_ir_check<<<1, RED_BLOCKS, 0, S>>>(1, h->prm.rel_tol, passes, h->partial, h->scal,
-                                          h->iflags);
+      k_ir_check<<<1, RED_BLOCKS, 0, S>>>(1, h->prm.rel_tol, passes, floor_tol, h->partial,
+                                          h->scal, h->iflags);
       FG_LAUNCHED(h, 2);
       for (int pass = 0; pass < passes; pass++) {
         if (pass > 0) reset_flags();
@@ -3197,8 +3203,8 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
         k_ir_residual<false><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
                                                          h->press_lo, h->ir_b, h->ir_e,
                                                          h->iflags, h->partial);
-        k_ir_check<<<1, RED_BLOCKS, 0, S>>>(0, h->prm.rel_tol, passes, h->partial, h->scal,
-                                            h->iflags);
+        k_ir_check<<<1, RED_BLOCKS, 0, S>>>(0, h->prm.rel_tol, passes, floor_tol, h->partial,
+                                            h->scal, h->iflags);
         FG_LAUNCHED(h, 3);
       }
       h->press_lo_valid = 1;

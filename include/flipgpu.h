@@ -383,8 +383,9 @@ int64_t flipgpu_launch_count(const FlipGpu *h);
 #define FLIPGPU_STAGE_SOLVE 5
 #define FLIPGPU_STAGE_GRAD 6       /* gradient + enforce_boundary */
 #define FLIPGPU_STAGE_EXTRAP 7     /* extrapolate + subtract_grid */
-#define FLIPGPU_STAGE_FLIP 8       /* G2P + FLIP blend */
-#define FLIPGPU_STAGE_ADVECT 9
+#define FLIPGPU_STAGE_FLIP 8       /* G2P + FLIP blend; in flipgpu_step also
+                                      advect_particle, fused with the blend */
+#define FLIPGPU_STAGE_ADVECT 9     /* advect_particle (empty in flipgpu_step) */
 #define FLIPGPU_STAGE_REPOSITION 10 /* stuck lists, placement, sort, resample */
 #define FLIPGPU_STAGE_CORRECT 11
 #define FLIPGPU_NSTAGES 12
