@@ -176,53 +176,6 @@ k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restric
   sdens[a] = d;
 }
 
-/* computeDensity in FAST arithmetic: k_density<FastArith> with each
- * contiguous run unrolled four particles at a time (their loads issued
- * together); a wall neighbour adds an exact zero, so the sums are those of
- * k_density<FastArith> bit for bit. */
-__global__ void __launch_bounds__(BLK)
-k_density_fast(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
-               const float4 *__restrict__ spos, float *__restrict__ dens,
-               float *__restrict__ sdens) {
-  int a = blockIdx.x * BLK + threadIdx.x;
-  if (a >= c.np) return;
-  const float4 P = spos[a];
-  const uint32_t p = perm[a];
-  if (unpack_type(P.w) == CELL_WALL) {
-    dens[p] = 1.0f;
-    sdens[a] = 1.0f;
-    return;
-  }
-  const int n = c.n;
-  const int ci = cell_clamp(P.x, c.fn, n), cj = cell_clamp(P.y, c.fn, n),
-            ck = cell_clamp(P.z, c.fn, n);
-  const int i0 = max(ci - 1, 0), i1 = min(ci + 1, n - 1), j0 = max(cj - 1, 0),
-            j1 = min(cj + 1, n - 1), k0 = max(ck - 1, 0), k1 = min(ck + 1, n - 1);
-  auto term = [&](const float4 &Q) {
-    const float w = FastArith::smooth_density(c, FastArith::hypot2(Q.x - P.x, Q.y - P.y, Q.z - P.z));
-    return unpack_type(Q.w) == CELL_WALL ? 0.0f : w;
-  };
-  float wsum = 0.0f;
-  for (int si = i0; si <= i1; si++)
-    for (int sj = j0; sj <= j1; sj++) {
-      const size_t base = ((size_t)si * n + sj) * n;
-      uint32_t x = __ldg(cs + base + k0);
-      const uint32_t e = __ldg(cs + base + k1 + 1);
-      for (; x + 4 <= e; x += 4) {
-        const float4 Q0 = __ldg(spos + x), Q1 = __ldg(spos + x + 1), Q2 = __ldg(spos + x + 2),
-                     Q3 = __ldg(spos + x + 3);
-        wsum += term(Q0);
-        wsum += term(Q1);
-        wsum += term(Q2);
-        wsum += term(Q3);
-      }
-      for (; x < e; x++) wsum += term(__ldg(spos + x));
-    }
-  const float d = wsum / c.max_dens;
-  dens[p] = d;
-  sdens[a] = d;
-}
-
 /* ------------------------------------------------------------ mapP2G */
 
 /* One MAC face per thread (src/mapper.cpp:17-88). The reference gathers
@@ -1220,10 +1173,10 @@ cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, floa
 }
 
 /* FAST arithmetic runs the gathers restructured for speed (P2G with one
- * thread per face cell, density unrolled, the corrector without near
- * lists); FLIPGPU_GATHER=particle in the environment selects the original
- * per-particle kernels instead (read at each launch, so one process can
- * compare the two: the results are identical) */
+ * thread per face cell, the corrector without near lists);
+ * FLIPGPU_GATHER=particle in the environment selects the per-particle
+ * kernels instead (read at each launch, so one process can compare the two:
+ * the results are identical) */
 static bool cell_gathers(const FlipGpu *h) {
   if (h->prm.arith != FLIPGPU_ARITH_FAST) return false;
   const char *e = getenv("FLIPGPU_GATHER");
@@ -1234,12 +1187,6 @@ cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
   const unsigned g = grid_for(h->np, BLK);
-  if (cell_gathers(h)) {
-    k_density_fast<<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
-                                             h->sdens);
-    FG_LAUNCHED(h, 1);
-    return cudaGetLastError();
-  }
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
     k_density<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
                                                    h->sdens);

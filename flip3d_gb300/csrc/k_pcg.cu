@@ -2648,6 +2648,8 @@ constexpr double IR_INNER_FLOOR = 1e-3; /* tightest inner tolerance asked for:
                                            follows its recursive one to about
                                            there (FLIPGPU_IR_FLOOR overrides) */
 
+constexpr int IR_BLOCKS = 4 * RED_BLOCKS; /* residual blocks (partials: 2 x IR_BLOCKS <= 8192) */
+
 /* r = b - A (xhi + xlo) on the liquid, rb = float(r), e = 0, and the block
  * partials of r.r (and, on the first pass, b.b). The first pass starts from
  * xlo = 0 and zeroes x off the liquid, as every FAST solve leaves it. */
@@ -2705,7 +2707,7 @@ k_ir_residual(SolveArgs s, const uint8_t *__restrict__ A, const float *__restric
   if (threadIdx.x == 0) part[blockIdx.x] = ff_to_double(t);
   if (FIRST) {
     const FF t2 = block_sum_ff<BLK>(bb);
-    if (threadIdx.x == 0) part[RED_BLOCKS + blockIdx.x] = ff_to_double(t2);
+    if (threadIdx.x == 0) part[IR_BLOCKS + blockIdx.x] = ff_to_double(t2);
   }
 }
 
@@ -2718,8 +2720,14 @@ k_ir_check(int first, double rel_tol, int max_passes, double floor_tol,
            const double *__restrict__ part, double *__restrict__ scal, int *__restrict__ iflags) {
   __shared__ double sh[RED_BLOCKS], sb[RED_BLOCKS];
   if (!first && iflags[IF_IR_DONE]) return;
-  sh[threadIdx.x] = part[threadIdx.x];
-  sb[threadIdx.x] = first ? part[RED_BLOCKS + threadIdx.x] : 0.0;
+  /* each thread first adds IR_BLOCKS / RED_BLOCKS partials in order */
+  double a = 0.0, bsum = 0.0;
+  for (int q = 0; q < IR_BLOCKS / RED_BLOCKS; q++) {
+    a += part[threadIdx.x * (IR_BLOCKS / RED_BLOCKS) + q];
+    if (first) bsum += part[IR_BLOCKS + threadIdx.x * (IR_BLOCKS / RED_BLOCKS) + q];
+  }
+  sh[threadIdx.x] = a;
+  sb[threadIdx.x] = bsum;
   __syncthreads();
   for (int w = RED_BLOCKS / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w) {
@@ -3185,7 +3193,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
         const double v = atof(ev);
         if (v > 0.0 && v < 1.0) floor_tol = v;
       }
-      k_ir_residual<true><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
+      k_ir_residual<true><<<IR_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
                                                       h->press_lo, h->ir_b, h->ir_e, h->iflags,
                                                       h->partial);
       k_ir_check<<<1, RED_BLOCKS, 0, S>>>(1, h->prm.rel_tol, passes, floor_tol, h->partial,
@@ -3200,7 +3208,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
           return FLIPGPU_ECUDA;
         }
         k_ir_update<<<ug, BLK, 0, S>>>(nc, h->A, h->ir_e, h->press, h->press_lo, h->iflags);
-        k_ir_residual<false><<<RED_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
+        k_ir_residual<false><<<IR_BLOCKS, BLK, 0, S>>>(sa, h->A, h->diag, h->div, h->press,
                                                          h->press_lo, h->ir_b, h->ir_e,
                                                          h->iflags, h->partial);
         k_ir_check<<<1, RED_BLOCKS, 0, S>>>(0, h->prm.rel_tol, passes, floor_tol, h->partial,

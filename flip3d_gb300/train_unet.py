@@ -27,11 +27,17 @@ def solver_params(n, count, seed=0):
                               precond=gpu.PRECOND_JACOBI, seed=seed)
 
 
-def collect(n, seeds, steps, every, device="cuda"):
-    """(A, L, b, x0, r0, x) of every `every`-th solve of each seeded scene,
-    as device tensors [systems, n^3]."""
+def collect(n, seeds, steps, every, device="cuda", keys=KEYS):
+    """(A, L, b, x0, r0, x) of every `every`-th solve of each seeded scene
+    (those of `keys`), as device tensors [systems, n^3] written in place into
+    tensors allocated once (20,000 systems at n = 64 hold about 90 GB
+    without L)."""
     import torch
-    out = {k: [] for k in KEYS}
+    seeds = list(seeds)
+    count = len(seeds) * (steps // every)
+    out = {k: torch.empty((count, n ** 3), dtype=torch.uint8 if k == "A" else torch.float32,
+                          device=device) for k in keys}
+    m = 0
     for seed in seeds:
         sc = scenes.random_scene(n, int(seed))
         sim = gpu.Simulation(solver_params(n, sc.count, int(seed)))
@@ -42,13 +48,12 @@ def collect(n, seeds, steps, every, device="cuda"):
             sim.step()
             if k % every:
                 continue
-            t = [torch.empty(n ** 3, dtype=torch.uint8, device=device)] + \
-                [torch.empty(n ** 3, dtype=torch.float32, device=device) for _ in range(5)]
-            sim.solve_system(dev=[x.data_ptr() for x in t])
+            dst = [out[key][m] if key in out else None for key in KEYS]
+            sim.solve_system(dev=[None if x is None else x.data_ptr() for x in dst])
             sim.sync()
-            for key, x in zip(KEYS, t):
-                out[key].append(x)
-    return {k: torch.stack(v) for k, v in out.items()}
+            m += 1
+        sim.close()
+    return out
 
 
 def train(net, data, n, epochs, batch=16, lr=1e-3, seed=0, log=None, lr_end=None):
@@ -104,10 +109,17 @@ def prediction_error(net, data, n):
     return float(np.median(errs)) if errs else 0.0
 
 
-def evaluate(net, data, n):
+PRECONDS = {"jacobi": (gpu.PRECOND_JACOBI, 0.0), "mic": (gpu.PRECOND_IC, 0.97),
+            "mg": (gpu.PRECOND_MG, 0.0)}
+
+
+def evaluate(net, data, n, precond="jacobi"):
     """Each held-out system solved from its previous-step guess and from the
-    learned warm start: CG iterations and device ms per solve."""
-    sim = gpu.Simulation(solver_params(n, 1))
+    learned warm start with the same preconditioner (refined to a true
+    relative residual of 1e-6): CG iterations and device ms per solve."""
+    prm = solver_params(n, 1)
+    prm.precond, prm.mic_tau = PRECONDS[precond]
+    sim = gpu.Simulation(prm)
     plain, learned = [], []
     for i in range(data["A"].shape[0]):
         A, L, b, x0 = (data[k][i].cpu().numpy() for k in ("A", "L", "b", "x0"))
@@ -171,6 +183,12 @@ def main(argv=None):
     ap.add_argument("--time-predict", type=int, default=0, metavar="N",
                     help="only time the forward pass on an N^3 system (both tensor paths)")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--eval-precond", default="jacobi",
+                    help="comma-separated preconditioners of the held-out evaluation "
+                         "(jacobi, mic, mg)")
+    ap.add_argument("--eval-n", default="",
+                    help="comma-separated further grid sizes to evaluate on, each with "
+                         "held-out scenes of its own (2 scenes, 20 steps)")
     a = ap.parse_args(argv)
     gpu.load()
     if a.time_predict:
@@ -182,22 +200,32 @@ def main(argv=None):
     t0 = time.perf_counter()
     train_seeds = range(1000 + a.seed, 1000 + a.seed + a.scenes)
     hold_seeds = range(5000 + a.seed, 5000 + a.seed + a.holdout)
-    data = collect(a.n, train_seeds, a.steps, a.every)
+    data = collect(a.n, train_seeds, a.steps, a.every, keys=("A", "b", "x0", "r0", "x"))
     held = collect(a.n, hold_seeds, a.steps, a.every)
     t1 = time.perf_counter()
     net = gpu.UNet(seed=a.seed)
     if a.init:
         net.load(a.init)
     net.set_coarsening(a.coarsen)
-    before = evaluate(net, held, a.n)
+    pres = [p for p in a.eval_precond.split(",") if p]
+    before = {p: evaluate(net, held, a.n, p) for p in pres}
     hist = train(net, data, a.n, a.epochs, a.batch, a.lr, a.seed, log=print)
     t2 = time.perf_counter()
-    after = evaluate(net, held, a.n)
+    n_train = int(data["A"].shape[0])
+    del data
+    after = {p: evaluate(net, held, a.n, p) for p in pres}
     if a.out:
-        net.save(a.out, trained_n=a.n, train_systems=int(data["A"].shape[0]))
-    print(json.dumps({"n": a.n, "train_systems": int(data["A"].shape[0]),
+        net.save(a.out, trained_n=a.n, train_systems=n_train, epochs=a.epochs, batch=a.batch,
+                 lr=a.lr)
+    other = {}
+    for m in [int(x) for x in a.eval_n.split(",") if x]:
+        hm = collect(m, range(7000 + a.seed, 7002 + a.seed), 20, 5)
+        other[m] = {p: evaluate(net, hm, m, p) for p in pres}
+        del hm
+    print(json.dumps({"n": a.n, "train_systems": n_train,
                       "heldout_systems": int(held["A"].shape[0]), "collect_s": t1 - t0,
-                      "train_s": t2 - t1, "loss": hist, "untrained": before, "trained": after}))
+                      "train_s": t2 - t1, "loss": hist, "untrained": before, "trained": after,
+                      "other_sizes": other}))
 
 
 if __name__ == "__main__":

@@ -162,15 +162,17 @@ static void read_cells(sorter *s, int n, uint32_t *cs, uint32_t *perm) {
   cs[n * n * n] = at;
 }
 
-template <class T> static void to3(T ***g, int w, int h, int d, const T *flat) {
+/* flat arrays are float (or char) whatever FLOAT is: the FP64 build
+ * (FLOAT = double) widens on the way in and rounds on the way out */
+template <class T, class U> static void to3(T ***g, int w, int h, int d, const U *flat) {
   for (int i = 0; i < w; i++)
     for (int j = 0; j < h; j++)
-      for (int k = 0; k < d; k++) g[i][j][k] = flat[(i * h + j) * d + k];
+      for (int k = 0; k < d; k++) g[i][j][k] = (T)flat[(i * h + j) * d + k];
 }
-template <class T> static void from3(T ***g, int w, int h, int d, T *flat) {
+template <class T, class U> static void from3(T ***g, int w, int h, int d, U *flat) {
   for (int i = 0; i < w; i++)
     for (int j = 0; j < h; j++)
-      for (int k = 0; k < d; k++) flat[(i * h + j) * d + k] = g[i][j][k];
+      for (int k = 0; k < d; k++) flat[(i * h + j) * d + k] = (U)g[i][j][k];
 }
 
 /* -------------------------------------------------------- sorter / mapper */
@@ -410,9 +412,38 @@ extern "C" void fr_sim_get_grid(float *u0, float *u1, float *u2, uint8_t *Aout,
   from3(press, N, N, N, pout);
 }
 
+/* The driver's state at FLOAT resolution (the FP64 build's double values
+ * unrounded): particle positions, velocities and densities, the face grids,
+ * the levelset and the pressure. */
+extern "C" void fr_sim_get_d(double *pos, double *vel, double *dens) {
+  for (int q = 0; q < g_pool_n; q++) {
+    for (int c = 0; c < 3; c++) {
+      if (pos) pos[3 * q + c] = g_pool[q].p[c];
+      if (vel) vel[3 * q + c] = g_pool[q].u[c];
+    }
+    if (dens) dens[q] = g_pool[q].dens;
+  }
+}
+
+extern "C" void fr_sim_get_grid_d(double *u0, double *u1, double *u2, double *Lout,
+                                  double *pout) {
+  from3(u[0], N + 1, N, N, u0);
+  from3(u[1], N, N + 1, N, u1);
+  from3(u[2], N, N, N + 1, u2);
+  from3(L, N, N, N, Lout);
+  from3(press, N, N, N, pout);
+}
+
+extern "C" void fr_sim_set_max_density_d(double md) { max_dens = (FLOAT)md; }
+
+static FLOAT max_density_impl(void);
+
 /* Max-density calibration through the reference's computeDensity on the
  * lattice of src/flip3D.cpp:689-709. */
-extern "C" float fr_max_density(void) {
+extern "C" float fr_max_density(void) { return (float)max_density_impl(); }
+extern "C" double fr_max_density_d(void) { return (double)max_density_impl(); }
+
+static FLOAT max_density_impl(void) {
   if (!sort) sort = new sorter(N);
   FLOAT h = DENSITY / N;
   int np = 1000;
@@ -430,7 +461,7 @@ extern "C" float fr_max_density(void) {
   sort->sort(particles);
   max_dens = 1.0;
   computeDensity();
-  float md = 0.0f;
+  FLOAT md = 0.0;
   for (int q = 0; q < np; q++) md = fmax(md, g_pool[q].dens);
   particles.clear();
   return md;

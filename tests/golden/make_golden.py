@@ -185,6 +185,95 @@ def task_driver(out: str, steps: int = 10, rel_tol: float = 1e-6):
     np.savez_compressed(out, **rec)
 
 
+def load_ref64(n: int):
+    """The FP64 oracle: the reference built with FLOAT = double and its
+    driver's N = n (oracle/build_ref64.sh)."""
+    path = os.path.join(ROOT, "oracle", "_ref", f"libflipref64_n{n}.so")
+    subprocess.check_call(["sh", os.path.join(ROOT, "oracle", "build_ref64.sh"), str(n)],
+                          stdout=subprocess.DEVNULL)
+    L = C.CDLL(path)
+    f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+    L.fr_sim_setup.argtypes = [C.c_int, f32p, f32p, u8p, f32p, C.c_float, C.c_uint64,
+                               C.c_double]
+    L.fr_sim_stage.argtypes = [C.c_int]
+    L.fr_sim_get.argtypes = [f32p, f32p, f32p, u8p]
+    L.fr_sim_get_d.argtypes = [f64p, f64p, f64p]
+    L.fr_sim_get_grid_d.argtypes = [f64p, f64p, f64p, f64p, f64p]
+    L.fr_sim_get_grid.argtypes = [f32p, f32p, f32p, u8p, f32p, f32p]
+    L.fr_max_density_d.restype = C.c_double
+    L.fr_sim_set_max_density_d.argtypes = [C.c_double]
+    L.fr_grid_n.restype = C.c_int
+    return L
+
+
+# FP64 runs: (scene, grid, snapshot steps). Config 1 of the benchmark (the
+# N=32 pool + sphere, 200 steps) and config 2 (the N=128 dam break), the
+# latter for its first steps (an FP64 step of the reference takes minutes on
+# one core).
+FP64_RUNS = {32: ("pool_sphere", (1, 10, 50, 200)), 128: ("dam_break", (1, 5, 10))}
+
+
+def task_fp64(out: str, n: int):
+    """The reference's own step in FP64 from a seeded scene: particle
+    subsets, pressure and face velocities on the i = n/4 plane, and
+    full-set aggregates at the snapshot steps."""
+    L = load_ref64(n)
+    assert L.fr_grid_n() == n
+    scene, snaps = FP64_RUNS[n]
+    sc = getattr(scenes, scene)(n, seed=0)
+    md = L.fr_max_density_d()
+    L.fr_sim_setup(sc.count, sc.pos, sc.vel, sc.type, sc.nrm, np.float32(md), SEED, 1e-6)
+    L.fr_sim_set_max_density_d(md)
+    P = sc.count
+    fs = (n + 1) * n * n
+    rng = np.random.default_rng(SEED + 5)
+    sub = np.sort(rng.choice(P, min(SUBSET, P), replace=False))
+    fluid = sc.type == 1
+    # the i = n/4 plane: through the liquid of both scenes (the dam break's
+    # column ends at x = 0.4)
+    plane_i = n // 4
+    rec = {"n": n, "scene": scene, "seed": SEED, "rel_tol": 1e-6, "max_dens": md,
+           "snaps": np.array(snaps), "subset": sub, "scene_pos_sha": digest(sc.pos),
+           "count": P, "plane": plane_i}
+
+    def plane(a, shape):
+        return np.ascontiguousarray(a.reshape(shape)[plane_i])
+
+    def snap(k):
+        pos = np.zeros((P, 3), np.float64)
+        vel = np.zeros((P, 3), np.float64)
+        dens = np.zeros(P, np.float64)
+        L.fr_sim_get_d(pos, vel, dens)
+        u = [np.zeros(fs, np.float64) for _ in range(3)]
+        Ls = np.zeros(n ** 3, np.float64)
+        pr = np.zeros(n ** 3, np.float64)
+        L.fr_sim_get_grid_d(u[0], u[1], u[2], Ls, pr)
+        A = np.zeros(n ** 3, np.uint8)
+        L.fr_sim_get_grid(np.zeros(fs, np.float32), np.zeros(fs, np.float32),
+                          np.zeros(fs, np.float32), A, np.zeros(n ** 3, np.float32),
+                          np.zeros(n ** 3, np.float32))
+        t = f"step{k}"
+        rec[f"{t}_pos"] = pos[sub]
+        rec[f"{t}_vel"] = np.where(fluid[sub, None], vel[sub], 0.0)
+        rec[f"{t}_dens"] = dens[sub]
+        rec[f"{t}_press"] = plane(pr, (n, n, n))
+        rec[f"{t}_A"] = plane(A, (n, n, n))
+        rec[f"{t}_u0"] = plane(u[0], (n + 1, n, n))
+        rec[f"{t}_u1"] = plane(u[1], (n, n + 1, n))
+        rec[f"{t}_u2"] = plane(u[2], (n, n, n + 1))
+        fp, fv = pos[fluid], vel[fluid]
+        rec[f"{t}_com"] = fp.mean(axis=0)
+        rec[f"{t}_ke"] = 0.5 * float((fv * fv).sum()) / fp.shape[0]
+        rec[f"{t}_pmax"] = float(np.abs(pr).max())
+
+    for k in range(1, max(snaps) + 1):
+        for st in range(5):
+            L.fr_sim_stage(st)
+        if k in snaps:
+            snap(k)
+    np.savez_compressed(out, **rec)
+
+
 def _mesh_arrays(L, counts):
     nv, nf = int(counts[0]), int(counts[1])
     v = np.zeros(3 * nv, np.float64)
@@ -340,6 +429,8 @@ TASKS = {
     "checkpoint_n32": task_checkpoint,
     "export_n16": task_export,
     "preview_n32": task_preview,
+    "fp64_n32": lambda out: task_fp64(out, 32),
+    "fp64_n128": lambda out: task_fp64(out, 128),
 }
 
 
