@@ -1014,8 +1014,11 @@ k_p2g_cells(SimConst c, int enforce, const uint32_t *__restrict__ cs,
  * instead of through k_spring's and k_resample's per-thread near lists
  * (which hold 24 KB of shared memory per block); the same pairs in the same
  * order, so the same results. */
+/* five resident blocks per SM: 48 registers (a few spilled) instead of 56;
+ * the kernel is issue- and occupancy-bound, and this is 5 % faster at N=256
+ * (six blocks spill more and gain less) */
 template <class AR>
-__global__ void __launch_bounds__(BLK)
+__global__ void __launch_bounds__(BLK, 5)
 k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
                 const float4 *__restrict__ spos, const float *__restrict__ nx,
                 const float *__restrict__ ny, const float *__restrict__ nz,

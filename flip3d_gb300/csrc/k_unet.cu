@@ -3,11 +3,12 @@
  *
  * A 3D U-Net maps, per cell, (liquid mask, right-hand side b, previous
  * pressure x0) to a correction d of the initial guess; the solve then
- * starts from x0 + g*d, where g minimises the A-norm error over that line
- * (g = d.r0 / d.Ad with r0 = b - A x0). The line contains x0 (g = 0), so
- * the guess is never worse than the previous-step guess in the norm CG
- * minimises, and CG still iterates to the same relative residual: the
- * answer is the plain method's answer.
+ * starts from x0 + g*d, where g minimises the residual over that line
+ * (g = (Ad).r0 / (Ad).(Ad) with r0 = b - A x0; or, with
+ * FLIPGPU_WARM_STEP=anorm, the A-norm error: g = d.r0 / d.Ad). The line
+ * contains x0 (g = 0), so the starting residual is never above the
+ * previous-step guess's, and CG still iterates to the same relative
+ * residual: the answer is the plain method's answer.
  *
  * Network: 4 levels (16/32/48/64 channels), two 3x3x3 convolutions with
  * ReLU per level and side, 2x2x2 average pooling down, nearest upsampling
@@ -27,6 +28,7 @@
  * cells in fixed-size chunks whose partial sums are added in a fixed order,
  * so training is deterministic. Adam updates the FP32 masters.
  */
+#include <cstdlib>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -750,11 +752,13 @@ __global__ void k_wm_dots(size_t nc, const uint8_t *__restrict__ A, const float 
   if (threadIdx.x < 5) part[blockIdx.x * 5 + threadIdx.x] = sh[0][threadIdx.x];
 }
 
-/* g = d.r / d.w (0 when not positive and finite); x0 += g d; res = the
+/* minres: g = r.w / w.w, the step along d that minimises the residual
+ * ||r0 - g A d|| (never above ||r0||); else g = d.r / d.w, the step that
+ * minimises the A-norm error. 0 when not finite. x0 += g d; res = the
  * squared residual norms before and after */
 __global__ void k_wm_apply(size_t nc, const uint8_t *__restrict__ A, const double *__restrict__ part,
                            const float *__restrict__ d, float *__restrict__ x0,
-                           double *__restrict__ res) {
+                           double *__restrict__ res, int minres) {
   __shared__ double tot[5];
   if (threadIdx.x < 5) {
     double s = 0.0;
@@ -763,7 +767,11 @@ __global__ void k_wm_apply(size_t nc, const uint8_t *__restrict__ A, const doubl
   }
   __syncthreads();
   double g = 0.0;
-  if (tot[1] > 0.0 && isfinite(tot[0] / tot[1])) g = tot[0] / tot[1];
+  if (minres) {
+    if (tot[4] > 0.0 && isfinite(tot[3] / tot[4])) g = tot[3] / tot[4];
+  } else if (tot[1] > 0.0 && isfinite(tot[0] / tot[1])) {
+    g = tot[0] / tot[1];
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     res[0] = tot[2];
     res[1] = tot[2] - 2.0 * g * tot[3] + g * g * tot[4];
@@ -1357,7 +1365,7 @@ int flipunet_train_step(FlipUNet *u, int n, int batch, const uint8_t *A, const f
 } // extern "C"
 
 /* The solver's warm start (FAST mode): x0 += g d with d the network's
- * correction and g the A-norm optimal step along d. */
+ * correction and g the least-residual step along d (k_wm_apply). */
 int warm_start_apply(FlipGpu *h, float inv_h2_f, double *out3, float *ms) {
   FlipUNet *u = h->warm;
   cudaStream_t keep = u->stream;
@@ -1381,7 +1389,10 @@ int warm_start_apply(FlipGpu *h, float inv_h2_f, double *out3, float *ms) {
   if (r == FLIPGPU_OK) {
     k_wm_matvec<<<eg(nc), EBLK, 0, h->stream>>>(n, inv_h2_f, h->A, h->diag, d, w);
     k_wm_dots<<<RB, EBLK, 0, h->stream>>>(nc, h->A, rr, d, w, h->wpart);
-    k_wm_apply<<<RB, EBLK, 0, h->stream>>>(nc, h->A, h->wpart, d, h->press, h->wpart + RB * 5);
+    const char *ev = getenv("FLIPGPU_WARM_STEP");
+    const int minres = !(ev && strcmp(ev, "anorm") == 0);
+    k_wm_apply<<<RB, EBLK, 0, h->stream>>>(nc, h->A, h->wpart, d, h->press, h->wpart + RB * 5,
+                                           minres);
     FG_LAUNCHED(h, 3);
     cudaEventRecord(h->wev[1], h->stream);
     if (cudaMemcpyAsync(out3, h->wpart + RB * 5, 3 * sizeof(double), cudaMemcpyDeviceToHost,

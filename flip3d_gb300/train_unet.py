@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import time
 
 import numpy as np
@@ -186,6 +187,10 @@ def main(argv=None):
     ap.add_argument("--eval-precond", default="jacobi",
                     help="comma-separated preconditioners of the held-out evaluation "
                          "(jacobi, mic, mg)")
+    ap.add_argument("--eval-steps", default="minres",
+                    help="comma-separated step rules along the network's correction to "
+                         "evaluate: minres (least residual, the library's default) and/or "
+                         "anorm (least A-norm error); set through FLIPGPU_WARM_STEP")
     ap.add_argument("--eval-n", default="",
                     help="comma-separated further grid sizes to evaluate on, each with "
                          "held-out scenes of its own (2 scenes, 20 steps)")
@@ -208,19 +213,29 @@ def main(argv=None):
         net.load(a.init)
     net.set_coarsening(a.coarsen)
     pres = [p for p in a.eval_precond.split(",") if p]
-    before = {p: evaluate(net, held, a.n, p) for p in pres}
+    rules = [r for r in a.eval_steps.split(",") if r]
+
+    def evaluate_all(data, m):
+        out = {}
+        for rule in rules:
+            os.environ["FLIPGPU_WARM_STEP"] = rule
+            out[rule] = {p: evaluate(net, data, m, p) for p in pres}
+        os.environ.pop("FLIPGPU_WARM_STEP", None)
+        return out
+
+    before = evaluate_all(held, a.n)
     hist = train(net, data, a.n, a.epochs, a.batch, a.lr, a.seed, log=print)
     t2 = time.perf_counter()
     n_train = int(data["A"].shape[0])
     del data
-    after = {p: evaluate(net, held, a.n, p) for p in pres}
+    after = evaluate_all(held, a.n)
     if a.out:
         net.save(a.out, trained_n=a.n, train_systems=n_train, epochs=a.epochs, batch=a.batch,
                  lr=a.lr)
     other = {}
     for m in [int(x) for x in a.eval_n.split(",") if x]:
         hm = collect(m, range(7000 + a.seed, 7002 + a.seed), 20, 5)
-        other[m] = {p: evaluate(net, hm, m, p) for p in pres}
+        other[m] = evaluate_all(hm, m)
         del hm
     print(json.dumps({"n": a.n, "train_systems": n_train,
                       "heldout_systems": int(held["A"].shape[0]), "collect_s": t1 - t0,

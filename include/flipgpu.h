@@ -449,9 +449,11 @@ int flipbatch_sync(FlipBatch *b);
  * accumulation, tensor-core implicit-GEMM convolutions) maps (liquid mask,
  * b, previous pressure x0 and its residual r0 = b - A x0) to a correction d
  * (an approximation of A^-1 r0). With a network attached, a
- * FAST-mode solve starts from x0 + g d, where g = d.r0 / d.Ad minimises the
- * A-norm error along d (so the guess is never worse than x0 in that norm)
- * and CG still runs to the same relative residual. Grids must be a multiple
+ * FAST-mode solve starts from x0 + g d, where g = (Ad).r0 / (Ad).(Ad)
+ * minimises the residual along d (so the starting residual is never above
+ * the previous-step guess's: g = 0 is on the line; FLIPGPU_WARM_STEP=anorm
+ * in the environment selects g = d.r0 / d.Ad, the least A-norm error
+ * instead) and CG still runs to the same relative residual. Grids must be a multiple
  * of 8 cells per axis. All array arguments of the flipunet_* calls are
  * device pointers to batch systems of n^3 cells each, concatenated. */
 int64_t flipunet_param_count(void);
@@ -470,7 +472,7 @@ int flipunet_set_tensor_path(FlipUNet *u, int tcgen05);
 /* Coarsened warm start (levels 0..3, default 0): the 16 input features are
  * computed on the solver's grid n, average-pooled `levels` times, the
  * network runs on the (n >> levels)^3 grid and its output is prolonged
- * trilinearly back to n before the A-norm-optimal step. Training targets
+ * trilinearly back to n before the step along it. Training targets
  * are the liquid-cell averages of x and x0 over each coarse cell. n must be
  * a multiple of 8 << levels. */
 int flipunet_set_coarsening(FlipUNet *u, int levels);

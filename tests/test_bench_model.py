@@ -37,6 +37,17 @@ def test_solve_bytes_per_preconditioner():
 
 
 def test_roofline_note():
-    assert bench.roofline_note(None, 10) is None
-    assert "stays in L2" in bench.roofline_note(39_000_000, 2_000_000_000)
-    assert "stays in L2" not in bench.roofline_note(1_900_000_000, 2_000_000_000)
+    assert bench.roofline_note("solve", None, 10) is None
+    assert "stays in L2" in bench.roofline_note("solve", 39_000_000, 2_000_000_000)
+    assert "stays in L2" not in bench.roofline_note("solve", 1_900_000_000, 2_000_000_000)
+    assert "L1 data pipe" in bench.roofline_note("correct", None, 10)
+
+
+def test_traffic_scales_with_particles(tmp_path, monkeypatch):
+    f = tmp_path / "traffic.txt"
+    f.write_text("# stage n bytes particles\ncorrect 128 1000 100\n")
+    monkeypatch.setattr(bench, "TRAFFIC", str(f))
+    assert bench.measured_traffic("correct", 128, 100) == (1000, "measured")
+    t, src = bench.measured_traffic("correct", 256, 400)
+    assert t == 4000 and "scaled" in src
+    assert bench.measured_traffic("p2g", 256, 400) == (None, None)

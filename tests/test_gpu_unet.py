@@ -188,10 +188,9 @@ def test_warm_start_is_never_worse_and_keeps_the_answer(gpu):
 def test_trained_warm_start_on_heldout_scenes(gpu, torch):
     """A short training run on N=32 scenes, evaluated on held-out seeds: the
     training loss falls, the prediction error of the correction falls, and
-    the solve from the learned start takes no more CG iterations than from
-    the previous-step guess (the start is A-norm optimal along the
-    correction, so it cannot be worse than the previous-step guess in the
-    norm CG minimises)."""
+    the starting residual after the least-residual step along the
+    correction falls further below the previous-step guess's than with the
+    untrained network."""
     from flip3d_gb300 import train_unet as T
     n = 32
     data = T.collect(n, range(100, 106), steps=24, every=3)
@@ -203,7 +202,31 @@ def test_trained_warm_start_on_heldout_scenes(gpu, torch):
     print(before, res, hist[0], hist[-1])
     assert hist[-1] < hist[0]
     assert res["pred_rel_err"] < before["pred_rel_err"]
-    assert res["learned_iters"] <= res["plain_iters"] + 1.0
+    assert res["residual_ratio"] < before["residual_ratio"] <= 1.0
+
+
+def test_shipped_weights_on_heldout_scenes(gpu, torch):
+    """The shipped weights (flip3d_gb300/unet_weights.bin: trained with the
+    project's kernels on 20,000 systems from seeded N=64 random scenes,
+    batch 16, Adam lr 1e-3, 8 epochs) on scenes they were not trained on.
+    What the network gains: the least-residual step along its correction
+    starts the solve from a residual below the previous-step guess's (the
+    median over the systems at most 0.95 of it; never above it, by the
+    step's construction), and the MIC(0) solve still meets the same true
+    residual. What it does not gain: CG iterations; they stay within 5 % of
+    the previous-step start's (the reference's own warm start, already most
+    of the answer on these systems)."""
+    import os
+
+    from flip3d_gb300 import train_unet as T
+    n = 64
+    held = T.collect(n, range(9000, 9004), steps=30, every=5)
+    net = gpu.UNet(seed=0)
+    net.load(os.path.join(os.path.dirname(T.__file__), "unet_weights.bin"))
+    res = T.evaluate(net, held, n, "mic")
+    print(res)
+    assert res["residual_ratio"] <= 0.95
+    assert res["learned_iters"] <= 1.05 * res["plain_iters"]
 
 
 def test_autotuned_convolutions_match_the_defaults(gpu, torch):
