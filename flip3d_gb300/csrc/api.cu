@@ -170,8 +170,8 @@ void free_all(FlipGpu *h) {
                   h->div, h->press_lo, h->ir_b, h->ir_e, h->r, h->z, h->s, h->s1, h->w, h->w1, h->pdir, h->chunk_off, h->chunk_list, h->bar, h->P, h->Pf, h->diag,
                   h->partial, h->scal,
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
-                  h->water_idx, h->stage, h->brick_order, h->fflag, h->bflag,
-                  h->ticket, h->brick_part, h->dstep, h->repo_draw, h->repo_res, h->repo_old,
+                  h->water_idx, h->stage,
+                  h->ticket, h->dstep, h->repo_draw, h->repo_res, h->repo_old,
                   h->repo_cnt, h->repo_start, h->repo_list, h->repo_state};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -358,24 +358,8 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->repo_draw, cap) AL(h->repo_res, cap) AL(h->repo_old, cap)
   AL(h->repo_cnt, cap + 1) AL(h->repo_start, cap + 1) AL(h->repo_list, cap)
   AL(h->repo_state, cap)
-  h->nbx = (p->n + 15) / 16; /* 16^3 wavefront bricks (k_pcg.cu BRK) */
-  h->nbricks = h->nbx * h->nbx * h->nbx;
-  AL(h->brick_order, h->nbricks) AL(h->fflag, h->nbricks) AL(h->bflag, h->nbricks)
-  AL(h->ticket, 1) AL(h->brick_part, h->nbricks) AL(h->dstep, 1)
+  AL(h->ticket, 1) AL(h->dstep, 1)
 #undef AL
-  {
-    /* bricks by increasing i+j+k: every brick's dependencies come earlier */
-    std::vector<unsigned> order;
-    const int nb = h->nbx;
-    for (int d = 0; d <= 3 * (nb - 1); d++)
-      for (int i = 0; i < nb; i++)
-        for (int j = 0; j < nb; j++) {
-          int k = d - i - j;
-          if (k >= 0 && k < nb) order.push_back((unsigned)((i * nb + j) * nb + k));
-        }
-    cudaMemcpy(h->brick_order, order.data(), order.size() * sizeof(unsigned),
-               cudaMemcpyHostToDevice);
-  }
   for (int c = 0; c < 3; c++) {
     cudaMemsetAsync(h->u[c], 0, nf * sizeof(float), h->stream);
     cudaMemsetAsync(h->us[c], 0, nf * sizeof(float), h->stream);
@@ -398,10 +382,21 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   }
   if (cg_grid_size(h->cg_grid) != 0)
     for (int v = 0; v < CG_VARIANTS; v++) h->cg_grid[v] = 0;
-  /* the multigrid buffers now, so that a captured step never allocates */
+  /* the multigrid or wavefront buffers now, so that a captured step never
+   * allocates */
   if (p->precond == FLIPGPU_PRECOND_MG && p->n % 4 == 0 && p->n >= 8) {
     int r = mg_alloc(h);
     if (r != FLIPGPU_OK) {
+      free_all(h);
+      cudaStreamDestroy(h->own_stream);
+      delete h;
+      return r;
+    }
+  }
+  if (p->precond == FLIPGPU_PRECOND_IC && p->solve_mode == FLIPGPU_SOLVE_FAST) {
+    int r = ic_alloc(h);
+    if (r != FLIPGPU_OK) {
+      mg_free(h);
       free_all(h);
       cudaStreamDestroy(h->own_stream);
       delete h;
@@ -426,6 +421,7 @@ int flipgpu_destroy(FlipGpu *h) {
   export_free(h);
   mesh_free(h);
   mg_free(h);
+  ic_free(h);
   if (h->xstream) {
     cudaStreamSynchronize(h->xstream);
     for (int e = 0; e < 3; e++) cudaEventDestroy(h->xev[e]);
@@ -458,6 +454,10 @@ int flipgpu_set_params(FlipGpu *h, const FlipGpuParams *p) {
   if (p->precond == FLIPGPU_PRECOND_MG && p->n % 4 == 0 && p->n >= 8) {
     int r = mg_alloc(h);
     if (r != FLIPGPU_OK) return fail(h, r, "set_params: multigrid buffers");
+  }
+  if (p->precond == FLIPGPU_PRECOND_IC && p->solve_mode == FLIPGPU_SOLVE_FAST) {
+    int r = ic_alloc(h);
+    if (r != FLIPGPU_OK) return fail(h, r, "set_params: wavefront buffers");
   }
   h->prm = *p;
   return FLIPGPU_OK;

@@ -29,6 +29,17 @@ __device__ __forceinline__ int cell_clamp_macro(float p, float fn) {
   return (int)mx;
 }
 
+/* (i, j, k) of linear index c over extents (., e1, e2), k fastest, in 32-bit
+ * arithmetic (grids are at most 1024^3 cells or 1025 x 1024^2 faces, so
+ * every index fits; 64-bit division costs several times more) */
+__device__ __forceinline__ void decode_index(size_t c, int e1, int e2, int &i, int &j, int &k) {
+  const unsigned c32 = (unsigned)c, u1 = (unsigned)e1, u2 = (unsigned)e2;
+  const unsigned row = c32 / u2;
+  k = (int)(c32 - row * u2);
+  i = (int)(row / u1);
+  j = (int)(row - (unsigned)i * u1);
+}
+
 __device__ __forceinline__ size_t cell_id(int n, int i, int j, int k) {
   return ((size_t)i * n + j) * n + k;
 }

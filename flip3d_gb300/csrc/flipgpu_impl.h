@@ -140,9 +140,15 @@ struct FlipGpu {
   int cg_grid[CG_VARIANTS]; /* cooperative CG grids (0 = none): REF, FAST, FAST single-
                                reduction (small blocks), FAST IC, single-reduction (large),
                                FAST MG */
-  int nbx, nbricks;   /* 8^3 bricks of the IC wavefront */
-  unsigned *brick_order, *fflag, *bflag, *ticket;
-  float2 *brick_part;
+  unsigned *ticket;   /* task ticket of the IC wavefront */
+  /* IC(0)/MIC(0) line wavefront (k_pcg.cu ic_alloc) */
+  int ic_njb, ic_tasks;              /* 32-j line blocks; tasks */
+  unsigned *ic_order, *ic_line;      /* tasks in wavefront order; lines holding liquid */
+  uint8_t *ic_cf;                    /* per cell: liquid flag, MIC(0) counts */
+  float *ic_pf;                      /* skewed factor */
+  unsigned long long *ic_psk, *ic_qsk, *ic_zsk; /* skewed tagged factor, q, z */
+  float2 *ic_part;                   /* per-task q.q partials */
+  unsigned *ic_ctr;                  /* tag counter of the word handoff */
   int npartial;
 
   /* reposition */
@@ -251,6 +257,8 @@ int read_solve_stats(FlipGpu *h, FlipGpuSolveStats *st);
 int cg_grid_size(int *out);
 int mg_alloc(FlipGpu *h);  /* MG preconditioner buffers (idempotent) */
 void mg_free(FlipGpu *h);
+int ic_alloc(FlipGpu *h);
+void ic_free(FlipGpu *h);
 int particles_init_device();
 
 /* device-wide exclusive scan of n uint32 (in may equal out) */

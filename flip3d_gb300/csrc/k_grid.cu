@@ -52,7 +52,8 @@ k_divergence(SimConst c, const uint8_t *__restrict__ A, const float *__restrict_
   const int n = c.n;
   const size_t nc = (size_t)n * n * n;
   if (cidx >= nc || A[cidx] != CELL_FLUID) return;
-  int k = (int)(cidx % n), j = (int)((cidx / n) % n), i = (int)(cidx / ((size_t)n * n));
+  int i, j, k;
+  decode_index(cidx, n, n, i, j, k);
   float d = u0[((size_t)(i + 1) * n + j) * n + k] - u0[((size_t)i * n + j) * n + k] +
             u1[((size_t)i * (n + 1) + j + 1) * n + k] - u1[((size_t)i * (n + 1) + j) * n + k] +
             u2[((size_t)i * n + j) * (n + 1) + k + 1] - u2[((size_t)i * n + j) * (n + 1) + k];
@@ -72,11 +73,9 @@ k_gradient_enforce(SimConst c, int subcell, int enforce, const uint8_t *__restri
   size_t f = (size_t)blockIdx.x * BLK + threadIdx.x;
   const size_t nf = (size_t)(n + 1) * n * n;
   if (f >= nf) return;
-  int ex[3] = {n, n, n};
-  ex[comp] = n + 1;
-  int k = (int)(f % ex[2]);
-  int j = (int)((f / ex[2]) % ex[1]);
-  int i = (int)(f / ((size_t)ex[2] * ex[1]));
+  const int ex[3] = {comp == 0 ? n + 1 : n, comp == 1 ? n + 1 : n, comp == 2 ? n + 1 : n};
+  int i, j, k;
+  decode_index(f, ex[1], ex[2], i, j, k);
   int a = comp == 0 ? i : (comp == 1 ? j : k);
   float *u = comp == 0 ? u0 : (comp == 1 ? u1 : u2);
   if (a == 0 || a == n) {
@@ -135,11 +134,9 @@ k_extrap_delta(SimConst c, const uint8_t *__restrict__ A, float *__restrict__ u0
   size_t f = (size_t)blockIdx.x * BLK + threadIdx.x;
   const size_t nf = (size_t)(n + 1) * n * n;
   if (f >= nf) return;
-  int ex[3] = {n, n, n};
-  ex[comp] = n + 1;
-  int k = (int)(f % ex[2]);
-  int j = (int)((f / ex[2]) % ex[1]);
-  int i = (int)(f / ((size_t)ex[2] * ex[1]));
+  const int ex[3] = {comp == 0 ? n + 1 : n, comp == 1 ? n + 1 : n, comp == 2 ? n + 1 : n};
+  int i, j, k;
+  decode_index(f, ex[1], ex[2], i, j, k);
   float *u = comp == 0 ? u0 : (comp == 1 ? u1 : u2);
   float *us = comp == 0 ? us0 : (comp == 1 ? us1 : us2);
   bool mark, wmark;

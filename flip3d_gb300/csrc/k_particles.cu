@@ -198,11 +198,9 @@ k_p2g(SimConst c, int enforce, const uint32_t *__restrict__ cs, const float4 *__
   size_t f = (size_t)(blockIdx.x / 3u) * BLK + threadIdx.x;
   const size_t nf = (size_t)(n + 1) * n * n;
   if (f >= nf) return;
-  int ex[3] = {n, n, n};
-  ex[comp] = n + 1;
-  int k = (int)(f % ex[2]);
-  int j = (int)((f / ex[2]) % ex[1]);
-  int i = (int)(f / ((size_t)ex[2] * ex[1]));
+  const int ex[3] = {comp == 0 ? n + 1 : n, comp == 1 ? n + 1 : n, comp == 2 ? n + 1 : n};
+  int i, j, k;
+  decode_index(f, ex[1], ex[2], i, j, k);
   float fp[3] = {(float)i + 0.5f, (float)j + 0.5f, (float)k + 0.5f};
   int lo[3] = {i - 1, j - 1, k - 1}, hi[3] = {i + 1, j + 1, k + 1};
   if (comp == 0) { fp[0] = (float)i; hi[0] = i; }
@@ -422,7 +420,8 @@ __global__ void k_deep_water(int n, const uint8_t *__restrict__ A, uint32_t *__r
   size_t cidx = (size_t)blockIdx.x * BLK + threadIdx.x;
   size_t nc = (size_t)n * n * n;
   if (cidx >= nc) return;
-  int k = (int)(cidx % n), j = (int)((cidx / n) % n), i = (int)(cidx / ((size_t)n * n));
+  int i, j, k;
+  decode_index(cidx, n, n, i, j, k);
   uint32_t ok = A[cidx] == CELL_FLUID;
   if (ok && i > 0 && A[cell_id(n, i - 1, j, k)] != CELL_FLUID) ok = 0;
   if (ok && i < n - 1 && A[cell_id(n, i + 1, j, k)] != CELL_FLUID) ok = 0;
@@ -891,7 +890,7 @@ k_resample(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restri
 /* ------------------------------------------- cell-per-thread gathers */
 
 __device__ __forceinline__ void cell_decode(size_t c, int n, int &i, int &j, int &k) {
-  const unsigned row = (unsigned)(c / (unsigned)n);
+  const unsigned row = (unsigned)c / (unsigned)n;
   k = (int)(c - (size_t)row * n);
   i = (int)(row / (unsigned)n);
   j = (int)(row - (unsigned)i * n);

@@ -50,9 +50,7 @@ __device__ __forceinline__ bool in_range(int n, int i, int j, int k) {
 }
 
 __device__ __forceinline__ void decode(size_t c, int n, int &i, int &j, int &k) {
-  k = (int)(c % n);
-  j = (int)((c / n) % n);
-  i = (int)(c / ((size_t)n * n));
+  decode_index(c, n, n, i, j, k);
 }
 
 /* A_diag (src/solver.cpp:103-117) in float with the reference's double
@@ -489,13 +487,15 @@ struct CgArgs {
   int max_iters;
   /* IC(0)/MIC(0) wavefront */
   float mic_tau;
-  float *Pic;                  /* factor: 1/sqrt(e) per FLUID cell */
-  int nbx;                     /* bricks per axis */
-  int nbricks;
-  const unsigned *brick_order; /* bricks by increasing i+j+k of the brick */
-  unsigned *fflag, *bflag;     /* epoch of the last forward / backward sweep done */
+  int ic_njb, ic_tasks;         /* 32-j line blocks; tasks (IC_W lines x 32 j) */
+  const unsigned *ic_order;     /* tasks by increasing i block + j block */
+  const unsigned *ic_line;      /* per line (i, j block): holds liquid */
+  const uint8_t *ic_cf;         /* per cell: liquid flag and MIC(0) counts */
+  float *ic_pf;                 /* skewed factor rows */
+  unsigned long long *ic_psk, *ic_qsk, *ic_zsk; /* skewed tagged factor, q, z */
+  float2 *ic_part;              /* per-task q.q partials */
+  unsigned *ic_ctr;             /* tag counter: this launch tags base + 1 .. */
   unsigned *ticket;
-  float2 *brick_part;          /* per-brick z.r partials */
   /* MG-preconditioned CG */
   float *p2, *q;               /* second direction buffer, A p */
   MgArgs mg;
@@ -2160,297 +2160,419 @@ __global__ void __launch_bounds__(BLK) k_mg_diag(const uint8_t *__restrict__ cf,
   diag[c] = (float)(d > 0 ? d : 1); /* a liquid cell walled in on all sides */
 }
 
-/* ------------------------------------------- IC(0)/MIC(0) as wavefronts */
+/* ------------------------------------------ IC(0)/MIC(0) as line wavefronts */
 
 /* The lexicographic incomplete-Cholesky factor of the reference's
  * buildPreconditioner (src/solver.cpp:125-139), with the neighbour test on
  * the cell flag instead of the value, plus the MIC(0) modification weighted
- * by tau; and its triangular solves (src/solver.cpp:141-180). A cell depends
- * on its -x/-y/-z neighbours (forward) or +x/+y/+z neighbours (backward), so
- * cells on one plane i+j+k are independent. The grid is cut into 16^3
- * bricks; a brick depends on the three bricks before it along the axes.
- * Bricks are handed to whole CTAs by an atomic ticket in wavefront order; a
- * CTA waits (bounded) for its three predecessors' epoch flags, loads the
- * brick and its halo into shared memory, runs the 46 intra-brick planes
- * separated by __syncthreads (one cell per thread per plane), writes back and
- * publishes its flag. Tickets are taken in an order where every dependency
- * has a smaller ticket, so a waiting CTA only waits for CTAs that already
- * run. A 16^3 brick gives 3(n/16)-2 brick levels per sweep (22 at n = 128)
- * where 8^3 warp bricks gave 46; each value is computed from the same
- * neighbours in the same order, so the brick size does not change it. */
-constexpr int BRK = 16;
-constexpr int BRK3 = BRK * BRK * BRK;
-constexpr int HB = BRK + 2;
-constexpr int HB3 = HB * HB * HB;
-constexpr int NPLANES = 3 * BRK - 2;
-constexpr unsigned long long FLAG_SPIN_LIMIT = 1ull << 24;
+ * by tau, and its triangular solves (src/solver.cpp:141-180). Cell (i,j,k)
+ * depends on its -x/-y/-z neighbours (factor, forward solve) or its
+ * +x/+y/+z neighbours (backward solve), so the cells of a plane i+j+k are
+ * independent and a sweep is 3n-2 planes deep.
+ *
+ * Line wavefront: a warp owns a line, one i and 32 consecutive j (one per
+ * lane), and walks k; lane l runs l steps behind lane 0, so at step s it
+ * computes k = s - l (mirrored for the backward solve), taking its
+ * j-neighbour from lane l-1's previous step (a shuffle) and its k-neighbour
+ * from its own previous step. A task is IC_W lines, i = IC_W I .. IC_W I +
+ * IC_W - 1 (one warp each) at one 32-j block; warp w takes its i-neighbour
+ * from warp w-1 of the task at the same step through a shared-memory ring
+ * with progress counters. Tasks go to whole CTAs by an atomic ticket in
+ * wavefront order, so every dependency has a smaller ticket and runs.
+ * Across tasks, values pass through skewed line buffers of 64-bit words
+ * that carry the value and the tag of the sweep that wrote it: the reader
+ * polls the word until the tag is its sweep's (bounded), so no flag, fence
+ * or barrier sits between a producer and a consumer in different CTAs.
+ *
+ * Skewed layout: line (i, jb) holds n + 31 rows of 32 words, row s slot l =
+ * cell (i, 32 jb + l, s - l), what the line's forward warp touches at step
+ * s: every warp step reads or writes one contiguous row, and the backward
+ * warp walks the rows in reverse with its lanes reversed. Each warp's reads
+ * of its line's rows, of its neighbour lines and of r (natural layout) are
+ * issued IC_D steps ahead with cp.async (16 bytes, L2 only) into per-warp
+ * shared rings.
+ *
+ * Lines and tasks without liquid are skipped; neighbours treat them as
+ * non-liquid. Every cell is computed from the same neighbours in the same
+ * order as the sequential sweeps (neighbours i, j, k in that order), so the
+ * tiling does not change a value. The preconditioned residual's dot z.r
+ * equals q.q for z = L^-T q, q = L^-1 r: it is summed in the forward solve. */
+constexpr int IC_W = CG_BLOCK / 32;
+constexpr int IC_D = 16;
+constexpr int IC_RING = 8;
+constexpr int IC_RQ = 32;
+constexpr unsigned IC_SPIN_LIMIT = 1u << 22;
+constexpr unsigned IC_TAG_WRAP = 0xf0000000u; /* tags left: > 2^28 */
+constexpr int IC_MAX_ITERS = 1 << 26;        /* 2^27 + 2 tags per launch at most */
+enum { IC_FACTOR = 0, IC_FORWARD = 1, IC_BACKWARD = 2 };
 
-struct BrickPlanes {
-  unsigned short cell[BRK3];       /* (i<<8)|(j<<4)|k sorted by i+j+k */
-  unsigned short start[NPLANES + 1];
+struct IcWarp {
+  float pf[IC_D][32];               /* own line: factor rows (solves) */
+  union {
+    unsigned long long qv[IC_D][32]; /* own line: tagged q rows (backward) */
+    float rn[32][IC_RQ];             /* r per lane, natural k order (forward) */
+  };
+  float2 ring[IC_RING][32];         /* (factor, value) for the next warp's line */
+  float jp[IC_D][4];                /* lane 0's j-neighbour: 16-byte factor chunk */
+  unsigned long long jv[IC_D][2];   /* ... and its tagged value chunk */
 };
-__constant__ BrickPlanes c_planes;
-
-struct BrickSmem {
-  float v[HB3];           /* r -> q (forward), q -> z (backward), diag -> P (build) */
-  float p[HB3];           /* factor */
-  unsigned char fl[HB3];  /* FLUID flags */
+struct IcSmem {
+  IcWarp w[IC_W];
+  float ip[IC_D][32];               /* warp 0's i-neighbour line: factor rows */
+  unsigned long long iv[IC_D][32];  /* ... tagged value rows */
+  int prog[IC_W];                   /* steps each warp of the task has handed on */
+  FF part[IC_W];
+  unsigned ticket;
+  int stop;
 };
 
-__device__ __forceinline__ int hidx(int i, int j, int k) { return ((i + 1) * HB + (j + 1)) * HB + (k + 1); }
+__device__ __forceinline__ unsigned long long ic_word(float v, unsigned tag) {
+  return ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+}
+__device__ __forceinline__ float ic_val(unsigned long long w) {
+  return __uint_as_float((unsigned)w);
+}
+__device__ __forceinline__ unsigned ic_tagof(unsigned long long w) { return (unsigned)(w >> 32); }
 
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ void cpa16(void *dst, const void *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_u64(unsigned long long *p, unsigned long long v) {
+  asm volatile("st.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-/* Thread 0 waits (bounded) until flag >= epoch with acquire loads; the block
- * barrier and fence then order the other threads' loads after it. */
-__device__ __forceinline__ void wait_flag(const unsigned *flag, unsigned epoch, int *iflags) {
-  if (threadIdx.x == 0) {
-    unsigned long long spins = 0;
-    while (ld_acquire(flag) < epoch) {
-      if (++spins > FLAG_SPIN_LIMIT) {
-        atomicExch(iflags + IF_TIMEOUT, 1);
-        break;
-      }
-      __nanosleep(64);
+/* The word at p once it carries `tag` (w: a copy read earlier). Bounded:
+ * gives up with FLIPGPU_ETIMEOUT (value 0), or at once when another wait
+ * has already timed out. */
+__device__ __forceinline__ unsigned long long ic_poll(const unsigned long long *p,
+                                                   unsigned long long w, unsigned tag,
+                                                   int *iflags) {
+  unsigned spins = 0;
+  while (ic_tagof(w) != tag) {
+    if ((++spins & 255u) == 0 &&
+        (spins > IC_SPIN_LIMIT || *(volatile int *)(iflags + IF_TIMEOUT) != 0)) {
+      atomicExch(iflags + IF_TIMEOUT, 1);
+      return (unsigned long long)tag << 32;
     }
+    __nanosleep(20);
+    w = ld_cg_u64(p);
   }
-  __syncthreads();
-  __threadfence();
+  return w;
 }
 
-/* kind: 0 build the factor, 1 forward solve, 2 backward solve; the whole
- * CTA works on one brick */
-__device__ void brick_task(const CgArgs &a, BrickSmem &sm, const BrickPlanes &pl_tab, int brick,
-                           int kind, unsigned epoch_f, unsigned epoch_b, const float *r,
-                           float *qz) {
-  const int tid = threadIdx.x;
-  const int n = a.s.n, nbx = a.nbx;
-  const int BI = brick / (nbx * nbx), BJ = (brick / nbx) % nbx, BK = brick % nbx;
-  const int i0 = BI * BRK, j0 = BJ * BRK, k0 = BK * BRK;
-  const uint8_t *A = a.A;
-  auto cidx = [&](int i, int j, int k) { return ((size_t)i * n + j) * n + k; };
-  auto inside = [&](int i, int j, int k) {
-    return i >= 0 && i < n && j >= 0 && j < n && k >= 0 && k < n;
-  };
-  /* All loads of a phase are issued unconditionally and together (the
-   * fluid mask is applied afterwards), so a phase costs one L2 round trip
-   * instead of one per cell. */
-  constexpr int OWN = BRK3 / CG_BLOCK;            /* own cells per thread */
-  constexpr int HALO = 3 * BRK * BRK / CG_BLOCK;  /* halo cells per thread */
-  static_assert(OWN * CG_BLOCK == BRK3 && HALO * CG_BLOCK == 3 * BRK * BRK, "brick tiling");
-  auto own_cell = [&](int u, int &h, size_t &c, bool &in) {
-    int t = tid + CG_BLOCK * u;
-    int bi = t >> 8, bj = (t >> 4) & 15, bk = t & 15;
-    h = hidx(bi, bj, bk);
-    in = inside(i0 + bi, j0 + bj, k0 + bk);
-    c = in ? cidx(i0 + bi, j0 + bj, k0 + bk) : 0;
-  };
-  /* own cells, independent of other bricks */
-  {
-    unsigned char fa[OWN];
-    float va[OWN], pa[OWN];
-#pragma unroll
-    for (int u = 0; u < OWN; u++) {
-      int h;
-      size_t c;
-      bool in;
-      own_cell(u, h, c, in);
-      fa[u] = in ? A[c] : (unsigned char)CELL_AIR;
-      va[u] = !in ? 0.0f : (kind == 0 ? __ldg(a.diag + c) : (kind == 1 ? __ldcg(r + c) : 0.0f));
-      pa[u] = (in && kind != 0) ? __ldcg(a.Pic + c) : 0.0f;
+/* Wait until the shared counter reaches target. Bounded: gives up with
+ * FLIPGPU_ETIMEOUT, or at once when another wait has already timed out. */
+__device__ __forceinline__ int ic_wait_prog(const int *p, int target, int *iflags) {
+  int v = *(const volatile int *)p;
+  unsigned spins = 0;
+  while (v < target) {
+    if ((++spins & 1023u) == 0 &&
+        (spins > IC_SPIN_LIMIT || *(volatile int *)(iflags + IF_TIMEOUT) != 0)) {
+      atomicExch(iflags + IF_TIMEOUT, 1);
+      return 0x3fffffff;
     }
-#pragma unroll
-    for (int u = 0; u < OWN; u++) {
-      int h;
-      size_t c;
-      bool in;
-      own_cell(u, h, c, in);
-      unsigned char f = fa[u] == CELL_FLUID;
-      sm.fl[h] = f;
-      sm.v[h] = f ? va[u] : 0.0f;
-      sm.p[h] = f ? pa[u] : 0.0f;
-    }
+    v = *(const volatile int *)p;
   }
-  /* dependencies */
-  const int dir = kind == 2 ? 1 : -1;
-  const int nbI = BI + dir, nbJ = BJ + dir, nbK = BK + dir;
-  const unsigned *flags = kind == 2 ? a.bflag : a.fflag;
-  const unsigned ep = kind == 2 ? epoch_b : epoch_f;
-  if (kind == 2) {
-    /* the forward solve of this brick wrote q */
-    wait_flag(a.fflag + brick, epoch_f, a.iflags);
-    float qa[OWN];
-#pragma unroll
-    for (int u = 0; u < OWN; u++) {
-      int h;
-      size_t c;
-      bool in;
-      own_cell(u, h, c, in);
-      qa[u] = in ? __ldcg(qz + c) : 0.0f;
-    }
-#pragma unroll
-    for (int u = 0; u < OWN; u++) {
-      int h;
-      size_t c;
-      bool in;
-      own_cell(u, h, c, in);
-      sm.v[h] = sm.fl[h] ? qa[u] : 0.0f;
-    }
-  }
-  if (nbI >= 0 && nbI < nbx) wait_flag(flags + (nbI * nbx + BJ) * nbx + BK, ep, a.iflags);
-  if (nbJ >= 0 && nbJ < nbx) wait_flag(flags + (BI * nbx + nbJ) * nbx + BK, ep, a.iflags);
-  if (nbK >= 0 && nbK < nbx) wait_flag(flags + (BI * nbx + BJ) * nbx + nbK, ep, a.iflags);
-  /* halo faces: -1 (build/forward) or +1 (backward) along each axis */
-  const int hf = kind == 2 ? BRK : -1;
-  {
-    unsigned char fa[HALO];
-    float va[HALO], pa[HALO];
-    int ha[HALO];
-#pragma unroll
-    for (int u = 0; u < HALO; u++) {
-      int t = tid + CG_BLOCK * u;
-      int face = t / (BRK * BRK), uu = (t / BRK) % BRK, w = t % BRK;
-      /* face 0: (hf,uu,w), face 1: (uu,hf,w), face 2: (uu,w,hf) */
-      int bi = face == 0 ? hf : uu, bj = face == 1 ? hf : (face == 0 ? uu : w),
-          bk = face == 2 ? hf : w;
-      int i = i0 + bi, j = j0 + bj, k = k0 + bk;
-      ha[u] = hidx(bi, bj, bk);
-      bool in = inside(i, j, k);
-      size_t c = in ? cidx(i, j, k) : 0;
-      fa[u] = in ? A[c] : (unsigned char)CELL_AIR;
-      pa[u] = in ? __ldcg(a.Pic + c) : 0.0f;
-      va[u] = (in && kind != 0) ? __ldcg(qz + c) : 0.0f;
-    }
-#pragma unroll
-    for (int u = 0; u < HALO; u++) {
-      unsigned char f = fa[u] == CELL_FLUID;
-      sm.fl[ha[u]] = f;
-      sm.p[ha[u]] = f ? pa[u] : 0.0f;
-      sm.v[ha[u]] = f ? va[u] : 0.0f;
-    }
-  }
-  __syncthreads();
+  __threadfence_block();
+  return v;
+}
+
+/* One line of a task: the factor (KIND = IC_FACTOR, writes the factor's
+ * plain and tagged rows), the forward solve (reads r, writes tagged q and
+ * adds q.q to qq) or the backward solve (reads tagged q, writes z in the
+ * natural layout and tagged). tag: this sweep's; tagq: the forward solve's
+ * (backward only). */
+template <int KIND>
+__device__ void ic_line(const CgArgs &a, IcSmem &sm, int I, int jb, unsigned tag, unsigned tagq,
+                        FF &qq) {
+  constexpr bool MIR = KIND == IC_BACKWARD;
+  const unsigned FULL = 0xffffffffu;
+  const int n = a.s.n, njb = a.ic_njb, sl = n + 31;
+  const int lane = threadIdx.x & 31, rho = threadIdx.x >> 5;
+  const int i = MIR ? I * IC_W + (IC_W - 1 - rho) : I * IC_W + rho;
+  if (i >= n || !__ldg(a.ic_line + (size_t)i * njb + jb)) return;
+  IcWarp &ws = sm.w[rho];
+  const int J0 = 32 * jb;
+  const int j = MIR ? J0 + 31 - lane : J0 + lane;
+  const int lf = MIR ? 31 - lane : lane; /* slot in the skewed rows */
+  const bool jon = j < n;
+  const size_t lbase = ((size_t)i * njb + jb) * (size_t)sl * 32;
+  /* i-neighbour line: the previous warp's (ring) or another task's */
+  const int ip = MIR ? i + 1 : i - 1;
+  const bool ipon = ip >= 0 && ip < n && __ldg(a.ic_line + (size_t)ip * njb + jb);
+  const size_t ibase = ((size_t)(ipon ? ip : 0) * njb + jb) * (size_t)sl * 32;
+  /* lane 0's j-neighbour: the last (forward) or first (backward) slot of
+   * the neighbouring block's line */
+  const int jbn = MIR ? jb + 1 : jb - 1, jn = MIR ? J0 + 32 : J0 - 1, jlf = MIR ? 0 : 31;
+  const bool jpon = jn >= 0 && jn < n && __ldg(a.ic_line + (size_t)i * njb + jbn);
+  const size_t jbase = ((size_t)i * njb + (jpon ? jbn : 0)) * (size_t)sl * 32;
+  /* the next warp's line takes this line's values through the ring */
+  const int inext = MIR ? i - 1 : i + 1;
+  const bool cons = rho + 1 < IC_W && inext >= 0 && inext < n &&
+                    __ldg(a.ic_line + (size_t)inext * njb + jb);
+  const unsigned long long *vsrc =
+      KIND == IC_FACTOR ? a.ic_psk : (KIND == IC_FORWARD ? a.ic_qsk : a.ic_zsk);
+  unsigned long long *vdst =
+      KIND == IC_FACTOR ? a.ic_psk : (KIND == IC_FORWARD ? a.ic_qsk : a.ic_zsk);
+  const bool natvec = (n & 3) == 0; /* 16-byte rows of r and z */
+  const size_t rowbase = ((size_t)i * n + (jon ? j : 0)) * n;
   const float tau = a.mic_tau;
-  for (int pl = 0; pl < NPLANES; pl++) {
-    const int d = kind == 2 ? NPLANES - 1 - pl : pl;
-    for (int e = pl_tab.start[d] + tid; e < pl_tab.start[d + 1]; e += CG_BLOCK) {
-      unsigned cc = pl_tab.cell[e];
-      int bi = cc >> 8, bj = (cc >> 4) & 15, bk = cc & 15;
-      int h = hidx(bi, bj, bk);
-      if (!sm.fl[h]) continue;
-      const int hm[3] = {hidx(bi - 1, bj, bk), hidx(bi, bj - 1, bk), hidx(bi, bj, bk - 1)};
-      const int hp[3] = {hidx(bi + 1, bj, bk), hidx(bi, bj + 1, bk), hidx(bi, bj, bk + 1)};
-      if (kind == 0) {
-        float diag = sm.v[h];
-        float ev = diag;
-        for (int ax = 0; ax < 3; ax++) {
-          if (!sm.fl[hm[ax]]) continue;
-          float pm = sm.p[hm[ax]];
-          ev -= pm * pm;
-          if (tau != 0.0f) {
-            /* the two other plus-side couplings of that neighbour */
-            int mi = i0 + bi - (ax == 0), mj = j0 + bj - (ax == 1), mk = k0 + bk - (ax == 2);
-            int cnt = 0;
-            for (int ax2 = 0; ax2 < 3; ax2++) {
-              if (ax2 == ax) continue;
-              int qi = mi + (ax2 == 0), qj = mj + (ax2 == 1), qk = mk + (ax2 == 2);
-              if (inside(qi, qj, qk) && __ldg(A + cidx(qi, qj, qk)) == CELL_FLUID) cnt++;
-            }
-            ev -= tau * (float)cnt * pm * pm;
+
+  auto prefetch = [&](int t) {
+    if (t < sl) {
+      const int r = MIR ? n + 30 - t : t, slot = t % IC_D;
+      if (KIND != IC_FACTOR && lane < 8)
+        cpa16(&ws.pf[slot][4 * lane], a.ic_pf + lbase + (size_t)r * 32 + 4 * lane);
+      if (KIND == IC_BACKWARD && lane >= 8 && lane < 24)
+        cpa16(&ws.qv[slot][2 * (lane - 8)], a.ic_qsk + lbase + (size_t)r * 32 + 2 * (lane - 8));
+      if (KIND == IC_FORWARD && natvec && jon) {
+        const int kk = t - lane;
+        if (kk >= 0 && kk < n && (kk & 3) == 0) cpa16(&ws.rn[lane][kk % IC_RQ], a.r + rowbase + kk);
+      }
+      if (rho == 0 && ipon) {
+        if (KIND != IC_FACTOR && lane < 8)
+          cpa16(&sm.ip[slot][4 * lane], a.ic_pf + ibase + (size_t)r * 32 + 4 * lane);
+        if (lane >= 8 && lane < 24)
+          cpa16(&sm.iv[slot][2 * (lane - 8)], vsrc + ibase + (size_t)r * 32 + 2 * (lane - 8));
+      }
+      if (jpon && t < n) {
+        const size_t rj = jbase + (size_t)(MIR ? n - 1 - t : t + 31) * 32;
+        if (KIND != IC_FACTOR && lane == 24) cpa16(&ws.jp[slot][0], a.ic_pf + rj + (jlf & ~3));
+        if (lane == 25) cpa16(&ws.jv[slot][0], vsrc + rj + (jlf & ~1));
+      }
+    }
+    cpa_commit();
+  };
+
+#pragma unroll 1
+  for (int t = 0; t < IC_D; t++) prefetch(t);
+  float2 last = make_float2(0.0f, 0.0f);
+  float4 zq = make_float4(0.0f, 0.0f, 0.0f, 0.0f); /* backward: z of k .. k+3 */
+  int seen_prev = 0, seen_next = 0;
+  const int *prev_prog = rho > 0 ? &sm.prog[rho - 1] : &sm.prog[0];
+  const int *next_prog = rho + 1 < IC_W ? &sm.prog[rho + 1] : &sm.prog[0];
+  const IcWarp &wprev = sm.w[rho > 0 ? rho - 1 : 0];
+#pragma unroll 1
+  for (int s = 0; s < sl; s++) {
+    /* step s's copies have landed (issued IC_D steps ago) */
+    cpa_wait<IC_D - 1>();
+    __syncwarp();
+    const int slot = s % IC_D, srow = MIR ? n + 30 - s : s;
+    const int kk = s - lane;
+    const bool valid = jon && kk >= 0 && kk < n;
+    const int k = MIR ? n - 1 - kk : kk;
+    /* i-neighbour at this step */
+    float pi = 0.0f, vi = 0.0f;
+    if (ipon) {
+      if (rho > 0) {
+        if (seen_prev <= s) seen_prev = ic_wait_prog(prev_prog, s + 1, a.iflags);
+        const float2 e = wprev.ring[s % IC_RING][lane];
+        pi = e.x;
+        vi = e.y;
+      } else if (valid) {
+        unsigned long long w = sm.iv[slot][lf];
+        if (ic_tagof(w) != tag) w = ic_poll(vsrc + ibase + (size_t)srow * 32 + lf, w, tag, a.iflags);
+        if (KIND == IC_FACTOR) {
+          pi = ic_val(w);
+        } else {
+          pi = sm.ip[slot][lf];
+          vi = ic_val(w);
+        }
+      }
+    }
+    /* j-neighbour: lane l-1's previous step; lane 0: the neighbouring line */
+    float pj = __shfl_up_sync(FULL, last.x, 1), vj = __shfl_up_sync(FULL, last.y, 1);
+    if (lane == 0) {
+      pj = vj = 0.0f;
+      if (jpon && valid) {
+        unsigned long long w = ws.jv[slot][jlf & 1];
+        if (ic_tagof(w) != tag)
+          w = ic_poll(vsrc + jbase + (size_t)(MIR ? n - 1 - s : s + 31) * 32 + jlf, w, tag,
+                      a.iflags);
+        if (KIND == IC_FACTOR) {
+          pj = ic_val(w);
+        } else {
+          pj = ws.jp[slot][jlf & 3];
+          vj = ic_val(w);
+        }
+      }
+    }
+    /* k-neighbour: this lane's previous step */
+    const float pk = last.x, vk = last.y;
+    float p = 0.0f, v = 0.0f;
+    if (valid) {
+      const size_t c = rowbase + k;
+      if (KIND == IC_FACTOR) {
+        const unsigned cf = __ldg(a.ic_cf + c);
+        if (cf & 1u) {
+          const float diag = __ldg(a.diag + c);
+          float ev = diag;
+          const float pm[3] = {pi, pj, pk};
+#pragma unroll
+          for (int ax = 0; ax < 3; ax++) {
+            if (pm[ax] == 0.0f) continue;
+            ev -= pm[ax] * pm[ax];
+            if (tau != 0.0f) ev -= tau * (float)((cf >> (1 + 2 * ax)) & 3u) * pm[ax] * pm[ax];
+          }
+          if (ev < 0.25f * diag) ev = diag;
+          p = 1.0f / sqrtf(ev);
+        }
+      } else {
+        p = ws.pf[slot][lf];
+        if (KIND == IC_FORWARD) {
+          if (p != 0.0f) {
+            float t = natvec ? ws.rn[lane][kk % IC_RQ] : __ldcg(a.r + c);
+            if (pi != 0.0f) t += pi * vi;
+            if (pj != 0.0f) t += pj * vj;
+            if (pk != 0.0f) t += pk * vk;
+            v = t * p;
+            ff_add_prod(qq, v, v);
+          }
+        } else {
+          unsigned long long w = ws.qv[slot][lf];
+          if (ic_tagof(w) != tagq)
+            w = ic_poll(a.ic_qsk + lbase + (size_t)srow * 32 + lf, w, tagq, a.iflags);
+          if (p != 0.0f) {
+            float t = 0.0f;
+            if (pi != 0.0f) t += vi;
+            if (pj != 0.0f) t += vj;
+            if (pk != 0.0f) t += vk;
+            v = (ic_val(w) + p * t) * p;
           }
         }
-        if (ev < 0.25f * diag) ev = diag;
-        sm.p[h] = 1.0f / sqrtf(ev);
-      } else if (kind == 1) {
-        float t = sm.v[h];
-        for (int ax = 0; ax < 3; ax++)
-          if (sm.fl[hm[ax]]) t += sm.p[hm[ax]] * sm.v[hm[ax]];
-        sm.v[h] = t * sm.p[h];
+      }
+      const size_t o = lbase + (size_t)srow * 32 + lf;
+      if (KIND == IC_FACTOR) {
+        a.ic_pf[o] = p;
+        st_u64(vdst + o, ic_word(p, tag));
       } else {
-        float t = 0.0f;
-        for (int ax = 0; ax < 3; ax++)
-          if (sm.fl[hp[ax]]) t += sm.v[hp[ax]];
-        sm.v[h] = (sm.v[h] + sm.p[h] * t) * sm.p[h];
+        st_u64(vdst + o, ic_word(v, tag));
+      }
+      if (KIND == IC_BACKWARD) {
+        if (natvec) {
+          zq = make_float4(v, zq.x, zq.y, zq.z);
+          if ((k & 3) == 0) *reinterpret_cast<float4 *>(a.z + c) = zq;
+        } else {
+          a.z[c] = v;
+        }
       }
     }
-    __syncthreads();
-  }
-  /* write back, per-brick z.r for the backward solve, publish */
-  FF zr = ff_zero();
-  for (int t = tid; t < BRK3; t += CG_BLOCK) {
-    int bi = t >> 8, bj = (t >> 4) & 15, bk = t & 15;
-    int i = i0 + bi, j = j0 + bj, k = k0 + bk;
-    int h = hidx(bi, bj, bk);
-    if (!inside(i, j, k)) continue;
-    size_t c = cidx(i, j, k);
-    if (kind == 0) {
-      a.Pic[c] = sm.fl[h] ? sm.p[h] : 0.0f;
-    } else {
-      qz[c] = sm.v[h];
-      if (kind == 2 && sm.fl[h]) ff_add_prod(zr, sm.v[h], __ldcg(r + c));
+    last = valid ? make_float2(p, v) : make_float2(0.0f, 0.0f);
+    if (cons) {
+      /* the slot's previous value (step s - IC_RING) has been taken */
+      if (seen_next < s - IC_RING + 1)
+        seen_next = ic_wait_prog(next_prog, s - IC_RING + 1, a.iflags);
+      ws.ring[s % IC_RING][lane] = last;
     }
+    /* steps done: what the next warp may read, and what the previous warp
+     * may overwrite */
+    __threadfence_block();
+    __syncwarp();
+    if (lane == 0) *(volatile int *)&sm.prog[rho] = s + 1;
+    /* every lane has read this step's slots: refill them for step s + IC_D */
+    __syncwarp();
+    prefetch(s + IC_D);
   }
-  if (kind == 2) {
-    const FF tot = block_sum_ff<CG_BLOCK>(zr);
-    if (tid == 0) a.brick_part[brick] = make_float2(tot.hi, tot.lo);
-  }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) st_release((kind == 2 ? a.bflag : a.fflag) + brick, kind == 2 ? epoch_b : epoch_f);
+  cpa_wait<0>();
+  __syncwarp();
 }
 
-/* Run one factor build (tasks = nbricks) or one forward+backward apply
- * (tasks = 2*nbricks) over the ticket counter, one brick per CTA at a time. */
-__device__ void wavefront(const CgArgs &a, BrickSmem *sm, const BrickPlanes &pl_tab, bool build,
-                          unsigned epoch_f, unsigned epoch_b, const float *r, float *qz) {
-  __shared__ unsigned s_ticket;
-  __shared__ int s_stop;
-  const unsigned tasks = build ? (unsigned)a.nbricks : 2u * (unsigned)a.nbricks;
+/* One task: IC_W lines at one 32-j block; the forward solve leaves the
+ * task's q.q in ic_part[task]. */
+template <int KIND>
+__device__ void ic_task(const CgArgs &a, IcSmem &sm, int task, unsigned tag, unsigned tagq) {
+  const int I = task / a.ic_njb, jb = task - I * a.ic_njb;
+  if (threadIdx.x < IC_W) sm.prog[threadIdx.x] = 0;
+  __syncthreads();
+  FF qq = ff_zero();
+  ic_line<KIND>(a, sm, I, jb, tag, tagq, qq);
+  if (KIND == IC_FORWARD) {
+    for (int o = 16; o > 0; o >>= 1) qq = ff_merge(qq, ff_shfl_down(qq, o));
+    if ((threadIdx.x & 31) == 0) sm.part[threadIdx.x >> 5] = qq;
+  }
+  __syncthreads();
+  if (KIND == IC_FORWARD && threadIdx.x == 0) {
+    FF t = sm.part[0];
+    for (int w = 1; w < IC_W; w++) t = ff_merge(t, sm.part[w]);
+    a.ic_part[task] = make_float2(t.hi, t.lo);
+  }
+}
+
+/* The factor (tasks = ic_tasks) or one preconditioner application, forward
+ * then backward (2 ic_tasks), over the ticket counter. */
+__device__ void ic_sweeps(const CgArgs &a, IcSmem &sm, bool factor, unsigned tag_f,
+                          unsigned tag_b) {
+  const unsigned T = (unsigned)a.ic_tasks, tasks = factor ? T : 2u * T;
   while (true) {
     if (threadIdx.x == 0) {
-      s_ticket = atomicAdd(a.ticket, 1u);
-      s_stop = *(volatile int *)(a.iflags + IF_TIMEOUT);
+      sm.ticket = atomicAdd(a.ticket, 1u);
+      sm.stop = *(volatile int *)(a.iflags + IF_TIMEOUT);
     }
     __syncthreads();
-    const unsigned t = s_ticket;
-    const int stop = s_stop;
-    __syncthreads(); /* every thread has read the ticket before the next one overwrites it */
+    const unsigned t = sm.ticket;
+    const int stop = sm.stop;
+    __syncthreads(); /* every thread has the ticket before the next one overwrites it */
     if (t >= tasks || stop) break;
-    if (t < (unsigned)a.nbricks)
-      brick_task(a, *sm, pl_tab, a.brick_order[t], build ? 0 : 1, epoch_f, epoch_b, r, qz);
+    if (factor)
+      ic_task<IC_FACTOR>(a, sm, (int)__ldg(a.ic_order + t), tag_f, 0u);
+    else if (t < T)
+      ic_task<IC_FORWARD>(a, sm, (int)__ldg(a.ic_order + t), tag_f, 0u);
     else
-      brick_task(a, *sm, pl_tab, a.brick_order[2 * a.nbricks - 1 - t], 2, epoch_f, epoch_b, r,
-                 qz);
+      ic_task<IC_BACKWARD>(a, sm, (int)__ldg(a.ic_order + (2u * T - 1u - t)), tag_b, tag_f);
   }
 }
 
-/* Sum of the per-brick partials in brick order (identical in every block). */
-__device__ __forceinline__ double sum_brick_parts(const CgArgs &a) {
+/* z.r (as q.q) from the per-task partials in task order (identical in every block). */
+__device__ __forceinline__ double ic_sum_parts(const CgArgs &a) {
   FF v = ff_zero();
-  for (int b = threadIdx.x; b < a.nbricks; b += CG_BLOCK) {
-    float2 p = __ldcg(a.brick_part + b);
+  for (int b = threadIdx.x; b < a.ic_tasks; b += CG_BLOCK) {
+    const float2 p = __ldcg(a.ic_part + b);
     v = ff_merge(v, FF{p.x, p.y});
   }
   return ff_to_double(block_sum_ff<CG_BLOCK>(v));
 }
 
+/* Per cell: bit 0 liquid; bits 1-2, 3-4, 5-6: how many of the -x, -y, -z
+ * neighbour's two other + neighbours are liquid (the MIC(0) terms of the
+ * factor); per line (i, 32-j block): whether it holds liquid (ic_line zeroed
+ * before). */
+__global__ void __launch_bounds__(BLK) k_ic_prep(int n, int njb, const uint8_t *__restrict__ A,
+                                                 uint8_t *__restrict__ cf,
+                                                 unsigned *__restrict__ line) {
+  const size_t c = (size_t)blockIdx.x * BLK + threadIdx.x;
+  if (c >= (size_t)n * n * n) return;
+  int i, j, k;
+  decode_index(c, n, n, i, j, k);
+  auto liq = [&](int x, int y, int z) -> unsigned {
+    return x >= 0 && x < n && y >= 0 && y < n && z >= 0 && z < n &&
+           A[((size_t)x * n + y) * n + z] == CELL_FLUID;
+  };
+  unsigned v = 0;
+  if (A[c] == CELL_FLUID) {
+    v = 1u;
+    v |= (liq(i - 1, j + 1, k) + liq(i - 1, j, k + 1)) << 1;
+    v |= (liq(i + 1, j - 1, k) + liq(i, j - 1, k + 1)) << 3;
+    v |= (liq(i + 1, j, k - 1) + liq(i, j + 1, k - 1)) << 5;
+    line[(size_t)i * njb + (j >> 5)] = 1u;
+  }
+  cf[c] = (uint8_t)v;
+}
+
 /* FAST-mode PCG with the wavefront IC(0)/MIC(0) preconditioner. */
 __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   if (ir_skipped(a)) return;
-  extern __shared__ unsigned char dyn[];
-  BrickSmem *sm = reinterpret_cast<BrickSmem *>(dyn);
-  /* the intra-brick plane table, read with lane-varying indices */
-  __shared__ BrickPlanes pl_tab;
-  for (int i = threadIdx.x; i < BRK3; i += CG_BLOCK) pl_tab.cell[i] = c_planes.cell[i];
-  for (int i = threadIdx.x; i <= NPLANES; i += CG_BLOCK) pl_tab.start[i] = c_planes.start[i];
-  __syncthreads();
+  extern __shared__ __align__(16) unsigned char dyn[];
+  IcSmem &sm = *reinterpret_cast<IcSmem *>(dyn);
   const unsigned nb = gridDim.x;
   const size_t stride = (size_t)nb * CG_BLOCK;
   const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
@@ -2458,10 +2580,24 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   const size_t nc = a.nc;
   constexpr int M = FLIPGPU_SOLVE_FAST;
   unsigned apply = 0; /* preconditioner applications so far */
+  /* this launch's tags: base + 1 (factor), base + 2a, base + 2a + 1
+   * (application a); the counter moves past them when the launch ends */
+  unsigned base = *(volatile const unsigned *)a.ic_ctr;
+  auto leave = [&]() {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.ic_ctr = base + 2u * apply + 2u;
+  };
+  if (base > IC_TAG_WRAP) {
+    /* near the end of the tag space: clear every word, start again at 0 */
+    const size_t words = (size_t)a.s.n * a.ic_njb * (size_t)(a.s.n + 31) * 32;
+    for (size_t e = t0; e < words; e += stride) a.ic_psk[e] = a.ic_qsk[e] = a.ic_zsk[e] = 0ull;
+    base = 0;
+    if (!grid_barrier(a.bar, a.iflags)) return leave();
+  }
 
-  /* factor (forward-type sweep, epoch 1) */
-  wavefront(a, sm, pl_tab, true, 1u, 0u, nullptr, nullptr);
-  if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
+  /* factor */
+  ic_sweeps(a, sm, true, base + 1u, 0u);
+  if (!grid_barrier(a.bar, a.iflags, a.ticket)) return leave();
+
   /* r = b - A x; b.b, r.r */
   FF pbb = ff_zero(), prr = ff_zero();
   for (size_t c = t0; c < nc; c += stride) {
@@ -2481,7 +2617,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   }
   store_partial(a.part, 0, nb, pbb);
   store_partial(a.part, 1, nb, prr);
-  if (!grid_barrier(a.bar, a.iflags)) return;
+  if (!grid_barrier(a.bar, a.iflags)) return leave();
   double b2, rr, unused;
   sum_partials(a.part, 0, 1, nb, b2, rr);
   const double rt = cg_rel_tol(a);
@@ -2490,13 +2626,14 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
   double e2 = rr, azr = 0.0;
   if (!done) {
     apply++;
-    wavefront(a, sm, pl_tab, false, apply + 1, apply, a.r, a.z);
-    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
-    azr = sum_brick_parts(a);
+    ic_sweeps(a, sm, false, base + 2u * apply, base + 2u * apply + 1u);
+    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return leave();
+    azr = ic_sum_parts(a);
   }
   float *so = a.s0, *sn = a.s1;
   float beta_f = 0.0f;
   bool first = true;
+  __shared__ float s_bcast;
   while (!done) {
     /* phase A: s = z + beta s, w = A s; w.s */
     FF pws = ff_zero();
@@ -2512,10 +2649,9 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
       a.w[c] = wv;
     }
     store_partial(a.part, 3, nb, pws);
-    if (!grid_barrier(a.bar, a.iflags)) return;
+    if (!grid_barrier(a.bar, a.iflags)) return leave();
     double ws;
     sum_partials(a.part, 3, -1, nb, ws, unused);
-    __shared__ float s_bcast;
     if (threadIdx.x == 0) s_bcast = (float)(azr / ws); /* one FP64 division per block */
     __syncthreads();
     const float alpha_f = s_bcast;
@@ -2529,18 +2665,18 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
       ff_add_prod(prr2, rv, rv);
     }
     store_partial(a.part, 4, nb, prr2);
-    if (!grid_barrier(a.bar, a.iflags)) return;
+    if (!grid_barrier(a.bar, a.iflags)) return leave();
     sum_partials(a.part, 4, -1, nb, rr, unused);
     iters++;
     e2 = rr;
     if (e2 <= eps) { done = 1; break; }
     if (!(e2 == e2)) { done = 2; break; }
     if (iters >= a.max_iters) { done = 3; break; }
-    /* z = M^-1 r by the two wavefront sweeps; z.r per brick */
+    /* z = M^-1 r by the two wavefront sweeps; z.r = q.q per task */
     apply++;
-    wavefront(a, sm, pl_tab, false, apply + 1, apply, a.r, a.z);
-    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return;
-    const double zr = sum_brick_parts(a);
+    ic_sweeps(a, sm, false, base + 2u * apply, base + 2u * apply + 1u);
+    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return leave();
+    const double zr = ic_sum_parts(a);
     __syncthreads();
     if (threadIdx.x == 0) s_bcast = (float)(zr / azr);
     __syncthreads();
@@ -2559,6 +2695,7 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
     a.scal[SC_B2] = b2;
     a.scal[SC_EPS] = eps;
   }
+  leave();
 }
 
 } // namespace
@@ -2946,6 +3083,59 @@ void mg_free(FlipGpu *h) {
   h->mg_nlev = 0;
 }
 
+/* Buffers of the IC(0)/MIC(0) line wavefront (FAST mode). */
+int ic_alloc(FlipGpu *h) {
+  if (h->ic_tasks > 0) return FLIPGPU_OK;
+  const int n = h->n, njb = (n + 31) / 32, nis = (n + IC_W - 1) / IC_W;
+  const size_t lines = (size_t)n * njb, words = lines * (size_t)(n + 31) * 32;
+  const int tasks = nis * njb;
+  bool ok = cudaMalloc(&h->ic_order, tasks * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc(&h->ic_line, lines * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc(&h->ic_cf, h->nc) == cudaSuccess &&
+            cudaMalloc(&h->ic_pf, words * sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&h->ic_psk, words * 8) == cudaSuccess &&
+            cudaMalloc(&h->ic_qsk, words * 8) == cudaSuccess &&
+            cudaMalloc(&h->ic_zsk, words * 8) == cudaSuccess &&
+            cudaMalloc(&h->ic_part, tasks * sizeof(float2)) == cudaSuccess &&
+            cudaMalloc(&h->ic_ctr, sizeof(unsigned)) == cudaSuccess;
+  if (ok) {
+    /* tasks by increasing i block + j block: every task's dependencies
+     * (i block - 1, j block - 1) come earlier */
+    std::vector<unsigned> order;
+    for (int d = 0; d <= nis + njb - 2; d++)
+      for (int I = 0; I < nis; I++) {
+        const int jb = d - I;
+        if (jb >= 0 && jb < njb) order.push_back((unsigned)(I * njb + jb));
+      }
+    ok = cudaMemcpy(h->ic_order, order.data(), order.size() * sizeof(unsigned),
+                    cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(h->ic_psk, 0, words * 8) == cudaSuccess &&
+         cudaMemset(h->ic_qsk, 0, words * 8) == cudaSuccess &&
+         cudaMemset(h->ic_zsk, 0, words * 8) == cudaSuccess &&
+         cudaMemset(h->ic_ctr, 0, sizeof(unsigned)) == cudaSuccess;
+  }
+  if (!ok) {
+    ic_free(h);
+    return FLIPGPU_ENOMEM;
+  }
+  h->ic_njb = njb;
+  h->ic_tasks = tasks;
+  return FLIPGPU_OK;
+}
+
+void ic_free(FlipGpu *h) {
+  void *ptrs[] = {h->ic_order, h->ic_line, h->ic_cf, h->ic_pf, h->ic_psk,
+                  h->ic_qsk,   h->ic_zsk,  h->ic_part, h->ic_ctr};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  h->ic_order = h->ic_line = h->ic_ctr = nullptr;
+  h->ic_cf = nullptr;
+  h->ic_pf = nullptr;
+  h->ic_psk = h->ic_qsk = h->ic_zsk = nullptr;
+  h->ic_part = nullptr;
+  h->ic_tasks = 0;
+}
+
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   const int n = h->n;
   const size_t nc = h->nc;
@@ -3025,6 +3215,13 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
                                     "cooperative launch");
     return FLIPGPU_EINVAL;
   }
+  if (precond == FLIPGPU_PRECOND_IC) {
+    const int r = ic_alloc(h);
+    if (r != FLIPGPU_OK) {
+      snprintf(h->err, sizeof h->err, "solve: wavefront buffers (%d)", r);
+      return r;
+    }
+  }
   if (persistent && mode == FLIPGPU_SOLVE_REF) {
     int exotic = 0;
     cudaMemcpyAsync(&exotic, h->iflags + IF_EXOTIC, sizeof(int), cudaMemcpyDeviceToHost, S);
@@ -3058,14 +3255,18 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.ref_eps = ref_eps;
     a.max_iters = max_iters;
     a.mic_tau = (float)h->prm.mic_tau;
-    a.Pic = h->Pf;
-    a.nbx = h->nbx;
-    a.nbricks = h->nbricks;
-    a.brick_order = h->brick_order;
-    a.fflag = h->fflag;
-    a.bflag = h->bflag;
     a.ticket = h->ticket;
-    a.brick_part = h->brick_part;
+    a.ic_njb = h->ic_njb;
+    a.ic_tasks = h->ic_tasks;
+    a.ic_order = h->ic_order;
+    a.ic_line = h->ic_line;
+    a.ic_cf = h->ic_cf;
+    a.ic_pf = h->ic_pf;
+    a.ic_psk = h->ic_psk;
+    a.ic_qsk = h->ic_qsk;
+    a.ic_zsk = h->ic_zsk;
+    a.ic_part = h->ic_part;
+    a.ic_ctr = h->ic_ctr;
     cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
     void *kargs[] = {&a};
     const void *kern = mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
@@ -3161,8 +3362,12 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       kern = (const void *)k_cg_ic;
       grid = h->cg_grid[3];
       smem = ic_smem_bytes();
-      cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
-      cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
+      if (a.max_iters > IC_MAX_ITERS) a.max_iters = IC_MAX_ITERS;
+      /* liquid flags, MIC(0) counts and liquid lines (A is fixed during
+       * the solve) */
+      cudaMemsetAsync(h->ic_line, 0, (size_t)n * h->ic_njb * sizeof(unsigned), S);
+      k_ic_prep<<<grid_for(nc, BLK), BLK, 0, S>>>(n, h->ic_njb, h->A, h->ic_cf, h->ic_line);
+      FG_LAUNCHED(h, 1);
       cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
     }
     a.ir_skip = nullptr;
@@ -3170,11 +3375,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     const int block = cg_block_of(kern);
     auto reset_flags = [&]() {
       cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
-      if (precond == FLIPGPU_PRECOND_IC) {
-        cudaMemsetAsync(h->fflag, 0, h->nbricks * sizeof(unsigned), S);
-        cudaMemsetAsync(h->bflag, 0, h->nbricks * sizeof(unsigned), S);
-        cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
-      }
+      if (precond == FLIPGPU_PRECOND_IC) cudaMemsetAsync(h->ticket, 0, sizeof(unsigned), S);
     };
     if (mode == FLIPGPU_SOLVE_FAST && h->prm.refine_steps > 0) {
       /* mixed-precision iterative refinement: the iterate is the
@@ -3349,7 +3550,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   return FLIPGPU_OK;
 }
 
-size_t ic_smem_bytes() { return sizeof(BrickSmem); }
+size_t ic_smem_bytes() { return sizeof(IcSmem); }
 
 void launch_pressure_double(FlipGpu *h, double *out) {
   k_pressure_double<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(
@@ -3357,23 +3558,12 @@ void launch_pressure_double(FlipGpu *h, double *out) {
   FG_LAUNCHED(h, 1);
 }
 
-/* Intra-brick plane lists, uploaded once per device. */
+/* Dynamic shared memory limits of the IC and MG kernels, once per device. */
 int ic_init_device() {
   static bool done[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
   if (done[dev]) return 0;
-  BrickPlanes bp;
-  int e = 0;
-  for (int d = 0; d < NPLANES; d++) {
-    bp.start[d] = (unsigned short)e;
-    for (int i = 0; i < BRK; i++)
-      for (int j = 0; j < BRK; j++)
-        for (int k = 0; k < BRK; k++)
-          if (i + j + k == d) bp.cell[e++] = (unsigned short)((i << 8) | (j << 4) | k);
-  }
-  bp.start[NPLANES] = (unsigned short)e;
-  if (cudaMemcpyToSymbol(c_planes, &bp, sizeof bp) != cudaSuccess) return -1;
   if (cudaFuncSetAttribute(k_cg_ic, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)ic_smem_bytes()) != cudaSuccess)
     return -1;
