@@ -495,6 +495,7 @@ struct CgArgs {
   unsigned long long *ic_psk, *ic_qsk, *ic_zsk; /* skewed tagged factor, q, z */
   float2 *ic_part;              /* per-task q.q partials */
   unsigned *ic_ctr;             /* tag counter: this launch tags base + 1 .. */
+  int ic_factor;                /* build the factor (else the previous launch's) */
   unsigned *ticket;
   /* MG-preconditioned CG */
   float *p2, *q;               /* second direction buffer, A p */
@@ -2177,7 +2178,7 @@ __global__ void __launch_bounds__(BLK) k_mg_diag(const uint8_t *__restrict__ cf,
  * from its own previous step. A task is IC_W lines, i = IC_W I .. IC_W I +
  * IC_W - 1 (one warp each) at one 32-j block; warp w takes its i-neighbour
  * from warp w-1 of the task at the same step through a shared-memory ring
- * with progress counters. Tasks go to whole CTAs by an atomic ticket in
+ * guarded by mbarriers (full / empty per slot). Tasks go to whole CTAs by an atomic ticket in
  * wavefront order, so every dependency has a smaller ticket and runs.
  * Across tasks, values pass through skewed line buffers of 64-bit words
  * that carry the value and the tag of the sweep that wrote it: the reader
@@ -2189,8 +2190,8 @@ __global__ void __launch_bounds__(BLK) k_mg_diag(const uint8_t *__restrict__ cf,
  * s: every warp step reads or writes one contiguous row, and the backward
  * warp walks the rows in reverse with its lanes reversed. Each warp's reads
  * of its line's rows, of its neighbour lines and of r (natural layout) are
- * issued IC_D steps ahead with cp.async (16 bytes, L2 only) into per-warp
- * shared rings.
+ * issued IC_D steps ahead, IC_G steps at a time, with cp.async (16 bytes,
+ * L2 only) into per-warp shared rings.
  *
  * Lines and tasks without liquid are skipped; neighbours treat them as
  * non-liquid. Every cell is computed from the same neighbours in the same
@@ -2201,6 +2202,7 @@ constexpr int IC_W = CG_BLOCK / 32;
 constexpr int IC_D = 16;
 constexpr int IC_RING = 8;
 constexpr int IC_RQ = 32;
+constexpr int IC_G = 4;           /* steps per copy group */
 constexpr unsigned IC_SPIN_LIMIT = 1u << 22;
 constexpr unsigned IC_TAG_WRAP = 0xf0000000u; /* tags left: > 2^28 */
 constexpr int IC_MAX_ITERS = 1 << 26;        /* 2^27 + 2 tags per launch at most */
@@ -2220,7 +2222,9 @@ struct IcSmem {
   IcWarp w[IC_W];
   float ip[IC_D][32];               /* warp 0's i-neighbour line: factor rows */
   unsigned long long iv[IC_D][32];  /* ... tagged value rows */
-  int prog[IC_W];                   /* steps each warp of the task has handed on */
+  /* ring slot s % IC_RING of warp w: full (written for step s) and empty
+   * (read by warp w+1) barriers, 32 arrivals each */
+  unsigned long long full[IC_W][IC_RING], empty[IC_W][IC_RING];
   FF part[IC_W];
   unsigned ticket;
   int stop;
@@ -2234,11 +2238,14 @@ __device__ __forceinline__ float ic_val(unsigned long long w) {
 }
 __device__ __forceinline__ unsigned ic_tagof(unsigned long long w) { return (unsigned)(w >> 32); }
 
+/* The copies are issued without a compiler memory barrier: their shared
+ * destinations are read only after cp.async.wait_group (which has one) and
+ * a __syncwarp. */
 __device__ __forceinline__ void cpa16(void *dst, const void *src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src));
 }
-__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;"); }
 template <int N> __device__ __forceinline__ void cpa_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
@@ -2246,9 +2253,6 @@ __device__ __forceinline__ unsigned long long ld_cg_u64(const unsigned long long
   unsigned long long v;
   asm volatile("ld.global.cg.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
-}
-__device__ __forceinline__ void st_u64(unsigned long long *p, unsigned long long v) {
-  asm volatile("st.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 /* The word at p once it carries `tag` (w: a copy read earlier). Bounded:
@@ -2264,38 +2268,60 @@ __device__ __forceinline__ unsigned long long ic_poll(const unsigned long long *
       atomicExch(iflags + IF_TIMEOUT, 1);
       return (unsigned long long)tag << 32;
     }
-    __nanosleep(20);
+    if (spins > 32) __nanosleep(64);
     w = ld_cg_u64(p);
   }
   return w;
 }
 
-/* Wait until the shared counter reaches target. Bounded: gives up with
+/* Shared-memory barriers of the rings between a task's warps. */
+__device__ __forceinline__ unsigned icb_addr(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void icb_init(unsigned long long *b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(icb_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void icb_inval(unsigned long long *b) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(icb_addr(b)) : "memory");
+}
+__device__ __forceinline__ void icb_arrive(unsigned long long *b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(icb_addr(b)) : "memory");
+}
+__device__ __forceinline__ bool icb_test(unsigned long long *b, unsigned parity) {
+  unsigned done;
+  asm volatile("{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+               "selp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(done)
+               : "r"(icb_addr(b)), "r"(parity)
+               : "memory");
+  return done != 0;
+}
+/* Wait for the barrier's phase of this parity: polled (the neighbour warp
+ * is usually a step ahead), napping after a while. Bounded: gives up with
  * FLIPGPU_ETIMEOUT, or at once when another wait has already timed out. */
-__device__ __forceinline__ int ic_wait_prog(const int *p, int target, int *iflags) {
-  int v = *(const volatile int *)p;
-  unsigned spins = 0;
-  while (v < target) {
-    if ((++spins & 1023u) == 0 &&
-        (spins > IC_SPIN_LIMIT || *(volatile int *)(iflags + IF_TIMEOUT) != 0)) {
+__device__ __forceinline__ void icb_wait(unsigned long long *b, unsigned parity, int *iflags) {
+  for (unsigned spin = 0;; spin++) {
+    if (icb_test(b, parity)) return;
+    if (spin > 64) __nanosleep(32);
+    if ((spin & 255u) == 255u &&
+        (spin > IC_SPIN_LIMIT || *(volatile int *)(iflags + IF_TIMEOUT) != 0)) {
       atomicExch(iflags + IF_TIMEOUT, 1);
-      return 0x3fffffff;
+      return;
     }
-    v = *(const volatile int *)p;
   }
-  __threadfence_block();
-  return v;
 }
 
 /* One line of a task: the factor (KIND = IC_FACTOR, writes the factor's
  * plain and tagged rows), the forward solve (reads r, writes tagged q and
  * adds q.q to qq) or the backward solve (reads tagged q, writes z in the
  * natural layout and tagged). tag: this sweep's; tagq: the forward solve's
- * (backward only). */
+ * (backward only). Every per-step address is a per-lane pointer advanced by
+ * a fixed stride; each shared word is read once per step. */
 template <int KIND>
 __device__ void ic_line(const CgArgs &a, IcSmem &sm, int I, int jb, unsigned tag, unsigned tagq,
                         FF &qq) {
   constexpr bool MIR = KIND == IC_BACKWARD;
+  constexpr bool SOLVE = KIND != IC_FACTOR;
   const unsigned FULL = 0xffffffffu;
   const int n = a.s.n, njb = a.ic_njb, sl = n + 31;
   const int lane = threadIdx.x & 31, rho = threadIdx.x >> 5;
@@ -2306,16 +2332,18 @@ __device__ void ic_line(const CgArgs &a, IcSmem &sm, int I, int jb, unsigned tag
   const int j = MIR ? J0 + 31 - lane : J0 + lane;
   const int lf = MIR ? 31 - lane : lane; /* slot in the skewed rows */
   const bool jon = j < n;
-  const size_t lbase = ((size_t)i * njb + jb) * (size_t)sl * 32;
-  /* i-neighbour line: the previous warp's (ring) or another task's */
+  const size_t lsize = (size_t)sl * 32;
+  const size_t lbase = ((size_t)i * njb + jb) * lsize;
+  /* i-neighbour line: the previous warp's (ring) or another task's (warp 0) */
   const int ip = MIR ? i + 1 : i - 1;
   const bool ipon = ip >= 0 && ip < n && __ldg(a.ic_line + (size_t)ip * njb + jb);
-  const size_t ibase = ((size_t)(ipon ? ip : 0) * njb + jb) * (size_t)sl * 32;
-  /* lane 0's j-neighbour: the last (forward) or first (backward) slot of
-   * the neighbouring block's line */
+  const bool iglob = rho == 0 && ipon;
+  const size_t ibase = ((size_t)(ipon ? ip : 0) * njb + jb) * lsize;
+  /* lane 0's j-neighbour: slot 31 (forward) or 0 (backward) of the
+   * neighbouring block's line, row s + 31 or n - 1 - s */
   const int jbn = MIR ? jb + 1 : jb - 1, jn = MIR ? J0 + 32 : J0 - 1, jlf = MIR ? 0 : 31;
   const bool jpon = jn >= 0 && jn < n && __ldg(a.ic_line + (size_t)i * njb + jbn);
-  const size_t jbase = ((size_t)i * njb + (jpon ? jbn : 0)) * (size_t)sl * 32;
+  const size_t jbase = ((size_t)i * njb + (jpon ? jbn : 0)) * lsize;
   /* the next warp's line takes this line's values through the ring */
   const int inext = MIR ? i - 1 : i + 1;
   const bool cons = rho + 1 < IC_W && inext >= 0 && inext < n &&
@@ -2327,161 +2355,201 @@ __device__ void ic_line(const CgArgs &a, IcSmem &sm, int I, int jb, unsigned tag
   const bool natvec = (n & 3) == 0; /* 16-byte rows of r and z */
   const size_t rowbase = ((size_t)i * n + (jon ? j : 0)) * n;
   const float tau = a.mic_tau;
+  /* skewed rows advance by dstep words per step (backward: row n + 30 - s) */
+  const long dstep = MIR ? -32 : 32;
+  const size_t row0 = MIR ? (size_t)(n + 30) * 32 : 0;
 
-  auto prefetch = [&](int t) {
-    if (t < sl) {
-      const int r = MIR ? n + 30 - t : t, slot = t % IC_D;
-      if (KIND != IC_FACTOR && lane < 8)
-        cpa16(&ws.pf[slot][4 * lane], a.ic_pf + lbase + (size_t)r * 32 + 4 * lane);
-      if (KIND == IC_BACKWARD && lane >= 8 && lane < 24)
-        cpa16(&ws.qv[slot][2 * (lane - 8)], a.ic_qsk + lbase + (size_t)r * 32 + 2 * (lane - 8));
+  /* Copies go in groups of IC_G steps: a group's rows of a line are one
+   * contiguous block (512 bytes of factor, 1 KB of tagged words), copied by
+   * all 32 lanes at once, IC_D steps ahead. Lane l takes 16-byte chunk l
+   * (factor) or chunks l and l + 32 (words) of the block; memory row m of a
+   * group is step t0 + m (forward) or t0 + 3 - m (backward). */
+  constexpr int G = IC_G, GD = IC_D / IC_G;
+  const long gstep = MIR ? -32 * G : 32 * G; /* floats or words per group */
+  const int mr = lane >> 3, col = 4 * (lane & 7);
+  const int ta_of = MIR ? G - 1 - mr : mr;
+  const size_t mrow = MIR ? (size_t)(n + 31 - G + mr) * 32 : (size_t)mr * 32;
+  const float *pfg = a.ic_pf + lbase + mrow + col;
+  const float *ipg = a.ic_pf + ibase + mrow + col;
+  const int qc = 2 * (lane & 15), qm0 = lane >> 4, qm1 = qm0 + 2;
+  const int tq0 = MIR ? G - 1 - qm0 : qm0, tq1 = MIR ? G - 1 - qm1 : qm1;
+  const size_t qrow0 = MIR ? (size_t)(n + 31 - G + qm0) * 32 : (size_t)qm0 * 32;
+  const size_t qrow1 = MIR ? (size_t)(n + 31 - G + qm1) * 32 : (size_t)qm1 * 32;
+  const unsigned long long *qg0 = a.ic_qsk + lbase + qrow0 + qc;
+  const unsigned long long *qg1 = a.ic_qsk + lbase + qrow1 + qc;
+  const unsigned long long *ig0 = vsrc + ibase + qrow0 + qc;
+  const unsigned long long *ig1 = vsrc + ibase + qrow1 + qc;
+  /* lane 0's j-neighbour row at step t: t + 31 (forward) or n - 1 - t */
+  const long jstep = MIR ? -32 : 32;
+  const size_t jrow0 = MIR ? (size_t)(n - 1) * 32 : (size_t)31 * 32;
+  const float *r_row = a.r + rowbase;
+
+  auto prefetch = [&](int g) {
+    const int t0 = G * g;
+    if (t0 < sl) {
+      const long og = (long)g * gstep;
+      const int ta = t0 + ta_of, t1 = t0 + tq0, t2 = t0 + tq1;
+      if (SOLVE && ta < sl) {
+        cpa16(&ws.pf[ta & (IC_D - 1)][col], pfg + og);
+        if (iglob) cpa16(&sm.ip[ta & (IC_D - 1)][col], ipg + og);
+      }
+      if (KIND == IC_BACKWARD) {
+        if (t1 < sl) cpa16(&ws.qv[t1 & (IC_D - 1)][qc], qg0 + og);
+        if (t2 < sl) cpa16(&ws.qv[t2 & (IC_D - 1)][qc], qg1 + og);
+      }
+      if (iglob) {
+        if (t1 < sl) cpa16(&sm.iv[t1 & (IC_D - 1)][qc], ig0 + og);
+        if (t2 < sl) cpa16(&sm.iv[t2 & (IC_D - 1)][qc], ig1 + og);
+      }
+      if (jpon && lane < 2 * G) {
+        const int tj = t0 + (lane & (G - 1));
+        if (tj < n) {
+          const size_t rj = jbase + jrow0 + (long)tj * jstep;
+          if (lane < G) {
+            if (SOLVE) cpa16(&ws.jp[tj & (IC_D - 1)][0], a.ic_pf + rj + (jlf & ~3));
+          } else {
+            cpa16(&ws.jv[tj & (IC_D - 1)][0], vsrc + rj + (jlf & ~1));
+          }
+        }
+      }
       if (KIND == IC_FORWARD && natvec && jon) {
-        const int kk = t - lane;
-        if (kk >= 0 && kk < n && (kk & 3) == 0) cpa16(&ws.rn[lane][kk % IC_RQ], a.r + rowbase + kk);
-      }
-      if (rho == 0 && ipon) {
-        if (KIND != IC_FACTOR && lane < 8)
-          cpa16(&sm.ip[slot][4 * lane], a.ic_pf + ibase + (size_t)r * 32 + 4 * lane);
-        if (lane >= 8 && lane < 24)
-          cpa16(&sm.iv[slot][2 * (lane - 8)], vsrc + ibase + (size_t)r * 32 + 2 * (lane - 8));
-      }
-      if (jpon && t < n) {
-        const size_t rj = jbase + (size_t)(MIR ? n - 1 - t : t + 31) * 32;
-        if (KIND != IC_FACTOR && lane == 24) cpa16(&ws.jp[slot][0], a.ic_pf + rj + (jlf & ~3));
-        if (lane == 25) cpa16(&ws.jv[slot][0], vsrc + rj + (jlf & ~1));
+        /* the one chunk of 4 cells whose first cell this lane reaches in
+         * the group */
+        const int kc = (t0 + G - 1 - lane) & ~3;
+        if (kc >= 0 && kc < n) cpa16(&ws.rn[lane][kc & (IC_RQ - 1)], r_row + kc);
       }
     }
     cpa_commit();
   };
 
 #pragma unroll 1
-  for (int t = 0; t < IC_D; t++) prefetch(t);
+  for (int g = 0; g < GD; g++) prefetch(g);
   float2 last = make_float2(0.0f, 0.0f);
   float4 zq = make_float4(0.0f, 0.0f, 0.0f, 0.0f); /* backward: z of k .. k+3 */
-  int seen_prev = 0, seen_next = 0;
-  const int *prev_prog = rho > 0 ? &sm.prog[rho - 1] : &sm.prog[0];
-  const int *next_prog = rho + 1 < IC_W ? &sm.prog[rho + 1] : &sm.prog[0];
   const IcWarp &wprev = sm.w[rho > 0 ? rho - 1 : 0];
+  const int rprev = rho > 0 ? rho - 1 : 0;
+  /* this lane's output word and factor at step 0 (valid steps only) */
+  unsigned long long *out = vdst + lbase + row0 + lf;
+  float *pf_out = a.ic_pf + lbase + row0 + lf;
+  const int ngroups = (sl + G - 1) / G;
 #pragma unroll 1
-  for (int s = 0; s < sl; s++) {
-    /* step s's copies have landed (issued IC_D steps ago) */
-    cpa_wait<IC_D - 1>();
+  for (int g = 0; g < ngroups; g++) {
+    /* the group's copies have landed (issued IC_D steps ago) */
+    cpa_wait<GD - 1>();
     __syncwarp();
-    const int slot = s % IC_D, srow = MIR ? n + 30 - s : s;
-    const int kk = s - lane;
-    const bool valid = jon && kk >= 0 && kk < n;
-    const int k = MIR ? n - 1 - kk : kk;
-    /* i-neighbour at this step */
-    float pi = 0.0f, vi = 0.0f;
-    if (ipon) {
-      if (rho > 0) {
-        if (seen_prev <= s) seen_prev = ic_wait_prog(prev_prog, s + 1, a.iflags);
-        const float2 e = wprev.ring[s % IC_RING][lane];
-        pi = e.x;
-        vi = e.y;
-      } else if (valid) {
-        unsigned long long w = sm.iv[slot][lf];
-        if (ic_tagof(w) != tag) w = ic_poll(vsrc + ibase + (size_t)srow * 32 + lf, w, tag, a.iflags);
-        if (KIND == IC_FACTOR) {
-          pi = ic_val(w);
-        } else {
-          pi = sm.ip[slot][lf];
-          vi = ic_val(w);
-        }
-      }
-    }
-    /* j-neighbour: lane l-1's previous step; lane 0: the neighbouring line */
-    float pj = __shfl_up_sync(FULL, last.x, 1), vj = __shfl_up_sync(FULL, last.y, 1);
-    if (lane == 0) {
-      pj = vj = 0.0f;
-      if (jpon && valid) {
-        unsigned long long w = ws.jv[slot][jlf & 1];
-        if (ic_tagof(w) != tag)
-          w = ic_poll(vsrc + jbase + (size_t)(MIR ? n - 1 - s : s + 31) * 32 + jlf, w, tag,
-                      a.iflags);
-        if (KIND == IC_FACTOR) {
-          pj = ic_val(w);
-        } else {
-          pj = ws.jp[slot][jlf & 3];
-          vj = ic_val(w);
-        }
-      }
-    }
-    /* k-neighbour: this lane's previous step */
-    const float pk = last.x, vk = last.y;
-    float p = 0.0f, v = 0.0f;
-    if (valid) {
-      const size_t c = rowbase + k;
-      if (KIND == IC_FACTOR) {
-        const unsigned cf = __ldg(a.ic_cf + c);
-        if (cf & 1u) {
-          const float diag = __ldg(a.diag + c);
-          float ev = diag;
-          const float pm[3] = {pi, pj, pk};
 #pragma unroll
-          for (int ax = 0; ax < 3; ax++) {
-            if (pm[ax] == 0.0f) continue;
-            ev -= pm[ax] * pm[ax];
-            if (tau != 0.0f) ev -= tau * (float)((cf >> (1 + 2 * ax)) & 3u) * pm[ax] * pm[ax];
-          }
-          if (ev < 0.25f * diag) ev = diag;
-          p = 1.0f / sqrtf(ev);
-        }
-      } else {
-        p = ws.pf[slot][lf];
-        if (KIND == IC_FORWARD) {
-          if (p != 0.0f) {
-            float t = natvec ? ws.rn[lane][kk % IC_RQ] : __ldcg(a.r + c);
-            if (pi != 0.0f) t += pi * vi;
-            if (pj != 0.0f) t += pj * vj;
-            if (pk != 0.0f) t += pk * vk;
-            v = t * p;
-            ff_add_prod(qq, v, v);
-          }
-        } else {
-          unsigned long long w = ws.qv[slot][lf];
-          if (ic_tagof(w) != tagq)
-            w = ic_poll(a.ic_qsk + lbase + (size_t)srow * 32 + lf, w, tagq, a.iflags);
-          if (p != 0.0f) {
-            float t = 0.0f;
-            if (pi != 0.0f) t += vi;
-            if (pj != 0.0f) t += vj;
-            if (pk != 0.0f) t += vk;
-            v = (ic_val(w) + p * t) * p;
+    for (int u = 0; u < G; u++) {
+      const int s = G * g + u;
+      if (s >= sl) break;
+      const int slot = s & (IC_D - 1);
+      const int kk = s - lane;
+      const bool valid = jon && kk >= 0 && kk < n;
+      const int k = MIR ? n - 1 - kk : kk;
+      const long os = (long)s * dstep;
+      /* i-neighbour at this step */
+      float pi = 0.0f, vi = 0.0f;
+      if (ipon) {
+        if (rho > 0) {
+          /* the previous warp's step s; hand the slot back */
+          icb_wait(&sm.full[rprev][s & (IC_RING - 1)], (unsigned)(s / IC_RING) & 1u, a.iflags);
+          const float2 e = wprev.ring[s & (IC_RING - 1)][lane];
+          icb_arrive(&sm.empty[rprev][s & (IC_RING - 1)]);
+          pi = e.x;
+          vi = e.y;
+        } else if (valid) {
+          /* a copy taken before its producer wrote it: read it again */
+          unsigned long long wi = sm.iv[slot][lf];
+          if (ic_tagof(wi) != tag) wi = ic_poll(vsrc + ibase + row0 + os + lf, wi, tag, a.iflags);
+          if (KIND == IC_FACTOR) {
+            pi = ic_val(wi);
+          } else {
+            pi = sm.ip[slot][lf];
+            vi = ic_val(wi);
           }
         }
       }
-      const size_t o = lbase + (size_t)srow * 32 + lf;
-      if (KIND == IC_FACTOR) {
-        a.ic_pf[o] = p;
-        st_u64(vdst + o, ic_word(p, tag));
-      } else {
-        st_u64(vdst + o, ic_word(v, tag));
-      }
-      if (KIND == IC_BACKWARD) {
-        if (natvec) {
-          zq = make_float4(v, zq.x, zq.y, zq.z);
-          if ((k & 3) == 0) *reinterpret_cast<float4 *>(a.z + c) = zq;
-        } else {
-          a.z[c] = v;
+      /* j-neighbour: lane l-1's previous step; lane 0: the neighbouring line */
+      float pj = __shfl_up_sync(FULL, last.x, 1), vj = __shfl_up_sync(FULL, last.y, 1);
+      if (lane == 0) {
+        pj = vj = 0.0f;
+        if (jpon && valid) {
+          unsigned long long wj = ws.jv[slot][jlf & 1];
+          if (ic_tagof(wj) != tag)
+            wj = ic_poll(vsrc + jbase + jrow0 + (long)s * jstep + jlf, wj, tag, a.iflags);
+          if (KIND == IC_FACTOR) {
+            pj = ic_val(wj);
+          } else {
+            pj = ws.jp[slot][jlf & 3];
+            vj = ic_val(wj);
+          }
         }
+      }
+      /* k-neighbour: this lane's previous step */
+      const float pk = last.x, vk = last.y;
+      float p = 0.0f, v = 0.0f;
+      if (valid) {
+        const size_t c = rowbase + k;
+        if (KIND == IC_FACTOR) {
+          const unsigned cf = __ldg(a.ic_cf + c);
+          if (cf & 1u) {
+            const float diag = __ldg(a.diag + c);
+            float ev = diag;
+            const float pm[3] = {pi, pj, pk};
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) {
+              if (pm[ax] == 0.0f) continue;
+              ev -= pm[ax] * pm[ax];
+              if (tau != 0.0f) ev -= tau * (float)((cf >> (1 + 2 * ax)) & 3u) * pm[ax] * pm[ax];
+            }
+            if (ev < 0.25f * diag) ev = diag;
+            p = 1.0f / sqrtf(ev);
+          }
+          pf_out[os] = p;
+          out[os] = ic_word(p, tag);
+        } else {
+          p = ws.pf[slot][lf];
+          if (KIND == IC_FORWARD) {
+            if (p != 0.0f) {
+              float t = natvec ? ws.rn[lane][kk & (IC_RQ - 1)] : __ldcg(a.r + c);
+              if (pi != 0.0f) t += pi * vi;
+              if (pj != 0.0f) t += pj * vj;
+              if (pk != 0.0f) t += pk * vk;
+              v = t * p;
+              ff_add_prod(qq, v, v);
+            }
+          } else {
+            unsigned long long wq = ws.qv[slot][lf];
+            if (ic_tagof(wq) != tagq)
+              wq = ic_poll(a.ic_qsk + lbase + row0 + os + lf, wq, tagq, a.iflags);
+            if (p != 0.0f) {
+              float t = 0.0f;
+              if (pi != 0.0f) t += vi;
+              if (pj != 0.0f) t += vj;
+              if (pk != 0.0f) t += vk;
+              v = (ic_val(wq) + p * t) * p;
+            }
+            if (natvec) {
+              zq = make_float4(v, zq.x, zq.y, zq.z);
+              if ((k & 3) == 0) *reinterpret_cast<float4 *>(a.z + c) = zq;
+            } else {
+              a.z[c] = v;
+            }
+          }
+          out[os] = ic_word(v, tag);
+        }
+      }
+      last = valid ? make_float2(p, v) : make_float2(0.0f, 0.0f);
+      if (cons) {
+        /* the slot's previous value (step s - IC_RING) has been taken */
+        if (s >= IC_RING)
+          icb_wait(&sm.empty[rho][s & (IC_RING - 1)], (unsigned)(s / IC_RING - 1) & 1u, a.iflags);
+        ws.ring[s & (IC_RING - 1)][lane] = last;
+        icb_arrive(&sm.full[rho][s & (IC_RING - 1)]);
       }
     }
-    last = valid ? make_float2(p, v) : make_float2(0.0f, 0.0f);
-    if (cons) {
-      /* the slot's previous value (step s - IC_RING) has been taken */
-      if (seen_next < s - IC_RING + 1)
-        seen_next = ic_wait_prog(next_prog, s - IC_RING + 1, a.iflags);
-      ws.ring[s % IC_RING][lane] = last;
-    }
-    /* steps done: what the next warp may read, and what the previous warp
-     * may overwrite */
-    __threadfence_block();
+    /* every lane has read the group's slots: refill them IC_D steps ahead */
     __syncwarp();
-    if (lane == 0) *(volatile int *)&sm.prog[rho] = s + 1;
-    /* every lane has read this step's slots: refill them for step s + IC_D */
-    __syncwarp();
-    prefetch(s + IC_D);
+    prefetch(g + GD);
   }
   cpa_wait<0>();
   __syncwarp();
@@ -2492,7 +2560,9 @@ __device__ void ic_line(const CgArgs &a, IcSmem &sm, int I, int jb, unsigned tag
 template <int KIND>
 __device__ void ic_task(const CgArgs &a, IcSmem &sm, int task, unsigned tag, unsigned tagq) {
   const int I = task / a.ic_njb, jb = task - I * a.ic_njb;
-  if (threadIdx.x < IC_W) sm.prog[threadIdx.x] = 0;
+  unsigned long long *bars = &sm.full[0][0];
+  constexpr int NB = 2 * IC_W * IC_RING; /* full then empty, contiguous */
+  for (int b = threadIdx.x; b < NB; b += CG_BLOCK) icb_init(bars + b, 32);
   __syncthreads();
   FF qq = ff_zero();
   ic_line<KIND>(a, sm, I, jb, tag, tagq, qq);
@@ -2501,6 +2571,8 @@ __device__ void ic_task(const CgArgs &a, IcSmem &sm, int task, unsigned tag, uns
     if ((threadIdx.x & 31) == 0) sm.part[threadIdx.x >> 5] = qq;
   }
   __syncthreads();
+  /* the next task initialises them afresh */
+  for (int b = threadIdx.x; b < NB; b += CG_BLOCK) icb_inval(bars + b);
   if (KIND == IC_FORWARD && threadIdx.x == 0) {
     FF t = sm.part[0];
     for (int w = 1; w < IC_W; w++) t = ff_merge(t, sm.part[w]);
@@ -2569,7 +2641,7 @@ __global__ void __launch_bounds__(BLK) k_ic_prep(int n, int njb, const uint8_t *
 }
 
 /* FAST-mode PCG with the wavefront IC(0)/MIC(0) preconditioner. */
-__global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
+__global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_ic(CgArgs a) {
   if (ir_skipped(a)) return;
   extern __shared__ __align__(16) unsigned char dyn[];
   IcSmem &sm = *reinterpret_cast<IcSmem *>(dyn);
@@ -2594,9 +2666,12 @@ __global__ void __launch_bounds__(CG_BLOCK) k_cg_ic(CgArgs a) {
     if (!grid_barrier(a.bar, a.iflags)) return leave();
   }
 
-  /* factor */
-  ic_sweeps(a, sm, true, base + 1u, 0u);
-  if (!grid_barrier(a.bar, a.iflags, a.ticket)) return leave();
+  /* factor (the refinement's later passes keep the first pass's: A and
+   * the diagonal are fixed during a solve) */
+  if (a.ic_factor) {
+    ic_sweeps(a, sm, true, base + 1u, 0u);
+    if (!grid_barrier(a.bar, a.iflags, a.ticket)) return leave();
+  }
 
   /* r = b - A x; b.b, r.r */
   FF pbb = ff_zero(), prr = ff_zero();
@@ -3267,6 +3342,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     a.ic_zsk = h->ic_zsk;
     a.ic_part = h->ic_part;
     a.ic_ctr = h->ic_ctr;
+    a.ic_factor = 1;
     cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), S);
     void *kargs[] = {&a};
     const void *kern = mode == FLIPGPU_SOLVE_REF ? (const void *)k_cg<FLIPGPU_SOLVE_REF>
@@ -3402,6 +3478,7 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       FG_LAUNCHED(h, 2);
       for (int pass = 0; pass < passes; pass++) {
         if (pass > 0) reset_flags();
+        a.ic_factor = pass == 0;
         cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
         FG_LAUNCHED(h, 1);
         if (e != cudaSuccess) {
