@@ -462,7 +462,11 @@ def run_reference(args):
                       "solver": "the reference's PCG (its preconditioner, FP32 x), relative "
                                 "tolerance 1e-6 on its recursive residual",
                       "time_caps_s": {"warmup": REF_WARMUP_CAP_S, "timed": REF_TIMED_CAP_S},
-                      "capped": capped},
+                      "capped": capped,
+                      "note": "the reference's own method: the GPU arm solves with multigrid "
+                              "PCG refined to a true relative residual of 1e-6 and FAST "
+                              "gathers, so a ratio of the two arms includes that change of "
+                              "method"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                             "sample": f"{warm} warm-up + {steps} timed full steps of "
                                       f"{args.scene} N={args.n} ({sc.count} particles), "
@@ -591,6 +595,9 @@ def main():
     peak, peak_kind = hbm_peak()
     achieved = nbytes / (dom_ms / 1e3) / 1e9
     traffic, traffic_src = measured_traffic(dom, args.n, P)
+    if dom == "solve" and args.precond != "mg":
+        # the solve's captures are of the multigrid solve
+        traffic, traffic_src = None, None
 
     # end to end through the C ABI with pinned host buffers: every step
     # uploads the particle state, steps and downloads it (flipgpu_step_host,
