@@ -268,6 +268,13 @@ cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out,
 cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
                                uint32_t *tmp, size_t tmp_blocks);
 size_t scan_tmp_blocks(size_t n);
+/* the same over the first *nlive + 1 entries only (a count on the device) */
+cudaError_t scan_exclusive_live(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
+                                const int *nlive);
+/* ordered compactions: idx = ascending indices of the set particle flags /
+ * of the deep-water cells, *count their number (device) */
+cudaError_t compact_flags(FlipGpu *h, const uint8_t *flag, size_t n, uint32_t *idx, int *count);
+cudaError_t compact_deep_water(FlipGpu *h, uint32_t *idx, int *count);
 
 /* learned warm start (k_unet.cu): x0 += g*d before CG; out3 = {r0.r0 of
  * the previous-step guess, of the new guess, g} */

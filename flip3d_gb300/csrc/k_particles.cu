@@ -416,35 +416,11 @@ k_flip_advect(SimConst c, float *__restrict__ px, float *__restrict__ py, float 
 
 /* Deep-water cells: FLUID with every in-range face neighbour FLUID
  * (src/flip3D.cpp:412-421). */
-__global__ void k_deep_water(int n, const uint8_t *__restrict__ A, uint32_t *__restrict__ flag) {
-  size_t cidx = (size_t)blockIdx.x * BLK + threadIdx.x;
-  size_t nc = (size_t)n * n * n;
-  if (cidx >= nc) return;
-  int i, j, k;
-  decode_index(cidx, n, n, i, j, k);
-  uint32_t ok = A[cidx] == CELL_FLUID;
-  if (ok && i > 0 && A[cell_id(n, i - 1, j, k)] != CELL_FLUID) ok = 0;
-  if (ok && i < n - 1 && A[cell_id(n, i + 1, j, k)] != CELL_FLUID) ok = 0;
-  if (ok && j > 0 && A[cell_id(n, i, j - 1, k)] != CELL_FLUID) ok = 0;
-  if (ok && j < n - 1 && A[cell_id(n, i, j + 1, k)] != CELL_FLUID) ok = 0;
-  if (ok && k > 0 && A[cell_id(n, i, j, k - 1)] != CELL_FLUID) ok = 0;
-  if (ok && k < n - 1 && A[cell_id(n, i, j, k + 1)] != CELL_FLUID) ok = 0;
-  flag[cidx] = ok;
-}
-
-__global__ void k_u8_to_u32(size_t n, const uint8_t *__restrict__ in, uint32_t *__restrict__ out) {
-  size_t i = (size_t)blockIdx.x * BLK + threadIdx.x;
-  if (i < n) out[i] = in[i];
-}
-
-/* Stable compaction: idx[offset[i]] = i where flag[i]; count in *count. */
-__global__ void k_compact(size_t n, const uint32_t *__restrict__ flag,
-                          const uint32_t *__restrict__ offset, uint32_t *__restrict__ idx,
-                          int *__restrict__ count) {
-  size_t i = (size_t)blockIdx.x * BLK + threadIdx.x;
-  if (i >= n) return;
-  if (flag[i]) idx[offset[i]] = (uint32_t)i;
-  if (i == n - 1) *count = (int)(offset[i] + flag[i]);
+/* cnt[0 .. m] = 0 for the m stuck particles (the shuffle's live counts) */
+__global__ void k_zero_live(const int *__restrict__ m, uint32_t *__restrict__ cnt) {
+  const int e = *m;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= e; q += gridDim.x * blockDim.x)
+    cnt[q] = 0u;
 }
 
 /* reposition (src/flip3D.cpp:405-441): the first m deep-water cells in cell
@@ -1288,27 +1264,20 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
     if (stuck_host) *stuck_host = 0;
     return cudaSuccess;
   }
-  {
-    k_u8_to_u32<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, h->flag, h->scan_a);
-    FG_LAUNCHED(h, 1);
-    if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->np)) != cudaSuccess) return e;
-    k_compact<<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(h->np, h->scan_a, h->scan_b,
-                                                           h->stuck_idx, h->iflags + IF_NSTUCK);
-    FG_LAUNCHED(h, 1);
-  }
-  k_deep_water<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->n, h->A, h->scan_a);
-  FG_LAUNCHED(h, 1);
-  if ((e = scan_exclusive(h, h->scan_a, h->scan_b, h->nc)) != cudaSuccess) return e;
-  k_compact<<<grid_for(h->nc, BLK), BLK, 0, h->stream>>>(h->nc, h->scan_a, h->scan_b,
-                                                         h->water_idx, h->iflags + IF_NWATER);
-  /* my_rand_shuffle: draws, lists of the steps per position, chains */
+  /* the stuck particles and the deep-water cells, each in ascending order */
+  if ((e = compact_flags(h, h->flag, h->np, h->stuck_idx, h->iflags + IF_NSTUCK)) != cudaSuccess)
+    return e;
+  if ((e = compact_deep_water(h, h->water_idx, h->iflags + IF_NWATER)) != cudaSuccess) return e;
+  /* my_rand_shuffle: draws, lists of the steps per position, chains (over
+   * the m stuck particles only) */
   {
     const size_t np1 = (size_t)h->np + 1;
-    if ((e = cudaMemsetAsync(h->repo_cnt, 0, np1 * sizeof(uint32_t), h->stream)) != cudaSuccess)
-      return e;
+    k_zero_live<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags + IF_NSTUCK, h->repo_cnt);
     k_shuffle_draws<<<REPO_GRID, BLK, 0, h->stream>>>(c, h->iflags, h->repo_draw, h->repo_cnt);
-    FG_LAUNCHED(h, 1);
-    if ((e = scan_exclusive(h, h->repo_cnt, h->repo_start, np1)) != cudaSuccess) return e;
+    FG_LAUNCHED(h, 2);
+    if ((e = scan_exclusive_live(h, h->repo_cnt, h->repo_start, np1, h->iflags + IF_NSTUCK)) !=
+        cudaSuccess)
+      return e;
     k_shuffle_fill<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->repo_draw, h->repo_start,
                                                      h->repo_cnt, h->repo_list);
     k_shuffle_sort<<<REPO_GRID, BLK, 0, h->stream>>>(h->iflags, h->repo_start, h->repo_list);

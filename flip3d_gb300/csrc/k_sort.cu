@@ -48,8 +48,21 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t &t
   return warp_off + x - v;
 }
 
+/* nlive (optional): only the first *nlive + 1 entries are scanned; the
+ * tiles past them write a zero block sum and nothing else. */
+__device__ __forceinline__ size_t scan_len(size_t n, const int *nlive) {
+  if (!nlive) return n;
+  const size_t m = (size_t)max(*nlive, 0) + 1;
+  return m < n ? m : n;
+}
+
 __global__ void k_scan_reduce(const uint32_t *__restrict__ in, size_t n,
-                              uint32_t *__restrict__ bsum) {
+                              uint32_t *__restrict__ bsum, const int *__restrict__ nlive) {
+  n = scan_len(n, nlive);
+  if ((size_t)blockIdx.x * SCAN_TILE >= n) {
+    if (threadIdx.x == 0) bsum[blockIdx.x] = 0u;
+    return;
+  }
   size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
   uint32_t s = 0;
 #pragma unroll
@@ -73,7 +86,10 @@ __global__ void k_scan_spine(uint32_t *__restrict__ bsum, size_t nb) {
 }
 
 __global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
-                            size_t n, const uint32_t *__restrict__ bsum) {
+                            size_t n, const uint32_t *__restrict__ bsum,
+                            const int *__restrict__ nlive) {
+  n = scan_len(n, nlive);
+  if ((size_t)blockIdx.x * SCAN_TILE >= n) return;
   size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
   uint32_t v[SCAN_ITEMS];
   uint32_t s = 0;
@@ -219,16 +235,107 @@ __global__ void k_payload_vel(SimConst c, int apply_gravity, const uint32_t *__r
   svel[a] = make_float4(ux, uy, uz, 0.0f);
 }
 
+/* Ordered compaction over tiles of SCAN_TILE: count each tile's selected
+ * elements, scan the tile counts (k_scan_spine), then each tile writes its
+ * selected indices in ascending order at its offset. Reads the predicate's
+ * inputs twice and writes only the list. */
+template <class Pred>
+__global__ void k_cmp_count(size_t n, Pred pred, uint32_t *__restrict__ tile_cnt) {
+  const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++)
+    if (base + i < n && pred(base + i)) s++;
+  const uint32_t tot = block_sum_u32<SCAN_BLOCK>(s);
+  if (threadIdx.x == 0) tile_cnt[blockIdx.x] = tot;
+}
+
+template <class Pred>
+__global__ void k_cmp_write(size_t n, Pred pred, const uint32_t *__restrict__ tile_off,
+                            uint32_t *__restrict__ idx, int *__restrict__ count) {
+  const size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  uint32_t bits = 0, s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++)
+    if (base + i < n && pred(base + i)) {
+      bits |= 1u << i;
+      s++;
+    }
+  uint32_t tot;
+  uint32_t off = block_exclusive_scan(s, tot) + tile_off[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++)
+    if (bits & (1u << i)) idx[off++] = (uint32_t)(base + i);
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *count = (int)(tile_off[blockIdx.x] + tot);
+}
+
+/* a particle flag set */
+struct PredFlag {
+  const uint8_t *f;
+  __device__ __forceinline__ bool operator()(size_t i) const { return f[i] != 0; }
+};
+
+/* a deep-water cell: FLUID with its six in-grid neighbours FLUID
+ * (src/flip3D.cpp:409-421) */
+struct PredDeepWater {
+  int n;
+  const uint8_t *A;
+  __device__ __forceinline__ bool operator()(size_t c) const {
+    if (A[c] != CELL_FLUID) return false;
+    int i, j, k;
+    decode_index(c, n, n, i, j, k);
+    if (i > 0 && A[cell_id(n, i - 1, j, k)] != CELL_FLUID) return false;
+    if (i < n - 1 && A[cell_id(n, i + 1, j, k)] != CELL_FLUID) return false;
+    if (j > 0 && A[cell_id(n, i, j - 1, k)] != CELL_FLUID) return false;
+    if (j < n - 1 && A[cell_id(n, i, j + 1, k)] != CELL_FLUID) return false;
+    if (k > 0 && A[cell_id(n, i, j, k - 1)] != CELL_FLUID) return false;
+    if (k < n - 1 && A[cell_id(n, i, j, k + 1)] != CELL_FLUID) return false;
+    return true;
+  }
+};
+
+template <class Pred>
+cudaError_t compact(FlipGpu *h, size_t n, Pred pred, uint32_t *idx, int *count) {
+  if (n == 0) return cudaMemsetAsync(count, 0, sizeof(int), h->stream);
+  const size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb > h->scan_cap) return cudaErrorInvalidValue;
+  k_cmp_count<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(n, pred, h->scan_tmp);
+  k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(h->scan_tmp, nb);
+  k_cmp_write<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(n, pred, h->scan_tmp, idx, count);
+  FG_LAUNCHED(h, 3);
+  return cudaGetLastError();
+}
+
 } // namespace
+
+cudaError_t compact_flags(FlipGpu *h, const uint8_t *flag, size_t n, uint32_t *idx, int *count) {
+  return compact(h, n, PredFlag{flag}, idx, count);
+}
+
+cudaError_t compact_deep_water(FlipGpu *h, uint32_t *idx, int *count) {
+  return compact(h, h->nc, PredDeepWater{h->n, h->A}, idx, count);
+}
+
+cudaError_t scan_exclusive_live(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
+                                const int *nlive) {
+  if (n == 0) return cudaSuccess;
+  size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (nb > h->scan_cap) return cudaErrorInvalidValue;
+  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, h->scan_tmp, nlive);
+  k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(h->scan_tmp, nb);
+  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, h->scan_tmp, nlive);
+  FG_LAUNCHED(h, 3);
+  return cudaGetLastError();
+}
 
 cudaError_t scan_exclusive_tmp(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t n,
                                uint32_t *tmp, size_t tmp_blocks) {
   if (n == 0) return cudaSuccess;
   size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
   if (nb > tmp_blocks) return cudaErrorInvalidValue;
-  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, tmp);
+  k_scan_reduce<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, n, tmp, nullptr);
   k_scan_spine<<<1, SCAN_BLOCK, 0, h->stream>>>(tmp, nb);
-  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, tmp);
+  k_scan_down<<<(unsigned)nb, SCAN_BLOCK, 0, h->stream>>>(in, out, n, tmp, nullptr);
   FG_LAUNCHED(h, 3);
   return cudaGetLastError();
 }
