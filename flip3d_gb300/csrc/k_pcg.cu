@@ -596,10 +596,11 @@ __device__ __forceinline__ bool count_barrier(unsigned *bar, unsigned &epoch, in
 
 /* Sums of the nb float-pair partials of slots k0 and k1 (k1 < 0: none),
  * identical in every block: strided loads, then a fixed merge tree. */
+template <int BLOCK = CG_BLOCK>
 __device__ __forceinline__ void sum_partials(const float2 *part, int k0, int k1, unsigned nb,
                                              double &out0, double &out1) {
   FF v0 = ff_zero(), v1 = ff_zero();
-  for (unsigned i = threadIdx.x; i < nb; i += CG_BLOCK) {
+  for (unsigned i = threadIdx.x; i < nb; i += BLOCK) {
     float2 a = __ldcg(part + (size_t)k0 * nb + i);
     v0 = ff_merge(v0, FF{a.x, a.y});
     if (k1 >= 0) {
@@ -607,8 +608,8 @@ __device__ __forceinline__ void sum_partials(const float2 *part, int k0, int k1,
       v1 = ff_merge(v1, FF{b.x, b.y});
     }
   }
-  out0 = ff_to_double(block_sum_ff<CG_BLOCK>(v0));
-  out1 = k1 >= 0 ? ff_to_double(block_sum_ff<CG_BLOCK>(v1)) : 0.0;
+  out0 = ff_to_double(block_sum_ff<BLOCK>(v0));
+  out1 = k1 >= 0 ? ff_to_double(block_sum_ff<BLOCK>(v1)) : 0.0;
 }
 
 /* Dot-product term: REF mode sums the float-rounded product, as
@@ -620,8 +621,9 @@ template <int MODE> __device__ __forceinline__ void dot_acc(FF &acc, float x, fl
     ff_add_prod(acc, x, y);
 }
 
+template <int BLOCK = CG_BLOCK>
 __device__ __forceinline__ void store_partial(float2 *part, int k, unsigned nb, FF v) {
-  FF t = block_sum_ff<CG_BLOCK>(v);
+  FF t = block_sum_ff<BLOCK>(v);
   if (threadIdx.x == 0) part[(size_t)k * nb + blockIdx.x] = make_float2(t.hi, t.lo);
 }
 
@@ -2198,7 +2200,8 @@ __global__ void __launch_bounds__(BLK) k_mg_diag(const uint8_t *__restrict__ cf,
  * order as the sequential sweeps (neighbours i, j, k in that order), so the
  * tiling does not change a value. The preconditioned residual's dot z.r
  * equals q.q for z = L^-T q, q = L^-1 r: it is summed in the forward solve. */
-constexpr int IC_W = CG_BLOCK / 32;
+constexpr int IC_BLOCK = 512;         /* threads of the IC kernel: 16 lines per task */
+constexpr int IC_W = IC_BLOCK / 32;
 constexpr int IC_D = 16;
 constexpr int IC_RING = 8;
 constexpr int IC_RQ = 32;
@@ -2562,7 +2565,7 @@ __device__ void ic_task(const CgArgs &a, IcSmem &sm, int task, unsigned tag, uns
   const int I = task / a.ic_njb, jb = task - I * a.ic_njb;
   unsigned long long *bars = &sm.full[0][0];
   constexpr int NB = 2 * IC_W * IC_RING; /* full then empty, contiguous */
-  for (int b = threadIdx.x; b < NB; b += CG_BLOCK) icb_init(bars + b, 32);
+  for (int b = threadIdx.x; b < NB; b += IC_BLOCK) icb_init(bars + b, 32);
   __syncthreads();
   FF qq = ff_zero();
   ic_line<KIND>(a, sm, I, jb, tag, tagq, qq);
@@ -2572,7 +2575,7 @@ __device__ void ic_task(const CgArgs &a, IcSmem &sm, int task, unsigned tag, uns
   }
   __syncthreads();
   /* the next task initialises them afresh */
-  for (int b = threadIdx.x; b < NB; b += CG_BLOCK) icb_inval(bars + b);
+  for (int b = threadIdx.x; b < NB; b += IC_BLOCK) icb_inval(bars + b);
   if (KIND == IC_FORWARD && threadIdx.x == 0) {
     FF t = sm.part[0];
     for (int w = 1; w < IC_W; w++) t = ff_merge(t, sm.part[w]);
@@ -2607,11 +2610,11 @@ __device__ void ic_sweeps(const CgArgs &a, IcSmem &sm, bool factor, unsigned tag
 /* z.r (as q.q) from the per-task partials in task order (identical in every block). */
 __device__ __forceinline__ double ic_sum_parts(const CgArgs &a) {
   FF v = ff_zero();
-  for (int b = threadIdx.x; b < a.ic_tasks; b += CG_BLOCK) {
+  for (int b = threadIdx.x; b < a.ic_tasks; b += IC_BLOCK) {
     const float2 p = __ldcg(a.ic_part + b);
     v = ff_merge(v, FF{p.x, p.y});
   }
-  return ff_to_double(block_sum_ff<CG_BLOCK>(v));
+  return ff_to_double(block_sum_ff<IC_BLOCK>(v));
 }
 
 /* Per cell: bit 0 liquid; bits 1-2, 3-4, 5-6: how many of the -x, -y, -z
@@ -2641,13 +2644,13 @@ __global__ void __launch_bounds__(BLK) k_ic_prep(int n, int njb, const uint8_t *
 }
 
 /* FAST-mode PCG with the wavefront IC(0)/MIC(0) preconditioner. */
-__global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_ic(CgArgs a) {
+__global__ void __launch_bounds__(IC_BLOCK, 1) k_cg_ic(CgArgs a) {
   if (ir_skipped(a)) return;
   extern __shared__ __align__(16) unsigned char dyn[];
   IcSmem &sm = *reinterpret_cast<IcSmem *>(dyn);
   const unsigned nb = gridDim.x;
-  const size_t stride = (size_t)nb * CG_BLOCK;
-  const size_t t0 = (size_t)blockIdx.x * CG_BLOCK + threadIdx.x;
+  const size_t stride = (size_t)nb * IC_BLOCK;
+  const size_t t0 = (size_t)blockIdx.x * IC_BLOCK + threadIdx.x;
   const int n = a.s.n;
   const size_t nc = a.nc;
   constexpr int M = FLIPGPU_SOLVE_FAST;
@@ -2690,11 +2693,11 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_ic(CgArgs a) {
     }
     a.r[c] = rv;
   }
-  store_partial(a.part, 0, nb, pbb);
-  store_partial(a.part, 1, nb, prr);
+  store_partial<IC_BLOCK>(a.part, 0, nb, pbb);
+  store_partial<IC_BLOCK>(a.part, 1, nb, prr);
   if (!grid_barrier(a.bar, a.iflags)) return leave();
   double b2, rr, unused;
-  sum_partials(a.part, 0, 1, nb, b2, rr);
+  sum_partials<IC_BLOCK>(a.part, 0, 1, nb, b2, rr);
   const double rt = cg_rel_tol(a);
   const double eps = rt * rt * b2;
   int done = rr <= eps ? 1 : 0, iters = 0;
@@ -2723,10 +2726,10 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_ic(CgArgs a) {
       sn[c] = snv;
       a.w[c] = wv;
     }
-    store_partial(a.part, 3, nb, pws);
+    store_partial<IC_BLOCK>(a.part, 3, nb, pws);
     if (!grid_barrier(a.bar, a.iflags)) return leave();
     double ws;
-    sum_partials(a.part, 3, -1, nb, ws, unused);
+    sum_partials<IC_BLOCK>(a.part, 3, -1, nb, ws, unused);
     if (threadIdx.x == 0) s_bcast = (float)(azr / ws); /* one FP64 division per block */
     __syncthreads();
     const float alpha_f = s_bcast;
@@ -2739,9 +2742,9 @@ __global__ void __launch_bounds__(CG_BLOCK, 2) k_cg_ic(CgArgs a) {
       a.r[c] = rv;
       ff_add_prod(prr2, rv, rv);
     }
-    store_partial(a.part, 4, nb, prr2);
+    store_partial<IC_BLOCK>(a.part, 4, nb, prr2);
     if (!grid_barrier(a.bar, a.iflags)) return leave();
-    sum_partials(a.part, 4, -1, nb, rr, unused);
+    sum_partials<IC_BLOCK>(a.part, 4, -1, nb, rr, unused);
     iters++;
     e2 = rr;
     if (e2 <= eps) { done = 1; break; }
@@ -3101,6 +3104,7 @@ static int cg_block_of(const void *kern) {
   if (kern == (const void *)k_cg_cg1<CG1_BLOCK_SMALL>) return CG1_BLOCK_SMALL;
   if (kern == (const void *)k_cg_cg1<CG1_BLOCK_LARGE>) return CG1_BLOCK_LARGE;
   if (kern == (const void *)k_cg_mg<CG_MG_BLOCK>) return CG_MG_BLOCK;
+  if (kern == (const void *)k_cg_ic) return IC_BLOCK;
   return CG_BLOCK;
 }
 

@@ -470,14 +470,16 @@ def _fast_sim(gpu, sc, seed=3, precond=None):
     return s
 
 
-@pytest.mark.parametrize("mg", [False, True])
-def test_async_and_graph_steps_match_plain_steps(gpu, mg):
+@pytest.mark.parametrize("precond", ["jacobi", "mg", "ic"])
+def test_async_and_graph_steps_match_plain_steps(gpu, precond):
     """flipgpu_step_async and a captured CUDA graph replay compute exactly
     what flipgpu_step computes (the device step counter keys the draws),
-    with the Jacobi and the multigrid persistent solves (the graph is
-    captured before any solve ran, so nothing may allocate inside it)."""
+    with the Jacobi, the multigrid and the IC(0) wavefront persistent solves
+    (the graph is captured before any solve ran, so nothing may allocate
+    inside it; the wavefront's word tags come from a counter on the device,
+    so replays of the same launches never reuse a tag)."""
     sc = scenes.dam_break(32, seed=4)
-    pre = gpu.PRECOND_MG if mg else gpu.PRECOND_JACOBI
+    pre = {"jacobi": gpu.PRECOND_JACOBI, "mg": gpu.PRECOND_MG, "ic": gpu.PRECOND_IC}[precond]
     ref, asy, gra = (_fast_sim(gpu, sc, precond=pre), _fast_sim(gpu, sc, precond=pre),
                      _fast_sim(gpu, sc, precond=pre))
     gra.capture_step()
