@@ -15,9 +15,10 @@ Stated tolerances (each assert below): per-particle positions and
 velocities while the flow is still deterministic at this resolution
 (N=32: steps 1 and 10; N=128: steps 1, 5 and 10), pressure and face
 velocities on the plane (fluid cells), and the fluid's centre of mass and
-kinetic energy at every snapshot, including after 50 and 200 steps at N=32,
-where individual particles have left the FP64 trajectories (the flow is
-chaotic) but the aggregates have not. The errors are printed."""
+kinetic energy at every snapshot, including after 50 and 200 steps at N=32
+and 25 and 50 steps at N=128, where individual particles have left the
+FP64 trajectories (the flow is chaotic) but the aggregates have not. The
+errors are printed."""
 import os
 
 import numpy as np
