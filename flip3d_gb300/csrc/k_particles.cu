@@ -113,6 +113,46 @@ __device__ __forceinline__ void visit_cells(int n, const uint32_t *__restrict__ 
     }
 }
 
+/* visit_cells restricted to a ball of radius sqrt(r2) around (px, py, pz):
+ * rows (si, sj) whose cells lie wholly outside the ball are skipped and
+ * each row's k-range is trimmed to the cells the ball reaches. A cell's
+ * particles lie in its interval [s h, (s+1) h) of each axis, except the
+ * first and last cells, which also hold the clamped particles outside the
+ * grid (their interval is open on that side). Callers pass r2 a little
+ * above their own cut-off (the corrector's reach), so every particle that
+ * passes their exact distance test is visited, in the same order. */
+template <class F>
+__device__ __forceinline__ void visit_ball(int n, float fn, float h, const uint32_t *__restrict__ cs,
+                                           float px, float py, float pz, float r2, int i0, int i1,
+                                           int j0, int j1, int k0, int k1, F f) {
+  i0 = max(i0, 0);
+  i1 = min(i1, n - 1);
+  j0 = max(j0, 0);
+  j1 = min(j1, n - 1);
+  k0 = max(k0, 0);
+  k1 = min(k1, n - 1);
+  if (k0 > k1) return;
+  auto gap = [&](float p, int s) -> float {
+    const float lo = s == 0 ? -INFINITY : (float)s * h;
+    const float hi = s == n - 1 ? INFINITY : (float)(s + 1) * h;
+    return fmaxf(0.0f, fmaxf(lo - p, p - hi));
+  };
+  for (int si = i0; si <= i1; si++) {
+    const float gx = gap(px, si), gx2 = gx * gx;
+    if (gx2 > r2) continue;
+    for (int sj = j0; sj <= j1; sj++) {
+      const float gy = gap(py, sj), g2 = gx2 + gy * gy;
+      if (g2 > r2) continue;
+      const float rem = sqrtf(r2 - g2);
+      const int ka = max(k0, (int)floorf(fn * (pz - rem))), kb = min(k1, (int)floorf(fn * (pz + rem)));
+      if (ka > kb) continue;
+      const size_t base = ((size_t)si * n + sj) * n;
+      const uint32_t s = __ldg(cs + base + ka), e = __ldg(cs + base + kb + 1);
+      for (uint32_t b = s; b < e; b++) f(b);
+    }
+  }
+}
+
 /* linear() (src/mapper.cpp:96-106) with the k clamp of the reference (h-2);
  * k+1 is kept inside the row where the reference reads one past it. */
 __device__ __forceinline__ float linear(const float *__restrict__ q, float x, float y, float z,
@@ -1011,7 +1051,8 @@ k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__r
   reach_range(P.y, c.corr_reach, c.fn, c.n, y, j0, j1);
   reach_range(P.z, c.corr_reach, c.fn, c.n, z, k0, k1);
   float spring[3] = {0.0f, 0.0f, 0.0f};
-  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+  const float reach2 = c.corr_reach * c.corr_reach;
+  visit_ball(c.n, c.fn, c.h, cs, P.x, P.y, P.z, reach2, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     if (b == (uint32_t)a) return;
     const float4 Q = __ldg(spos + b);
     if (AR::hypot2(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
@@ -1061,7 +1102,8 @@ k_resample_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *_
   reach_range(T[2], c.corr_reach, c.fn, c.n, ck, k0, k1);
   float u[3] = {0.0f, 0.0f, 0.0f};
   float wsum = 0.0f;
-  visit_cells(c.n, cs, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+  const float reach2 = c.corr_reach * c.corr_reach;
+  visit_ball(c.n, c.fn, c.h, cs, T[0], T[1], T[2], reach2, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
     const float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) != CELL_FLUID) return;
     const float d2 = AR::hypot2(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
