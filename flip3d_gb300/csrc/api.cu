@@ -1097,6 +1097,24 @@ int flipgpu_set_profiling(FlipGpu *h, int on) {
   return FLIPGPU_OK;
 }
 
+int flipgpu_set_ic_tag_counter(FlipGpu *h, unsigned value) {
+  if (!h) return FLIPGPU_EINVAL;
+  int r = ic_alloc(h);
+  if (r != FLIPGPU_OK) return fail(h, r, "set_ic_tag_counter: wavefront buffers");
+  CK(h, cudaMemcpyAsync(h->ic_ctr, &value, sizeof value, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_ic_tag_counter(FlipGpu *h, unsigned *value) {
+  if (!h || !value) return FLIPGPU_EINVAL;
+  int r = ic_alloc(h);
+  if (r != FLIPGPU_OK) return fail(h, r, "get_ic_tag_counter: wavefront buffers");
+  CK(h, cudaMemcpyAsync(value, h->ic_ctr, sizeof *value, cudaMemcpyDeviceToHost, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
 int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max) {
   if (!h || max < 0) return FLIPGPU_EINVAL;
   for (int i = 0; i < FLIPGPU_NSTAGES && i < max; i++) {

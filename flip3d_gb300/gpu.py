@@ -119,6 +119,8 @@ SIGNATURES = {
     "flipgpu_launch_count": (C.c_int64, [C.c_void_p]),
     "flipgpu_put_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipgpu_set_ic_tag_counter": (C.c_int, [C.c_void_p, C.c_uint]),
+    "flipgpu_get_ic_tag_counter": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "flipgpu_get_profile": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     "flipgpu_sort_cells_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
@@ -458,6 +460,15 @@ class Simulation:
         self._ck(self.lib.flipgpu_resample(self.h, pts.shape[0], _ptr(pts), _ptr(out),
                                            C.c_float(re), 0), "resample")
         return out
+
+    def ic_tag_counter(self, value=None):
+        """The IC wavefront's tag counter (a testing aid): set it when value
+        is given; returns the current value."""
+        if value is not None:
+            self._ck(self.lib.flipgpu_set_ic_tag_counter(self.h, int(value)), "set_ic_tag_counter")
+        out = C.c_uint(0)
+        self._ck(self.lib.flipgpu_get_ic_tag_counter(self.h, C.byref(out)), "get_ic_tag_counter")
+        return out.value
 
     def set_profiling(self, on=True):
         self._ck(self.lib.flipgpu_set_profiling(self.h, int(on)), "set_profiling")

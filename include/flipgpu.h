@@ -393,6 +393,16 @@ int flipgpu_set_profiling(FlipGpu *h, int on);
 /* ms[i] and calls[i] accumulated since profiling was switched on. */
 int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max);
 
+/* Testing aid (no reference counterpart): set the counter from which the
+ * IC(0)/MIC(0) wavefront's solves take the tags of their words (each solve
+ * advances it by two per preconditioner application). A value near the end
+ * of the 32-bit range makes the next solve clear the tagged buffers and
+ * start again at 0, which a test checks gives the same result. Allocates
+ * the wavefront buffers if needed; runs on the handle's stream. */
+int flipgpu_set_ic_tag_counter(FlipGpu *h, unsigned value);
+/* its current value (synchronises) */
+int flipgpu_get_ic_tag_counter(FlipGpu *h, unsigned *value);
+
 /* Cell sort that allocates no device memory. It has no counterpart in the
  * reference. It is for callers that may not allocate on the GPU, such as a
  * plugin inside a host application that owns all device memory, or a frame

@@ -78,3 +78,30 @@ def test_mic_repeats_bit_for_bit_and_refines_at_n128(gpu, orc):
     print(f"N=128 MIC(0): {st.refine_passes} passes, {st.iterations} iterations, "
           f"{st.ms:.2f} ms, true rel-res {rel:.3g}")
     assert rel <= 1e-6, rel
+
+
+def test_tag_counter_wrap_gives_the_same_solve(gpu, orc):
+    """The wavefront's words carry the tag of the sweep that wrote them; the
+    tags come from a 32-bit counter on the device. Near the end of its range
+    a solve clears the tagged buffers and starts again at 0. Solves before,
+    across and after that restart give the same bits, and the counter has
+    restarted."""
+    n = 40
+    A, L, b = system(orc, n)
+    sim = gpu.Simulation(gpu.default_params(n, 1, rel_tol=1e-6, solve_mode=gpu.SOLVE_FAST,
+                                            precond=gpu.PRECOND_IC, mic_tau=0.97,
+                                            refine_steps=2))
+    results = []
+    for start in (None, 0xF0000000 - 6, None, 0xFFFFFF00, None):
+        if start is not None:
+            sim.ic_tag_counter(start)
+        sim.set_grid(A=A, L=L, press=np.zeros(n ** 3, np.float32), div=b)
+        st = sim.solve()
+        assert st.status == 0
+        results.append((sim.get_pressure(), sim.ic_tag_counter()))
+    sim.close()
+    for x, _ in results[1:]:
+        assert np.array_equal(x, results[0][0])
+    # the near-wrap starts were followed by a restart at 0: small counters
+    assert results[1][1] < 0x10000000 or results[2][1] < 0x10000000
+    assert results[3][1] < 0x10000000
