@@ -76,9 +76,13 @@ def run_batch(args):
             s.step()
             s.sync()
     t_seq = time.perf_counter() - t0
-    # together
+    # together, the solves' share of the GPU tuned on the systems of one step
     b = gpu.Batch(sims)
     b.capture()
+    b.step()
+    b.sync()
+    share = b.tune()
+    tuning = [ln for ln in gpu.autotune_report().splitlines() if ln.startswith("batch solve share")]
     clocks = ClockSampler(0)
     clocks.start()
     clocks.wait_first()
@@ -110,6 +114,8 @@ def run_batch(args):
                    "l2": "inputs larger than L2"},
         "one_at_a_time": {"value": P * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},
         "speedup_vs_one_at_a_time": t_seq / t_bat,
+        "solve_share": {"share": share, "grids": [s.solve_blocks() for s in sims],
+                        "tuning": tuning[-1] if tuning else None},
         "gpu_launches": launches, "clocks": clk}))
 
 

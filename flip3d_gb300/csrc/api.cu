@@ -2,6 +2,7 @@
  * api.cu — the C ABI of include/flipgpu.h: handle lifetime, transfers and
  * the orchestration of the per-step stages.
  */
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -10,6 +11,7 @@
 #include <new>
 #include <vector>
 
+#include "autotune.h"
 #include "devcommon.cuh"
 
 namespace {
@@ -1075,6 +1077,159 @@ int flipbatch_step(FlipBatch *b) {
 int flipbatch_sync(FlipBatch *b) {
   if (!b) return FLIPGPU_EINVAL;
   for (FlipGpu *h : b->sims) CK(h, cudaStreamSynchronize(h->stream));
+  return FLIPGPU_OK;
+}
+
+int flipgpu_set_solve_blocks(FlipGpu *h, int blocks) {
+  if (!h || blocks < 0) return FLIPGPU_EINVAL;
+  h->solve_blocks = blocks;
+  return FLIPGPU_OK;
+}
+
+int flipgpu_get_solve_blocks(const FlipGpu *h, int *blocks) {
+  if (!h || !blocks) return FLIPGPU_EINVAL;
+  *blocks = h->solve_blocks;
+  return FLIPGPU_OK;
+}
+
+/* Member i's persistent solve gets max(1, share * C_i * cells_i / cells of
+ * all members) blocks, C_i its solve kernel's co-resident grid: at share 1
+ * the members' solves fit on the GPU side by side. share <= 0 lifts the
+ * caps. Members without a persistent solve (the IC wavefront, no
+ * preconditioner) keep none. */
+static void batch_share(FlipBatch *b, double share) {
+  double cells = 0.0;
+  for (FlipGpu *h : b->sims) cells += (double)h->nc;
+  for (FlipGpu *h : b->sims) {
+    if (share <= 0.0 || h->solve_capacity <= 0) {
+      h->solve_blocks = 0;
+      continue;
+    }
+    const double v = share * h->solve_capacity * (double)h->nc / cells;
+    h->solve_blocks = v < 1.0 ? 1 : (int)std::lround(v);
+  }
+}
+
+/* The tuner's trial: every member solves its current system (the one its
+ * last step solved) on its own stream, all at once, from the saved warm
+ * start. Returns the span in ms, or < 0 on a CUDA error. */
+static float batch_solve_trial(FlipBatch *b, cudaStream_t root, cudaEvent_t t0, cudaEvent_t t1,
+                               const std::vector<cudaEvent_t> &done,
+                               const std::vector<float *> &saved) {
+  for (size_t m = 0; m < b->sims.size(); m++) {
+    FlipGpu *h = b->sims[m];
+    const size_t bytes = (size_t)h->nc * sizeof(float);
+    if (cudaMemcpyAsync(h->press, saved[m], bytes, cudaMemcpyDeviceToDevice, h->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(h->press_lo, saved[m] + h->nc, bytes, cudaMemcpyDeviceToDevice,
+                        h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      return -1.0f;
+  }
+  if (cudaEventRecord(t0, root) != cudaSuccess) return -1.0f;
+  for (size_t m = 0; m < b->sims.size(); m++) {
+    FlipGpu *h = b->sims[m];
+    if (cudaStreamWaitEvent(h->stream, t0, 0) != cudaSuccess) return -1.0f;
+    h->async_mode = 1;
+    const int r = run_solve(h, nullptr);
+    h->async_mode = 0;
+    if (r != FLIPGPU_OK || cudaEventRecord(done[m], h->stream) != cudaSuccess ||
+        cudaStreamWaitEvent(root, done[m], 0) != cudaSuccess)
+      return -1.0f;
+  }
+  float ms = -1.0f;
+  if (cudaEventRecord(t1, root) != cudaSuccess || cudaEventSynchronize(t1) != cudaSuccess ||
+      cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess)
+    return -1.0f;
+  return ms;
+}
+
+int flipbatch_tune(FlipBatch *b, double *share_out) {
+  if (!b) return FLIPGPU_EINVAL;
+  if (share_out) *share_out = 0.0;
+  bool any = false;
+  for (FlipGpu *h : b->sims) {
+    if (h->step == 0)
+      return fail(h, FLIPGPU_EINVAL, "batch_tune: step the batch once before tuning it");
+    any = any || h->solve_capacity > 0;
+  }
+  if (!any) return FLIPGPU_OK;
+  for (FlipGpu *h : b->sims) CK(h, cudaStreamSynchronize(h->stream));
+  FlipGpu *h0 = b->sims[0];
+  const double shares[] = {0.0, 0.5, 1.0, 2.0, 4.0, 8.0, 16.0};
+  const int ns = (int)(sizeof shares / sizeof shares[0]);
+  std::vector<std::string> names;
+  for (int c = 0; c < ns; c++) {
+    char nm[32];
+    snprintf(nm, sizeof nm, c == 0 ? "uncapped" : "share %.1f", shares[c]);
+    names.push_back(nm);
+  }
+  std::vector<float> ms(ns, -1.0f);
+  std::vector<float *> saved(b->sims.size(), nullptr);
+  std::vector<int> lo_valid(b->sims.size(), 0);
+  std::vector<cudaEvent_t> done(b->sims.size(), nullptr);
+  cudaStream_t root = nullptr;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int rc = FLIPGPU_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&root, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&t1);
+  for (size_t m = 0; e == cudaSuccess && m < b->sims.size(); m++) {
+    FlipGpu *h = b->sims[m];
+    e = cudaEventCreateWithFlags(&done[m], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMalloc(&saved[m], 2 * (size_t)h->nc * sizeof(float));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(saved[m], h->press, (size_t)h->nc * sizeof(float), cudaMemcpyDeviceToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(saved[m] + h->nc, h->press_lo, (size_t)h->nc * sizeof(float),
+                     cudaMemcpyDeviceToDevice);
+    lo_valid[m] = h->press_lo_valid;
+  }
+  if (e != cudaSuccess) rc = fail(h0, FLIPGPU_ECUDA, "batch_tune: setup: %s", cudaGetErrorString(e));
+  /* one warm-up trial per candidate, then the median of three */
+  for (int c = 0; rc == FLIPGPU_OK && c < ns; c++) {
+    batch_share(b, shares[c]);
+    float t[4];
+    for (int r = 0; r < 4 && rc == FLIPGPU_OK; r++) {
+      t[r] = batch_solve_trial(b, root, t0, t1, done, saved);
+      if (t[r] < 0.0f) rc = fail(h0, FLIPGPU_ECUDA, "batch_tune: trial solve failed");
+    }
+    if (rc != FLIPGPU_OK) break;
+    std::sort(t + 1, t + 4);
+    ms[c] = t[2];
+  }
+  int best = 0;
+  for (int c = 1; c < ns; c++)
+    if (ms[c] >= 0.0f && (ms[best] < 0.0f || ms[c] < ms[best])) best = c;
+  batch_share(b, rc == FLIPGPU_OK ? shares[best] : 0.0);
+  /* the members' pressure as their last step left it */
+  for (size_t m = 0; m < b->sims.size(); m++) {
+    FlipGpu *h = b->sims[m];
+    if (saved[m]) {
+      const size_t bytes = (size_t)h->nc * sizeof(float);
+      cudaError_t e2 = cudaMemcpy(h->press, saved[m], bytes, cudaMemcpyDeviceToDevice);
+      if (e2 == cudaSuccess)
+        e2 = cudaMemcpy(h->press_lo, saved[m] + h->nc, bytes, cudaMemcpyDeviceToDevice);
+      if (e2 != cudaSuccess && rc == FLIPGPU_OK)
+        rc = fail(h, FLIPGPU_ECUDA, "batch_tune: restore: %s", cudaGetErrorString(e2));
+      cudaFree(saved[m]);
+    }
+    h->press_lo_valid = lo_valid[m];
+    if (done[m]) cudaEventDestroy(done[m]);
+  }
+  if (t0) cudaEventDestroy(t0);
+  if (t1) cudaEventDestroy(t1);
+  if (root) cudaStreamDestroy(root);
+  if (rc != FLIPGPU_OK) return rc;
+  char key[96];
+  double cells = 0.0;
+  for (FlipGpu *h : b->sims) cells += (double)h->nc;
+  snprintf(key, sizeof key, "batch solve share (%zu simulations, %.0f cells)", b->sims.size(),
+           cells);
+  autotune::record(key, names, ms, best);
+  if (share_out) *share_out = shares[best];
+  /* the captured steps hold the old grids */
+  if (b->graphs) return flipbatch_capture(b);
   return FLIPGPU_OK;
 }
 

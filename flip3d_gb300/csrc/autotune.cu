@@ -84,6 +84,16 @@ int choose(const std::string &key, const std::vector<std::string> &names, cudaSt
   return best;
 }
 
+void record(const std::string &key, const std::vector<std::string> &names,
+            const std::vector<float> &ms, int choice) {
+  Decision d;
+  d.names = names;
+  d.ms = ms;
+  d.choice = choice;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_table[key] = d;
+}
+
 } // namespace autotune
 
 extern "C" {

@@ -23,4 +23,9 @@ namespace autotune {
 int choose(const std::string &key, const std::vector<std::string> &names, cudaStream_t st,
            const std::function<cudaError_t(int)> &run);
 
+/* enter a decision timed elsewhere (ms < 0: the candidate failed) so that
+ * flipgpu_autotune_report lists it */
+void record(const std::string &key, const std::vector<std::string> &names,
+            const std::vector<float> &ms, int choice);
+
 } // namespace autotune

@@ -140,6 +140,9 @@ struct FlipGpu {
   int cg_grid[CG_VARIANTS]; /* cooperative CG grids (0 = none): REF, FAST, FAST single-
                                reduction (small blocks), FAST IC, single-reduction (large),
                                FAST MG */
+  int solve_blocks;   /* cap on the persistent solve's grid (0 = none; not the IC
+                         wavefront), so that concurrent simulations' solves share the GPU */
+  int solve_capacity; /* co-resident grid of the last solve's kernel */
   unsigned *ticket;   /* task ticket of the IC wavefront */
   /* IC(0)/MIC(0) line wavefront (k_pcg.cu ic_alloc) */
   int ic_njb, ic_tasks;              /* 32-j line blocks; tasks */

@@ -3434,9 +3434,12 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
      * cells per thread): small grids keep short barriers and leave the rest
      * of the GPU to other simulations */
     if (precond != FLIPGPU_PRECOND_IC) {
+      h->solve_capacity = grid;
       const size_t per_block = (size_t)cg_block_of(kern) * 8;
       const size_t want = (nc + per_block - 1) / per_block;
       if (want < (size_t)grid) grid = want > 0 ? (int)want : 1;
+      /* the caller's share of the GPU (flipgpu_set_solve_blocks) */
+      if (h->solve_blocks > 0 && h->solve_blocks < grid) grid = h->solve_blocks;
     }
     if (mode == FLIPGPU_SOLVE_FAST && precond == FLIPGPU_PRECOND_IC) {
       kern = (const void *)k_cg_ic;

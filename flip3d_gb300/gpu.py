@@ -136,6 +136,9 @@ SIGNATURES = {
     "flipbatch_capture": (C.c_int, [C.c_void_p]),
     "flipbatch_step": (C.c_int, [C.c_void_p]),
     "flipbatch_sync": (C.c_int, [C.c_void_p]),
+    "flipbatch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "flipgpu_set_solve_blocks": (C.c_int, [C.c_void_p, C.c_int]),
+    "flipgpu_get_solve_blocks": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "flipunet_param_count": (C.c_int64, []),
     "flipunet_create": (C.c_int, [C.c_uint64, C.POINTER(C.c_void_p)]),
     "flipunet_destroy": (C.c_int, [C.c_void_p]),
@@ -461,6 +464,15 @@ class Simulation:
                                            C.c_float(re), 0), "resample")
         return out
 
+    def solve_blocks(self, value=None) -> int:
+        """The cap on the persistent solve's grid (0 = none); sets it first
+        when value is given."""
+        if value is not None:
+            self._ck(self.lib.flipgpu_set_solve_blocks(self.h, int(value)), "set_solve_blocks")
+        out = C.c_int()
+        self._ck(self.lib.flipgpu_get_solve_blocks(self.h, C.byref(out)), "get_solve_blocks")
+        return out.value
+
     def ic_tag_counter(self, value=None):
         """The IC wavefront's tag counter (a testing aid): set it when value
         is given; returns the current value."""
@@ -752,3 +764,10 @@ class Batch:
 
     def sync(self):
         self._ck(self.lib.flipbatch_sync(self.h), "sync")
+
+    def tune(self) -> float:
+        """Share the GPU between the members' solves (flipbatch_tune): the
+        chosen share, 0.0 for uncapped grids. The members must have stepped."""
+        out = C.c_double()
+        self._ck(self.lib.flipbatch_tune(self.h, C.byref(out)), "tune")
+        return out.value

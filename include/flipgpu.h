@@ -449,6 +449,25 @@ int flipbatch_capture(FlipBatch *b);
 /* one step of every member (graphs if captured, else asynchronous steps) */
 int flipbatch_step(FlipBatch *b);
 int flipbatch_sync(FlipBatch *b);
+/* Share the GPU between the members' pressure solves. Member i's
+ * persistent solve gets max(1, share * C_i * cells_i / cells of all
+ * members) blocks, C_i its solve kernel's co-resident grid (at share 1 all
+ * members' solves fit side by side). The tuner times the candidate shares
+ * (uncapped, 0.5, 1, 2, 4, 8, 16) on every member's current system, solved by
+ * all members at once from the saved warm start, keeps the fastest and
+ * puts each member's pressure back as its last step left it; the decision
+ * appears in flipgpu_autotune_report. Every member must have stepped at
+ * least once. Captured graphs are re-recorded with the new grids. The
+ * grids change the order of the solve's sums, so a member's bits then
+ * match a lone handle with the same flipgpu_set_solve_blocks. share_out
+ * (optional) receives the chosen share, 0 for uncapped; flipgpu_last_solve_stats
+ * then reports the last trial. */
+int flipbatch_tune(FlipBatch *b, double *share_out);
+/* cap on the persistent pressure solve's grid (0 = none, the default): a
+ * simulation that shares the GPU with others leaves them SMs. The IC(0)
+ * wavefront keeps its full grid. */
+int flipgpu_set_solve_blocks(FlipGpu *h, int blocks);
+int flipgpu_get_solve_blocks(const FlipGpu *h, int *blocks);
 
 /* ---------------------------------------------------------------------------
  * Learned warm start (no counterpart in the reference; the reference starts

@@ -511,6 +511,43 @@ def test_batch_of_uneven_scenes_matches_one_at_a_time(gpu):
             assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("precond", ["jacobi", "mg"])
+def test_tuned_batch_matches_lone_handles_with_its_grids(gpu, precond):
+    """flipbatch_tune times the members' solves with shared grids and puts
+    every member's pressure back: after it, the members hold what one step
+    left (the same pressure as lone handles), and stepping on with the tuned
+    grids (re-captured graphs) gives the bits of lone handles given the
+    same flipgpu_set_solve_blocks."""
+    scs = [scenes.batch_scene(s) for s in (5, 6, 7, 8, 9)]
+    pc = gpu.PRECOND_MG if precond == "mg" else gpu.PRECOND_JACOBI
+    # multigrid wants N a multiple of 4 (every batch_scene size is)
+    alone = [_fast_sim(gpu, sc, seed=i, precond=pc) for i, sc in enumerate(scs)]
+    batched = [_fast_sim(gpu, sc, seed=i, precond=pc) for i, sc in enumerate(scs)]
+    b = gpu.Batch(batched)
+    b.capture()
+    for s in alone:
+        s.step()
+    b.step()
+    b.sync()
+    share = b.tune()
+    caps = [t.solve_blocks() for t in batched]
+    print(f"{precond}: share {share}, grids {caps}\n{gpu.autotune_report()}")
+    assert share in (0.0, 0.5, 1.0, 2.0, 4.0, 8.0, 16.0)
+    assert (share == 0.0) == all(c == 0 for c in caps)
+    for s, t in zip(alone, batched):
+        assert np.array_equal(s.get_pressure(), t.get_pressure())
+        s.solve_blocks(t.solve_blocks())
+    for _ in range(3):
+        for s in alone:
+            assert s.step().status == 0
+        b.step()
+    b.sync()
+    for s, t in zip(alone, batched):
+        assert t.last_solve_stats().status == 0
+        for x, y in zip(s.get_particles(), t.get_particles()):
+            assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("fast", [False, True])
 def test_step_host_matches_put_step_get(gpu, fast):
     """flipgpu_step_host (transfers overlapped with the step on a second
