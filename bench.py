@@ -48,6 +48,10 @@ def run_batch(args):
     """Aggregate particle-steps/s of many small scenes stepped together
     (one CUDA graph per scene, every scene on its own stream, no host waits
     between scenes) against the same scenes stepped one at a time."""
+    # the members' streams get hardware work queues of their own (the
+    # default 8 queues make streams that share one wait for each other);
+    # read when the CUDA context is created
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
 
     from flip3d_gb300 import gpu, scenes
@@ -60,7 +64,9 @@ def run_batch(args):
         s = gpu.Simulation(gpu.default_params(sc.n, sc.count, rel_tol=1e-6, seed=i,
                                               solve_mode=gpu.SOLVE_FAST,
                                               precond=gpu.PRECOND_MG if mg else gpu.PRECOND_JACOBI,
-                                              mg_sweeps=MG_SWEEPS))
+                                              mg_sweeps=MG_SWEEPS,
+                                              arith=gpu.ARITH_FAST if args.arith == "fast"
+                                              else gpu.ARITH_REF))
         s.set_scene(sc)
         s.calibrate_max_density()
         sims.append(s)
@@ -109,7 +115,11 @@ def run_batch(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{len(scs)} scenes, N uniform from {{24,32,48,64,96}} "
                                f"({sizes}), pool U(0.1,0.4) + sphere r U(0.08,0.2), "
-                               f"{P} particles in all", "solver": f"FP32 PCG {args.precond}, FP64 dots",
+                               f"{P} particles in all",
+                   "solver": f"FP32 PCG {args.precond}, double-float dots, refined to a true "
+                             f"relative residual of 1e-6",
+                   "arith": f"particle gathers {args.arith}",
+                   "queues": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                    "timing": "host wall clock around device-synchronised steps",
                    "l2": "inputs larger than L2"},
         "one_at_a_time": {"value": P * args.steps / t_seq, "ms_per_step": t_seq / args.steps * 1e3},

@@ -84,6 +84,12 @@ int choose(const std::string &key, const std::vector<std::string> &names, cudaSt
   return best;
 }
 
+int cached(const std::string &key) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_table.find(key);
+  return it == g_table.end() ? 0 : it->second.choice;
+}
+
 void record(const std::string &key, const std::vector<std::string> &names,
             const std::vector<float> &ms, int choice) {
   Decision d;

@@ -23,6 +23,10 @@ namespace autotune {
 int choose(const std::string &key, const std::vector<std::string> &names, cudaStream_t st,
            const std::function<cudaError_t(int)> &run);
 
+/* the decision stored for key, or 0 (the default) when there is none; times
+ * nothing, so it suits launches that must not wait for the device */
+int cached(const std::string &key);
+
 /* enter a decision timed elsewhere (ms < 0: the candidate failed) so that
  * flipgpu_autotune_report lists it */
 void record(const std::string &key, const std::vector<std::string> &names,

@@ -15,9 +15,14 @@
  * evaluates the same formulas in native FP32 with fused multiply-adds and
  * the fast division intrinsic (FLIPGPU_ARITH_FAST).
  */
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
 
+#include "autotune.h"
 #include "devcommon.cuh"
 
 using namespace refmath;
@@ -188,12 +193,12 @@ __device__ __forceinline__ void fetch_velocity(int n, float fn, const float *__r
 
 /* ------------------------------------------------------ computeDensity */
 
-template <class AR>
-__global__ void __launch_bounds__(BLK)
+template <class AR, int B = BLK>
+__global__ void __launch_bounds__(B)
 k_density(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
           const float4 *__restrict__ spos, float *__restrict__ dens,
           float *__restrict__ sdens) {
-  int a = blockIdx.x * BLK + threadIdx.x;
+  int a = blockIdx.x * B + threadIdx.x;
   if (a >= c.np) return;
   float4 P = spos[a];
   uint32_t p = perm[a];
@@ -918,15 +923,15 @@ __device__ __forceinline__ void cell_decode(size_t c, int n, int &i, int &j, int
  * lie in cells [i-1, i+1] x [j-1, j+1] x [k-1, k+1]: each particle there is
  * loaded once and tested against each face whose own cells hold it, which
  * keeps every face's sums in k_p2g's order. */
-template <class AR>
-__global__ void __launch_bounds__(BLK)
+template <class AR, int B = BLK>
+__global__ void __launch_bounds__(B)
 k_p2g_cells(SimConst c, int enforce, const uint32_t *__restrict__ cs,
             const float4 *__restrict__ spg, const float4 *__restrict__ svel,
             const uint8_t *__restrict__ A, float *__restrict__ u0, float *__restrict__ u1,
             float *__restrict__ u2, float *__restrict__ us0, float *__restrict__ us1,
             float *__restrict__ us2) {
   const int n = c.n, m1 = n + 1;
-  const size_t t = (size_t)blockIdx.x * BLK + threadIdx.x;
+  const size_t t = (size_t)blockIdx.x * B + threadIdx.x;
   if (t >= (size_t)m1 * m1 * m1) return;
   int i, j, k;
   cell_decode(t, m1, i, j, k);
@@ -1029,16 +1034,16 @@ k_p2g_cells(SimConst c, int enforce, const uint32_t *__restrict__ cs,
  * instead of through k_spring's and k_resample's per-thread near lists
  * (which hold 24 KB of shared memory per block); the same pairs in the same
  * order, so the same results. */
-/* five resident blocks per SM: 48 registers (a few spilled) instead of 56;
- * the kernel is issue- and occupancy-bound, and this is 5 % faster at N=256
- * (six blocks spill more and gain less) */
-template <class AR>
-__global__ void __launch_bounds__(BLK, 5)
+/* 1280 resident threads per SM (five blocks of 256): 48 registers (a few
+ * spilled) instead of 56; the kernel is issue- and occupancy-bound, and
+ * this is 5 % faster at N=256 (six blocks spill more and gain less) */
+template <class AR, int B = BLK>
+__global__ void __launch_bounds__(B, 1280 / B)
 k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
                 const float4 *__restrict__ spos, const float *__restrict__ nx,
                 const float *__restrict__ ny, const float *__restrict__ nz,
                 float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz) {
-  const int a = blockIdx.x * BLK + threadIdx.x;
+  const int a = blockIdx.x * B + threadIdx.x;
   if (a >= c.np) return;
   const float4 P = __ldg(spos + a);
   if (unpack_type(P.w) != CELL_FLUID) return;
@@ -1082,14 +1087,14 @@ k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__r
   pz[pid] = P.z + c.dt_f * spring[2];
 }
 
-template <class AR>
-__global__ void __launch_bounds__(BLK)
+template <class AR, int B = BLK>
+__global__ void __launch_bounds__(B)
 k_resample_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
                   const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                   const float *__restrict__ px, const float *__restrict__ py,
                   const float *__restrict__ pz, float *__restrict__ vx, float *__restrict__ vy,
                   float *__restrict__ vz) {
-  const int a = blockIdx.x * BLK + threadIdx.x;
+  const int a = blockIdx.x * B + threadIdx.x;
   if (a >= c.np) return;
   if (unpack_type(__ldg(spos + a).w) != CELL_FLUID) return;
   const uint32_t p = __ldg(perm + a);
@@ -1203,16 +1208,54 @@ static bool cell_gathers(const FlipGpu *h) {
   return !(e && strcmp(e, "particle") == 0);
 }
 
+/* The FAST gathers' block size, tuned per kernel and problem size (key: the
+ * kernel, N and the power of two at or above its thread count) over 256
+ * (the default, and the choice while a stream is being captured or an
+ * asynchronous step runs), 128 and 512 threads. Every thread computes one
+ * particle's or face cell's sums on its own, so the results do not depend
+ * on the choice; each kernel only writes outputs that it does not read, so
+ * the tuner's repeated launches leave the same state. FLIPGPU_GATHER_BLOCK
+ * = 128, 256 or 512 in the environment (read at each launch) fixes it. */
+template <class L>
+static cudaError_t tuned_gather(FlipGpu *h, const char *kernel, size_t threads, L launch) {
+  auto run = [&](int i) -> cudaError_t {
+    if (i == 1)
+      launch(std::integral_constant<int, 128>{});
+    else if (i == 2)
+      launch(std::integral_constant<int, 512>{});
+    else
+      launch(std::integral_constant<int, 256>{});
+    return cudaGetLastError();
+  };
+  const char *e = getenv("FLIPGPU_GATHER_BLOCK");
+  int pick = 0;
+  if (e && e[0]) {
+    const int b = atoi(e);
+    pick = b == 128 ? 1 : (b == 512 ? 2 : 0);
+  } else {
+    int lg = 0;
+    while (((size_t)1 << lg) < threads) lg++;
+    char key[96];
+    snprintf(key, sizeof key, "%s block n=%d threads<=2^%d", kernel, h->n, lg);
+    static const std::vector<std::string> names = {"256", "128", "512"};
+    pick = h->async_mode ? autotune::cached(key) : autotune::choose(key, names, h->stream, run);
+  }
+  cudaError_t err = run(pick);
+  FG_LAUNCHED(h, 1);
+  return err;
+}
+
 cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
-  const unsigned g = grid_for(h->np, BLK);
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
-    k_density<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
-                                                   h->sdens);
-  else
-    k_density<RefArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->dens,
-                                                  h->sdens);
+    return tuned_gather(h, "density", h->np, [&](auto B) {
+      constexpr int b = decltype(B)::value;
+      k_density<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
+          c, h->cell_start, h->perm, h->spos, h->dens, h->sdens);
+    });
+  k_density<RefArith><<<grid_for(h->np, BLK), BLK, 0, h->stream>>>(c, h->cell_start, h->perm,
+                                                                   h->spos, h->dens, h->sdens);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -1220,12 +1263,13 @@ cudaError_t launch_density(FlipGpu *h) {
 cudaError_t launch_p2g(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
   if (cell_gathers(h)) {
-    const size_t m1 = (size_t)h->n + 1;
-    k_p2g_cells<FastArith><<<grid_for(m1 * m1 * m1, BLK), BLK, 0, h->stream>>>(
-        c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0], h->u[1], h->u[2], h->us[0],
-        h->us[1], h->us[2]);
-    FG_LAUNCHED(h, 1);
-    return cudaGetLastError();
+    const size_t m1 = (size_t)h->n + 1, cells = m1 * m1 * m1;
+    return tuned_gather(h, "p2g_cells", cells, [&](auto B) {
+      constexpr int b = decltype(B)::value;
+      k_p2g_cells<FastArith, b><<<grid_for(cells, b), b, 0, h->stream>>>(
+          c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0], h->u[1], h->u[2], h->us[0],
+          h->us[1], h->us[2]);
+    });
   }
   const unsigned grid = 3u * grid_for(h->nf, BLK);
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
@@ -1374,18 +1418,18 @@ cudaError_t launch_correct(FlipGpu *h) {
   const unsigned g = grid_for(h->np, BLK);
   const bool fast = h->prm.arith == FLIPGPU_ARITH_FAST;
   if (cell_gathers(h)) {
-    k_spring_inline<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
-                                                         h->nx, h->ny, h->nz, h->px, h->py,
-                                                         h->pz);
-    FG_LAUNCHED(h, 1);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = tuned_gather(h, "spring", h->np, [&](auto B) {
+      constexpr int b = decltype(B)::value;
+      k_spring_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
+          c, h->cell_start, h->perm, h->spos, h->nx, h->ny, h->nz, h->px, h->py, h->pz);
+    });
     if (e != cudaSuccess) return e;
     if (h->xfer_pos_out && (e = xfer_positions_out(h)) != cudaSuccess) return e;
-    k_resample_inline<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos,
-                                                           h->svel, h->px, h->py, h->pz, h->vx,
-                                                           h->vy, h->vz);
-    FG_LAUNCHED(h, 1);
-    return cudaGetLastError();
+    return tuned_gather(h, "resample", h->np, [&](auto B) {
+      constexpr int b = decltype(B)::value;
+      k_resample_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
+          c, h->cell_start, h->perm, h->spos, h->svel, h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+    });
   }
   if (fast)
     k_spring<FastArith><<<g, BLK, 0, h->stream>>>(c, h->cell_start, h->perm, h->spos, h->nx,

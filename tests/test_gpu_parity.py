@@ -462,9 +462,10 @@ def test_fast_arithmetic_tracks_the_reference_step(gpu, orc):
         assert np.array_equal(x, y)
 
 
-def _fast_sim(gpu, sc, seed=3, precond=None):
+def _fast_sim(gpu, sc, seed=3, precond=None, arith=None):
     s = make_sim(gpu, sc.n, sc.count, rel_tol=1e-6, seed=seed, solve_mode=gpu.SOLVE_FAST,
-                 precond=gpu.PRECOND_JACOBI if precond is None else precond)
+                 precond=gpu.PRECOND_JACOBI if precond is None else precond,
+                 arith=gpu.ARITH_REF if arith is None else arith)
     s.set_scene(sc)
     s.calibrate_max_density()
     return s
@@ -520,9 +521,11 @@ def test_tuned_batch_matches_lone_handles_with_its_grids(gpu, precond):
     same flipgpu_set_solve_blocks."""
     scs = [scenes.batch_scene(s) for s in (5, 6, 7, 8, 9)]
     pc = gpu.PRECOND_MG if precond == "mg" else gpu.PRECOND_JACOBI
-    # multigrid wants N a multiple of 4 (every batch_scene size is)
-    alone = [_fast_sim(gpu, sc, seed=i, precond=pc) for i, sc in enumerate(scs)]
-    batched = [_fast_sim(gpu, sc, seed=i, precond=pc) for i, sc in enumerate(scs)]
+    # multigrid wants N a multiple of 4 (every batch_scene size is); it runs
+    # with the FAST gathers, as the batch benchmark does
+    ar = gpu.ARITH_FAST if precond == "mg" else gpu.ARITH_REF
+    alone = [_fast_sim(gpu, sc, seed=i, precond=pc, arith=ar) for i, sc in enumerate(scs)]
+    batched = [_fast_sim(gpu, sc, seed=i, precond=pc, arith=ar) for i, sc in enumerate(scs)]
     b = gpu.Batch(batched)
     b.capture()
     for s in alone:
@@ -545,6 +548,25 @@ def test_tuned_batch_matches_lone_handles_with_its_grids(gpu, precond):
     for s, t in zip(alone, batched):
         assert t.last_solve_stats().status == 0
         for x, y in zip(s.get_particles(), t.get_particles()):
+            assert np.array_equal(x, y)
+
+
+def test_gather_block_sizes_give_the_same_bits(gpu, monkeypatch):
+    """The FAST gathers' block size (tuned per kernel and problem size)
+    changes no bit: three steps with 128, 256 and 512 threads per block, and
+    with the tuner's own choice, agree."""
+    sc = scenes.dam_break(40, seed=2)
+    outs = []
+    for blk in ("128", "256", "512", ""):
+        monkeypatch.setenv("FLIPGPU_GATHER_BLOCK", blk)
+        s = _fast_sim(gpu, sc, seed=4, precond=gpu.PRECOND_MG, arith=gpu.ARITH_FAST)
+        for _ in range(3):
+            assert s.step().status == 0
+        outs.append(s.get_particles())
+        s.close()
+    print(gpu.autotune_report())
+    for o in outs[1:]:
+        for x, y in zip(outs[0], o):
             assert np.array_equal(x, y)
 
 
