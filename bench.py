@@ -203,19 +203,19 @@ def solver_comparison(gpu, sim, prm, n, systems=3):
     return out
 
 
-def measured_traffic(stage, n, particles):
-    """DRAM bytes per call of the stage (its kernels' dram__bytes_read.sum +
-    dram__bytes_write.sum) from the ncu summaries in profiles/, and how it
-    was obtained: measured at this grid size, or scaled from a capture of a
-    smaller workload by the particle count (the gathers' traffic grows with
-    the particles they touch). (None, None) when the stage was not
-    captured."""
+def measured_traffic(kernel, n, particles):
+    """DRAM bytes of the kernel per step (per solve for a solve kernel; its
+    dram__bytes_read.sum + dram__bytes_write.sum) from the ncu summaries in
+    profiles/, and how it was obtained: measured at this grid size, or
+    scaled from a capture of a smaller workload by the particle count (the
+    gathers' traffic grows with the particles they touch). (None, None)
+    when the kernel was not captured."""
     rows = []
     try:
         with open(TRAFFIC) as f:
             for line in f:
                 parts = line.split()
-                if len(parts) == 4 and not line.startswith("#") and parts[0] == stage:
+                if len(parts) == 4 and not line.startswith("#") and parts[0] == kernel:
                     rows.append((int(parts[1]), int(parts[2]), int(parts[3])))
     except OSError:
         pass
@@ -228,13 +228,38 @@ def measured_traffic(stage, n, particles):
     return None, None
 
 
-GATHER_STAGES = ("density", "p2g", "correct")
+GATHER_KERNELS = ("k_density", "k_p2g_cells", "k_spring_inline", "k_resample_inline")
+PROFILED_STEPS = 2
 
 
-def roofline_note(stage, traffic, nbytes):
+def kernel_bytes(kernel, P, n, steps, iters, sweep_cells=None, precond="jacobi"):
+    """Algorithmic bytes of all launches of one of the profiled kernels over
+    `steps` steps whose solves took `iters` iterations in all, by the model
+    of stage_bytes(): the persistent solve kernel its iterations (the
+    refinement's residual and update kernels are not part of it), each
+    gather one call of its stage; the corrector's two kernels split its
+    bytes: the spring reads the sorted positions and the permutation and
+    writes positions (32 B per particle), the resample reads the sorted
+    positions and velocities, the moved position and the permutation and
+    writes velocities (60 B); both read the cell starts."""
+    C = n ** 3
+    if kernel.startswith("k_cg"):
+        per = stage_bytes("solve", P, n, 1, sweep_cells, precond) - 21 * C
+        return per * iters
+    per_step = {
+        "k_density": stage_bytes("density", P, n, 0),
+        "k_p2g_cells": stage_bytes("p2g", P, n, 0),
+        "k_spring_inline": P * 32 + 4 * C,
+        "k_resample_inline": P * 60 + 4 * C,
+        "k_flip_advect": stage_bytes("g2p_flip", P, n, 0),
+    }.get(kernel, 0)
+    return per_step * steps
+
+
+def roofline_note(kernel, traffic, nbytes):
     """Reading of the roofline fraction against the kernel's DRAM traffic."""
     notes = []
-    if stage in GATHER_STAGES:
+    if kernel in GATHER_KERNELS:
         notes.append("a particle gather: bound by the L1 data pipe (one 16-byte neighbour "
                      "load per particle pair, 85-91 % of its peak in ncu), not by HBM")
     if traffic is not None and nbytes:
@@ -597,23 +622,29 @@ def main():
     ms = max_over_ranks(ms, world, "cuda")
     value = replica_throughput(P, world, args.steps, ms / 1e3)
 
-    # per-stage profile (separate pass; events between stages)
+    # per-stage and per-kernel profile (a separate pass: CUDA events between
+    # the stages and around each launch of the main kernels)
     sim.set_profiling(True)
-    for _ in range(2):
+    prof_iters = []
+    for _ in range(PROFILED_STEPS):
         st = sim.step()
+        prof_iters.append(int(st.iterations))
     prof = sim.profile()
+    kprof = sim.kernel_profile()
     sim.set_profiling(False)
-    dom = max(prof, key=lambda s: prof[s][0])
-    dom_ms = prof[dom][0] / max(prof[dom][1], 1)
-    it_prof = int(st.iterations)
     sweep_cells = liquid_chunk_cells(sim.get_grid()[1])
-    nbytes = stage_bytes(dom, P, args.n, it_prof, sweep_cells, args.precond)
+    # the roofline's kernel: the one with the most device time
+    dom = max(kprof, key=lambda k: kprof[k][0])
+    k_ms, k_calls = kprof[dom]
+    dom_ms = k_ms / max(k_calls, 1)
+    nbytes = kernel_bytes(dom, P, args.n, PROFILED_STEPS, sum(prof_iters), sweep_cells,
+                          args.precond) / max(k_calls, 1)
     peak, peak_kind = hbm_peak()
     achieved = nbytes / (dom_ms / 1e3) / 1e9
     traffic, traffic_src = measured_traffic(dom, args.n, P)
-    if dom == "solve" and args.precond != "mg":
-        # the solve's captures are of the multigrid solve
-        traffic, traffic_src = None, None
+    if traffic is not None:
+        # a row is per step (per solve for a solve kernel): per launch here
+        traffic = int(traffic * PROFILED_STEPS / max(k_calls, 1))
 
     # end to end through the C ABI with pinned host buffers: every step
     # uploads the particle state, steps and downloads it (flipgpu_step_host,
@@ -690,9 +721,15 @@ def main():
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind, "algorithmic_bytes": nbytes,
                          "ms_per_launch": dom_ms,
-                         "bytes_model": "stage_bytes(): every input read once, every output "
-                                        "written once; the solve counts its solver-grid "
-                                        "passes over the liquid chunks only",
+                         "launches_per_step": k_calls / PROFILED_STEPS,
+                         "timing": "CUDA events around each launch on the handle's stream, "
+                                   f"{PROFILED_STEPS} profiled steps after the timed ones",
+                         "bytes_model": "kernel_bytes(): every input read once, every output "
+                                        "written once, per launch; a solve kernel counts its "
+                                        "solver-grid passes over the liquid chunks only",
+                         "kernels_ms_per_step": {k: round(v[0] / PROFILED_STEPS, 4)
+                                                 for k, v in sorted(kprof.items(),
+                                                                    key=lambda t: -t[1][0])},
                          "sweep_cells": sweep_cells, "traffic_source": traffic_src,
                          "note": roofline_note(dom, traffic, nbytes)},
             "cpu_baseline": cpu,

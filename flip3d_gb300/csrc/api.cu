@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "autotune.h"
@@ -193,6 +194,7 @@ struct StageClock {
     order[nmark++] = stage;
   }
   void flush() {
+    ktime_flush(h);
     if (!h->prof_on || nmark < 2) return;
     cudaEventSynchronize(h->prof_ev[nmark - 1]);
     for (int i = 0; i + 1 < nmark; i++) {
@@ -205,6 +207,45 @@ struct StageClock {
 };
 
 } // namespace
+
+void ktime_begin(FlipGpu *h, const char *name) {
+  if (!h->prof_on || h->kt_n >= FlipGpu::KT_SLOTS) return;
+  if (!h->kt_ready) {
+    for (int i = 0; i < 2 * FlipGpu::KT_SLOTS; i++)
+      if (cudaEventCreate(&h->kt_ev[i]) != cudaSuccess) return;
+    h->kt_ready = 1;
+  }
+  cudaEventRecord(h->kt_ev[2 * h->kt_n], h->stream);
+  h->kt_pending[h->kt_n] = name;
+}
+
+void ktime_end(FlipGpu *h) {
+  if (!h->prof_on || !h->kt_ready || h->kt_n >= FlipGpu::KT_SLOTS) return;
+  cudaEventRecord(h->kt_ev[2 * h->kt_n + 1], h->stream);
+  h->kt_n++;
+}
+
+void ktime_flush(FlipGpu *h) {
+  if (h->kt_n == 0) return;
+  cudaEventSynchronize(h->kt_ev[2 * h->kt_n - 1]);
+  for (int i = 0; i < h->kt_n; i++) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, h->kt_ev[2 * i], h->kt_ev[2 * i + 1]) != cudaSuccess) continue;
+    int k = 0;
+    while (k < h->kt_nnames && strcmp(h->kt_name[k], h->kt_pending[i]) != 0) k++;
+    if (k == h->kt_nnames) {
+      if (k == FlipGpu::KT_NAMES) continue;
+      h->kt_name[k] = h->kt_pending[i];
+      h->kt_ms[k] = 0.0;
+      h->kt_calls[k] = 0;
+      h->kt_nnames++;
+    }
+    h->kt_ms[k] += ms;
+    h->kt_calls[k]++;
+  }
+  h->kt_n = 0;
+  cudaGetLastError();
+}
 
 /* After the corrector's spring: the positions are final, so the transfer
  * stream interleaves them into the sorted grid-position buffer (unused by
@@ -444,6 +485,8 @@ int flipgpu_destroy(FlipGpu *h) {
   cudaEventDestroy(h->ev0);
   cudaEventDestroy(h->ev1);
   for (int i = 0; i <= FLIPGPU_NSTAGES; i++) cudaEventDestroy(h->prof_ev[i]);
+  if (h->kt_ready)
+    for (int i = 0; i < 2 * FlipGpu::KT_SLOTS; i++) cudaEventDestroy(h->kt_ev[i]);
   cudaStreamDestroy(h->own_stream);
   delete h;
   return FLIPGPU_OK;
@@ -1244,12 +1287,31 @@ int flipgpu_put_state(FlipGpu *h, const float *pos, const float *vel, int on_dev
 
 int flipgpu_set_profiling(FlipGpu *h, int on) {
   if (!h) return FLIPGPU_EINVAL;
+  ktime_flush(h);
   h->prof_on = on;
   for (int i = 0; i < FLIPGPU_NSTAGES; i++) {
     h->prof_ms[i] = 0.0;
     h->prof_calls[i] = 0;
   }
+  h->kt_nnames = 0;
   return FLIPGPU_OK;
+}
+
+int flipgpu_get_kernel_profile(FlipGpu *h, char *buf, int len) {
+  if (!h || len < 0) return FLIPGPU_EINVAL;
+  ktime_flush(h);
+  std::string s;
+  char line[160];
+  for (int k = 0; k < h->kt_nnames; k++) {
+    snprintf(line, sizeof line, "%s\t%.6f\t%lld\n", h->kt_name[k], h->kt_ms[k],
+             (long long)h->kt_calls[k]);
+    s += line;
+  }
+  if (buf && len > 0) {
+    strncpy(buf, s.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)s.size();
 }
 
 int flipgpu_set_ic_tag_counter(FlipGpu *h, unsigned value) {

@@ -183,7 +183,25 @@ struct FlipGpu {
   cudaEvent_t prof_ev[FLIPGPU_NSTAGES + 1];
   double prof_ms[FLIPGPU_NSTAGES];
   int64_t prof_calls[FLIPGPU_NSTAGES];
+  /* per-kernel profiling of the main kernels (ktime_*): event pairs of the
+   * launches not yet read, and the totals per kernel name */
+  static constexpr int KT_SLOTS = 64, KT_NAMES = 24;
+  cudaEvent_t kt_ev[2 * KT_SLOTS];
+  const char *kt_pending[KT_SLOTS];
+  int kt_n, kt_ready;
+  const char *kt_name[KT_NAMES];
+  double kt_ms[KT_NAMES];
+  int64_t kt_calls[KT_NAMES];
+  int kt_nnames;
 };
+
+/* Per-kernel clock of the profiling mode: events on the handle's stream
+ * before and after one launch of the named kernel (a string literal);
+ * ktime_flush waits for them and adds each launch's time to its kernel's
+ * total. Does nothing unless profiling is on. */
+void ktime_begin(FlipGpu *h, const char *name);
+void ktime_end(FlipGpu *h);
+void ktime_flush(FlipGpu *h);
 
 /* Device scalar slots (FlipGpu::scal). */
 enum {

@@ -1240,7 +1240,9 @@ static cudaError_t tuned_gather(FlipGpu *h, const char *kernel, size_t threads, 
     static const std::vector<std::string> names = {"256", "128", "512"};
     pick = h->async_mode ? autotune::cached(key) : autotune::choose(key, names, h->stream, run);
   }
+  ktime_begin(h, kernel);
   cudaError_t err = run(pick);
+  ktime_end(h);
   FG_LAUNCHED(h, 1);
   return err;
 }
@@ -1249,7 +1251,7 @@ cudaError_t launch_density(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
-    return tuned_gather(h, "density", h->np, [&](auto B) {
+    return tuned_gather(h, "k_density", h->np, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_density<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
           c, h->cell_start, h->perm, h->spos, h->dens, h->sdens);
@@ -1264,7 +1266,7 @@ cudaError_t launch_p2g(FlipGpu *h, int enforce) {
   SimConst c = make_const(h);
   if (cell_gathers(h)) {
     const size_t m1 = (size_t)h->n + 1, cells = m1 * m1 * m1;
-    return tuned_gather(h, "p2g_cells", cells, [&](auto B) {
+    return tuned_gather(h, "k_p2g_cells", cells, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_p2g_cells<FastArith, b><<<grid_for(cells, b), b, 0, h->stream>>>(
           c, enforce, h->cell_start, h->spg, h->svel, h->A, h->u[0], h->u[1], h->u[2], h->us[0],
@@ -1313,6 +1315,7 @@ cudaError_t launch_flip_advect(FlipGpu *h) {
   if (h->np == 0) return cudaSuccess;
   SimConst c = make_const(h);
   const unsigned g = grid_for(h->np, BLK);
+  ktime_begin(h, "k_flip_advect");
   if (h->prm.arith == FLIPGPU_ARITH_FAST)
     k_flip_advect<FastArith><<<g, BLK, 0, h->stream>>>(
         c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
@@ -1321,6 +1324,7 @@ cudaError_t launch_flip_advect(FlipGpu *h) {
     k_flip_advect<RefArith><<<g, BLK, 0, h->stream>>>(
         c, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens, h->u[0], h->u[1], h->u[2],
         h->us[0], h->us[1], h->us[2], h->A, h->wall_start, h->wall_pos, h->wall_nrm, h->flag);
+  ktime_end(h);
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -1418,14 +1422,14 @@ cudaError_t launch_correct(FlipGpu *h) {
   const unsigned g = grid_for(h->np, BLK);
   const bool fast = h->prm.arith == FLIPGPU_ARITH_FAST;
   if (cell_gathers(h)) {
-    cudaError_t e = tuned_gather(h, "spring", h->np, [&](auto B) {
+    cudaError_t e = tuned_gather(h, "k_spring_inline", h->np, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_spring_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
           c, h->cell_start, h->perm, h->spos, h->nx, h->ny, h->nz, h->px, h->py, h->pz);
     });
     if (e != cudaSuccess) return e;
     if (h->xfer_pos_out && (e = xfer_positions_out(h)) != cudaSuccess) return e;
-    return tuned_gather(h, "resample", h->np, [&](auto B) {
+    return tuned_gather(h, "k_resample_inline", h->np, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_resample_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
           c, h->cell_start, h->perm, h->spos, h->svel, h->px, h->py, h->pz, h->vx, h->vy, h->vz);

@@ -3215,6 +3215,16 @@ void ic_free(FlipGpu *h) {
   h->ic_tasks = 0;
 }
 
+/* the persistent solve kernel's name in the per-kernel profile */
+static const char *solve_kernel_name(const void *kern) {
+  if (kern == (const void *)k_cg_mg<CG_MG_BLOCK>) return "k_cg_mg";
+  if (kern == (const void *)k_cg_ic) return "k_cg_ic";
+  if (kern == (const void *)k_cg_cg1<CG1_BLOCK_SMALL> ||
+      kern == (const void *)k_cg_cg1<CG1_BLOCK_LARGE>)
+    return "k_cg_cg1";
+  return "k_cg";
+}
+
 int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
   const int n = h->n;
   const size_t nc = h->nc;
@@ -3486,7 +3496,9 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
       for (int pass = 0; pass < passes; pass++) {
         if (pass > 0) reset_flags();
         a.ic_factor = pass == 0;
+        ktime_begin(h, solve_kernel_name(kern));
         cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
+        ktime_end(h);
         FG_LAUNCHED(h, 1);
         if (e != cudaSuccess) {
           snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));
@@ -3511,7 +3523,9 @@ int run_solve(FlipGpu *h, FlipGpuSolveStats *st) {
     }
     /* FAST mode without refinement: CG stops on its recursive residual with
      * x in FP32, and the true residual b - A x is evaluated in FP64 after */
+    ktime_begin(h, solve_kernel_name(kern));
     cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), kargs, smem, S);
+    ktime_end(h);
     FG_LAUNCHED(h, 1);
     if (e != cudaSuccess) {
       snprintf(h->err, sizeof h->err, "solve: cooperative launch: %s", cudaGetErrorString(e));

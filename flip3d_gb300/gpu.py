@@ -122,6 +122,7 @@ SIGNATURES = {
     "flipgpu_set_ic_tag_counter": (C.c_int, [C.c_void_p, C.c_uint]),
     "flipgpu_get_ic_tag_counter": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "flipgpu_get_profile": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+    "flipgpu_get_kernel_profile": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "flipgpu_sort_cells_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                              C.c_void_p, C.c_void_p]),
     "flipgpu_set_params": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
@@ -491,6 +492,20 @@ class Simulation:
         self._ck(self.lib.flipgpu_get_profile(self.h, _ptr(ms), _ptr(calls), len(STAGES)),
                  "get_profile")
         return {s: (float(ms[i]), int(calls[i])) for i, s in enumerate(STAGES)}
+
+    def kernel_profile(self):
+        """{kernel: (ms, launches)} of the main kernels since profiling was
+        switched on (flipgpu_get_kernel_profile)."""
+        size = self.lib.flipgpu_get_kernel_profile(self.h, None, 0)
+        if size < 0:
+            raise FlipGpuError(f"get_kernel_profile failed ({size})")
+        buf = C.create_string_buffer(size + 1)
+        self.lib.flipgpu_get_kernel_profile(self.h, buf, size + 1)
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, ms, calls = line.split("\t")
+            out[name] = (float(ms), int(calls))
+        return out
 
     @property
     def launches(self):

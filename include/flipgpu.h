@@ -392,6 +392,14 @@ int64_t flipgpu_launch_count(const FlipGpu *h);
 int flipgpu_set_profiling(FlipGpu *h, int on);
 /* ms[i] and calls[i] accumulated since profiling was switched on. */
 int flipgpu_get_profile(FlipGpu *h, double *ms, int64_t *calls, int max);
+/* The main kernels' own device time since profiling was switched on (CUDA
+ * events around each launch on the handle's stream): one line per kernel,
+ * "name<TAB>ms<TAB>launches". The persistent solve (k_cg_mg, k_cg_cg1,
+ * k_cg_ic, k_cg), the FAST gathers (k_density, k_p2g_cells,
+ * k_spring_inline, k_resample_inline) and k_flip_advect are timed. Writes
+ * at most len - 1 characters and a terminating zero; returns the length of
+ * the whole text. */
+int flipgpu_get_kernel_profile(FlipGpu *h, char *buf, int len);
 
 /* Testing aid (no reference counterpart): set the counter from which the
  * IC(0)/MIC(0) wavefront's solves take the tags of their words (each solve

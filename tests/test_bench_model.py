@@ -36,18 +36,43 @@ def test_solve_bytes_per_preconditioner():
                                        15 * (4 * bench.MG_SWEEPS + 2) * bench.mg_coarse_cells(n)))
 
 
+def test_kernel_bytes():
+    n, P, cells = 128, 1000, 657280
+    C = n ** 3
+    # the solve kernel: its iterations only (the refinement's setup pass is
+    # in other kernels)
+    mg1 = bench.stage_bytes("solve", 0, n, 1, cells, "mg") - 21 * C
+    assert bench.kernel_bytes("k_cg_mg", P, n, 2, 17, cells, "mg") == mg1 * 17
+    # a gather: its stage's bytes once per step
+    assert bench.kernel_bytes("k_density", P, n, 2, 17) == 2 * bench.stage_bytes("density", P, n, 0)
+    # the corrector's two kernels
+    assert bench.kernel_bytes("k_spring_inline", P, n, 1, 0) == 32 * P + 4 * C
+    assert bench.kernel_bytes("k_resample_inline", P, n, 1, 0) == 60 * P + 4 * C
+    assert bench.kernel_bytes("k_unknown", P, n, 1, 0) == 0
+
+
 def test_roofline_note():
-    assert bench.roofline_note("solve", None, 10) is None
-    assert "stays in L2" in bench.roofline_note("solve", 39_000_000, 2_000_000_000)
-    assert "stays in L2" not in bench.roofline_note("solve", 1_900_000_000, 2_000_000_000)
-    assert "L1 data pipe" in bench.roofline_note("correct", None, 10)
+    assert bench.roofline_note("k_cg_mg", None, 10) is None
+    assert "stays in L2" in bench.roofline_note("k_cg_mg", 39_000_000, 2_000_000_000)
+    assert "stays in L2" not in bench.roofline_note("k_cg_mg", 1_900_000_000, 2_000_000_000)
+    assert "L1 data pipe" in bench.roofline_note("k_spring_inline", None, 10)
 
 
 def test_traffic_scales_with_particles(tmp_path, monkeypatch):
     f = tmp_path / "traffic.txt"
-    f.write_text("# stage n bytes particles\ncorrect 128 1000 100\n")
+    f.write_text("# kernel n bytes particles\nk_density 128 1000 100\n")
     monkeypatch.setattr(bench, "TRAFFIC", str(f))
-    assert bench.measured_traffic("correct", 128, 100) == (1000, "measured")
-    t, src = bench.measured_traffic("correct", 256, 400)
+    assert bench.measured_traffic("k_density", 128, 100) == (1000, "measured")
+    t, src = bench.measured_traffic("k_density", 256, 400)
     assert t == 4000 and "scaled" in src
-    assert bench.measured_traffic("p2g", 256, 400) == (None, None)
+    assert bench.measured_traffic("k_p2g_cells", 256, 400) == (None, None)
+
+
+def test_committed_traffic_rows_name_profiled_kernels():
+    """Every row of profiles/traffic.txt names a kernel that the per-kernel
+    profile reports, so the bench can find it."""
+    kernels = {"k_density", "k_p2g_cells", "k_spring_inline", "k_resample_inline",
+               "k_flip_advect", "k_cg_mg", "k_cg_cg1", "k_cg_ic", "k_cg"}
+    with open(bench.TRAFFIC) as f:
+        rows = [ln.split() for ln in f if ln.strip() and not ln.startswith("#")]
+    assert rows and all(len(r) == 4 and r[0] in kernels for r in rows)

@@ -551,6 +551,41 @@ def test_tuned_batch_matches_lone_handles_with_its_grids(gpu, precond):
             assert np.array_equal(x, y)
 
 
+def test_stage_and_kernel_profiles(gpu):
+    """The profiling mode's stage times and its per-kernel times (CUDA events
+    around the main kernels' launches) cover the step: one launch of each
+    FAST gather per step, the refined multigrid solve's launches, and kernel
+    times that fit inside their stages; profiling changes no bit."""
+    sc = scenes.dam_break(48, seed=7)
+    sims = [_fast_sim(gpu, sc, seed=2, precond=gpu.PRECOND_MG, arith=gpu.ARITH_FAST)
+            for _ in range(2)]
+    sims[0].set_profiling(True)
+    steps = 3
+    for _ in range(steps):
+        for s in sims:
+            assert s.step().status == 0
+    stages = sims[0].profile()
+    kern = sims[0].kernel_profile()
+    sims[0].set_profiling(False)
+    print(stages, kern)
+    for k in ("k_density", "k_p2g_cells", "k_spring_inline", "k_resample_inline",
+              "k_flip_advect"):
+        assert kern[k][1] == steps, k
+        assert kern[k][0] > 0.0
+    assert kern["k_cg_mg"][1] >= steps
+    assert kern["k_density"][0] <= stages["density"][0] * 1.001
+    assert kern["k_p2g_cells"][0] <= stages["p2g"][0] * 1.001
+    assert kern["k_cg_mg"][0] <= stages["solve"][0] * 1.001
+    assert (kern["k_spring_inline"][0] + kern["k_resample_inline"][0]
+            <= stages["correct"][0] * 1.001)
+    for x, y in zip(sims[0].get_particles(), sims[1].get_particles()):
+        assert np.array_equal(x, y)
+    # switching profiling on again starts from zero
+    sims[0].set_profiling(True)
+    assert sims[0].kernel_profile() == {}
+    sims[0].set_profiling(False)
+
+
 def test_gather_block_sizes_give_the_same_bits(gpu, monkeypatch):
     """The FAST gathers' block size (tuned per kernel and problem size)
     changes no bit: three steps with 128, 256 and 512 threads per block, and
