@@ -917,7 +917,7 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
   StageClock clk(h);
   /* sort + add_ExtForce fused into the payload, then computeDensity */
   clk.mark(FLIPGPU_STAGE_SORT);
-  CK(h, launch_sort(h, 1));
+  CK(h, launch_sort(h, 1, PL_SPG | PL_SVEL)); /* the density stage writes sdens */
   clk.mark(FLIPGPU_STAGE_DENSITY);
   CK(h, launch_density(h));
   if (h->defer_vel) {
@@ -936,7 +936,7 @@ static int step_body(FlipGpu *h, FlipGpuSolveStats *st) {
   CK(h, launch_flip_advect(h));
   clk.mark(FLIPGPU_STAGE_ADVECT);
   clk.mark(FLIPGPU_STAGE_REPOSITION);
-  CK(h, launch_reposition(h, nullptr));
+  CK(h, launch_reposition(h, nullptr, true));
   clk.mark(FLIPGPU_STAGE_CORRECT);
   CK(h, launch_correct(h));
   clk.mark(FLIPGPU_NSTAGES);

@@ -239,8 +239,14 @@ enum {
 SimConst make_const(const FlipGpu *h);
 
 /* launchers (one per reference stage or sub-stage); return cudaError_t */
-cudaError_t launch_sort(FlipGpu *h, int apply_gravity);
-cudaError_t launch_payload(FlipGpu *h, int apply_gravity);
+/* Sorted copies written by the sort's payload besides spos. A step leaves
+ * out what it rewrites before reading (sdens: the density stage) or never
+ * reads (after the reposition's sort: spg, sdens, and svel, which the
+ * reposition refreshes); the lists then stop being valid at the step's
+ * end, so later calls sort again. */
+enum { PL_SPG = 1, PL_SVEL = 2, PL_SDENS = 4, PL_ALL = 7 };
+cudaError_t launch_sort(FlipGpu *h, int apply_gravity, int fields = PL_ALL);
+cudaError_t launch_payload(FlipGpu *h, int apply_gravity, int fields = PL_ALL);
 /* the velocity half of the payload: the deferred one (FlipGpu::defer_vel)
  * or a refresh of the sorted velocities */
 cudaError_t launch_payload_vel(FlipGpu *h, int apply_gravity);
@@ -259,7 +265,9 @@ cudaError_t launch_flip_blend(FlipGpu *h);
 cudaError_t launch_advect(FlipGpu *h);
 /* launch_flip_blend + launch_advect in one kernel (one grid sample) */
 cudaError_t launch_flip_advect(FlipGpu *h);
-cudaError_t launch_reposition(FlipGpu *h, int *stuck_host);
+/* in_step: the step's own reposition, whose sort writes only spos (see
+ * PL_*) */
+cudaError_t launch_reposition(FlipGpu *h, int *stuck_host, bool in_step = false);
 cudaError_t launch_correct(FlipGpu *h);
 cudaError_t launch_fetch_points(FlipGpu *h, int count, const float *pts, float *out);
 cudaError_t launch_resample_points(FlipGpu *h, int count, const float *pts, float *vel,

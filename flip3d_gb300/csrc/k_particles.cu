@@ -1347,7 +1347,7 @@ cudaError_t launch_advect(FlipGpu *h) {
 
 /* Compute stuck and deep-water lists, place the stuck particles. The sort
  * and the ordered resample follow in launch_reposition_resample. */
-cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
+cudaError_t launch_reposition(FlipGpu *h, int *stuck_host, bool in_step) {
   SimConst c = make_const(h);
   cudaError_t e;
   if (h->np == 0) {
@@ -1380,7 +1380,7 @@ cudaError_t launch_reposition(FlipGpu *h, int *stuck_host) {
   FG_LAUNCHED(h, 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   /* sorter::sort (src/flip3D.cpp:443), shared with the corrector's sort. */
-  if ((e = launch_sort(h, 0)) != cudaSuccess) return e;
+  if ((e = launch_sort(h, 0, in_step ? 0 : PL_ALL)) != cudaSuccess) return e;
   /* corrector::resample of each stuck particle in order (src/flip3D.cpp:445-450) */
   int *left = h->iflags + IF_REPO_LEFT;
   if ((e = cudaMemsetAsync(left, 0, sizeof(int), h->stream)) != cudaSuccess) return e;

@@ -175,6 +175,10 @@ __global__ void k_sort_fixup(size_t nc, const uint32_t *__restrict__ cell_start,
 
 /* Sorted payload; with apply_gravity also add_ExtForce (src/flip3D.cpp:
  * 870-875) on the fluid velocities, canonical and sorted. */
+/* The sorted copies a caller needs (spos always): PL_SPG, PL_SVEL, PL_SDENS
+ * (flipgpu_impl.h). add_ExtForce updates the canonical velocity whichever
+ * copies are written. */
+template <int FIELDS>
 __global__ void k_payload(SimConst c, int apply_gravity, const uint32_t *__restrict__ perm,
                           const float *__restrict__ px, const float *__restrict__ py,
                           const float *__restrict__ pz, float *__restrict__ vx,
@@ -187,23 +191,27 @@ __global__ void k_payload(SimConst c, int apply_gravity, const uint32_t *__restr
   uint32_t p = perm[a];
   float x = px[p], y = py[p], z = pz[p];
   uint8_t t = type[p];
-  float ux = vx[p], uy = vy[p], uz = vz[p];
-  if (apply_gravity && t == CELL_FLUID) {
-    uy = refmath::add_fd(uy, c.grav_h, c.grav_l, c.grav);
-    vy[p] = uy;
-  }
   float tw = pack_type(t);
   spos[a] = make_float4(x, y, z, tw);
-  /* FLOAT x = fmax(0, fmin(gn, gn*p)) (src/mapper.cpp:28-30) */
-  spg[a] = make_float4(fmaxf(0.0f, fminf(c.fn, c.fn * x)), fmaxf(0.0f, fminf(c.fn, c.fn * y)),
-                       fmaxf(0.0f, fminf(c.fn, c.fn * z)), tw);
-  svel[a] = make_float4(ux, uy, uz, 0.0f);
-  sdens[a] = dens[p];
+  if (FIELDS & PL_SPG)
+    /* FLOAT x = fmax(0, fmin(gn, gn*p)) (src/mapper.cpp:28-30) */
+    spg[a] = make_float4(fmaxf(0.0f, fminf(c.fn, c.fn * x)), fmaxf(0.0f, fminf(c.fn, c.fn * y)),
+                         fmaxf(0.0f, fminf(c.fn, c.fn * z)), tw);
+  if ((FIELDS & PL_SVEL) || apply_gravity) {
+    float ux = vx[p], uy = vy[p], uz = vz[p];
+    if (apply_gravity && t == CELL_FLUID) {
+      uy = refmath::add_fd(uy, c.grav_h, c.grav_l, c.grav);
+      vy[p] = uy;
+    }
+    if (FIELDS & PL_SVEL) svel[a] = make_float4(ux, uy, uz, 0.0f);
+  }
+  if (FIELDS & PL_SDENS) sdens[a] = dens[p];
 }
 
 /* The payload in two parts, for steps whose velocities arrive while the
  * sort runs: positions, grid positions and densities first, the velocities
  * (with add_ExtForce) once they are on the device. Same values as k_payload. */
+template <bool SDENS>
 __global__ void k_payload_pos(SimConst c, const uint32_t *__restrict__ perm,
                               const float *__restrict__ px, const float *__restrict__ py,
                               const float *__restrict__ pz, const uint8_t *__restrict__ type,
@@ -217,7 +225,7 @@ __global__ void k_payload_pos(SimConst c, const uint32_t *__restrict__ perm,
   spos[a] = make_float4(x, y, z, tw);
   spg[a] = make_float4(fmaxf(0.0f, fminf(c.fn, c.fn * x)), fmaxf(0.0f, fminf(c.fn, c.fn * y)),
                        fmaxf(0.0f, fminf(c.fn, c.fn * z)), tw);
-  sdens[a] = dens[p];
+  if (SDENS) sdens[a] = dens[p];
 }
 
 __global__ void k_payload_vel(SimConst c, int apply_gravity, const uint32_t *__restrict__ perm,
@@ -346,20 +354,35 @@ cudaError_t scan_exclusive(FlipGpu *h, const uint32_t *in, uint32_t *out, size_t
 
 size_t scan_tmp_blocks(size_t n) { return (n + SCAN_TILE - 1) / SCAN_TILE + 1; }
 
-cudaError_t launch_payload(FlipGpu *h, int apply_gravity) {
+cudaError_t launch_payload(FlipGpu *h, int apply_gravity, int fields) {
   SimConst c = make_const(h);
   if (h->np == 0) return cudaSuccess;
+  const unsigned g = grid_for(h->np, 256);
   if (h->defer_vel) {
     /* the velocities are still being uploaded (flipgpu_step_host) */
-    k_payload_pos<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
-        c, h->perm, h->px, h->py, h->pz, h->type, h->dens, h->spos, h->spg, h->sdens);
+    if (fields & PL_SDENS)
+      k_payload_pos<true><<<g, 256, 0, h->stream>>>(c, h->perm, h->px, h->py, h->pz, h->type,
+                                                    h->dens, h->spos, h->spg, h->sdens);
+    else
+      k_payload_pos<false><<<g, 256, 0, h->stream>>>(c, h->perm, h->px, h->py, h->pz, h->type,
+                                                     h->dens, h->spos, h->spg, h->sdens);
     FG_LAUNCHED(h, 1);
     h->defer_gravity = apply_gravity;
     return cudaGetLastError();
   }
-  k_payload<<<grid_for(h->np, 256), 256, 0, h->stream>>>(
-      c, apply_gravity, h->perm, h->px, h->py, h->pz, h->vx, h->vy, h->vz, h->type, h->dens,
-      h->spos, h->spg, h->svel, h->sdens);
+#define PAYLOAD(F)                                                                            \
+  k_payload<F><<<g, 256, 0, h->stream>>>(c, apply_gravity, h->perm, h->px, h->py, h->pz, h->vx, \
+                                         h->vy, h->vz, h->type, h->dens, h->spos, h->spg,       \
+                                         h->svel, h->sdens)
+  if (fields == PL_ALL)
+    PAYLOAD(PL_ALL);
+  else if (fields == (PL_SPG | PL_SVEL))
+    PAYLOAD(PL_SPG | PL_SVEL);
+  else if (fields == 0)
+    PAYLOAD(0);
+  else
+    return cudaErrorInvalidValue;
+#undef PAYLOAD
   FG_LAUNCHED(h, 1);
   return cudaGetLastError();
 }
@@ -373,7 +396,7 @@ cudaError_t launch_payload_vel(FlipGpu *h, int apply_gravity) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_sort(FlipGpu *h, int apply_gravity) {
+cudaError_t launch_sort(FlipGpu *h, int apply_gravity, int fields) {
   SimConst c = make_const(h);
   cudaError_t e = cudaMemsetAsync(h->cell_count, 0, (h->nc + 1) * sizeof(uint32_t), h->stream);
   if (e != cudaSuccess) return e;
@@ -393,7 +416,7 @@ cudaError_t launch_sort(FlipGpu *h, int apply_gravity) {
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = launch_payload(h, apply_gravity);
+  e = launch_payload(h, apply_gravity, fields);
   h->cells_valid = true;
   h->lists_exist = true;
   return e;
