@@ -551,6 +551,41 @@ def test_tuned_batch_matches_lone_handles_with_its_grids(gpu, precond):
             assert np.array_equal(x, y)
 
 
+def test_batch_tune_needs_a_step_and_leaves_the_wavefront_uncapped(gpu):
+    """flipbatch_tune refuses a batch whose members have not stepped; in a
+    batch that mixes a multigrid member with an IC(0) wavefront member (which
+    keeps its full grid) it caps only the former, and both then step as lone
+    handles with the same caps do."""
+    scs = [scenes.batch_scene(s) for s in (11, 12)]
+    pcs = [gpu.PRECOND_MG, gpu.PRECOND_IC]
+    mk = lambda: [_fast_sim(gpu, sc, seed=i, precond=pc, arith=gpu.ARITH_FAST)
+                  for i, (sc, pc) in enumerate(zip(scs, pcs))]
+    alone, batched = mk(), mk()
+    b = gpu.Batch(batched)
+    with pytest.raises(gpu.FlipGpuError):
+        b.tune()
+    for s in alone:
+        assert s.step().status == 0
+    b.step()
+    b.sync()
+    share = b.tune()
+    caps = [t.solve_blocks() for t in batched]
+    print(f"share {share}, grids {caps}")
+    assert caps[1] == 0
+    assert (share == 0.0) == (caps[0] == 0)
+    for s, t in zip(alone, batched):
+        s.solve_blocks(t.solve_blocks())
+    for _ in range(2):
+        for s in alone:
+            assert s.step().status == 0
+        b.step()
+    b.sync()
+    for s, t in zip(alone, batched):
+        assert t.last_solve_stats().status == 0
+        for x, y in zip(s.get_particles(), t.get_particles()):
+            assert np.array_equal(x, y)
+
+
 def test_stage_and_kernel_profiles(gpu):
     """The profiling mode's stage times and its per-kernel times (CUDA events
     around the main kernels' launches) cover the step: one launch of each
