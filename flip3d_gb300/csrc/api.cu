@@ -175,7 +175,7 @@ void free_all(FlipGpu *h) {
                   h->iflags, h->flag, h->scan_a, h->scan_b, h->scan_tmp, h->stuck_idx,
                   h->water_idx, h->stage,
                   h->ticket, h->dstep, h->repo_draw, h->repo_res, h->repo_old,
-                  h->repo_cnt, h->repo_start, h->repo_list, h->repo_state};
+                  h->repo_cnt, h->repo_start, h->repo_list, h->repo_state, h->cell_mid};
   for (void *p : ptrs)
     if (p) cudaFree(p);
 }
@@ -387,7 +387,7 @@ int flipgpu_create(const FlipGpuParams *p, FlipGpu **out) {
   AL(h->dens, cap) AL(h->type, cap) AL(h->nx, cap) AL(h->ny, cap) AL(h->nz, cap)
   AL(h->key, cap) AL(h->rank, cap) AL(h->perm, cap) AL(h->cell_start, nc + 1)
   AL(h->cell_count, nc + 1) AL(h->spos, cap) AL(h->spg, cap) AL(h->svel, cap)
-  AL(h->sdens, cap) AL(h->wall_start, nc + 1)
+  AL(h->sdens, cap) AL(h->wall_start, nc + 1) AL(h->cell_mid, nc)
   for (int c = 0; c < 3; c++) {
     AL(h->u[c], nf) AL(h->us[c], nf)
   }

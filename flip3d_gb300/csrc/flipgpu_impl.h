@@ -92,6 +92,8 @@ struct FlipGpu {
 
   /* cell lists */
   uint32_t *key, *rank, *perm, *cell_start, *cell_count;
+  uint32_t *cell_mid; /* FAST arithmetic: first slot of each cell's upper z half
+                         (k_sort.cu k_sort_fixup_halves) */
   float4 *spos;       /* world position, w = type */
   float4 *spg;        /* clamp(n*pos, 0, n), w = type (P2G) */
   float4 *svel;       /* velocity, w unused */

@@ -123,13 +123,19 @@ __device__ __forceinline__ void visit_cells(int n, const uint32_t *__restrict__ 
  * each row's k-range is trimmed to the cells the ball reaches. A cell's
  * particles lie in its interval [s h, (s+1) h) of each axis, except the
  * first and last cells, which also hold the clamped particles outside the
- * grid (their interval is open on that side). Callers pass r2 a little
- * above their own cut-off (the corrector's reach), so every particle that
- * passes their exact distance test is visited, in the same order. */
+ * grid (their interval is open on that side). With mid (the lists of
+ * FAST arithmetic, each cell's lower z half first), a row's run also
+ * starts at the first cell's upper half, or stops before the last cell's
+ * upper half, when the ball's z-extent lies wholly on the other side of
+ * that cell's mid-plane (k + 0.5) h: the sort placed the particles by an
+ * exact compare with that plane. Callers pass r2 a little above their own
+ * cut-off (the corrector's reach), so every particle that passes their
+ * exact distance test is visited, in the same order. */
 template <class F>
 __device__ __forceinline__ void visit_ball(int n, float fn, float h, const uint32_t *__restrict__ cs,
-                                           float px, float py, float pz, float r2, int i0, int i1,
-                                           int j0, int j1, int k0, int k1, F f) {
+                                           const uint32_t *__restrict__ mid, float px, float py,
+                                           float pz, float r2, int i0, int i1, int j0, int j1,
+                                           int k0, int k1, F f) {
   i0 = max(i0, 0);
   i1 = min(i1, n - 1);
   j0 = max(j0, 0);
@@ -152,7 +158,11 @@ __device__ __forceinline__ void visit_ball(int n, float fn, float h, const uint3
       const int ka = max(k0, (int)floorf(fn * (pz - rem))), kb = min(k1, (int)floorf(fn * (pz + rem)));
       if (ka > kb) continue;
       const size_t base = ((size_t)si * n + sj) * n;
-      const uint32_t s = __ldg(cs + base + ka), e = __ldg(cs + base + kb + 1);
+      uint32_t s = __ldg(cs + base + ka), e = __ldg(cs + base + kb + 1);
+      if (mid) {
+        if (pz - rem >= ((float)ka + 0.5f) * h) s = __ldg(mid + base + ka);
+        if (pz + rem < ((float)kb + 0.5f) * h) e = __ldg(mid + base + kb);
+      }
       for (uint32_t b = s; b < e; b++) f(b);
     }
   }
@@ -1039,8 +1049,9 @@ k_p2g_cells(SimConst c, int enforce, const uint32_t *__restrict__ cs,
  * this is 5 % faster at N=256 (six blocks spill more and gain less) */
 template <class AR, int B = BLK>
 __global__ void __launch_bounds__(B, 1280 / B)
-k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
-                const float4 *__restrict__ spos, const float *__restrict__ nx,
+k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ mid,
+                const uint32_t *__restrict__ perm, const float4 *__restrict__ spos,
+                const float *__restrict__ nx,
                 const float *__restrict__ ny, const float *__restrict__ nz,
                 float *__restrict__ px, float *__restrict__ py, float *__restrict__ pz) {
   const int a = blockIdx.x * B + threadIdx.x;
@@ -1057,7 +1068,8 @@ k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__r
   reach_range(P.z, c.corr_reach, c.fn, c.n, z, k0, k1);
   float spring[3] = {0.0f, 0.0f, 0.0f};
   const float reach2 = c.corr_reach * c.corr_reach;
-  visit_ball(c.n, c.fn, c.h, cs, P.x, P.y, P.z, reach2, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+  visit_ball(c.n, c.fn, c.h, cs, mid, P.x, P.y, P.z, reach2, i0, i1, j0, j1, k0, k1,
+             [&](uint32_t b) {
     if (b == (uint32_t)a) return;
     const float4 Q = __ldg(spos + b);
     if (AR::hypot2(P.x - Q.x, P.y - Q.y, P.z - Q.z) > c.corr_cut2) return;
@@ -1089,7 +1101,8 @@ k_spring_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__r
 
 template <class AR, int B = BLK>
 __global__ void __launch_bounds__(B)
-k_resample_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *__restrict__ perm,
+k_resample_inline(SimConst c, const uint32_t *__restrict__ cs,
+                  const uint32_t *__restrict__ mid, const uint32_t *__restrict__ perm,
                   const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                   const float *__restrict__ px, const float *__restrict__ py,
                   const float *__restrict__ pz, float *__restrict__ vx, float *__restrict__ vy,
@@ -1108,7 +1121,8 @@ k_resample_inline(SimConst c, const uint32_t *__restrict__ cs, const uint32_t *_
   float u[3] = {0.0f, 0.0f, 0.0f};
   float wsum = 0.0f;
   const float reach2 = c.corr_reach * c.corr_reach;
-  visit_ball(c.n, c.fn, c.h, cs, T[0], T[1], T[2], reach2, i0, i1, j0, j1, k0, k1, [&](uint32_t b) {
+  visit_ball(c.n, c.fn, c.h, cs, mid, T[0], T[1], T[2], reach2, i0, i1, j0, j1, k0, k1,
+             [&](uint32_t b) {
     const float4 Q = __ldg(spos + b);
     if (unpack_type(Q.w) != CELL_FLUID) return;
     const float d2 = AR::hypot2(T[0] - Q.x, T[1] - Q.y, T[2] - Q.z);
@@ -1425,14 +1439,16 @@ cudaError_t launch_correct(FlipGpu *h) {
     cudaError_t e = tuned_gather(h, "k_spring_inline", h->np, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_spring_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
-          c, h->cell_start, h->perm, h->spos, h->nx, h->ny, h->nz, h->px, h->py, h->pz);
+          c, h->cell_start, h->cell_mid, h->perm, h->spos, h->nx, h->ny, h->nz, h->px, h->py,
+          h->pz);
     });
     if (e != cudaSuccess) return e;
     if (h->xfer_pos_out && (e = xfer_positions_out(h)) != cudaSuccess) return e;
     return tuned_gather(h, "k_resample_inline", h->np, [&](auto B) {
       constexpr int b = decltype(B)::value;
       k_resample_inline<FastArith, b><<<grid_for(h->np, b), b, 0, h->stream>>>(
-          c, h->cell_start, h->perm, h->spos, h->svel, h->px, h->py, h->pz, h->vx, h->vy, h->vz);
+          c, h->cell_start, h->cell_mid, h->perm, h->spos, h->svel, h->px, h->py, h->pz, h->vx,
+          h->vy, h->vz);
     });
   }
   if (fast)

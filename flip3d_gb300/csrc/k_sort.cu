@@ -7,7 +7,8 @@
  *   scan     cell_start = exclusive prefix sum of the counts
  *   scatter  perm[cell_start[key] + rank] = particle
  *   fixup    each cell's slots sorted by particle index, which makes the
- *            lists identical to the reference's push_back order
+ *            lists identical to the reference's push_back order (FAST
+ *            arithmetic: by the z half of the cell first, then by index)
  *   payload  sorted copies of position / clamped grid position / velocity
  *            for the gather stages (optionally applying add_ExtForce)
  *
@@ -107,17 +108,24 @@ __global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restric
   }
 }
 
+/* key = the particle's cell; with HALVES (FAST arithmetic) bit 31 also
+ * marks a particle at or above its cell's mid-plane in z, (k + 0.5) h, and
+ * the scatter carries that bit into perm for k_sort_fixup_halves (cell ids
+ * and particle indices stay below 2^31). */
+template <bool HALVES>
 __global__ void k_sort_count(SimConst c, const float *__restrict__ px,
                              const float *__restrict__ py, const float *__restrict__ pz,
                              uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                              uint32_t *__restrict__ count) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= c.np) return;
+  const float z = pz[p];
   int i = cell_clamp(px[p], c.fn, c.n);
   int j = cell_clamp(py[p], c.fn, c.n);
-  int k = cell_clamp(pz[p], c.fn, c.n);
+  int k = cell_clamp(z, c.fn, c.n);
   uint32_t kk = (uint32_t)cell_id(c.n, i, j, k);
-  key[p] = kk;
+  const bool up = HALVES && z >= ((float)k + 0.5f) * c.h;
+  key[p] = kk | (up ? 0x80000000u : 0u);
   rank[p] = atomicAdd(&count[kk], 1u);
 }
 
@@ -127,7 +135,8 @@ __global__ void k_sort_scatter(int np, const uint32_t *__restrict__ key,
                                uint32_t *__restrict__ perm) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= np) return;
-  perm[cell_start[key[p]] + rank[p]] = (uint32_t)p;
+  const uint32_t kk = key[p];
+  perm[cell_start[kk & 0x7fffffffu] + rank[p]] = (uint32_t)p | (kk & 0x80000000u);
 }
 
 /* Order each cell's slots by particle index: insertion sort for the usual
@@ -171,6 +180,59 @@ __global__ void k_sort_fixup(size_t nc, const uint32_t *__restrict__ cell_start,
     a[end] = t;
     sift(0, end);
   }
+}
+
+/* FAST arithmetic: each cell's slots ordered by (z half, particle index),
+ * the particles below the cell's mid-plane (k + 0.5) h first, and
+ * cell_mid[c] the slot where the upper half starts, so that a walk along a
+ * row of cells can start or stop at half a cell. The half arrives in bit
+ * 31 of each slot (k_sort_count<true>, k_sort_scatter), which makes it the
+ * leading sort key; the bit is cleared at the end. */
+__global__ void k_sort_fixup_halves(size_t nc, const uint32_t *__restrict__ cell_start,
+                                    uint32_t *__restrict__ perm,
+                                    uint32_t *__restrict__ cell_mid) {
+  size_t cidx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cidx >= nc) return;
+  const uint32_t s = cell_start[cidx], e = cell_start[cidx + 1];
+  const uint32_t len = e - s;
+  uint32_t *a = perm + s;
+  uint32_t low = 0;
+  for (uint32_t i = 0; i < len; i++) low += a[i] >> 31 ? 0u : 1u;
+  cell_mid[cidx] = s + low;
+  if (len >= 2) {
+    if (len <= 32) {
+      for (uint32_t i = 1; i < len; i++) {
+        uint32_t v = a[i];
+        uint32_t j = i;
+        while (j > 0 && a[j - 1] > v) {
+          a[j] = a[j - 1];
+          j--;
+        }
+        a[j] = v;
+      }
+    } else {
+      auto sift = [&](uint32_t root, uint32_t end) {
+        while (true) {
+          uint32_t child = 2 * root + 1;
+          if (child >= end) break;
+          if (child + 1 < end && a[child] < a[child + 1]) child++;
+          if (a[root] >= a[child]) break;
+          uint32_t t = a[root];
+          a[root] = a[child];
+          a[child] = t;
+          root = child;
+        }
+      };
+      for (uint32_t i = len / 2; i-- > 0;) sift(i, len);
+      for (uint32_t end = len - 1; end > 0; end--) {
+        uint32_t t = a[0];
+        a[0] = a[end];
+        a[end] = t;
+        sift(0, end);
+      }
+    }
+  }
+  for (uint32_t i = low; i < len; i++) a[i] &= 0x7fffffffu;
 }
 
 /* Sorted payload; with apply_gravity also add_ExtForce (src/flip3D.cpp:
@@ -401,8 +463,12 @@ cudaError_t launch_sort(FlipGpu *h, int apply_gravity, int fields) {
   cudaError_t e = cudaMemsetAsync(h->cell_count, 0, (h->nc + 1) * sizeof(uint32_t), h->stream);
   if (e != cudaSuccess) return e;
   if (h->np > 0) {
-    k_sort_count<<<grid_for(h->np, 256), 256, 0, h->stream>>>(c, h->px, h->py, h->pz, h->key,
-                                                              h->rank, h->cell_count);
+    if (h->prm.arith == FLIPGPU_ARITH_FAST)
+      k_sort_count<true><<<grid_for(h->np, 256), 256, 0, h->stream>>>(
+          c, h->px, h->py, h->pz, h->key, h->rank, h->cell_count);
+    else
+      k_sort_count<false><<<grid_for(h->np, 256), 256, 0, h->stream>>>(
+          c, h->px, h->py, h->pz, h->key, h->rank, h->cell_count);
     FG_LAUNCHED(h, 1);
   }
   /* cell_count has nc+1 entries (last = 0), so cell_start[nc] = np. */
@@ -411,7 +477,11 @@ cudaError_t launch_sort(FlipGpu *h, int apply_gravity, int fields) {
   if (h->np > 0) {
     k_sort_scatter<<<grid_for(h->np, 256), 256, 0, h->stream>>>(h->np, h->key, h->rank,
                                                                 h->cell_start, h->perm);
-    k_sort_fixup<<<grid_for(h->nc, 256), 256, 0, h->stream>>>(h->nc, h->cell_start, h->perm);
+    if (h->prm.arith == FLIPGPU_ARITH_FAST)
+      k_sort_fixup_halves<<<grid_for(h->nc, 256), 256, 0, h->stream>>>(
+          h->nc, h->cell_start, h->perm, h->cell_mid);
+    else
+      k_sort_fixup<<<grid_for(h->nc, 256), 256, 0, h->stream>>>(h->nc, h->cell_start, h->perm);
     FG_LAUNCHED(h, 2);
   }
   e = cudaGetLastError();

@@ -15,7 +15,9 @@
  *   faces       u0 (n+1)*n*n, u1 n*(n+1)*n, u2 n*n*(n+1), x-major
  *   cell lists  cell_start[n^3+1], perm[count]: the particles of cell c are
  *               perm[cell_start[c] .. cell_start[c+1]) in particle order,
- *               exactly the lists sorter::sort builds
+ *               exactly the lists sorter::sort builds (FAST arithmetic lists
+ *               the particles below the cell's mid-plane in z, (k + 0.5)/n,
+ *               first, each half in particle order)
  *
  * Every call returns FLIPGPU_OK (0) or a negative FLIPGPU_E* code;
  * flipgpu_last_error() gives a message. Handles are not thread-safe, like
@@ -68,8 +70,11 @@ extern "C" {
  * corrector's spring and resample). REF: the reference's float expressions
  * and double promotions reproduced bit for bit (error-free transforms).
  * FAST: native FP32 with fused multiply-adds and the fast division
- * intrinsic; results agree with REF to FP32 rounding per step. The sort,
- * the grid stages and the solver are unaffected. */
+ * intrinsic; results agree with REF to FP32 rounding per step. FAST also
+ * orders each cell's particles by z half (see the cell lists above), so a
+ * sum over a cell runs in that order and the corrector's neighbour walk
+ * starts and stops at half cells. The grid stages and the solver are
+ * unaffected. */
 #define FLIPGPU_ARITH_REF 0
 #define FLIPGPU_ARITH_FAST 1
 

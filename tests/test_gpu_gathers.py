@@ -83,3 +83,27 @@ def test_fast_gathers_against_the_per_particle_kernels(gpu, crowd):
     for k in a:
         assert np.array_equal(a[k], b[k]), k
         assert np.array_equal(b[k], b2[k]), k      # deterministic
+
+
+@pytest.mark.parametrize("crowd", [False, True])
+def test_fast_cell_lists_put_the_lower_half_first(gpu, crowd):
+    """FAST arithmetic lists each cell's particles below its mid-plane in z,
+    (k + 0.5)/n, first and each half in particle order (the order the
+    corrector's half-cell walk relies on); REF keeps particle order."""
+    n = 48
+    sc = crowded_scene(n, 4) if crowd else scenes.pool_sphere(n, seed=4)
+    for arith in (gpu.ARITH_FAST, gpu.ARITH_REF):
+        prm = gpu.default_params(n, sc.count, solve_mode=gpu.SOLVE_FAST,
+                                 precond=gpu.PRECOND_MG, arith=arith)
+        sim = gpu.Simulation(prm)
+        sim.set_particles(sc.pos, sc.type, sc.vel, sc.nrm)
+        sim.sort()
+        cs, perm = sim.get_cells()
+        sim.close()
+        z = sc.pos[:, 2]
+        k = np.clip((z * np.float32(n)).astype(np.int64), 0, n - 1)
+        mid = ((k.astype(np.float32) + np.float32(0.5)) * np.float32(1.0 / n)).astype(np.float32)
+        up = (z >= mid).astype(np.int64)
+        cell = np.repeat(np.arange(n ** 3), np.diff(cs.astype(np.int64)))
+        key = (cell << 33) + ((up[perm] << 32) if arith == gpu.ARITH_FAST else 0) + perm
+        assert np.all(np.diff(key) > 0), arith
