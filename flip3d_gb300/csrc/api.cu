@@ -209,7 +209,8 @@ struct StageClock {
 } // namespace
 
 void ktime_begin(FlipGpu *h, const char *name) {
-  if (!h->prof_on || h->kt_n >= FlipGpu::KT_SLOTS) return;
+  if (!h->prof_on) return;
+  if (h->kt_n >= FlipGpu::KT_SLOTS) ktime_flush(h); /* calls outside a step: read as we go */
   if (!h->kt_ready) {
     for (int i = 0; i < 2 * FlipGpu::KT_SLOTS; i++)
       if (cudaEventCreate(&h->kt_ev[i]) != cudaSuccess) return;

@@ -111,7 +111,8 @@ __global__ void k_scan_down(const uint32_t *__restrict__ in, uint32_t *__restric
 /* key = the particle's cell; with HALVES (FAST arithmetic) bit 31 also
  * marks a particle at or above its cell's mid-plane in z, (k + 0.5) h, and
  * the scatter carries that bit into perm for k_sort_fixup_halves (cell ids
- * and particle indices stay below 2^31). */
+ * stay below 2^30, as flipgpu_create allows n <= 1024, and particle
+ * indices below 2^31). */
 template <bool HALVES>
 __global__ void k_sort_count(SimConst c, const float *__restrict__ px,
                              const float *__restrict__ py, const float *__restrict__ pz,
