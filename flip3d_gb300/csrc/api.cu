@@ -505,6 +505,9 @@ int flipgpu_set_params(FlipGpu *h, const FlipGpuParams *p) {
     int r = ic_alloc(h);
     if (r != FLIPGPU_OK) return fail(h, r, "set_params: wavefront buffers");
   }
+  /* the two arithmetics order a cell's particles differently (FAST by z
+   * half): lists sorted under the other one are sorted again before use */
+  if (p->arith != h->prm.arith) h->cells_valid = false;
   h->prm = *p;
   return FLIPGPU_OK;
 }

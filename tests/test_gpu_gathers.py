@@ -107,3 +107,23 @@ def test_fast_cell_lists_put_the_lower_half_first(gpu, crowd):
         cell = np.repeat(np.arange(n ** 3), np.diff(cs.astype(np.int64)))
         key = (cell << 33) + ((up[perm] << 32) if arith == gpu.ARITH_FAST else 0) + perm
         assert np.all(np.diff(key) > 0), arith
+
+
+def test_switching_arithmetic_sorts_again(gpu):
+    """Lists sorted under FAST arithmetic (lower z half first) are not used
+    by REF gathers after flipgpu_set_params switches to REF: the density
+    then equals a REF handle's bit for bit."""
+    n = 40
+    sc = scenes.pool_sphere(n, seed=6)
+    out = {}
+    for first in (gpu.ARITH_FAST, gpu.ARITH_REF):
+        prm = gpu.default_params(n, sc.count, arith=first)
+        sim = gpu.Simulation(prm)
+        sim.set_particles(sc.pos, sc.type, sc.vel, sc.nrm)
+        sim.set_max_density(25.0)
+        sim.sort()
+        sim.set_params(gpu.default_params(n, sc.count, arith=gpu.ARITH_REF))
+        sim.compute_density()
+        out[first] = sim.get_particles()[2]
+        sim.close()
+    assert np.array_equal(out[gpu.ARITH_FAST], out[gpu.ARITH_REF])
